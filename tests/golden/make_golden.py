@@ -1,0 +1,188 @@
+"""Generate the golden fixtures by running the reference pipeline itself.
+
+Test infrastructure, run in a container that has the reference checkout at
+``/root/reference`` (it is never read at test time).  Numba is not
+installed there, so ``numba_shim/`` (identity ``jit``, ``prange = range``) is
+put first on ``PYTHONPATH`` and the reference executes as plain Python with
+NumPy semantics.
+
+For every atmosphere in :data:`ATMOSPHERES` the script writes the ``.atm``
+(from :mod:`kurucz_py_joss_submission_gb300.workloads`), converts it with the
+reference's own ``synthe_py/tools/convert_atm_to_npz.py`` and keeps the
+fields the synthesis path reads (``atm_<name>.npz``).  For every case in
+:data:`CASES` it writes the seeded gfall file, runs
+``python -m synthe_py.cli`` with ``SYNTHE_PY_STAGE_DUMPS`` and stores the
+stage arrays (``case_<name>.npz``): TRANSP + valid mask + centre bins
+(stage 3), ASYNTH (stage 4), continuum and fluxes (stage 5), the ``.spec``
+columns, and the sha256 of the gfall text so a test can confirm that
+regenerating the line list from its seed gives the same file.
+
+Usage: ``python tests/golden/make_golden.py [case ...]``
+"""
+
+from __future__ import annotations
+
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+REFERENCE = Path("/root/reference")
+sys.path.insert(0, str(REPO))
+
+from kurucz_py_joss_submission_gb300 import workloads  # noqa: E402
+
+# Fields of the converted atmosphere that the synthesis path reads
+# (synthe_py/io/atmosphere.py:82 load_cached, populations.py:131,
+# continuum.py:73).
+ATM_FIELDS = (
+    "depth", "temperature", "gas_pressure", "electron_density", "mass_density",
+    "turbulent_velocity", "hckt", "xnf_h", "xnf_he1", "xnf_h2",
+    "population_per_ion", "doppler_per_ion", "wledge", "half_edge",
+    "delta_edge", "cont_abs_coeff", "cont_scat_coeff", "cont_coeff_log10",
+    "teff", "glog",
+)
+
+ATMOSPHERES = {
+    "t5800g444": dict(teff=5800.0, logg=4.44, metallicity=0.0),
+    "t6000g430": dict(teff=6000.0, logg=4.30, metallicity=0.0),
+}
+
+# name: atmosphere, window, line draw.  Line windows extend 0.15 nm past the
+# synthesis window so margin lines (centre outside the grid, wings inside)
+# are exercised.
+CASES = {
+    "tiny_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
+                         n_lines=200, draw=(499.85, 501.15), log_uniform=False, seed=11),
+    "uv_300_302": dict(atm="t5800g444", wl_start=300.0, wl_end=302.0,
+                       n_lines=1500, draw=(299.85, 302.15), log_uniform=False, seed=12),
+    "strong_600_601": dict(atm="t6000g430", wl_start=600.0, wl_end=601.0,
+                           n_lines=300, draw=(599.85, 601.15), log_uniform=False, seed=13,
+                           strong=True),
+    "window_500_510": dict(atm="t5800g444", wl_start=500.0, wl_end=510.0,
+                           n_lines=20_000, draw=(500.0, 510.0), log_uniform=False, seed=20240),
+}
+
+# Cases too large to commit every stage array for: keep a subset.
+LARGE_CASES = {"window_500_510"}
+
+
+def _env() -> dict:
+    env = dict(os.environ)
+    env["PYTHONDONTWRITEBYTECODE"] = "1"
+    env["PYTHONPATH"] = f"{HERE / 'numba_shim'}:{REFERENCE}"
+    return env
+
+
+def case_lines(case: dict) -> workloads.LineDraw:
+    lines = workloads.random_atomic_lines(
+        case["n_lines"], case["draw"][0], case["draw"][1], case["seed"],
+        log_uniform=case["log_uniform"],
+    )
+    if case.get("strong"):
+        # push a handful of lines to saturation so the surface optical depth
+        # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)
+        idx = np.arange(0, len(lines), 25)
+        lines.log_gf[idx] = 2.5
+        lines.code[idx] = 20.01
+        lines.e_lower_cm[idx] = np.minimum(lines.e_lower_cm[idx], 50.0)
+    return lines
+
+
+def build_atmosphere(name: str, work: Path) -> Path:
+    spec = ATMOSPHERES[name]
+    atm_path = HERE / f"atm_{name}.atm"
+    workloads.grey_atmosphere_atm(atm_path, spec["teff"], spec["logg"], spec["metallicity"])
+    full_npz = work / f"{name}_full.npz"
+    subprocess.run(
+        [sys.executable, str(REFERENCE / "synthe_py/tools/convert_atm_to_npz.py"),
+         str(atm_path), str(full_npz),
+         "--atlas-tables", str(REFERENCE / "synthe_py/data/atlas_tables.npz")],
+        check=True, env=_env(), cwd=work, stdout=subprocess.DEVNULL,
+    )
+    with np.load(full_npz) as d:
+        kept = {k: np.asarray(d[k]) for k in ATM_FIELDS if k in d}
+    out = HERE / f"atm_{name}.npz"
+    np.savez_compressed(out, **kept)
+    return full_npz
+
+
+def run_case(name: str, full_npz: Path, work: Path) -> None:
+    case = CASES[name]
+    lines = case_lines(case)
+    text = workloads.format_gfall(lines)
+    gf = work / f"{name}.gf"
+    gf.write_text(text)
+    dumps = work / f"dumps_{name}"
+    dumps.mkdir(exist_ok=True)
+    spec = work / f"{name}.spec"
+    env = _env()
+    env["SYNTHE_PY_STAGE_DUMPS"] = str(dumps)
+    subprocess.run(
+        [sys.executable, "-m", "synthe_py.cli", str(full_npz), str(gf),
+         "--npz", str(full_npz), "--spec", str(spec),
+         "--wl-start", repr(case["wl_start"]), "--wl-end", repr(case["wl_end"]),
+         "--resolution", "300000", "--n-workers", "1",
+         "--cache", str(work / "cache"), "--log-level", "WARNING"],
+        check=True, env=env, cwd=work,
+    )
+    s3 = np.load(dumps / "stage_3_transp.npz")
+    s4 = np.load(dumps / "stage_4_asynth.npz")
+    s5 = np.load(dumps / "stage_5_rt.npz")
+    spec_cols = np.loadtxt(spec)
+    out = dict(
+        gfall_sha256=np.array(hashlib.sha256(text.encode()).hexdigest()),
+        wl_start=np.float64(case["wl_start"]), wl_end=np.float64(case["wl_end"]),
+        resolution=np.float64(300000.0),
+        wavelength=s5["wavelength"],
+        line_indices=np.asarray(s3["line_indices"], dtype=np.int64),
+        valid_mask=np.packbits(np.asarray(s3["valid_mask"], dtype=bool), axis=None),
+        valid_shape=np.array(s3["valid_mask"].shape),
+        flux_total_hz=s5["flux_total_hz"], flux_cont_hz=s5["flux_cont_hz"],
+        spec=spec_cols,
+    )
+    transp = np.asarray(s3["transp"])
+    asynth = np.asarray(s4["asynth"])
+    if name in LARGE_CASES:
+        rng = np.random.default_rng(7)
+        vi = np.argwhere(np.asarray(s3["valid_mask"]))
+        pick = vi[rng.choice(vi.shape[0], size=min(4000, vi.shape[0]), replace=False)]
+        out["transp_pairs"] = pick.astype(np.int64)
+        out["transp_values"] = transp[pick[:, 0], pick[:, 1]]
+        rows = np.array([0, 12, 24, 36, 48, 60, 71])
+        out["asynth_rows"] = rows
+        out["asynth"] = asynth[rows]
+        out["cont_abs_rows"] = np.asarray(s5["cont_abs"])[rows]
+        out["cont_scat_rows"] = np.asarray(s5["cont_scat"])[rows]
+    else:
+        out["transp"] = transp
+        out["asynth"] = asynth
+        out["cont_abs"] = np.asarray(s5["cont_abs"])
+        out["cont_scat"] = np.asarray(s5["cont_scat"])
+        out["stim"] = np.asarray(s4["stim"])
+        out["bnu"] = np.asarray(s4["bnu"])
+    np.savez_compressed(HERE / f"case_{name}.npz", **out)
+
+
+def main(argv: list[str]) -> int:
+    wanted = argv or list(CASES)
+    with tempfile.TemporaryDirectory(prefix="kgold_") as tmp:
+        work = Path(tmp)
+        built = {}
+        for name in wanted:
+            atm = CASES[name]["atm"]
+            if atm not in built:
+                built[atm] = build_atmosphere(atm, work)
+            run_case(name, built[atm], work)
+            print(f"wrote case_{name}.npz", flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main(sys.argv[1:]))
