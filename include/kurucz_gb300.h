@@ -1,0 +1,250 @@
+/*
+ * kurucz_gb300.h -- C ABI of the GB300 line-opacity and transfer library.
+ *
+ * The reference (synthe_py) is Python; its seams for this path are Python
+ * functions, listed beside each entry point that replaces one.  All entry
+ * points take plain pointers and sizes, return a ks_status and run on the
+ * CUDA stream they are given.  The fused entry points (ks_synthesize,
+ * ks_asynth) work in caller-provided workspace; the smaller seam helpers
+ * (ks_line_bins, ks_transp, ks_formal_solution) take stream-ordered
+ * temporaries (cudaMallocAsync) for a few bytes per line or wavelength.
+ * Device pointers are marked "device"; the library never frees caller
+ * memory.  ks_init_tables must be called once per process first; the first
+ * compute call on each device copies the tables to it synchronously, so that
+ * call must come before any CUDA-graph capture on that device.
+ *
+ * Errors: every call returns KS_OK or an error code; ks_last_error() returns
+ * the message of the last failure on the calling thread.  Numerical
+ * problems inside the data (NaN/Inf opacities) are masked as the reference
+ * masks them, not raised.
+ *
+ * Threading: calls are thread-safe; each call only touches the buffers and
+ * stream it is given.
+ */
+#ifndef KURUCZ_GB300_H
+#define KURUCZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t ks_status;
+enum {
+    KS_OK = 0,
+    KS_ERR_INVALID = 1,     /* bad argument (null pointer, size out of range) */
+    KS_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    KS_ERR_NOMEM = 3,       /* workspace too small / allocation failed */
+    KS_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+    KS_ERR_IO = 5,          /* file could not be read */
+    KS_ERR_UNSUPPORTED = 6, /* input outside what the kernels handle */
+    KS_ERR_DEVICE = 7       /* a kernel flagged an internal limit */
+};
+
+/* Arithmetic of the fused path.
+ * KS_PREC_MIXED: FP32 Voigt and profile evaluation with Kahan-compensated
+ *   tile sums, FP32 continuum and Planck, compensated FP32 tau integration,
+ *   FP32 Gauss-Seidel sweeps (the reference's own sweep precision).
+ * KS_PREC_FP64: every step in FP64 (the all-FP64 GPU path).              */
+typedef enum { KS_PREC_MIXED = 0, KS_PREC_FP64 = 1 } ks_precision;
+
+/* One model atmosphere, device pointers (synthe_py/io/atmosphere.py:17
+ * AtmosphereModel fields; sizes as in the converted .npz). */
+typedef struct {
+    int32_t n_layers;               /* L */
+    const double *rhox;             /* [L] column mass ("depth") */
+    const double *temperature;      /* [L] */
+    const double *electron_density; /* [L] */
+    const double *mass_density;     /* [L] */
+    const double *hckt;             /* [L] hc/kT per cm^-1 */
+    const double *xnf_h;            /* [L] (TXNXN inputs, populations.py:204) */
+    const double *xnf_he1;          /* [L] */
+    const double *xnf_h2;           /* [L] */
+    const double *population;       /* [L, n_ion, n_elem] population_per_ion */
+    const double *doppler;          /* [L, n_ion, n_elem] doppler_per_ion */
+    int32_t n_ion;                  /* 6 */
+    int32_t n_elem;                 /* 139 */
+    const double *wledge;           /* [n_edge] continuum edges (nm) */
+    const double *half_edge;        /* [n_edge-1] */
+    const double *delta_edge;       /* [n_edge-1] */
+    int32_t n_edge;
+    const double *cont_abs_coeff;   /* [L, n_edge-1, 3] log10 coefficients */
+    const double *cont_scat_coeff;  /* [L, n_edge-1, 3] */
+    int32_t coeff_log10;            /* 1: coefficients are log10 (always in practice) */
+} ks_atmos;
+
+/* The log-lambda grid, device pointer. */
+typedef struct {
+    int64_t n;                      /* number of grid points */
+    const double *wavelength;       /* [n] nm, built by ks_wavelength_grid */
+    double grid_origin;             /* first point of the unsubsampled grid */
+} ks_grid;
+
+/* Line catalog (LineCatalog, synthe_py/io/lines/atomic.py:237), device
+ * pointers, n_lines entries each, in catalog order. */
+typedef struct {
+    int64_t n_lines;
+    const double *wavelength;       /* nm (vacuum, from the level energies) */
+    const double *gf;               /* 10**log_gf */
+    const double *cgf;              /* 0.026538/1.77245 * gf / freq */
+    const double *gamma_rad;        /* normalised by 4 pi nu (atomic.py:501-504) */
+    const double *gamma_stark;
+    const double *gamma_vdw;
+    const double *elo_cm;           /* lower-level energy, cm^-1 */
+    const int32_t *element_idx;     /* Z-1, or -1 when unknown */
+    const int32_t *ion_stage;       /* 1 = neutral */
+    const int32_t *line_type;       /* 0 plain; see atomic.py:566-582 */
+    const uint8_t *process_mask;    /* 1 = TRANSP processes it (line_opacity.py:740-765) */
+    const uint8_t *asynth_mask;     /* 1 = centre added to ASYNTH (line_opacity.py:1094) */
+    int32_t sorted_by_wavelength;   /* 1 if wavelength is non-decreasing */
+} ks_lines;
+
+typedef struct {
+    double cutoff;          /* KAPMIN = continuum * cutoff (default 1e-3) */
+    double microturb_kms;   /* synthesis microturbulence (default 0) */
+    double rhoxj;           /* scattering scale height (0 = LTE, fscat = 0) */
+    int32_t precision;      /* ks_precision */
+    int32_t tile_bins;      /* accumulation tile width; 0 = autotuned default */
+    int32_t warps_per_tile; /* warps per accumulation CTA; 0 = default */
+    int32_t reserved;
+} ks_options;
+
+/* Counters of one synthesis (filled when a pointer is given). */
+typedef struct {
+    int64_t valid_pairs;        /* (line, depth) pairs that passed both KAPMIN gates */
+    int64_t evaluations;        /* line.depth.lambda contributions accumulated */
+    int64_t maxj_wavelengths;   /* total-flux solves that took the MAXJ=1 path */
+    int64_t iterations;         /* Gauss-Seidel sweeps summed over all solves */
+    int32_t device_flags;       /* nonzero when a kernel hit an internal limit */
+    int32_t reserved;
+} ks_stats;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Version of this ABI. */
+ks_status ks_version(int32_t *major, int32_t *minor);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *ks_last_error(void);
+
+/* Builds the constant tables from the SYNTHE source tables (host memory):
+ * the 81-point H1 Voigt table tabvi/tabh1 (synthe_py/physics/tables.py:249,
+ * expanded to 2001 points as VoigtTables.build does, :224), and the JOSH
+ * grid xtau[51], surface weights ch[51] and operator coefj[51*51]
+ * (synthe_py/physics/josh_tables.py:6,120,177).  Once per process. */
+ks_status ks_init_tables(const double *tabvi, const double *tabh1, int32_t n_tab,
+                         const double *xtau, const double *ch, const double *coefj);
+
+/* Host copies of the derived tables (2001-point H0/H1/H2, 1001-point
+ * EXTAB/EXTABF of tables.py:14-42), for verification.  Any pointer may be
+ * NULL. */
+ks_status ks_get_tables(double *h0, double *h1, double *h2, double *extab, double *extabf);
+
+/* ---- wavelength grid and bins ----------------------------------------- */
+
+/* Replaces synthe_py/engine/opacity.py:526 _build_wavelength_grid.
+ * Host function.  Returns the number of points; writes at most `cap`
+ * points to `out` (out may be NULL to query the size). */
+int64_t ks_wavelength_grid(double start, double end, double resolution,
+                           double *out, int64_t cap);
+
+/* Replaces synthe_py/engine/opacity.py:550 _nearest_grid_indices (centre
+ * bins, -1 / n outside the grid) and line_opacity.py:1030-1059 (wing bins
+ * relative to grid_origin).  wavelength, center_out, wing_out: device. */
+ks_status ks_line_bins(const ks_grid *grid, const double *wavelength, int64_t n_lines,
+                       int32_t *center_out, int32_t *wing_out, void *stream);
+
+/* ---- continuum --------------------------------------------------------- */
+
+/* Replaces synthe_py/physics/continuum.py:73 build_depth_continuum.
+ * Writes ACONT and SIGMAC, [L, n] row-major, as double (KS_PREC_FP64) or
+ * float (KS_PREC_MIXED).  Outputs: device. */
+ks_status ks_continuum(const ks_atmos *atm, const ks_grid *grid, int32_t precision,
+                       void *cont_abs, void *cont_scat, void *stream);
+
+/* ---- TRANSP ------------------------------------------------------------ */
+
+/* Replaces synthe_py/physics/line_opacity.py:620 compute_transp (with the
+ * Boltzmann factors of physics/populations.py:131).  FP64.
+ *   cont_kapmin: [L, n] ACONT+SIGMAC (device, double)
+ *   transp_out:  [n_lines, L] line-centre opacity (device, double)
+ *   valid_out:   [n_lines, L] 1 where both KAPMIN gates pass (device)
+ *   center_out:  [n_lines] centre bins (device, may be NULL)           */
+ks_status ks_transp(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                    const ks_options *opt, const double *cont_kapmin,
+                    double *transp_out, uint8_t *valid_out, int32_t *center_out,
+                    void *stream);
+
+/* ---- ASYNTH ------------------------------------------------------------ */
+
+/* Scratch bytes ks_asynth / ks_synthesize need for these sizes. */
+ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_t n_wavelengths,
+                            const ks_options *opt, size_t *bytes);
+
+/* Replaces synthe_py/physics/line_opacity.py:946 compute_asynth_from_transp
+ * (plain lines; stimulated emission applied).  FP64 in, FP64 out.
+ *   transp, valid: as produced by ks_transp (device)
+ *   asynth_out:    [L, n] (device, double)
+ *   workspace:     ks_workspace_size bytes of device memory            */
+ks_status ks_asynth(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                    const ks_options *opt, const double *transp, const uint8_t *valid,
+                    const double *cont_kapmin, void *workspace, size_t workspace_bytes,
+                    double *asynth_out, ks_stats *stats, void *stream);
+
+/* ---- formal solution ---------------------------------------------------- */
+
+/* Replaces synthe_py/engine/radiative.py:282 solve_lte_spectrum (JOSH
+ * surface flux, physics/josh_solver.py:367).  Field arrays [L, n] in the
+ * precision's type (double for KS_PREC_FP64, float for KS_PREC_MIXED);
+ * line_source may be NULL (Planck).  Fluxes are F_nu (device, double). */
+ks_status ks_formal_solution(const ks_atmos *atm, const ks_grid *grid, int32_t precision,
+                             const void *cont_abs, const void *cont_scat,
+                             const void *line_opacity, const void *line_scattering,
+                             const void *line_source, double *flux_total,
+                             double *flux_cont, ks_stats *stats, void *stream);
+
+/* ---- fused synthesis ------------------------------------------------------ */
+
+/* The hot section of synthe_py/engine/opacity.py:2084 run_synthesis, fused:
+ * continuum -> TRANSP -> ASYNTH -> line source -> JOSH, for one atmosphere.
+ * Fluxes are F_nu at the surface (device, double, [n]); the caller converts
+ * to F_lambda as opacity.py:3855-3861 does.  asynth_out (optional, device,
+ * [L, n], float for MIXED / double for FP64) receives the line opacity. */
+ks_status ks_synthesize(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                        const ks_options *opt, void *workspace, size_t workspace_bytes,
+                        double *flux_total, double *flux_cont, void *asynth_out,
+                        ks_stats *stats, void *stream);
+
+/* ---- gfall reader ---------------------------------------------------------- */
+
+/* Native reader of gfall line lists (synthe_py/io/lines/atomic.py:299
+ * load_catalog: fixed-width records, or the whitespace form for lines
+ * shorter than 98 columns; :762 filter_by_range DELLIM window; the TRANSP
+ * routing of physics/line_opacity.py:740-765 and the ASYNTH centre classes
+ * of :1094).  Host memory.  ks_gfall_read parses the file and keeps lines
+ * inside [wl_min - margin, wl_max + margin] (wl_max <= 0 keeps all);
+ * ks_gfall_sort orders them by wavelength (stable); ks_gfall_count gives the
+ * size; ks_gfall_fetch copies columns (any pointer may be NULL;
+ * catalog_index = position in the window-filtered catalog order, i.e. the
+ * reference's line index); ks_gfall_free releases the handle.  potion: the
+ * 999 ionisation potentials for the Stark/van der Waals defaults (may be
+ * NULL). */
+typedef struct ks_gfall ks_gfall;
+ks_status ks_gfall_read(const char *path, double wl_min, double wl_max,
+                        const double *potion, int32_t n_potion, ks_gfall **out);
+ks_status ks_gfall_sort(ks_gfall *g);
+int64_t ks_gfall_count(const ks_gfall *g);
+ks_status ks_gfall_fetch(const ks_gfall *g, double *wavelength, double *log_gf, double *gf,
+                         double *cgf, double *elo_cm, double *gamma_rad, double *gamma_stark,
+                         double *gamma_vdw, int32_t *element_idx, int32_t *ion_stage,
+                         int32_t *line_type, uint8_t *process_mask, uint8_t *asynth_mask,
+                         double *code, int64_t *catalog_index);
+void ks_gfall_free(ks_gfall *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KURUCZ_GB300_H */

@@ -1,0 +1,164 @@
+"""ctypes binding of ``libkurucz_gb300.so`` (the C ABI in ``include/kurucz_gb300.h``).
+
+Loading fails loudly when the library has not been built: there is no CPU
+fallback for the synthesis path.  On load the constant SYNTHE tables
+(``data/synthe_tables.npz``) are handed to ``ks_init_tables``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+from . import _build
+
+_lib: Optional[C.CDLL] = None
+_lock = threading.Lock()
+TABLES_NPZ = Path(__file__).resolve().parent / "data" / "synthe_tables.npz"
+
+KS_OK = 0
+KS_PREC_MIXED = 0
+KS_PREC_FP64 = 1
+
+P = C.c_void_p
+PD = C.POINTER(C.c_double)
+
+
+class KsError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"kurucz_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class KsAtmos(C.Structure):
+    _fields_ = [
+        ("n_layers", C.c_int32),
+        ("rhox", P), ("temperature", P), ("electron_density", P), ("mass_density", P),
+        ("hckt", P), ("xnf_h", P), ("xnf_he1", P), ("xnf_h2", P),
+        ("population", P), ("doppler", P),
+        ("n_ion", C.c_int32), ("n_elem", C.c_int32),
+        ("wledge", P), ("half_edge", P), ("delta_edge", P),
+        ("n_edge", C.c_int32),
+        ("cont_abs_coeff", P), ("cont_scat_coeff", P),
+        ("coeff_log10", C.c_int32),
+    ]
+
+
+class KsGrid(C.Structure):
+    _fields_ = [("n", C.c_int64), ("wavelength", P), ("grid_origin", C.c_double)]
+
+
+class KsLines(C.Structure):
+    _fields_ = [
+        ("n_lines", C.c_int64),
+        ("wavelength", P), ("gf", P), ("cgf", P), ("gamma_rad", P), ("gamma_stark", P),
+        ("gamma_vdw", P), ("elo_cm", P),
+        ("element_idx", P), ("ion_stage", P), ("line_type", P),
+        ("process_mask", P), ("asynth_mask", P),
+        ("sorted_by_wavelength", C.c_int32),
+    ]
+
+
+class KsOptions(C.Structure):
+    _fields_ = [
+        ("cutoff", C.c_double), ("microturb_kms", C.c_double), ("rhoxj", C.c_double),
+        ("precision", C.c_int32), ("tile_bins", C.c_int32), ("warps_per_tile", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class KsStats(C.Structure):
+    _fields_ = [
+        ("valid_pairs", C.c_int64), ("evaluations", C.c_int64),
+        ("maxj_wavelengths", C.c_int64), ("iterations", C.c_int64),
+        ("device_flags", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "ks_version": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ks_last_error": (C.c_char_p, []),
+    "ks_init_tables": (C.c_int32, [PD, PD, C.c_int32, PD, PD, PD]),
+    "ks_get_tables": (C.c_int32, [PD, PD, PD, PD, PD]),
+    "ks_wavelength_grid": (C.c_int64, [C.c_double, C.c_double, C.c_double, PD, C.c_int64]),
+    "ks_line_bins": (C.c_int32, [C.POINTER(KsGrid), P, C.c_int64, P, P, P]),
+    "ks_continuum": (C.c_int32, [C.POINTER(KsAtmos), C.POINTER(KsGrid), C.c_int32, P, P, P]),
+    "ks_transp": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
+                              C.POINTER(KsOptions), P, P, P, P, P]),
+    "ks_workspace_size": (C.c_int32, [C.c_int64, C.c_int32, C.c_int64, C.POINTER(KsOptions),
+                                      C.POINTER(C.c_size_t)]),
+    "ks_asynth": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
+                              C.POINTER(KsOptions), P, P, P, P, C.c_size_t, P,
+                              C.POINTER(KsStats), P]),
+    "ks_formal_solution": (C.c_int32, [C.POINTER(KsAtmos), C.POINTER(KsGrid), C.c_int32, P, P, P,
+                                       P, P, P, P, C.POINTER(KsStats), P]),
+    "ks_synthesize": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
+                                  C.POINTER(KsOptions), P, C.c_size_t, P, P, P,
+                                  C.POINTER(KsStats), P]),
+    "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,
+                                  C.POINTER(P)]),
+    "ks_gfall_sort": (C.c_int32, [P]),
+    "ks_gfall_count": (C.c_int64, [P]),
+    "ks_gfall_fetch": (C.c_int32, [P] + [P] * 15),
+    "ks_gfall_free": (None, [P]),
+}
+
+
+def lib_path() -> Path:
+    return _build.lib_path()
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Load the library (and initialise its tables) once per process."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = lib_path()
+        if not path.exists():
+            if build_if_missing:
+                _build.build()
+            else:
+                raise RuntimeError(
+                    f"native library {path} is missing: run "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` (needs nvcc)"
+                )
+        L = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        with np.load(TABLES_NPZ) as t:
+            tabvi = np.ascontiguousarray(t["tabvi"], dtype=np.float64)
+            tabh1 = np.ascontiguousarray(t["tabh1"], dtype=np.float64)
+            xtau = np.ascontiguousarray(t["xtau"], dtype=np.float64)
+            ch = np.ascontiguousarray(t["ch"], dtype=np.float64)
+            coefj = np.ascontiguousarray(t["coefj"], dtype=np.float64)
+        st = L.ks_init_tables(_pd(tabvi), _pd(tabh1), tabvi.size, _pd(xtau), _pd(ch), _pd(coefj))
+        if st != KS_OK:
+            raise KsError(st, L.ks_last_error().decode())
+        _lib = L
+        return _lib
+
+
+def _pd(a: np.ndarray):
+    return a.ctypes.data_as(PD)
+
+
+def check(status: int) -> None:
+    if status != KS_OK:
+        raise KsError(status, load().ks_last_error().decode())
+
+
+def exported_symbols() -> list:
+    return sorted(SIGNATURES)

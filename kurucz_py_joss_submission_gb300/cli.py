@@ -1,0 +1,69 @@
+"""Command-line entry point with the reference's flags (synthe_py/cli.py:15-154).
+
+``python -m kurucz_py_joss_submission_gb300.cli MODEL.atm LINES.gf --npz X.npz
+--spec out.spec --wl-start A --wl-end B`` behaves like ``python -m
+synthe_py.cli`` for the plain-line LTE path; --precision/--tile-bins/
+--warps-per-tile select the GPU arithmetic and tiling.
+"""
+
+from __future__ import annotations
+
+import argparse
+import logging
+from pathlib import Path
+from typing import Optional
+
+from . import config
+from .engine.opacity import run_synthesis
+
+
+def build_parser() -> argparse.ArgumentParser:
+    p = argparse.ArgumentParser(description="GB300 SYNTHE line-opacity and transfer synthesis")
+    p.add_argument("model", type=Path, help="Path to the model atmosphere file (.atm or .npz)")
+    p.add_argument("atomic", type=Path, help="Atomic line catalog (gfall format)")
+    p.add_argument("--npz", type=Path, default=None, help="Explicit .npz atmosphere path")
+    p.add_argument("--spec", type=Path, default=Path("spectrum.spec"), help="Output spectrum")
+    p.add_argument("--wl-start", type=float, default=300.0, help="Start wavelength (nm)")
+    p.add_argument("--wl-end", type=float, default=1800.0, help="End wavelength (nm)")
+    p.add_argument("--resolution", type=float, default=300_000.0, help="Resolving power")
+    p.add_argument("--no-vacuum", action="store_true", help="Treat wavelengths as air")
+    p.add_argument("--cutoff", type=float, default=1e-3, help="Opacity cutoff factor")
+    p.add_argument("--linout", type=int, default=30, help="Line output control flag")
+    p.add_argument("--cache", type=Path, default=None, help="Line cache directory (unused)")
+    p.add_argument("--allow-tfort-runtime", action="store_true", help="Accepted, unused")
+    p.add_argument("--n-workers", type=int, default=None, help="Accepted, unused (GPU)")
+    p.add_argument("--nlte", action="store_true", help="Accepted; LTE source only")
+    p.add_argument("--scat-iterations", type=int, default=8)
+    p.add_argument("--scat-tol", type=float, default=1e-3)
+    p.add_argument("--rhoxj", type=float, default=0.0, help="Scattering scale height RHOXJ")
+    p.add_argument("--log-level", type=str, default="INFO",
+                   choices=["DEBUG", "INFO", "WARNING", "ERROR"])
+    p.add_argument("--diagnostics", type=Path, default=None)
+    p.add_argument("--microturb", type=float, default=0.0, help="Microturbulence (km/s)")
+    p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    p.add_argument("--tile-bins", type=int, default=0)
+    p.add_argument("--warps-per-tile", type=int, default=0)
+    return p
+
+
+def main(argv: Optional[list] = None) -> int:
+    args = build_parser().parse_args(argv)
+    cfg = config.SynthesisConfig.from_cli(
+        spec_path=args.spec, diagnostics_path=args.diagnostics, atmosphere_path=args.model,
+        atomic_catalog=args.atomic, wl_start=args.wl_start, wl_end=args.wl_end,
+        resolution=args.resolution, velocity_microturb=args.microturb,
+        vacuum=not args.no_vacuum, cutoff=args.cutoff, linout=args.linout, nlte=args.nlte,
+        scattering_iterations=args.scat_iterations, scattering_tolerance=args.scat_tol,
+        rhoxj_scale=args.rhoxj, npz_path=args.npz, n_workers=args.n_workers,
+        allow_tfort_runtime=args.allow_tfort_runtime, precision=args.precision,
+        tile_bins=args.tile_bins, warps_per_tile=args.warps_per_tile,
+    )
+    cfg.log_level = args.log_level
+    logging.basicConfig(level=getattr(logging, args.log_level),
+                        format="%(asctime)s %(levelname)s %(name)s: %(message)s")
+    run_synthesis(cfg)
+    return 0
+
+
+if __name__ == "__main__":  # pragma: no cover
+    raise SystemExit(main())

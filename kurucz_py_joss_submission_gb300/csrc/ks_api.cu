@@ -1,0 +1,1001 @@
+// ks_api.cu -- the C ABI (include/kurucz_gb300.h): constant tables, workspace
+// layout, the precision-independent kernels (grid scalars, line bins, reach-
+// class partition) and the pipeline drivers.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/kurucz_gb300.h"
+#include "ks_common.cuh"
+#include "ks_internal.h"
+#include "ks_launch.h"
+
+using namespace ks;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string g_last_error;
+
+static ks_status fail(ks_status code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+static ks_status cuda_fail(cudaError_t e, const char* where) {
+    return fail(KS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define KS_CUDA(call)                                  \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+extern "C" const char* ks_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
+    if (major) *major = 1;
+    if (minor) *minor = 0;
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// constant tables
+// ---------------------------------------------------------------------------
+
+// Device copies of the constant tables (Voigt H0/H1/H2, FASTEX EXTAB/EXTABF,
+// JOSH XTAU/CH).  They are built on the host by ks_init_tables and copied to
+// every device on its first use.
+__device__ double g_h0d[VOIGT_N], g_h1d[VOIGT_N], g_h2d[VOIGT_N];
+__device__ float g_h0f[VOIGT_N], g_h1f[VOIGT_N], g_h2f[VOIGT_N];
+__device__ double g_extab[EXP_N], g_extabf[EXP_N];
+__device__ float g_extab_f[EXP_N], g_extabf_f[EXP_N];
+__device__ double g_xtau[NXTAU], g_ch[NXTAU];
+
+struct HostTables {
+    bool ready = false;
+    std::vector<double> h0, h1, h2, extab, extabf, xtau, ch, coefj;
+    CoefJ32 cj;
+};
+static HostTables g_tables;
+static std::mutex g_tables_mu;
+
+struct DevTables {
+    const double *h0d, *h1d, *h2d, *extab, *extabf, *xtau, *ch;
+    const float *h0f, *h1f, *h2f, *extab_f, *extabf_f;
+};
+static const int kMaxDevices = 64;
+static bool g_dev_ready[kMaxDevices];
+static DevTables g_dev[kMaxDevices];
+
+// MAP1 as used to build the 2001-point H1 table from the 81-point one
+// (synthe_py/physics/tables.py:275-391).
+static void map1_tables(const double* xold, const double* fold, int nold, const double* xnew,
+                        double* fnew, int nnew) {
+    std::vector<double> x1(nold + 2), f1(nold + 2);
+    for (int i = 0; i < nold; i++) {
+        x1[i + 1] = xold[i];
+        f1[i + 1] = fold[i];
+    }
+    int l = 2, ll = 0;
+    double a = 0, b = 0, c = 0, abac = 0, bbac = 0, cbac = 0, afor = 0, bfor = 0, cfor = 0;
+    for (int k = 1; k <= nnew; k++) {
+        double x = xnew[k - 1];
+        for (;;) {
+            if (x < x1[l]) break;
+            l++;
+            if (l > nold) break;
+        }
+        if (l > nold) {
+            if (l != ll) {
+                l = l < nold ? l : nold;
+                c = 0.0;
+                b = (f1[l] - f1[l - 1]) / (x1[l] - x1[l - 1]);
+                a = f1[l] - x1[l] * b;
+                ll = l;
+            }
+        } else if (l == ll) {
+        } else if (l == 2) {
+            c = 0.0;
+            b = (f1[l] - f1[l - 1]) / (x1[l] - x1[l - 1]);
+            a = f1[l] - x1[l] * b;
+            ll = l;
+        } else {
+            int l1 = l - 1;
+            bool done = false;
+            if (l > ll + 1 || l == 3) {
+                int l2 = l - 2;
+                double d = (f1[l1] - f1[l2]) / (x1[l1] - x1[l2]);
+                cbac = f1[l] / ((x1[l] - x1[l1]) * (x1[l] - x1[l2])) +
+                       (f1[l2] / (x1[l] - x1[l2]) - f1[l1] / (x1[l] - x1[l1])) / (x1[l1] - x1[l2]);
+                bbac = d - (x1[l1] + x1[l2]) * cbac;
+                abac = f1[l2] - x1[l2] * d + x1[l1] * x1[l2] * cbac;
+                if (l == nold) {
+                    c = cbac; b = bbac; a = abac; ll = l;
+                    done = true;
+                }
+            } else {
+                cbac = cfor; bbac = bfor; abac = afor;
+                if (l == nold) {
+                    c = cbac; b = bbac; a = abac; ll = l;
+                    done = true;
+                }
+            }
+            if (!done) {
+                double d = (f1[l] - f1[l1]) / (x1[l] - x1[l1]);
+                cfor = f1[l + 1] / ((x1[l + 1] - x1[l]) * (x1[l + 1] - x1[l1])) +
+                       (f1[l1] / (x1[l + 1] - x1[l1]) - f1[l] / (x1[l + 1] - x1[l])) / (x1[l] - x1[l1]);
+                bfor = d - (x1[l] + x1[l1]) * cfor;
+                afor = f1[l1] - x1[l1] * d + x1[l] * x1[l1] * cfor;
+                double wt = 0.0;
+                if (std::fabs(cfor) != 0.0) wt = std::fabs(cfor) / (std::fabs(cfor) + std::fabs(cbac));
+                a = afor + wt * (abac - afor);
+                b = bfor + wt * (bbac - bfor);
+                c = cfor + wt * (cbac - cfor);
+                ll = l;
+            }
+        }
+        fnew[k - 1] = a + (b + c * x) * x;
+    }
+}
+
+// Builds every derived table from the SYNTHE source tables: the Voigt
+// tables (tables.py:224-241), FASTEX tables (tables.py:21-27) and the
+// single-precision JOSH operator.  Host function; call once per process.
+extern "C" ks_status ks_init_tables(const double* tabvi, const double* tabh1, int32_t n_tab,
+                                    const double* xtau, const double* ch, const double* coefj) {
+    if (!tabvi || !tabh1 || n_tab < 3 || n_tab > 1000 || !xtau || !ch || !coefj)
+        return fail(KS_ERR_INVALID, "ks_init_tables: null or invalid table");
+    std::lock_guard<std::mutex> lk(g_tables_mu);
+    HostTables t;
+    t.h0.resize(VOIGT_N);
+    t.h1.resize(VOIGT_N);
+    t.h2.resize(VOIGT_N);
+    std::vector<double> grid(VOIGT_N);
+    for (int i = 0; i < VOIGT_N; i++) grid[i] = (double)i / 200.0;
+    map1_tables(tabvi, tabh1, n_tab, grid.data(), t.h1.data(), VOIGT_N);
+    for (int i = 0; i < VOIGT_N; i++) {
+        double v = (double)i / 200.0;
+        double vv = v * v;
+        t.h0[i] = std::exp(-vv);
+        t.h2[i] = t.h0[i] - (vv + vv) * t.h0[i];
+    }
+    t.extab.resize(EXP_N);
+    t.extabf.resize(EXP_N);
+    for (int i = 0; i < EXP_N; i++) {
+        t.extab[i] = std::exp(-((double)i));
+        t.extabf[i] = std::exp(-((double)i) * 0.001);
+    }
+    t.xtau.assign(xtau, xtau + NXTAU);
+    t.ch.assign(ch, ch + NXTAU);
+    t.coefj.assign(coefj, coefj + NXTAU * NXTAU);
+    for (int i = 0; i < NXTAU * NXTAU; i++) t.cj.c[i] = (float)coefj[i];
+    t.ready = true;
+    g_tables = std::move(t);
+    for (int i = 0; i < kMaxDevices; i++) g_dev_ready[i] = false;
+    return KS_OK;
+}
+
+// Copies of the host-built tables, for tests.
+extern "C" ks_status ks_get_tables(double* h0, double* h1, double* h2, double* extab, double* extabf) {
+    std::lock_guard<std::mutex> lk(g_tables_mu);
+    if (!g_tables.ready) return fail(KS_ERR_INVALID, "tables not initialised (ks_init_tables)");
+    if (h0) std::memcpy(h0, g_tables.h0.data(), sizeof(double) * VOIGT_N);
+    if (h1) std::memcpy(h1, g_tables.h1.data(), sizeof(double) * VOIGT_N);
+    if (h2) std::memcpy(h2, g_tables.h2.data(), sizeof(double) * VOIGT_N);
+    if (extab) std::memcpy(extab, g_tables.extab.data(), sizeof(double) * EXP_N);
+    if (extabf) std::memcpy(extabf, g_tables.extabf.data(), sizeof(double) * EXP_N);
+    return KS_OK;
+}
+
+template <typename T>
+static cudaError_t sym_addr(const T& sym, const void** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, sym);
+    *out = p;
+    return e;
+}
+
+// Ensures the current device holds the tables; the first call on a device
+// uploads them (synchronously), so it must come before any stream capture.
+static ks_status device_tables(DevTables* out) {
+    int dev = 0;
+    KS_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(KS_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_tables_mu);
+    if (!g_tables.ready) return fail(KS_ERR_INVALID, "tables not initialised (ks_init_tables)");
+    if (!g_dev_ready[dev]) {
+        const HostTables& t = g_tables;
+        std::vector<float> f0(VOIGT_N), f1(VOIGT_N), f2(VOIGT_N), ef(EXP_N), eff(EXP_N);
+        for (int i = 0; i < VOIGT_N; i++) {
+            f0[i] = (float)t.h0[i];
+            f1[i] = (float)t.h1[i];
+            f2[i] = (float)t.h2[i];
+        }
+        for (int i = 0; i < EXP_N; i++) {
+            ef[i] = (float)t.extab[i];
+            eff[i] = (float)t.extabf[i];
+        }
+        KS_CUDA(cudaMemcpyToSymbol(g_h0d, t.h0.data(), sizeof(double) * VOIGT_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_h1d, t.h1.data(), sizeof(double) * VOIGT_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_h2d, t.h2.data(), sizeof(double) * VOIGT_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_h0f, f0.data(), sizeof(float) * VOIGT_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_h1f, f1.data(), sizeof(float) * VOIGT_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_h2f, f2.data(), sizeof(float) * VOIGT_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_extab, t.extab.data(), sizeof(double) * EXP_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_extabf, t.extabf.data(), sizeof(double) * EXP_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_extab_f, ef.data(), sizeof(float) * EXP_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_extabf_f, eff.data(), sizeof(float) * EXP_N));
+        KS_CUDA(cudaMemcpyToSymbol(g_xtau, t.xtau.data(), sizeof(double) * NXTAU));
+        KS_CUDA(cudaMemcpyToSymbol(g_ch, t.ch.data(), sizeof(double) * NXTAU));
+        DevTables d;
+        const void* p;
+        KS_CUDA(sym_addr(g_h0d, &p)); d.h0d = (const double*)p;
+        KS_CUDA(sym_addr(g_h1d, &p)); d.h1d = (const double*)p;
+        KS_CUDA(sym_addr(g_h2d, &p)); d.h2d = (const double*)p;
+        KS_CUDA(sym_addr(g_h0f, &p)); d.h0f = (const float*)p;
+        KS_CUDA(sym_addr(g_h1f, &p)); d.h1f = (const float*)p;
+        KS_CUDA(sym_addr(g_h2f, &p)); d.h2f = (const float*)p;
+        KS_CUDA(sym_addr(g_extab, &p)); d.extab = (const double*)p;
+        KS_CUDA(sym_addr(g_extabf, &p)); d.extabf = (const double*)p;
+        KS_CUDA(sym_addr(g_extab_f, &p)); d.extab_f = (const float*)p;
+        KS_CUDA(sym_addr(g_extabf_f, &p)); d.extabf_f = (const float*)p;
+        KS_CUDA(sym_addr(g_xtau, &p)); d.xtau = (const double*)p;
+        KS_CUDA(sym_addr(g_ch, &p)); d.ch = (const double*)p;
+        g_dev[dev] = d;
+        g_dev_ready[dev] = true;
+    }
+    *out = g_dev[dev];
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host grid
+// ---------------------------------------------------------------------------
+
+extern "C" int64_t ks_wavelength_grid(double start, double end, double resolution, double* out,
+                                      int64_t cap) {
+    if (!(resolution > 0.0) || !(start > 0.0)) {
+        g_last_error = "ks_wavelength_grid: resolution and start must be positive";
+        return -1;
+    }
+    double ratio = 1.0 + 1.0 / resolution;
+    double rlog = std::log(ratio);
+    double ix_floor = std::floor(std::log(start) / rlog);
+    if (std::exp(ix_floor * rlog) < start) ix_floor += 1.0;
+    double wl = std::exp(ix_floor * rlog);
+    int64_t n = 0;
+    const double stop = end * (1.0 + 1e-9);
+    while (wl <= stop) {
+        if (out && n < cap) out[n] = wl;
+        n++;
+        wl *= ratio;
+    }
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// precision-independent kernels
+// ---------------------------------------------------------------------------
+
+// Grid scalars (opacity.py:570-574; line_opacity.py:235-239 RESOLU and
+// :1035-1058 WBEGIN / grid offset of the wing bins).
+__global__ void grid_params_kernel(const double* g, int64_t n, double grid_origin, GridPar* gp) {
+    GridPar p;
+    p.resolu = 300000.0;
+    p.ratiolg = 0.0;
+    p.ix_start = 0;
+    p.wbegin = 1.0;
+    p.grid_offset = 0;
+    p.first = n > 0 ? g[0] : 0.0;
+    p.last = n > 0 ? g[n - 1] : 0.0;
+    if (n > 1) {
+        double ratio = g[1] / g[0];
+        if (ratio > 1.0) p.resolu = 1.0 / (ratio - 1.0);
+        p.ratiolg = log(ratio);
+        p.ix_start = (int64_t)(log(g[0]) / p.ratiolg + 0.5);
+        double ix_floor = floor(log(grid_origin) / p.ratiolg);
+        double wb = exp(ix_floor * p.ratiolg);
+        if (wb < grid_origin) {
+            ix_floor += 1.0;
+            wb = exp(ix_floor * p.ratiolg);
+        }
+        p.wbegin = wb;
+        p.grid_offset = (int64_t)rint(log(g[0] / wb) / p.ratiolg);
+    }
+    *gp = p;
+}
+
+// Centre bins (opacity.py:550-592) and wing bins (line_opacity.py:1030-1059)
+// per line, plus the single-precision line copies of the mixed path.  Flags
+// non-monotone wing bins (the accumulation searches them).
+__global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __restrict__ wl,
+                                 const GridPar* __restrict__ gpp, int32_t* center_out,
+                                 int32_t* wing_out, const double* cgf, const double* elo,
+                                 const double* gr, const double* gs, const double* gw,
+                                 const double* gf, LineF* linef, int* flags) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_lines) return;
+    const GridPar gp = *gpp;
+    double w = wl[i];
+    int64_t c = 0, wb = 0;
+    if (n_wl >= 2) {
+        c = (int64_t)(log(w) / gp.ratiolg + 0.5) - gp.ix_start;
+        if (w < gp.first) c = -1;
+        if (w > gp.last) c = n_wl;
+        wb = (int64_t)rint(log(w / gp.wbegin) / gp.ratiolg) - gp.grid_offset;
+        if (i > 0) {
+            double wp = wl[i - 1];
+            int64_t wbp = (int64_t)rint(log(wp / gp.wbegin) / gp.ratiolg) - gp.grid_offset;
+            if (wbp > wb) atomicOr(flags, 8);
+        }
+    }
+    if (center_out) center_out[i] = (int32_t)c;
+    if (wing_out) wing_out[i] = (int32_t)wb;
+    if (linef) {
+        LineF f;
+        f.cgf = (float)cgf[i];
+        f.elo_hi = (float)elo[i];
+        f.elo_lo = (float)(elo[i] - (double)f.elo_hi);
+        f.gr = (float)gr[i];
+        f.gs = (float)gs[i];
+        f.gw = (float)gw[i];
+        f.gf = (float)gf[i];
+        f.pad = 0.f;
+        linef[i] = f;
+    }
+}
+
+// ---- deterministic stable partition of the pairs by reach class ----
+// Each depth's lines are cut into chunks of kChunk; counts per (depth,
+// chunk, class), an exclusive scan per (depth, class) over chunks, then a
+// scatter that keeps line order inside every class (warp ballots give each
+// lane its rank among equal classes).
+static const int kChunk = 4096;
+static const int kPartThreads = 256;
+
+__global__ void class_count_kernel(const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
+                                   int32_t* __restrict__ counts) {
+    __shared__ int c[N_REACH_CLASSES];
+    int d = blockIdx.y, ch = blockIdx.x;
+    if (threadIdx.x < N_REACH_CLASSES) c[threadIdx.x] = 0;
+    __syncthreads();
+    const uint8_t* base = cls + (int64_t)d * stride + (int64_t)ch * kChunk;
+    for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
+        uint8_t k = base[i];
+        if (k < N_REACH_CLASSES) atomicAdd(&c[k], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < N_REACH_CLASSES)
+        counts[((int64_t)d * nchunks + ch) * N_REACH_CLASSES + threadIdx.x] = c[threadIdx.x];
+}
+
+// One block per depth.  chunk_base[d][ch][k] = absolute start of chunk ch's
+// class-k lines; class_off[d][k] = absolute start of class k.
+__global__ void class_scan_kernel(const int32_t* __restrict__ counts, int nchunks, int64_t stride,
+                                  int64_t* __restrict__ chunk_base, int64_t* __restrict__ class_off,
+                                  unsigned long long* valid_pairs) {
+    __shared__ int64_t tot[N_REACH_CLASSES];
+    __shared__ int64_t off[N_REACH_CLASSES + 1];
+    int d = blockIdx.x;
+    int k = threadIdx.x;
+    const int32_t* cd = counts + (int64_t)d * nchunks * N_REACH_CLASSES;
+    if (k < N_REACH_CLASSES) {
+        int64_t s = 0;
+        for (int ch = 0; ch < nchunks; ch++) s += cd[(int64_t)ch * N_REACH_CLASSES + k];
+        tot[k] = s;
+    }
+    __syncthreads();
+    if (k == 0) {
+        int64_t b = (int64_t)d * stride;
+        for (int q = 0; q < N_REACH_CLASSES; q++) {
+            off[q] = b;
+            b += tot[q];
+        }
+        off[N_REACH_CLASSES] = b;
+        for (int q = 0; q <= N_REACH_CLASSES; q++)
+            class_off[(int64_t)d * (N_REACH_CLASSES + 1) + q] = off[q];
+        if (valid_pairs) atomicAdd(valid_pairs, (unsigned long long)(b - (int64_t)d * stride));
+    }
+    __syncthreads();
+    if (k < N_REACH_CLASSES) {
+        int64_t run = off[k];
+        int64_t* cb = chunk_base + (int64_t)d * nchunks * N_REACH_CLASSES;
+        for (int ch = 0; ch < nchunks; ch++) {
+            cb[(int64_t)ch * N_REACH_CLASSES + k] = run;
+            run += cd[(int64_t)ch * N_REACH_CLASSES + k];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPartThreads) class_scatter_kernel(
+    const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
+    const int64_t* __restrict__ chunk_base, int32_t* __restrict__ class_pos) {
+    constexpr int NW = kPartThreads / 32;
+    constexpr int PER_WARP = kChunk / NW;
+    __shared__ int wcount[NW][N_REACH_CLASSES];
+    __shared__ int64_t wbase[NW][N_REACH_CLASSES];
+    int d = blockIdx.y, ch = blockIdx.x;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint8_t* base = cls + (int64_t)d * stride + (int64_t)ch * kChunk + warp * PER_WARP;
+    if (lane < N_REACH_CLASSES) wcount[warp][lane] = 0;
+    __syncwarp();
+    for (int r = 0; r < PER_WARP; r += 32) {
+        uint8_t k = base[r + lane];
+        unsigned peers = __match_any_sync(0xffffffffu, (int)k);
+        if (k < N_REACH_CLASSES && (peers & ((1u << lane) - 1)) == 0)
+            wcount[warp][k] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    if (threadIdx.x < N_REACH_CLASSES) {
+        int k = threadIdx.x;
+        int64_t run = chunk_base[((int64_t)d * nchunks + ch) * N_REACH_CLASSES + k];
+        for (int w = 0; w < NW; w++) {
+            wbase[w][k] = run;
+            run += wcount[w][k];
+        }
+    }
+    __syncthreads();
+    int64_t line0 = (int64_t)ch * kChunk + warp * PER_WARP;
+    for (int r = 0; r < PER_WARP; r += 32) {
+        uint8_t k = base[r + lane];
+        unsigned peers = __match_any_sync(0xffffffffu, (int)k);
+        int rank = __popc(peers & ((1u << lane) - 1));
+        if (k < N_REACH_CLASSES) class_pos[wbase[warp][k] + rank] = (int32_t)(line0 + r + lane);
+        __syncwarp();
+        if (k < N_REACH_CLASSES && rank == 0) wbase[warp][k] += __popc(peers);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// workspace
+// ---------------------------------------------------------------------------
+
+struct Carve {
+    char* base;
+    size_t cap, used;
+    bool dry;
+    template <typename T>
+    T* take(size_t count) {
+        size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        T* p = dry ? nullptr : reinterpret_cast<T*>(base + used);
+        used += bytes;
+        return p;
+    }
+};
+
+struct Workspace {
+    GridPar* gp;
+    DepthPar* depth;
+    IonPar* ion;
+    LineF* linef;
+    int32_t *center, *wing;
+    void *cont_abs, *cont_scat, *asynth, *desc;
+    uint8_t* cls;
+    int32_t* counts;
+    int64_t *chunk_base, *class_off;
+    int32_t* class_pos;
+    unsigned long long* counters;  // [0] valid pairs, [1] evaluations
+    int32_t* iters;
+    int* flags;
+    int64_t stride;
+    int nchunks;
+};
+
+static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl, int n_ion,
+                   int n_elem, bool fp64, bool need_cont, bool need_asynth) {
+    size_t rs = fp64 ? 8 : 4;
+    w.stride = ((n_lines + kChunk - 1) / kChunk) * kChunk;
+    if (w.stride == 0) w.stride = kChunk;
+    w.nchunks = (int)(w.stride / kChunk);
+    w.gp = c.take<GridPar>(1);
+    w.depth = c.take<DepthPar>(L);
+    w.ion = c.take<IonPar>((size_t)L * n_ion * n_elem);
+    w.linef = c.take<LineF>(n_lines > 0 ? n_lines : 1);
+    w.center = c.take<int32_t>(n_lines > 0 ? n_lines : 1);
+    w.wing = c.take<int32_t>(n_lines > 0 ? n_lines : 1);
+    w.cont_abs = need_cont ? (void*)c.take<char>(rs * L * n_wl) : nullptr;
+    w.cont_scat = need_cont ? (void*)c.take<char>(rs * L * n_wl) : nullptr;
+    w.asynth = need_asynth ? (void*)c.take<char>(rs * L * n_wl) : nullptr;
+    w.desc = (void*)c.take<char>((fp64 ? sizeof(PairDesc<double>) : sizeof(PairDesc<float>)) *
+                                 (size_t)L * w.stride);
+    w.cls = c.take<uint8_t>((size_t)L * w.stride);
+    w.counts = c.take<int32_t>((size_t)L * w.nchunks * N_REACH_CLASSES);
+    w.chunk_base = c.take<int64_t>((size_t)L * w.nchunks * N_REACH_CLASSES);
+    w.class_off = c.take<int64_t>((size_t)L * (N_REACH_CLASSES + 1));
+    w.class_pos = c.take<int32_t>((size_t)L * w.stride);
+    w.counters = c.take<unsigned long long>(4);
+    w.iters = c.take<int32_t>(2 * (size_t)(n_wl > 0 ? n_wl : 1));
+    w.flags = c.take<int>(1);
+}
+
+extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_t n_wavelengths,
+                                       const ks_options* opt, size_t* bytes) {
+    if (!bytes || n_lines < 0 || n_layers <= 0 || n_wavelengths < 0)
+        return fail(KS_ERR_INVALID, "ks_workspace_size: invalid sizes");
+    bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    Carve c{nullptr, 0, 0, true};
+    Workspace w;
+    layout(c, w, n_lines, n_layers, n_wavelengths, 6, 139, fp64, true, true);
+    *bytes = c.used + 256;
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// argument checks
+// ---------------------------------------------------------------------------
+
+static ks_status check_atmos(const ks_atmos* a) {
+    if (!a) return fail(KS_ERR_INVALID, "atmosphere is NULL");
+    if (a->n_layers <= 0) return fail(KS_ERR_INVALID, "atmosphere has no layers");
+    if (a->n_layers > MAX_LAYERS)
+        return fail(KS_ERR_UNSUPPORTED, "atmosphere has more than 128 layers");
+    if (!a->rhox || !a->temperature || !a->electron_density || !a->mass_density || !a->hckt ||
+        !a->population || !a->doppler)
+        return fail(KS_ERR_INVALID, "atmosphere: required depth array is NULL");
+    if (a->n_ion <= 0 || a->n_elem <= 0) return fail(KS_ERR_INVALID, "atmosphere: bad population shape");
+    return KS_OK;
+}
+
+static ks_status check_cont(const ks_atmos* a) {
+    if (!a->wledge || !a->cont_abs_coeff || !a->cont_scat_coeff || a->n_edge < 2)
+        return fail(KS_ERR_INVALID,
+                    "continuum coefficients are missing (wledge, cont_abs_coeff, cont_scat_coeff)");
+    return KS_OK;
+}
+
+static ks_status check_grid(const ks_grid* g) {
+    if (!g || !g->wavelength) return fail(KS_ERR_INVALID, "grid is NULL");
+    if (g->n < 1) return fail(KS_ERR_INVALID, "grid is empty");
+    if (g->n > 0x7fffffffLL) return fail(KS_ERR_UNSUPPORTED, "grid larger than 2^31 points");
+    return KS_OK;
+}
+
+static ks_status check_lines(const ks_lines* l) {
+    if (!l) return fail(KS_ERR_INVALID, "lines is NULL");
+    if (l->n_lines < 0) return fail(KS_ERR_INVALID, "negative line count");
+    if (l->n_lines == 0) return KS_OK;
+    if (!l->wavelength || !l->gf || !l->cgf || !l->gamma_rad || !l->gamma_stark || !l->gamma_vdw ||
+        !l->elo_cm || !l->element_idx || !l->ion_stage || !l->line_type || !l->process_mask ||
+        !l->asynth_mask)
+        return fail(KS_ERR_INVALID, "lines: a required column is NULL");
+    if (!l->sorted_by_wavelength)
+        return fail(KS_ERR_INVALID, "lines must be sorted by wavelength (sorted_by_wavelength = 1)");
+    if (l->n_lines > 0x7fffffffLL) return fail(KS_ERR_UNSUPPORTED, "more than 2^31 lines");
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pipeline pieces
+// ---------------------------------------------------------------------------
+
+static PrepArgs prep_args(const ks_atmos* atm, const ks_options* opt, const Workspace& w) {
+    PrepArgs p;
+    p.n_layers = atm->n_layers;
+    p.n_ion = atm->n_ion;
+    p.n_elem = atm->n_elem;
+    p.rhox = atm->rhox;
+    p.temperature = atm->temperature;
+    p.electron_density = atm->electron_density;
+    p.mass_density = atm->mass_density;
+    p.hckt = atm->hckt;
+    p.xnf_h = atm->xnf_h;
+    p.xnf_he1 = atm->xnf_he1;
+    p.xnf_h2 = atm->xnf_h2;
+    p.population = atm->population;
+    p.doppler = atm->doppler;
+    p.microturb_kms = opt ? opt->microturb_kms : 0.0;
+    p.rhoxj = opt ? opt->rhoxj : 0.0;
+    p.gp = w.gp;
+    p.depth = w.depth;
+    p.ion = w.ion;
+    return p;
+}
+
+static ContArgs cont_args(const ks_atmos* atm, const ks_grid* g) {
+    ContArgs c;
+    c.n_layers = atm->n_layers;
+    c.n_edge = atm->n_edge;
+    c.coeff_log10 = atm->coeff_log10;
+    c.n = g->n;
+    c.grid = g->wavelength;
+    c.wledge = atm->wledge;
+    c.half_edge = atm->half_edge;
+    c.delta_edge = atm->delta_edge;
+    c.abs_coeff = atm->cont_abs_coeff;
+    c.scat_coeff = atm->cont_scat_coeff;
+    return c;
+}
+
+static PairArgs pair_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g,
+                          const ks_options* opt, const Workspace& w, const DevTables& t) {
+    PairArgs p;
+    std::memset(&p, 0, sizeof(p));
+    p.n_lines = l->n_lines;
+    p.n_wl = g->n;
+    p.stride = w.stride;
+    p.n_layers = atm->n_layers;
+    p.n_ion = atm->n_ion;
+    p.n_elem = atm->n_elem;
+    p.cutoff = opt ? opt->cutoff : 1e-3;
+    p.gp = w.gp;
+    p.wavelength = l->wavelength;
+    p.gf = l->gf;
+    p.cgf = l->cgf;
+    p.gamma_rad = l->gamma_rad;
+    p.gamma_stark = l->gamma_stark;
+    p.gamma_vdw = l->gamma_vdw;
+    p.elo_cm = l->elo_cm;
+    p.element_idx = l->element_idx;
+    p.ion_stage = l->ion_stage;
+    p.line_type = l->line_type;
+    p.process_mask = l->process_mask;
+    p.asynth_mask = l->asynth_mask;
+    p.center_idx = w.center;
+    p.wing_idx = w.wing;
+    p.linef = w.linef;
+    p.depth = w.depth;
+    p.ion = w.ion;
+    p.extab = t.extab;
+    p.extabf = t.extabf;
+    p.extab_f = t.extab_f;
+    p.extabf_f = t.extabf_f;
+    p.h0d = t.h0d;
+    p.h1d = t.h1d;
+    p.h2d = t.h2d;
+    p.h0f = t.h0f;
+    p.h1f = t.h1f;
+    p.h2f = t.h2f;
+    p.flags = w.flags;
+    return p;
+}
+
+static ks_status run_bins(const ks_lines* l, const ks_grid* g, const Workspace& w, bool mixed,
+                          cudaStream_t s) {
+    grid_params_kernel<<<1, 1, 0, s>>>(g->wavelength, g->n, g->grid_origin, w.gp);
+    KS_CUDA(cudaGetLastError());
+    if (l && l->n_lines > 0) {
+        line_bins_kernel<<<(unsigned)((l->n_lines + 255) / 256), 256, 0, s>>>(
+            l->n_lines, g->n, l->wavelength, w.gp, w.center, w.wing, l->cgf, l->elo_cm,
+            l->gamma_rad, l->gamma_stark, l->gamma_vdw, l->gf, mixed ? w.linef : nullptr, w.flags);
+        KS_CUDA(cudaGetLastError());
+    }
+    return KS_OK;
+}
+
+static ks_status run_partition(const Workspace& w, int L, cudaStream_t s) {
+    dim3 grid(w.nchunks, L);
+    class_count_kernel<<<grid, kPartThreads, 0, s>>>(w.cls, w.stride, w.nchunks, w.counts);
+    KS_CUDA(cudaGetLastError());
+    class_scan_kernel<<<L, 32, 0, s>>>(w.counts, w.nchunks, w.stride, w.chunk_base, w.class_off,
+                                       w.counters);
+    KS_CUDA(cudaGetLastError());
+    class_scatter_kernel<<<grid, kPartThreads, 0, s>>>(w.cls, w.stride, w.nchunks, w.chunk_base,
+                                                       w.class_pos);
+    KS_CUDA(cudaGetLastError());
+    return KS_OK;
+}
+
+static int default_tile(const ks_options* opt, bool fp64) {
+    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : (fp64 ? 512 : 1024);
+    return t;
+}
+static int default_warps(const ks_options* opt) {
+    return opt && opt->warps_per_tile > 0 ? opt->warps_per_tile : 8;
+}
+
+static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g,
+                        const ks_options* opt, const Workspace& w, const DevTables& t, bool fp64) {
+    AccArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n_lines = l->n_lines;
+    a.n_wl = g->n;
+    a.stride = w.stride;
+    a.n_layers = atm->n_layers;
+    a.tile_bins = default_tile(opt, fp64);
+    a.grid = g->wavelength;
+    a.wing_idx = w.wing;
+    a.class_pos = w.class_pos;
+    a.class_off = w.class_off;
+    a.depth = w.depth;
+    a.h0d = t.h0d;
+    a.h1d = t.h1d;
+    a.h2d = t.h2d;
+    a.h0f = t.h0f;
+    a.h1f = t.h1f;
+    a.h2f = t.h2f;
+    a.evals = w.counters + 1;
+    return a;
+}
+
+static TransferArgs transfer_args(const ks_atmos* atm, const ks_grid* g, const Workspace& w,
+                                  const DevTables& t, double* ft, double* fc, bool asynth_mode,
+                                  bool fp64) {
+    TransferArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = g->n;
+    a.n_layers = atm->n_layers;
+    a.asynth_mode = asynth_mode ? 1 : 0;
+    a.slinec_mode = fp64 ? 1 : 0;
+    a.grid = g->wavelength;
+    a.depth = w.depth;
+    a.xtau = t.xtau;
+    a.ch = t.ch;
+    a.flux_total = ft;
+    a.flux_cont = fc;
+    a.iters = w.iters;
+    return a;
+}
+
+static ks_status collect_stats(const Workspace& w, int64_t n_wl, ks_stats* stats, cudaStream_t s) {
+    unsigned long long ctr[2];
+    int flags = 0;
+    KS_CUDA(cudaMemcpyAsync(ctr, w.counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+    KS_CUDA(cudaMemcpyAsync(&flags, w.flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+    std::vector<int32_t> it(2 * (size_t)n_wl);
+    if (n_wl > 0)
+        KS_CUDA(cudaMemcpyAsync(it.data(), w.iters, sizeof(int32_t) * 2 * n_wl,
+                                cudaMemcpyDeviceToHost, s));
+    KS_CUDA(cudaStreamSynchronize(s));
+    if (stats) {
+        stats->valid_pairs = (int64_t)ctr[0];
+        stats->evaluations = (int64_t)ctr[1];
+        int64_t maxj = 0, iters = 0;
+        for (int64_t j = 0; j < n_wl; j++) {
+            int32_t v = it[2 * j + 1];
+            if (v < 0) maxj++;
+            iters += (v < 0 ? -v : v) + (it[2 * j] < 0 ? -it[2 * j] : it[2 * j]);
+        }
+        stats->maxj_wavelengths = maxj;
+        stats->iterations = iters;
+        stats->device_flags = flags;
+    }
+    if (flags & 8) return fail(KS_ERR_DEVICE, "wing bins are not monotone in the line order");
+    if (flags & FLAG_N10DOP_RANGE)
+        return fail(KS_ERR_DEVICE, "a pair exceeded a packed descriptor field (N10DOP or centre offset)");
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// entry points
+// ---------------------------------------------------------------------------
+
+extern "C" ks_status ks_line_bins(const ks_grid* grid, const double* wavelength, int64_t n_lines,
+                                  int32_t* center_out, int32_t* wing_out, void* stream) {
+    ks_status st = check_grid(grid);
+    if (st) return st;
+    if (n_lines < 0 || (n_lines > 0 && !wavelength)) return fail(KS_ERR_INVALID, "ks_line_bins: bad lines");
+    cudaStream_t s = (cudaStream_t)stream;
+    GridPar* gp = nullptr;
+    int* flags = nullptr;
+    KS_CUDA(cudaMallocAsync((void**)&gp, sizeof(GridPar) + 256, s));
+    flags = reinterpret_cast<int*>(reinterpret_cast<char*>(gp) + sizeof(GridPar) + 64);
+    KS_CUDA(cudaMemsetAsync(flags, 0, sizeof(int), s));
+    grid_params_kernel<<<1, 1, 0, s>>>(grid->wavelength, grid->n, grid->grid_origin, gp);
+    KS_CUDA(cudaGetLastError());
+    if (n_lines > 0) {
+        line_bins_kernel<<<(unsigned)((n_lines + 255) / 256), 256, 0, s>>>(
+            n_lines, grid->n, wavelength, gp, center_out, wing_out, nullptr, nullptr, nullptr,
+            nullptr, nullptr, nullptr, nullptr, flags);
+        KS_CUDA(cudaGetLastError());
+    }
+    KS_CUDA(cudaFreeAsync(gp, s));
+    return KS_OK;
+}
+
+extern "C" ks_status ks_continuum(const ks_atmos* atm, const ks_grid* grid, int32_t precision,
+                                  void* cont_abs, void* cont_scat, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_cont(atm);
+    if (st) return st;
+    if (!cont_abs || !cont_scat) return fail(KS_ERR_INVALID, "ks_continuum: NULL output");
+    cudaStream_t s = (cudaStream_t)stream;
+    ContArgs c = cont_args(atm, grid);
+    if (precision == KS_PREC_FP64) KS_CUDA(launch_continuum_f64(c, (double*)cont_abs, (double*)cont_scat, s));
+    else KS_CUDA(launch_continuum_f32(c, (float*)cont_abs, (float*)cont_scat, s));
+    return KS_OK;
+}
+
+extern "C" ks_status ks_transp(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                               const ks_options* opt, const double* cont_kapmin, double* transp_out,
+                               uint8_t* valid_out, int32_t* center_out, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_lines(lines);
+    if (st) return st;
+    if (!cont_kapmin || (lines->n_lines > 0 && (!transp_out || !valid_out)))
+        return fail(KS_ERR_INVALID, "ks_transp: NULL input/output");
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false);
+    char* buf = nullptr;
+    KS_CUDA(cudaMallocAsync((void**)&buf, dry.used + 256, s));
+    Carve c{buf, dry.used + 256, 0, false};
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false);
+    KS_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int), s));
+    PrepArgs pa = prep_args(atm, opt, w);
+    if ((st = run_bins(lines, grid, w, false, s))) return st;
+    KS_CUDA(launch_prep_f64(pa, s));
+    PairArgs p = pair_args(lines, atm, grid, opt, w, t);
+    p.transp_out = transp_out;
+    p.valid_out = valid_out;
+    KS_CUDA(launch_pair_setup_f64(p, true, cont_kapmin, nullptr, (PairDesc<double>*)w.desc, w.cls, s));
+    if (center_out && lines->n_lines > 0)
+        KS_CUDA(cudaMemcpyAsync(center_out, w.center, sizeof(int32_t) * lines->n_lines,
+                                cudaMemcpyDeviceToDevice, s));
+    KS_CUDA(cudaFreeAsync(buf, s));
+    return KS_OK;
+}
+
+extern "C" ks_status ks_asynth(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                               const ks_options* opt, const double* transp, const uint8_t* valid,
+                               const double* cont_kapmin, void* workspace, size_t workspace_bytes,
+                               double* asynth_out, ks_stats* stats, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_lines(lines);
+    if (st) return st;
+    if (!cont_kapmin || !asynth_out || (lines->n_lines > 0 && (!transp || !valid)))
+        return fail(KS_ERR_INVALID, "ks_asynth: NULL input/output");
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false);
+    if (!workspace || workspace_bytes < dry.used)
+        return fail(KS_ERR_NOMEM, "ks_asynth: workspace too small (see ks_workspace_size)");
+    Carve c{(char*)workspace, workspace_bytes, 0, false};
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false);
+    KS_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int), s));
+    KS_CUDA(cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned long long), s));
+    KS_CUDA(cudaMemsetAsync(w.cls, 0xff, (size_t)atm->n_layers * w.stride, s));
+    if ((st = run_bins(lines, grid, w, false, s))) return st;
+    KS_CUDA(launch_prep_f64(prep_args(atm, opt, w), s));
+    PairArgs p = pair_args(lines, atm, grid, opt, w, t);
+    p.transp_in = transp;
+    p.valid_in = valid;
+    KS_CUDA(launch_pair_setup_f64(p, false, cont_kapmin, nullptr, (PairDesc<double>*)w.desc, w.cls, s));
+    if ((st = run_partition(w, atm->n_layers, s))) return st;
+    AccArgs a = acc_args(lines, atm, grid, opt, w, t, true);
+    KS_CUDA(launch_accumulate_f64(a, default_warps(opt), (const PairDesc<double>*)w.desc, asynth_out, s));
+    if (stats) return collect_stats(w, 0, stats, s);
+    return KS_OK;
+}
+
+extern "C" ks_status ks_formal_solution(const ks_atmos* atm, const ks_grid* grid, int32_t precision,
+                                        const void* cont_abs, const void* cont_scat,
+                                        const void* line_opacity, const void* line_scattering,
+                                        const void* line_source, double* flux_total,
+                                        double* flux_cont, ks_stats* stats, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (st) return st;
+    if (!cont_abs || !cont_scat || !line_opacity || !flux_total || !flux_cont)
+        return fail(KS_ERR_INVALID, "ks_formal_solution: NULL input/output");
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    bool fp64 = precision == KS_PREC_FP64;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, 0, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, false, false);
+    char* buf = nullptr;
+    KS_CUDA(cudaMallocAsync((void**)&buf, dry.used + 256, s));
+    Carve c{buf, dry.used + 256, 0, false};
+    layout(c, w, 0, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, false, false);
+    KS_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int), s));
+    KS_CUDA(cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned long long), s));
+    if ((st = run_bins(nullptr, grid, w, false, s))) return st;
+    KS_CUDA(fp64 ? launch_prep_f64(prep_args(atm, nullptr, w), s) : launch_prep_f32(prep_args(atm, nullptr, w), s));
+    TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, false, fp64);
+    ta.slinec_mode = 0;
+    if (fp64)
+        KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, (const double*)cont_abs, (const double*)cont_scat,
+                                    (const double*)line_opacity, (const double*)line_scattering,
+                                    (const double*)line_source, s));
+    else
+        KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, (const float*)cont_abs, (const float*)cont_scat,
+                                    (const float*)line_opacity, (const float*)line_scattering,
+                                    (const float*)line_source, s));
+    if (stats) {
+        st = collect_stats(w, grid->n, stats, s);
+        cudaFreeAsync(buf, s);
+        return st;
+    }
+    KS_CUDA(cudaFreeAsync(buf, s));
+    return KS_OK;
+}
+
+template <typename R>
+static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                                 const ks_options* opt, Workspace& w, const DevTables& t,
+                                 double* flux_total, double* flux_cont, R* asynth,
+                                 cudaStream_t s) {
+    constexpr bool fp64 = sizeof(R) == 8;
+    ks_status st;
+    const int L = atm->n_layers;
+    KS_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int), s));
+    KS_CUDA(cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned long long), s));
+    KS_CUDA(cudaMemsetAsync(w.cls, 0xff, (size_t)L * w.stride, s));
+    if ((st = run_bins(lines, grid, w, !fp64, s))) return st;
+    PrepArgs pa = prep_args(atm, opt, w);
+    ContArgs ca = cont_args(atm, grid);
+    R* cabs = (R*)w.cont_abs;
+    R* cscat = (R*)w.cont_scat;
+    if constexpr (fp64) {
+        KS_CUDA(launch_prep_f64(pa, s));
+        KS_CUDA(launch_continuum_f64(ca, cabs, cscat, s));
+    } else {
+        KS_CUDA(launch_prep_f32(pa, s));
+        KS_CUDA(launch_continuum_f32(ca, cabs, cscat, s));
+    }
+    if (lines->n_lines > 0) {
+        PairArgs p = pair_args(lines, atm, grid, opt, w, t);
+        if constexpr (fp64)
+            KS_CUDA(launch_pair_setup_f64(p, true, cabs, cscat, (PairDesc<double>*)w.desc, w.cls, s));
+        else
+            KS_CUDA(launch_pair_setup_f32(p, true, cabs, cscat, (PairDesc<float>*)w.desc, w.cls, s));
+        if ((st = run_partition(w, L, s))) return st;
+    } else {
+        // no lines: every class list is empty
+        KS_CUDA(cudaMemsetAsync(w.class_off, 0, sizeof(int64_t) * L * (N_REACH_CLASSES + 1), s));
+    }
+    AccArgs a = acc_args(lines, atm, grid, opt, w, t, fp64);
+    int warps = default_warps(opt);
+    if constexpr (fp64)
+        KS_CUDA(launch_accumulate_f64(a, warps, (const PairDesc<double>*)w.desc, asynth, s));
+    else
+        KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
+    TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, true, fp64);
+    if constexpr (fp64)
+        KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
+    else
+        KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
+    return KS_OK;
+}
+
+extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                                   const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                   double* flux_total, double* flux_cont, void* asynth_out,
+                                   ks_stats* stats, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_lines(lines);
+    if (!st) st = check_cont(atm);
+    if (st) return st;
+    if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize: NULL flux output");
+    if (opt && (opt->tile_bins < 0 || opt->tile_bins > 8192 || (opt->tile_bins % 32) != 0))
+        return fail(KS_ERR_INVALID, "tile_bins must be a multiple of 32 in [32, 8192] (0 = default)");
+    if (opt && (opt->warps_per_tile < 0 || opt->warps_per_tile > 16))
+        return fail(KS_ERR_INVALID, "warps_per_tile must be in [1, 16] (0 = default)");
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    bool need_asynth = asynth_out == nullptr;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    if (!workspace || workspace_bytes < dry.used)
+        return fail(KS_ERR_NOMEM, "ks_synthesize: workspace too small (see ks_workspace_size)");
+    Carve c{(char*)workspace, workspace_bytes, 0, false};
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    void* asy = asynth_out ? asynth_out : w.asynth;
+    if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s);
+    else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s);
+    if (st) return st;
+    if (stats) return collect_stats(w, grid->n, stats, s);
+    return KS_OK;
+}

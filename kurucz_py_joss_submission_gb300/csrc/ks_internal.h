@@ -1,0 +1,123 @@
+// ks_internal.h -- argument records shared by the host API and the kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace ks {
+
+// Scalars derived from the wavelength grid (opacity.py:570-574,
+// line_opacity.py:1035-1058, :235-239), computed on the device.
+struct GridPar {
+    double ratiolg, wbegin, resolu, first, last;
+    int64_t ix_start, grid_offset;
+};
+
+// Per-depth state (populations.py:160-204, line_opacity.py:1009-1016,
+// radiative.py:33, opacity.py:2408-2414).
+struct DepthPar {
+    double rho, xne, txnxn, hckt, hkt, hkt_asynth, temperature, rhox, fscat;
+    float hckt_hi, hckt_lo, xne_f, txnxn_f;
+};
+
+// Per (depth, ion, element) entry.
+struct IonPar {
+    double pop, dop, dop_transp, xnfdop, dvoigt;
+    float xnfdop_f, dop_f, dvoigt_f, pop_over_rho_f;
+    int n10dop, pad;
+};
+
+// Per-line single-precision copies for the mixed path.
+struct LineF {
+    float cgf, elo_hi, elo_lo, gr, gs, gw, gf, pad;
+};
+
+// Wing descriptor of one valid (line, depth) pair.
+//   ctr_n10:     bits 0-3 centre-add code (0 none, else centre bin = wing_c +
+//                code - 8), bits 8-31 N10DOP
+//   maxstep_far: bits 0-30 MAXSTEP, bit 31 set when the far wing is used
+template <typename R>
+struct __align__(sizeof(R) == 4 ? 32 : 64) PairDesc {
+    R kappa0, adamp, dvoigt, xfar, kapcen;
+    int wing_c, maxstep_far, ctr_n10;
+};
+
+struct PrepArgs {
+    int n_layers, n_ion, n_elem;
+    const double *rhox, *temperature, *electron_density, *mass_density, *hckt;
+    const double *xnf_h, *xnf_he1, *xnf_h2, *population, *doppler;
+    double microturb_kms, rhoxj;
+    const GridPar *gp;
+    DepthPar *depth;
+    IonPar *ion;
+};
+
+struct ContArgs {
+    int n_layers, n_edge, coeff_log10;
+    int64_t n;
+    const double *grid, *wledge, *half_edge, *delta_edge, *abs_coeff, *scat_coeff;
+};
+
+struct LineBinArgs {
+    int64_t n_lines, n_wl;
+    const double *grid, *wavelength;
+    double grid_origin;
+    int32_t *center_out, *wing_out;
+    // optional mixed-path per-line copies
+    const double *cgf, *elo, *gr, *gs, *gw, *gf;
+    LineF *linef;
+    int *flags;
+};
+
+struct PairArgs {
+    int64_t n_lines, n_wl, stride;
+    int n_layers, n_ion, n_elem;
+    double cutoff;
+    const GridPar *gp;
+    const double *wavelength, *gf, *cgf, *gamma_rad, *gamma_stark, *gamma_vdw, *elo_cm;
+    const int32_t *element_idx, *ion_stage, *line_type;
+    const uint8_t *process_mask, *asynth_mask;
+    const int32_t *center_idx, *wing_idx;
+    const LineF *linef;
+    const DepthPar *depth;
+    const IonPar *ion;
+    const double *extab, *extabf;
+    const float *extab_f, *extabf_f;
+    const double *h0d, *h1d, *h2d;
+    const float *h0f, *h1f, *h2f;
+    // seam mode inputs (FP64, [n_lines, L])
+    const double *transp_in;
+    const uint8_t *valid_in;
+    // optional TRANSP outputs ([n_lines, L])
+    double *transp_out;
+    uint8_t *valid_out;
+    int *flags;
+};
+
+struct AccArgs {
+    int64_t n_lines, n_wl, stride;
+    int n_layers, tile_bins;
+    const double *grid;
+    const int32_t *wing_idx;
+    const int32_t *class_pos;   // per depth, per class: line positions, ascending
+    const int64_t *class_off;   // [L][N_REACH_CLASSES + 1] absolute offsets into class_pos
+    const DepthPar *depth;
+    const double *h0d, *h1d, *h2d;
+    const float *h0f, *h1f, *h2f;
+    unsigned long long *evals;
+};
+
+struct TransferArgs {
+    int64_t n;
+    int n_layers;
+    int asynth_mode;   // line opacity given as ASYNTH (split by FSCAT here)
+    int slinec_mode;   // source = SLINEC of the driver's frequency (FP64 path)
+    const double *grid;
+    const DepthPar *depth;
+    const double *xtau, *ch;
+    const float *coefj32;
+    double *flux_total, *flux_cont;
+    int32_t *iters;
+};
+
+}  // namespace ks

@@ -1,0 +1,1016 @@
+// ks_kernels.cuh -- the GB300 kernels of the line-opacity and transfer path,
+// templated on the working type R (float: KS_PREC_MIXED, double:
+// KS_PREC_FP64).  Included by ks_f32.cu and ks_f64.cu, which instantiate one
+// type each (the FP64 unit is compiled without multiply-add contraction so
+// its rounding follows the reference's separately rounded operations).
+//
+// Kernels, in pipeline order:
+//   prep_depth_kernel     per-depth state and the (depth, ion, element) table
+//   continuum_kernel      ACONT/SIGMAC on the grid        (continuum.py:73)
+//   pair_setup_kernel     TRANSP gates + wing descriptor  (line_opacity.py:56,1141,416)
+//   accumulate_kernel     ASYNTH on lambda tiles           (line_opacity.py:187,1091,1338)
+//   transfer_kernel       JOSH surface flux per lambda     (radiative.py:42, josh_solver.py:367)
+#pragma once
+
+#include "ks_common.cuh"
+#include "ks_internal.h"
+#include "ks_launch.h"
+
+namespace ks {
+
+// ---------------------------------------------------------------------------
+// per-depth preparation
+// ---------------------------------------------------------------------------
+
+// One thread per (depth, ion, element) entry; entry 0 of each depth also
+// fills the per-depth record.  populations.py:196-204 (TXNXN),
+// line_opacity.py:124-136 (XNFDOP = pop / (rho dop), microturbulence added to
+// DOPPLE for TRANSP only), :416-420 and :465 (N10DOP, DVOIGT from
+// DOPPLE = doppler width / wavelength).
+template <typename R>
+__global__ void prep_depth_kernel(PrepArgs a) {
+    int64_t per_depth = (int64_t)a.n_ion * a.n_elem;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_layers * per_depth) return;
+    int d = (int)(i / per_depth);
+    double temp_raw = a.temperature[d];
+    double rho = a.mass_density[d];
+    if (i % per_depth == 0) {
+        DepthPar p;
+        double temp = temp_raw > 1.0 ? temp_raw : 1.0;
+        double h = a.xnf_h ? a.xnf_h[d] : 0.0;
+        double he = a.xnf_he1 ? a.xnf_he1[d] : 0.0;
+        double h2 = a.xnf_h2 ? a.xnf_h2[d] : 0.0;
+        p.txnxn = (h + 0.42 * he + 0.85 * h2) * pow(temp / 10000.0, 0.3);
+        p.rho = rho;
+        p.xne = a.electron_density[d];
+        p.hckt = a.hckt[d];
+        p.hkt_asynth = H_PLANCK / (K_BOLTZ * temp);
+        p.hkt = H_PLANCK / (K_BOLTZ * temp_raw);
+        p.temperature = temp_raw;
+        p.rhox = a.rhox[d];
+        p.fscat = a.rhoxj > 0.0 ? exp(-p.rhox / a.rhoxj) : 0.0;
+        p.hckt_hi = (float)p.hckt;
+        p.hckt_lo = (float)(p.hckt - (double)p.hckt_hi);
+        p.xne_f = (float)p.xne;
+        p.txnxn_f = (float)p.txnxn;
+        a.depth[d] = p;
+    }
+    double pop = a.population[i];
+    double dop = a.doppler[i];
+    double micro = a.microturb_kms > 0.0 ? a.microturb_kms / C_LIGHT_KM : 0.0;
+    double dop_t = micro > 0.0 ? sqrt(dop * dop + micro * micro) : dop;
+    IonPar q;
+    q.pop = pop;
+    q.dop = dop;
+    q.dop_transp = dop_t;
+    q.xnfdop = (pop > 0.0 && dop_t > 0.0 && rho > 0.0) ? pop / (rho * dop_t) : 0.0;
+    const double resolu = a.gp->resolu;
+    int64_t n10 = dop > 0.0 ? (int64_t)(10.0 * dop * resolu) : 0;
+    q.n10dop = (int)(n10 > 0x7fffffff ? 0x7fffffff : n10);
+    q.dvoigt = dop > 0.0 ? 1.0 / (dop * resolu) : 1.0;
+    q.xnfdop_f = (float)q.xnfdop;
+    q.dop_f = (float)dop_t;
+    q.dvoigt_f = (float)q.dvoigt;
+    q.pop_over_rho_f = rho > 0.0 ? (float)(pop / rho) : 0.0f;
+    q.pad = 0;
+    a.ion[i] = q;
+}
+
+// ---------------------------------------------------------------------------
+// continuum
+// ---------------------------------------------------------------------------
+
+// One thread per wavelength, looping over depths so the edge search and the
+// Lagrange weights are computed once per wavelength.  continuum.py:146-256.
+template <typename R>
+__global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __restrict__ cont_scat) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    double w = a.grid[j];
+    double aw = fabs(w);
+    int lo = 0, hi = a.n_edge;
+    while (lo < hi) {  // searchsorted(|wledge|, |w|, side="right")
+        int mid = (lo + hi) >> 1;
+        if (fabs(a.wledge[mid]) <= aw) lo = mid + 1; else hi = mid;
+    }
+    int e = lo - 1;
+    e = e < 0 ? 0 : (e > a.n_edge - 2 ? a.n_edge - 2 : e);
+    double left = fabs(a.wledge[e]);
+    double right = fabs(a.wledge[e + 1]);
+    double half = a.half_edge ? a.half_edge[e] : 0.5 * (left + right);
+    double delta = a.delta_edge ? a.delta_edge[e] : 0.5 * (right - left) * (right - left);
+    if (delta == 0.0) delta = 1e-20;
+    double c1 = (w - half) * (w - right) / delta;
+    double c2 = (left - w) * (w - right) * 2.0 / delta;
+    double c3 = (w - left) * (w - half) / delta;
+    const int nseg = a.n_edge - 1;
+    for (int d = 0; d < a.n_layers; d++) {
+        const double* ca = a.abs_coeff + ((int64_t)d * nseg + e) * 3;
+        const double* cs = a.scat_coeff + ((int64_t)d * nseg + e) * 3;
+        R la, ls;
+        if (sizeof(R) == 8) {
+            la = (R)(ca[0] * c1 + ca[1] * c2 + ca[2] * c3);
+            ls = (R)(cs[0] * c1 + cs[1] * c2 + cs[2] * c3);
+        } else {
+            float fc1 = (float)c1, fc2 = (float)c2, fc3 = (float)c3;
+            la = (R)((float)ca[0] * fc1 + (float)ca[1] * fc2 + (float)ca[2] * fc3);
+            ls = (R)((float)cs[0] * fc1 + (float)cs[1] * fc2 + (float)cs[2] * fc3);
+        }
+        if (a.coeff_log10) {
+            la = la > R(38) ? R(38) : la;
+            ls = ls > R(38) ? R(38) : ls;
+            if (sizeof(R) == 8) {
+                la = (R)pow(10.0, (double)la);
+                ls = (R)pow(10.0, (double)ls);
+            } else {
+                la = (R)exp10f((float)la);
+                ls = (R)exp10f((float)ls);
+            }
+            const R mx = (R)MAX_OPACITY_REAL4;
+            la = la < R(0) ? R(0) : (la > mx ? mx : la);
+            ls = ls < R(0) ? R(0) : (ls > mx ? mx : ls);
+            if (!isfinite((double)la)) la = mx;
+            if (!isfinite((double)ls)) ls = mx;
+        }
+        cont_abs[(int64_t)d * a.n + j] = la;
+        cont_scat[(int64_t)d * a.n + j] = ls;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair setup: TRANSP gates + wing descriptor
+// ---------------------------------------------------------------------------
+
+// FASTEX (tables.py:29-42): exp(-x) from the EXTAB/EXTABF tables, in FP64.
+__device__ __forceinline__ double fast_ex(double x, const double* __restrict__ extab,
+                                          const double* __restrict__ extabf) {
+    if (x <= 0.0) return x == 0.0 ? 1.0 : exp(-x);
+    double fl = floor(x);
+    if (fl >= (double)EXP_N) return exp(-x);
+    int i = (int)fl;
+    double frac = __dadd_rn(x, -(double)i);
+    int j = (int)__dadd_rn(__dmul_rn(frac, 1000.0), 0.5);
+    j = j < 0 ? 0 : (j > EXP_N - 1 ? EXP_N - 1 : j);
+    return __dmul_rn(extab[i], extabf[j]);
+}
+
+// FASTEX for the mixed path.  The table cell (i, j) must be the one the
+// FP64 reference picks, so x = ELO*HCKT is formed as an unevaluated float
+// sum p + lo (error ~1e-14 relative) and j = int(frac*1000 + 0.5) is taken
+// from it; only when that value lies within 2e-4 of an integer -- where
+// single precision cannot decide -- is the index recomputed in FP64.
+__device__ __forceinline__ float fast_ex_mixed(float e_hi, float e_lo, float h_hi, float h_lo,
+                                               double elo, double hckt,
+                                               const float* __restrict__ extab,
+                                               const float* __restrict__ extabf) {
+    float p = e_hi * h_hi;
+    float perr = fmaf(e_hi, h_hi, -p);
+    float lo = perr + (e_hi * h_lo + e_lo * h_hi);
+    if (!(p > 0.0f)) {
+        double x = elo * hckt;
+        if (x <= 0.0) return x == 0.0 ? 1.0f : (float)exp(-x);
+    }
+    float fi = floorf(p);
+    float r = (p - fi) + lo;
+    if (r < 0.0f) { fi -= 1.0f; r += 1.0f; }
+    else if (r >= 1.0f) { fi += 1.0f; r -= 1.0f; }
+    if (fi >= (float)EXP_N) return __expf(-(p + lo));
+    float t = r * 1000.0f + 0.5f;
+    float tr = rintf(t);
+    int i = (int)fi, j;
+    if (fabsf(t - tr) < 2.0e-4f || fi < 0.0f) {
+        double x = __dmul_rn(elo, hckt);
+        double fl = floor(x);
+        if (fl >= (double)EXP_N) return (float)exp(-x);
+        i = (int)fl;
+        double frac = __dadd_rn(x, -(double)i);
+        j = (int)__dadd_rn(__dmul_rn(frac, 1000.0), 0.5);
+    } else {
+        j = (int)t;
+    }
+    j = j < 0 ? 0 : (j > EXP_N - 1 ? EXP_N - 1 : j);
+    return extab[i] * extabf[j];
+}
+
+// Near-zone wing profile at step `off` (line_opacity.py:474-491, :546-565).
+// The reference carries TABI incrementally; here it is 0.5 + off*tabstep,
+// which equals the incremental sum except when that sum lies within a few
+// ulps of an integer.
+template <typename R>
+__device__ __forceinline__ R near_profile(int off, R dvoigt, R adamp, R kappa0,
+                                          const R* __restrict__ h0, const R* __restrict__ h1,
+                                          const R* __restrict__ h2) {
+    R x = (R)off * dvoigt;
+    if (adamp < R(0.2)) {
+        if (x > R(10)) return kappa0 * (R(0.5642) * adamp / (x * x));
+        R tabi = R(0.5) + (R)off * (R(200) * dvoigt);
+        int idx = (int)tabi;
+        idx = idx < 0 ? 0 : (idx > VOIGT_N - 1 ? VOIGT_N - 1 : idx);
+        return kappa0 * (h0[idx] + adamp * h1[idx]);
+    }
+    return kappa0 * voigt_hv<R>(x, adamp, h0, h1, h2);
+}
+
+// One thread per (line, depth): depth = blockIdx.y, line = x index in the
+// catalog's (wavelength-sorted) order.  In the fused mode it evaluates the
+// TRANSP gates itself (line_opacity.py:101-184, Boltzmann factor from
+// populations.py:172); in the seam mode it takes TRANSP/valid as given
+// (compute_asynth_from_transp).  Then it recovers the wing parameters
+// (:1141-1272), scans the near wing for the KAPMIN cutoff (:474-537) and
+// writes the pair's descriptor and reach class (0xff: no contribution).
+// FP64 instantiation: the reference's arithmetic operation by operation.
+// FP32 instantiation: single precision after exact FASTEX table indices.
+template <typename R, bool FUSED>
+__global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
+                                  const R* __restrict__ kap_b, PairDesc<R>* __restrict__ desc,
+                                  uint8_t* __restrict__ cls) {
+    constexpr bool F32 = sizeof(R) == 4;
+    int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int d = blockIdx.y;
+    if (li >= a.n_lines) return;
+    const int L = a.n_layers;
+    int64_t slot = (int64_t)d * a.stride + li;
+    cls[slot] = 0xff;
+    if (FUSED && a.transp_out) {
+        a.transp_out[li * L + d] = 0.0;
+        a.valid_out[li * L + d] = 0;
+    }
+    const int e = a.element_idx[li];
+    const int ion = a.ion_stage[li];
+    const int lt = a.line_type[li];
+    if (e < 0 || e >= a.n_elem || ion <= 0 || ion > a.n_ion) return;
+    const DepthPar& dp = a.depth[d];
+    const IonPar& q = a.ion[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
+    const int c_ctr = a.center_idx[li];
+    const int c_wing = a.wing_idx[li];
+    const int64_t nwl = a.n_wl;
+    auto kap_at = [&](int c) -> double {
+        int cc = c < 0 ? 0 : (c > (int)nwl - 1 ? (int)nwl - 1 : c);
+        double v = (double)kap_a[(int64_t)d * nwl + cc];
+        if (kap_b) v += (double)kap_b[(int64_t)d * nwl + cc];
+        return v;
+    };
+
+    // ---------------- TRANSP (line_opacity.py:101-184) ----------------
+    R kapcen = R(0);
+    R kappa0_w = R(0);  // kappa0 for the wings
+    bool valid = false;
+    if (FUSED) {
+        if (a.process_mask[li] && q.pop > 0.0 && q.dop_transp > 0.0 && dp.rho > 0.0) {
+            if (!F32) {
+                const double lw = a.wavelength[li];
+                double kapmin = kap_at(c_ctr) * a.cutoff;
+                double k0pre = (lt == 1) ? a.gamma_vdw[li] * a.gf[li] * (q.pop / dp.rho)
+                                         : a.cgf[li] * q.xnfdop;
+                if (k0pre >= kapmin) {
+                    double post = k0pre * fast_ex(a.elo_cm[li] * dp.hckt, a.extab, a.extabf);
+                    if (post >= kapmin && post > 0.0) {
+                        double dw = q.dop_transp * lw;
+                        double dopple = lw > 0 ? dw / lw : 1e-6;
+                        double adamp = 0.0;
+                        if (dw > 0 && dopple > 0)
+                            adamp = (a.gamma_rad[li] + a.gamma_stark[li] * dp.xne +
+                                     a.gamma_vdw[li] * dp.txnxn) / dopple;
+                        if (adamp >= 0.0) {
+                            double kc;
+                            if (lt == 1) kc = post;
+                            else if (adamp < 0.2) kc = post * (1.0 - 1.128 * adamp);
+                            else kc = post * voigt_hv<double>(0.0, adamp, a.h0d, a.h1d, a.h2d);
+                            kapcen = (R)kc;
+                            valid = true;
+                        }
+                    }
+                }
+            } else {
+                const LineF lf = a.linef[li];
+                float kapmin = (float)(kap_at(c_ctr) * a.cutoff);
+                float k0pre = (lt == 1) ? lf.gw * lf.gf * q.pop_over_rho_f : lf.cgf * q.xnfdop_f;
+                if (k0pre >= kapmin) {
+                    float boltz = fast_ex_mixed(lf.elo_hi, lf.elo_lo, dp.hckt_hi, dp.hckt_lo,
+                                                a.elo_cm[li], dp.hckt, a.extab_f, a.extabf_f);
+                    float post = k0pre * boltz;
+                    if (post >= kapmin && post > 0.0f) {
+                        float adamp = (lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f) / q.dop_f;
+                        if (adamp >= 0.0f) {
+                            float vc = (lt == 1) ? 1.0f
+                                     : (adamp < 0.2f ? 1.0f - 1.128f * adamp
+                                                     : voigt_hv<float>(0.0f, adamp, a.h0f, a.h1f, a.h2f));
+                            kapcen = (R)(post * vc);
+                            kappa0_w = (R)post;
+                            valid = true;
+                        }
+                    }
+                }
+            }
+        }
+        if (a.transp_out && valid) {
+            a.transp_out[li * L + d] = (double)kapcen;
+            a.valid_out[li * L + d] = 1;
+        }
+    } else {
+        valid = a.valid_in[li * L + d] != 0;
+        kapcen = (R)a.transp_in[li * L + d];
+    }
+    if (!valid || !(kapcen > R(0))) return;
+
+    // ---------------- ASYNTH parameters (line_opacity.py:1161-1272) ----------------
+    int ctr_code = 0;  // centre add, line_opacity.py:1091-1102
+    if (a.asynth_mask[li] && c_ctr >= 0 && c_ctr < nwl) {
+        int dlt = c_ctr - c_wing;
+        if (dlt < -7 || dlt > 7) {
+            atomicOr(a.flags, FLAG_N10DOP_RANGE);
+            return;
+        }
+        ctr_code = dlt + 8;
+    }
+    PairDesc<R> out;
+    out.wing_c = c_wing;
+    out.kapcen = kapcen;
+    out.kappa0 = R(0);
+    out.adamp = R(0);
+    out.dvoigt = R(0);
+    out.xfar = R(0);
+    out.maxstep_far = 0;
+    int reach = 0;
+    int n10dop = 0;
+    const bool wings = (lt == 0) && q.dop > 0.0 && q.pop > 0.0 && a.wavelength[li] > 0.0 &&
+                       c_wing >= -MAX_PROFILE_STEPS && c_wing <= nwl - 1 + MAX_PROFILE_STEPS;
+    if (wings) {
+        R adamp, kappa0, dvoigt;
+        if (!F32) {
+            const double lw = a.wavelength[li];
+            double dw = q.dop * lw;
+            double dopple = dw / lw;
+            double ad = (a.gamma_rad[li] + a.gamma_stark[li] * dp.xne + a.gamma_vdw[li] * dp.txnxn) / dopple;
+            ad = ad > 1e-12 ? ad : 1e-12;
+            double vc = ad < 0.2 ? 1.0 - 1.128 * ad : voigt_hv<double>(0.0, ad, a.h0d, a.h1d, a.h2d);
+            kappa0 = (R)(vc > 0 ? (double)kapcen / vc : (double)kapcen);
+            adamp = (R)ad;
+            const double resolu = a.gp->resolu;
+            n10dop = (int)(int64_t)(10.0 * dopple * resolu);
+            dvoigt = (R)(dopple > 0 ? 1.0 / (dopple * resolu) : 1.0);
+        } else {
+            const LineF lf = a.linef[li];
+            float ad = (lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f) / (float)q.dop;
+            adamp = (R)(ad > 1e-12f ? ad : 1e-12f);
+            kappa0 = kappa0_w;
+            n10dop = q.n10dop;
+            dvoigt = (R)q.dvoigt_f;
+        }
+        if (n10dop > 0xffffff) {
+            atomicOr(a.flags, FLAG_N10DOP_RANGE);
+            return;
+        }
+        const R kapmin_ref = (R)(kap_at(c_wing) * a.cutoff);
+        const R* h0 = F32 ? (const R*)a.h0f : (const R*)a.h0d;
+        const R* h1 = F32 ? (const R*)a.h1f : (const R*)a.h1d;
+        const R* h2 = F32 ? (const R*)a.h2f : (const R*)a.h2d;
+        // near-wing KAPMIN scan (line_opacity.py:474-537)
+        int cut = -1;
+        R prof_n10 = R(0);
+        for (int ns = 1; ns <= n10dop; ns++) {
+            R p = near_profile<R>(ns, dvoigt, adamp, kappa0, h0, h1, h2);
+            if (ns == n10dop) prof_n10 = p;
+            if (p < kapmin_ref) {
+                cut = ns;
+                break;
+            }
+        }
+        bool far = false;
+        R xfar = R(0);
+        if (cut != -1) {
+            reach = cut;
+        } else {
+            far = true;
+            if (n10dop > 0 && prof_n10 > R(0) && kapmin_ref > R(0)) {
+                xfar = prof_n10 * (R)n10dop * (R)n10dop;
+                double ms = sqrt((double)xfar / (double)kapmin_ref) + 1.0;
+                reach = ms > (double)MAX_PROFILE_STEPS ? MAX_PROFILE_STEPS : (int)ms;
+            }
+        }
+        out.kappa0 = kappa0;
+        out.adamp = adamp;
+        out.dvoigt = dvoigt;
+        out.xfar = xfar;
+        out.maxstep_far = reach | (far ? (int)0x80000000 : 0);
+    }
+    if (ctr_code == 0 && reach == 0) return;
+    out.ctr_n10 = ctr_code | (n10dop << 8);
+    desc[slot] = out;
+    cls[slot] = (uint8_t)reach_class(reach);
+}
+
+// ---------------------------------------------------------------------------
+// accumulation
+// ---------------------------------------------------------------------------
+
+template <typename R> struct Acc;
+template <> struct Acc<float> {
+    float s, c;
+};
+template <> struct Acc<double> {
+    double s;
+};
+
+template <typename R>
+__device__ __forceinline__ void acc_add(R* sum, R* comp, int b, R v);
+template <>
+__device__ __forceinline__ void acc_add<float>(float* sum, float* comp, int b, float v) {
+    float s = sum[b], c = comp[b];
+    kahan_add(s, c, v);
+    sum[b] = s;
+    comp[b] = c;
+}
+template <>
+__device__ __forceinline__ void acc_add<double>(double* sum, double* comp, int b, double v) {
+    (void)comp;
+    sum[b] += v;
+}
+
+// Lower bound of `key` in keys[pos[lo..hi)] (pos are line positions whose
+// wing bins are non-decreasing).
+__device__ __forceinline__ int64_t lower_bound_pos(const int32_t* __restrict__ pos, int64_t lo,
+                                                   int64_t hi, const int32_t* __restrict__ wing,
+                                                   int64_t key) {
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)wing[pos[mid]] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// One CTA per (lambda tile, depth).  For every reach class k it selects the
+// pairs whose wing centre lies within 2^k (+1) bins of the tile -- a
+// contiguous range of that class's centre-sorted list -- and gives them to
+// its warps in a fixed round-robin order.  A warp adds one pair at a time
+// into its own shared-memory copy of the tile (lanes take consecutive wing
+// offsets; each offset's profile value goes to the red bin c+o and the blue
+// bin c-o), so no two lanes ever write the same word and no atomics are
+// needed.  The copies are then summed in a fixed order, multiplied by STIM
+// (line_opacity.py:1338) and written with coalesced stores.
+template <typename R>
+__global__ void __launch_bounds__(256) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
+                                                         R* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int W = a.tile_bins;
+    const int nwarps = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int d = blockIdx.y;
+    const int64_t T0 = (int64_t)blockIdx.x * W;
+    const int64_t T1 = min(T0 + (int64_t)W, a.n_wl);
+    const int span = (int)(T1 - T0);
+
+    R* tab = reinterpret_cast<R*>(smem_raw);  // h0[VOIGT_N], h1[VOIGT_N]
+    R* sh0 = tab;
+    R* sh1 = tab + VOIGT_N;
+    size_t tab_bytes = (2 * VOIGT_N * sizeof(R) + 15) & ~size_t(15);
+    R* acc = reinterpret_cast<R*>(smem_raw + tab_bytes);  // [nwarps][2][W] (float) or [nwarps][W]
+    __shared__ int64_t cls_lo[N_REACH_CLASSES], cls_hi[N_REACH_CLASSES];
+    __shared__ int64_t cls_base[N_REACH_CLASSES + 1];
+
+    const R* gh0 = sizeof(R) == 8 ? (const R*)a.h0d : (const R*)a.h0f;
+    const R* gh1 = sizeof(R) == 8 ? (const R*)a.h1d : (const R*)a.h1f;
+    const R* gh2 = sizeof(R) == 8 ? (const R*)a.h2d : (const R*)a.h2f;
+    for (int i = threadIdx.x; i < VOIGT_N; i += blockDim.x) {
+        sh0[i] = gh0[i];
+        sh1[i] = gh1[i];
+    }
+    const int acc_stride = (sizeof(R) == 4) ? 2 * W : W;
+    for (int i = threadIdx.x; i < nwarps * acc_stride; i += blockDim.x) acc[i] = R(0);
+    if (threadIdx.x < N_REACH_CLASSES) {
+        int k = threadIdx.x;
+        const int64_t* off = a.class_off + (int64_t)d * (N_REACH_CLASSES + 1);
+        int64_t lo = off[k], hi = off[k + 1];
+        int64_t h = class_halo(k) + 1;
+        int64_t s = lower_bound_pos(a.class_pos, lo, hi, a.wing_idx, T0 - h);
+        int64_t t = lower_bound_pos(a.class_pos, s, hi, a.wing_idx, T1 + h);
+        cls_lo[k] = s;
+        cls_hi[k] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t b = 0;
+        for (int k = 0; k < N_REACH_CLASSES; k++) {
+            cls_base[k] = b;
+            b += cls_hi[k] - cls_lo[k];
+        }
+        cls_base[N_REACH_CLASSES] = b;
+    }
+    __syncthreads();
+
+    R* my_sum = acc + warp * acc_stride;
+    R* my_cmp = (sizeof(R) == 4) ? my_sum + W : nullptr;
+    const int64_t total = cls_base[N_REACH_CLASSES];
+    const PairDesc<R>* drow = desc + (int64_t)d * a.stride;
+    int k = 0;
+    int64_t evals = 0;
+    for (int64_t item = warp; item < total; item += nwarps) {
+        while (item >= cls_base[k + 1]) k++;
+        int64_t p = a.class_pos[cls_lo[k] + (item - cls_base[k])];
+        const PairDesc<R> pd = drow[p];
+        const int64_t c = pd.wing_c;
+        // centre contribution
+        int ctr = pd.ctr_n10 & 15;
+        if (ctr) {
+            int64_t cb = c + (ctr - 8);
+            if (cb >= T0 && cb < T1) {
+                if (lane == 0) acc_add<R>(my_sum, my_cmp, (int)(cb - T0), pd.kapcen);
+                evals++;
+            }
+        }
+        const int reach = pd.maxstep_far & 0x7fffffff;
+        if (reach == 0) continue;
+        const bool far = pd.maxstep_far < 0;
+        const int n10 = pd.ctr_n10 >> 8;
+        // red offsets: c + o in [T0, T1); blue offsets: c - o in [T0, T1)
+        int64_t rlo = max((int64_t)1, T0 - c), rhi = min((int64_t)reach, T1 - 1 - c);
+        int64_t blo = max((int64_t)1, c - (T1 - 1)), bhi = min((int64_t)reach, c - T0);
+        bool rr = rlo <= rhi, bb = blo <= bhi;
+        if (!rr && !bb) continue;
+        int64_t olo = rr ? (bb ? min(rlo, blo) : rlo) : blo;
+        int64_t ohi = rr ? (bb ? max(rhi, bhi) : rhi) : bhi;
+        evals += (rr ? rhi - rlo + 1 : 0) + (bb ? bhi - blo + 1 : 0);
+        const R k0 = pd.kappa0, ad = pd.adamp, dv = pd.dvoigt, xf = pd.xfar;
+        for (int64_t o = olo + lane; o <= ohi; o += 32) {
+            R v;
+            if (far && o > n10) {
+                R oo = (R)o * (R)o;
+                if (sizeof(R) == 4) v = (R)__fdividef((float)xf, (float)oo);
+                else v = xf / oo;
+            } else {
+                v = near_profile<R>((int)o, dv, ad, k0, sh0, sh1, gh2);
+            }
+            if (rr && o >= rlo && o <= rhi) acc_add<R>(my_sum, my_cmp, (int)(c + o - T0), v);
+            if (bb && o >= blo && o <= bhi) acc_add<R>(my_sum, my_cmp, (int)(c - o - T0), v);
+        }
+    }
+    __syncthreads();
+    // combine the warp copies in warp order, apply STIM and store
+    const DepthPar dp = a.depth[d];
+    for (int b = threadIdx.x; b < span; b += blockDim.x) {
+        R v;
+        if (sizeof(R) == 4) {
+            float s = 0.f, cp = 0.f;
+            for (int w = 0; w < nwarps; w++) {
+                const float* ws = reinterpret_cast<const float*>(acc) + w * acc_stride;
+                kahan_add(s, cp, ws[b]);
+                kahan_add(s, cp, -ws[W + b]);
+            }
+            float freq = (float)(C_LIGHT_NM / a.grid[T0 + b]);
+            float stim = 1.0f - __expf(-freq * (float)dp.hkt_asynth);
+            v = (R)(s * stim);
+        } else {
+            double s = 0.0;
+            for (int w = 0; w < nwarps; w++) s += (double)acc[w * acc_stride + b];
+            double freq = C_LIGHT_NM / a.grid[T0 + b];
+            double stim = 1.0 - exp(-freq * dp.hkt_asynth);
+            v = (R)(s * stim);
+        }
+        out[(int64_t)d * a.n_wl + T0 + b] = v;
+    }
+    // evaluation counter (lane 0 of each warp holds the warp's count)
+    if (a.evals && lane == 0 && evals) atomicAdd((unsigned long long*)a.evals, (unsigned long long)evals);
+}
+
+// ---------------------------------------------------------------------------
+// transfer (JOSH)
+// ---------------------------------------------------------------------------
+
+// Parabolic coefficients of PARCOE after its boundary overrides
+// (josh_solver.py:110-152) at index j, before the smoothing pass.
+template <typename R>
+__device__ __forceinline__ void parcoe_raw(const R* f, const R* x, int n, int j, R& a, R& b, R& c) {
+    if (j == 0 || j == 1 || (j == 2 && n > 3) || j == n - 1) {
+        int j0 = (j == n - 1) ? n - 2 : j;
+        R den = x[j0 + 1] - x[j0];
+        b = den != R(0) ? (f[j0 + 1] - f[j0]) / den : R(0);
+        a = f[j] - x[j] * b;
+        c = R(0);
+        return;
+    }
+    int j1 = j - 1;
+    R den = x[j] - x[j1];
+    R dd = den != R(0) ? (f[j] - f[j1]) / den : R(0);
+    R den1 = (x[j + 1] - x[j]) * (x[j + 1] - x[j1]);
+    R term1 = den1 != R(0) ? f[j + 1] / den1 : R(0);
+    R den2 = x[j + 1] - x[j1];
+    R den3 = x[j + 1] - x[j];
+    R den4 = x[j] - x[j1];
+    R part = R(0);
+    if (den4 != R(0)) {
+        R t1 = den2 != R(0) ? f[j1] / den2 : R(0);
+        R t2 = den3 != R(0) ? f[j] / den3 : R(0);
+        part = (t1 - t2) / den4;
+    }
+    c = term1 + part;
+    b = dd - (x[j] + x[j1]) * c;
+    a = f[j1] - x[j1] * dd + x[j] * x[j1] * c;
+}
+
+// INTEG (josh_solver.py:171-189) over PARCOE with its smoothing pass
+// (:154-166) folded in, streaming over the layers.  FP32 accumulates tau
+// with Kahan compensation.
+template <typename R>
+__device__ void integ_tau(const R* x, const R* f, int n, R start, R* fint) {
+    fint[0] = start;
+    if (n == 1) return;
+    if (n == 2) {
+        R den = x[1] - x[0];
+        R b = den != R(0) ? (f[1] - f[0]) / den : R(0);
+        R a0 = f[0] - x[0] * b;
+        R dx = x[1] - x[0];
+        R term = a0 + R(0.5) * b * (x[1] + x[0]);
+        fint[1] = fint[0] + term * dx;
+        return;
+    }
+    R an, bn, cn;  // coefficients at i+1 after overrides (before smoothing)
+    R ai, bi, ci;
+    parcoe_raw<R>(f, x, n, 0, ai, bi, ci);
+    parcoe_raw<R>(f, x, n, 1, an, bn, cn);
+    R s = start, comp = R(0);
+    for (int i = 0; i < n - 1; i++) {
+        R a_i = ai, b_i = bi, c_i = ci;
+        if (i >= 1 && i <= n - 2) {
+            if (i == n - 2) {
+                // a[n1-1] = a[-1] (josh_solver.py:164-166)
+                R den = x[n - 1] - x[n - 2];
+                b_i = den != R(0) ? (f[n - 1] - f[n - 2]) / den : R(0);
+                a_i = f[n - 1] - x[n - 1] * b_i;
+                c_i = R(0);
+            } else if (ci != R(0)) {
+                R den = (cn < R(0) ? -cn : cn) + (ci < R(0) ? -ci : ci);
+                R wt = den > R(0) ? (cn < R(0) ? -cn : cn) / den : R(0);
+                a_i = an + wt * (ai - an);
+                b_i = bn + wt * (bi - bn);
+                c_i = cn + wt * (ci - cn);
+            }
+        }
+        R dx = x[i + 1] - x[i];
+        R term = a_i + R(0.5) * b_i * (x[i + 1] + x[i]);
+        term += (c_i / R(3)) * ((x[i + 1] + x[i]) * x[i + 1] + x[i] * x[i]);
+        R inc = term * dx;
+        if (sizeof(R) == 4) {
+            float sf = (float)s, cf = (float)comp;
+            kahan_add(sf, cf, (float)inc);
+            s = (R)sf;
+            comp = (R)cf;
+        } else {
+            s = s + inc;
+        }
+        fint[i + 1] = s;
+        ai = an; bi = bn; ci = cn;
+        if (i + 2 <= n - 1) parcoe_raw<R>(f, x, n, i + 2, an, bn, cn);
+    }
+}
+
+// DERIV (josh_solver.py:193-217)
+template <typename R>
+__device__ void deriv(const R* x, const R* f, int n, R* dfdx) {
+    dfdx[0] = (f[1] - f[0]) / (x[1] - x[0]);
+    dfdx[n - 1] = (f[n - 1] - f[n - 2]) / (x[n - 1] - x[n - 2]);
+    if (n == 2) return;
+    R s = x[1] != x[0] ? (R)(((x[1] - x[0]) < R(0)) ? -1 : 1) : R(1);
+    for (int j = 1; j < n - 1; j++) {
+        R sc = fabs(f[j - 1]);
+        R t = fabs(f[j]);
+        sc = t > sc ? t : sc;
+        t = fabs(f[j + 1]);
+        sc = t > sc ? t : sc;
+        sc = x[j] != R(0) ? sc / fabs(x[j]) : sc;
+        if (sc == R(0)) sc = R(1);
+        R d1 = (f[j + 1] - f[j]) / (x[j + 1] - x[j]) / sc;
+        R d0 = (f[j] - f[j - 1]) / (x[j] - x[j - 1]) / sc;
+        R tan1 = d1 / (s * sqrt(R(1) + d1 * d1) + R(1));
+        R tan0 = d0 / (s * sqrt(R(1) + d0 * d0) + R(1));
+        dfdx[j] = (tan1 + tan0) / (R(1) - tan1 * tan0) * sc;
+    }
+}
+
+// MAP1 (josh_solver.py:220-353) of fold(xold) onto the JOSH grid.
+template <typename R>
+__device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew, R* fnew) {
+    int l = 2, ll = 0;
+    R cfor = 0, bfor = 0, afor = 0, cbac = 0, bbac = 0, abac = 0, A = 0, B = 0, Cc = 0;
+    // 1-based views
+    const R* x1 = xold - 1;
+    const R* f1 = fold - 1;
+    for (int k = 1; k <= NXTAU; k++) {
+        R xk = xnew[k - 1];
+        for (;;) {
+            if (xk < x1[l]) {
+                if (l == ll) break;
+                if (l == 2 || l == 3) {
+                    l = l < nold ? l : nold;
+                    Cc = R(0);
+                    B = (f1[l] - f1[l - 1]) / (x1[l] - x1[l - 1]);
+                    A = f1[l] - x1[l] * B;
+                    ll = l;
+                    break;
+                }
+                int l1 = l - 1;
+                if (l > ll + 1 || l == 4) {
+                    int l2 = l - 2;
+                    R dd = (f1[l1] - f1[l2]) / (x1[l1] - x1[l2]);
+                    cbac = f1[l] / ((x1[l] - x1[l1]) * (x1[l] - x1[l2])) +
+                           (f1[l2] / (x1[l] - x1[l2]) - f1[l1] / (x1[l] - x1[l1])) /
+                               (x1[l1] - x1[l2]);
+                    bbac = dd - (x1[l1] + x1[l2]) * cbac;
+                    abac = f1[l2] - x1[l2] * dd + x1[l1] * x1[l2] * cbac;
+                    if (!(l < nold)) {
+                        Cc = cbac; B = bbac; A = abac; ll = l;
+                        break;
+                    }
+                } else {
+                    cbac = cfor; bbac = bfor; abac = afor;
+                    if (l == nold) {
+                        Cc = cbac; B = bbac; A = abac; ll = l;
+                        break;
+                    }
+                }
+                R dd = (f1[l] - f1[l1]) / (x1[l] - x1[l1]);
+                cfor = f1[l + 1] / ((x1[l + 1] - x1[l]) * (x1[l + 1] - x1[l1])) +
+                       (f1[l1] / (x1[l + 1] - x1[l1]) - f1[l] / (x1[l + 1] - x1[l])) /
+                           (x1[l] - x1[l1]);
+                bfor = dd - (x1[l] + x1[l1]) * cfor;
+                afor = f1[l1] - x1[l1] * dd + x1[l] * x1[l1] * cfor;
+                R acf = cfor < R(0) ? -cfor : cfor;
+                R acb = cbac < R(0) ? -cbac : cbac;
+                R wt = acf != R(0) ? acf / (acf + acb) : R(0);
+                A = afor + wt * (abac - afor);
+                B = bfor + wt * (bbac - bfor);
+                Cc = cfor + wt * (cbac - cfor);
+                ll = l;
+                break;
+            }
+            l += 1;
+            if (l > nold) {
+                l = nold;
+                Cc = R(0);
+                B = (f1[l] - f1[l - 1]) / (x1[l] - x1[l - 1]);
+                A = f1[l] - x1[l] * B;
+                ll = l;
+                break;
+            }
+        }
+        fnew[k - 1] = A + (B + Cc * xk) * xk;
+    }
+}
+
+// Gauss-Seidel scattering sweeps of the reference (josh_solver.py:24-92), in
+// single precision as the reference runs them, with the reference's
+// summation order and no fused multiply-add.
+static __device__ __noinline__ int josh_sweeps_ref(const float* __restrict__ coefj, float* xs,
+                                            const float* xalpha, const float* xsbar_mod) {
+    float diag[NXTAU];
+    for (int k = 0; k < NXTAU; k++) diag[k] = __fsub_rn(1.0f, __fmul_rn(xalpha[k], coefj[k * NXTAU + k]));
+    for (int it = 0; it < NXTAU; it++) {
+        int iferr = 0;
+        for (int k = NXTAU - 1; k >= 0; k--) {
+            float delxs = 0.0f;
+            for (int m = 0; m < NXTAU; m++) delxs = __fadd_rn(delxs, __fmul_rn(coefj[k * NXTAU + m], xs[m]));
+            delxs = __fdiv_rn(__fsub_rn(__fadd_rn(__fmul_rn(delxs, xalpha[k]), xsbar_mod[k]), xs[k]), diag[k]);
+            float errorx = xs[k] != 0.0f ? fabsf(__fdiv_rn(delxs, xs[k])) : __int_as_float(0x7f800000);
+            if (errorx > 1.0e-5f) iferr = 1;
+            float nv = __fadd_rn(xs[k], delxs);
+            xs[k] = nv > 1.0e-38f ? nv : 1.0e-38f;
+        }
+        if (!iferr) return it + 1;
+    }
+    return NXTAU;
+}
+
+// Fast sweeps: the same iteration with the 51x51 operator in the kernel's
+// constant bank (a __grid_constant__ parameter), XS in registers (fully
+// unrolled) and four interleaved partial dot products per row.
+__device__ __forceinline__ int josh_sweeps_fast(const CoefJ32& cj, const float* xa, const float* xm,
+                                                float* xs_io) {
+    float xs[NXTAU];
+#pragma unroll
+    for (int m = 0; m < NXTAU; m++) xs[m] = xs_io[m];
+    int it_done = NXTAU;
+    for (int it = 0; it < NXTAU; it++) {
+        bool err = false;
+#pragma unroll
+        for (int k = NXTAU - 1; k >= 0; k--) {
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+            for (int m = 0; m + 3 < NXTAU; m += 4) {
+                s0 = fmaf(cj.c[k * NXTAU + m], xs[m], s0);
+                s1 = fmaf(cj.c[k * NXTAU + m + 1], xs[m + 1], s1);
+                s2 = fmaf(cj.c[k * NXTAU + m + 2], xs[m + 2], s2);
+                s3 = fmaf(cj.c[k * NXTAU + m + 3], xs[m + 3], s3);
+            }
+#pragma unroll
+            for (int m = (NXTAU / 4) * 4; m < NXTAU; m++) s0 = fmaf(cj.c[k * NXTAU + m], xs[m], s0);
+            float s = (s0 + s1) + (s2 + s3);
+            float xak = xa[k];
+            float diag = 1.0f - xak * cj.c[k * NXTAU + k];
+            float dl = __fdividef(fmaf(s, xak, xm[k]) - xs[k], diag);
+            float xk = xs[k];
+            err |= (xk == 0.0f) || (fabsf(dl) > 1.0e-5f * fabsf(xk));
+            float nv = xk + dl;
+            xs[k] = nv > 1.0e-38f ? nv : 1.0e-38f;
+        }
+        if (!err) {
+            it_done = it + 1;
+            break;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < NXTAU; m++) xs_io[m] = xs[m];
+    return it_done;
+}
+
+// JOSH surface flux for one column (josh_solver.py:367-767).
+template <typename R, bool REF_SWEEP>
+__device__ double josh_flux(int n, const R* acont, const R* scont, const R* aline, const R* sline,
+                            const R* sigmac, const R* sigmal, const R* rho, const R* xtau,
+                            const double* ch, const CoefJ32& cj, int* iters_out) {
+    R abtot[MAX_LAYERS], alpha[MAX_LAYERS], snubar[MAX_LAYERS], taunu[MAX_LAYERS];
+    const R eps = (R)EPS38;
+    for (int j = 0; j < n; j++) {
+        R ab = acont[j] + aline[j] + sigmac[j] + sigmal[j];
+        abtot[j] = ab > eps ? ab : (ab != ab ? ab : eps);
+        R sc = sigmac[j] + sigmal[j];
+        R al = abtot[j] > R(0) ? sc / abtot[j] : R(0);
+        alpha[j] = al < R(0) ? R(0) : (al > R(1) ? R(1) : al);
+        R den = acont[j] + aline[j];
+        snubar[j] = den > R(0) ? (acont[j] * scont[j] + aline[j] * sline[j]) / den : scont[j];
+    }
+    // rho ascending after solve_lte_frequency's reversal, so needs_reverse
+    // (josh_solver.py:465) is false here.
+    integ_tau<R>(rho, abtot, n, abtot[0] * rho[0], taunu);
+    if (taunu[0] > xtau[NXTAU - 1]) {
+        // MAXJ = 1 path (josh_solver.py:700-727)
+        R snu[MAX_LAYERS], hnu[MAX_LAYERS], jm[MAX_LAYERS];
+        for (int j = 0; j < n; j++) snu[j] = snubar[j];
+        int it_done = 0;
+        for (int it = 0; it < NXTAU; it++) {
+            deriv<R>(taunu, snu, n, hnu);
+            for (int j = 0; j < n; j++) hnu[j] = hnu[j] / R(3);
+            deriv<R>(taunu, hnu, n, jm);
+            R err = R(0);
+            for (int j = 0; j < n; j++) {
+                R jnu = jm[j] + snu[j];
+                R snew = (R(1) - alpha[j]) * snubar[j] + alpha[j] * jnu;
+                R an = snew < R(0) ? -snew : snew;
+                R dn = an > eps ? an : eps;
+                R df = snew - snu[j];
+                err += (df < R(0) ? -df : df) / dn;
+                snu[j] = snew;
+            }
+            it_done = it + 1;
+            if (err < R(1.0e-5)) break;
+        }
+        *iters_out = -it_done;
+        return (double)hnu[0];
+    }
+    R xsbar[NXTAU], xalpha[NXTAU];
+    map1_xtau<R>(taunu, snubar, n, xtau, xsbar);
+    map1_xtau<R>(taunu, alpha, n, xtau, xalpha);
+    float xs32[NXTAU], xa32[NXTAU], xm32[NXTAU];
+    R s0 = snubar[0] > eps ? snubar[0] : eps;
+    R a0 = alpha[0] < R(0) ? R(0) : (alpha[0] > R(1) ? R(1) : alpha[0]);
+    for (int l = 0; l < NXTAU; l++) {
+        R xb = xsbar[l] > eps ? xsbar[l] : eps;
+        R xa = xalpha[l] < R(0) ? R(0) : (xalpha[l] > R(1) ? R(1) : xalpha[l]);
+        if (xtau[l] < taunu[0]) {
+            xb = s0;
+            xa = a0;
+        }
+        xs32[l] = (float)xb;
+        xa32[l] = (float)xa;
+        xm32[l] = (float)(xb * (R(1) - xa));
+    }
+    int it;
+    if (REF_SWEEP) it = josh_sweeps_ref(cj.c, xs32, xa32, xm32);
+    else it = josh_sweeps_fast(cj, xa32, xm32, xs32);
+    *iters_out = it;
+    double flux = 0.0;
+    for (int l = 0; l < NXTAU; l++) flux += ch[l] * (double)xs32[l];
+    return flux;
+}
+
+// Planck function B_nu (radiative.py:20-39).
+template <typename R>
+__device__ __forceinline__ R planck_nu(double freq, double hkt) {
+    if (sizeof(R) == 8) {
+        double freq15 = freq / 1.0e15;
+        double ehvkt = exp(-freq * hkt);
+        double stim = 1.0 - ehvkt;
+        double bnu = 1.47439e-2 * pow(freq15, 3.0) * ehvkt / stim;
+        return (R)(bnu != bnu ? 0.0 : bnu);
+    } else {
+        float freq15 = (float)(freq / 1.0e15);
+        float x = (float)(freq * hkt);
+        float ehvkt = __expf(-x);
+        float bnu = 1.47439e-2f * freq15 * freq15 * freq15 * ehvkt / (-expm1f(-x));
+        return (R)(bnu != bnu ? 0.0f : bnu);
+    }
+}
+
+// One thread per wavelength (radiative.py:42-218 and the per-lambda loop of
+// :282-494).  Field arrays are [L, n]; asynth is the stimulated-emission-
+// corrected line opacity, split by FSCAT into absorption and scattering
+// (opacity.py:2408-2420).
+template <typename R, bool REF_SWEEP>
+__global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __grid_constant__ CoefJ32 cj,
+                                                       const R* __restrict__ cont_abs,
+                                                       const R* __restrict__ cont_scat,
+                                                       const R* __restrict__ line_op,
+                                                       const R* __restrict__ line_sc,
+                                                       const R* __restrict__ line_src) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    const int L = a.n_layers;
+    R mass[MAX_LAYERS], ca[MAX_LAYERS], cs[MAX_LAYERS], la[MAX_LAYERS], ls[MAX_LAYERS],
+        src[MAX_LAYERS], pl[MAX_LAYERS];
+    double hkts[MAX_LAYERS];
+    const double wl = a.grid[j];
+    const double freq = C_LIGHT_NM / (wl > 1e-12 ? wl : 1e-12);
+    int m = 0;
+    for (int d = 0; d < L; d++) {
+        const DepthPar dp = a.depth[d];
+        double cm = dp.rhox;
+        R aa = cont_abs[(int64_t)d * a.n + j];
+        R ss = cont_scat[(int64_t)d * a.n + j];
+        R lo, lsg;
+        if (a.asynth_mode) {
+            R A = line_op[(int64_t)d * a.n + j];
+            R fs = (R)dp.fscat;
+            lo = A * (R(1) - fs);
+            R one_m = R(1) - fs;
+            R alinec = lo / (one_m > R(1e-12) ? one_m : R(1e-12));
+            lsg = alinec * fs;
+        } else {
+            lo = line_op[(int64_t)d * a.n + j];
+            lsg = line_sc ? line_sc[(int64_t)d * a.n + j] : R(0);
+        }
+        const R mx = (R)MAX_OPACITY_REAL4;
+        bool ok = cm >= 0.0 && isfinite(cm) && isfinite((double)aa) && isfinite((double)ss) &&
+                  isfinite((double)lo) && isfinite((double)lsg) && aa < mx && ss < mx && lo < mx &&
+                  lsg < mx;
+        if (!ok || !(cm > 0.0)) continue;
+        mass[m] = (R)cm;
+        ca[m] = aa;
+        cs[m] = ss;
+        la[m] = lo;
+        ls[m] = lsg;
+        hkts[m] = dp.hkt;
+        if (line_src) {
+            R v = line_src[(int64_t)d * a.n + j];
+            src[m] = isfinite((double)v) ? v : planck_nu<R>(freq, dp.hkt);
+        } else if (a.slinec_mode && sizeof(R) == 8) {
+            // SLINEC = BNU*STIM/(1-EHVKT) with the driver's frequency
+            // (opacity.py:2215-2227, bfudge.py:144-145)
+            double fr = C_LIGHT_CM / (wl * 1.0e-7);
+            double f15 = fr / 1.0e15;
+            double eh = exp(-fr * dp.hkt);
+            double st = 1.0 - eh;
+            double bnu = 1.47439e-02 * pow(f15, 3.0) * eh / st;
+            double v = (bnu * st) / (1.0 - eh);
+            src[m] = isfinite(v) ? (R)v : planck_nu<R>(freq, dp.hkt);
+        }
+        m++;
+    }
+    if (m == 0) {
+        a.flux_total[j] = 0.0;
+        a.flux_cont[j] = 0.0;
+        return;
+    }
+    if (m > 1 && !(mass[0] < mass[m - 1])) {
+        for (int q = 0; q < m / 2; q++) {
+            int r = m - 1 - q;
+            R t;
+            t = mass[q]; mass[q] = mass[r]; mass[r] = t;
+            t = ca[q]; ca[q] = ca[r]; ca[r] = t;
+            t = cs[q]; cs[q] = cs[r]; cs[r] = t;
+            t = la[q]; la[q] = la[r]; la[r] = t;
+            t = ls[q]; ls[q] = ls[r]; ls[r] = t;
+            t = src[q]; src[q] = src[r]; src[r] = t;
+            double h = hkts[q]; hkts[q] = hkts[r]; hkts[r] = h;
+        }
+    }
+    const bool src_is_planck = !line_src && !(a.slinec_mode && sizeof(R) == 8);
+    for (int q = 0; q < m; q++) {
+        pl[q] = planck_nu<R>(freq, hkts[q]);
+        if (src_is_planck) src[q] = pl[q];
+    }
+    R zero[MAX_LAYERS];
+    for (int q = 0; q < m; q++) zero[q] = R(0);
+    R xtau[NXTAU];
+    for (int l = 0; l < NXTAU; l++) xtau[l] = (R)a.xtau[l];
+    int itc = 0, itt = 0;
+    double fc = josh_flux<R, REF_SWEEP>(m, ca, pl, zero, pl, cs, zero, mass, xtau, a.ch, cj, &itc);
+    double ft = josh_flux<R, REF_SWEEP>(m, ca, pl, la, src, cs, ls, mass, xtau, a.ch, cj, &itt);
+    a.flux_cont[j] = fc;
+    a.flux_total[j] = ft;
+    if (a.iters) {
+        a.iters[2 * j] = itc;
+        a.iters[2 * j + 1] = itt;
+    }
+}
+
+}  // namespace ks

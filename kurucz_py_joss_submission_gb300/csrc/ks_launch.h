@@ -1,0 +1,32 @@
+// ks_launch.h -- host-side launchers of the per-precision kernel units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ks_internal.h"
+
+namespace ks {
+
+// JOSH mean-intensity operator in single precision, passed to the fast
+// sweep kernel by value so it lives in the kernel's constant bank.
+struct CoefJ32 {
+    float c[51 * 51];
+};
+
+#define KS_DECLARE_LAUNCHERS(R, SUF)                                                              \
+    cudaError_t launch_prep_##SUF(const PrepArgs& a, cudaStream_t s);                             \
+    cudaError_t launch_continuum_##SUF(const ContArgs& a, R* ca, R* cs, cudaStream_t s);         \
+    cudaError_t launch_pair_setup_##SUF(const PairArgs& a, bool fused, const R* kap_a,           \
+                                        const R* kap_b, PairDesc<R>* desc, uint8_t* cls,         \
+                                        cudaStream_t s);                                          \
+    cudaError_t launch_accumulate_##SUF(const AccArgs& a, int warps, const PairDesc<R>* desc,    \
+                                        R* out, cudaStream_t s);                                  \
+    cudaError_t launch_transfer_##SUF(const TransferArgs& a, const CoefJ32* cj, const R* ca,     \
+                                      const R* cs, const R* lo, const R* lsc, const R* src,      \
+                                      cudaStream_t s);                                            \
+    size_t accumulate_smem_bytes_##SUF(int tile_bins, int warps);
+
+KS_DECLARE_LAUNCHERS(float, f32)
+KS_DECLARE_LAUNCHERS(double, f64)
+
+}  // namespace ks

@@ -1,0 +1,211 @@
+"""Device-resident inputs and the fused synthesis plan.
+
+``DeviceAtmosphere``, ``DeviceGrid`` and ``DeviceCatalog`` hold the inputs in
+HBM (torch tensors own the memory) and expose the C-ABI records that point
+at them.  ``Synthesizer`` sizes one workspace for a (catalog, atmosphere,
+grid) triple and runs ``ks_synthesize`` on the current CUDA stream, so a
+synthesis is one call with no allocation once the plan exists.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Dict, Optional
+
+import numpy as np
+import torch
+
+from . import _native
+from .io.atmosphere import AtmosphereModel
+from .io.lines.atomic import LineCatalog
+
+PRECISIONS = {"mixed": _native.KS_PREC_MIXED, "fp64": _native.KS_PREC_FP64}
+
+
+def _require_cuda(device) -> torch.device:
+    dev = torch.device(device)
+    if dev.type != "cuda":
+        raise RuntimeError("the synthesis kernels run on a CUDA device only (no CPU fallback)")
+    if not torch.cuda.is_available():
+        raise RuntimeError("CUDA is not available: the GB300 synthesis path needs a GPU")
+    return dev
+
+
+def _dev(a: np.ndarray, dtype, device) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(device, non_blocking=False)
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def stream_handle(stream: Optional[torch.cuda.Stream] = None) -> C.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class DeviceAtmosphere:
+    """One converted atmosphere in HBM."""
+
+    def __init__(self, atm: AtmosphereModel, device="cuda"):
+        dev = _require_cuda(device)
+        L = atm.layers
+        f64 = np.float64
+        self.n_layers = L
+        self.t: Dict[str, torch.Tensor] = {}
+
+        def put(name, arr):
+            if arr is None:
+                return None
+            self.t[name] = _dev(arr, f64, dev)
+            return self.t[name]
+
+        put("rhox", atm.depth)
+        put("temperature", atm.temperature)
+        put("electron_density", atm.electron_density)
+        put("mass_density", atm.mass_density)
+        put("hckt", atm.hckt)
+        put("xnf_h", atm.xnf_h)
+        put("xnf_he1", atm.xnf_he1)
+        put("xnf_h2", atm.xnf_h2)
+        pop = atm.population_per_ion if atm.population_per_ion is not None else np.zeros((L, 1, 1))
+        dop = atm.doppler_per_ion if atm.doppler_per_ion is not None else np.zeros((L, 1, 1))
+        put("population", pop)
+        put("doppler", dop)
+        put("wledge", atm.continuum_wledge)
+        put("half_edge", atm.continuum_half_edge)
+        put("delta_edge", atm.continuum_delta_edge)
+        put("cont_abs_coeff", atm.continuum_abs_coeff)
+        put("cont_scat_coeff", atm.continuum_scat_coeff)
+        rec = _native.KsAtmos()
+        rec.n_layers = L
+        for name in ("rhox", "temperature", "electron_density", "mass_density", "hckt", "xnf_h",
+                     "xnf_he1", "xnf_h2", "population", "doppler", "wledge", "half_edge",
+                     "delta_edge", "cont_abs_coeff", "cont_scat_coeff"):
+            t = self.t.get(name)
+            setattr(rec, name, t.data_ptr() if t is not None else None)
+        rec.n_ion = int(pop.shape[1])
+        rec.n_elem = int(pop.shape[2])
+        rec.n_edge = int(atm.continuum_wledge.size) if atm.continuum_wledge is not None else 0
+        rec.coeff_log10 = 1 if atm.continuum_coeff_log10 else 0
+        self.rec = rec
+
+
+class DeviceGrid:
+    """The log-lambda grid in HBM."""
+
+    def __init__(self, wavelength: np.ndarray, grid_origin: Optional[float] = None, device="cuda"):
+        dev = _require_cuda(device)
+        self.wavelength_host = np.ascontiguousarray(wavelength, dtype=np.float64)
+        self.wavelength = _dev(self.wavelength_host, np.float64, dev)
+        self.n = int(self.wavelength_host.size)
+        rec = _native.KsGrid()
+        rec.n = self.n
+        rec.wavelength = self.wavelength.data_ptr()
+        rec.grid_origin = float(grid_origin if grid_origin is not None else
+                                (self.wavelength_host[0] if self.n else 0.0))
+        self.rec = rec
+
+
+class DeviceCatalog:
+    """A line catalog in HBM, sorted by wavelength (the kernels require it).
+
+    ``order`` maps device rows to catalog rows, for returning per-line
+    results in catalog order."""
+
+    COLUMNS_F64 = ("wavelength", "gf", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw",
+                   "excitation_energy")
+    COLUMNS_I32 = ("element_idx", "ion_stages", "line_types")
+    COLUMNS_U8 = ("process_mask", "asynth_mask")
+
+    def __init__(self, cat: LineCatalog, device="cuda"):
+        dev = _require_cuda(device)
+        if cat.is_sorted():
+            self.order = None
+            src = cat
+        else:
+            self.order = np.argsort(cat.wavelength, kind="stable")
+            src = cat.take(self.order)
+        self.n_lines = len(src)
+        self.t: Dict[str, torch.Tensor] = {}
+        for k in self.COLUMNS_F64:
+            self.t[k] = _dev(getattr(src, k), np.float64, dev)
+        for k in self.COLUMNS_I32:
+            self.t[k] = _dev(getattr(src, k), np.int32, dev)
+        for k in self.COLUMNS_U8:
+            self.t[k] = _dev(getattr(src, k), np.uint8, dev)
+        self.host = src
+        rec = _native.KsLines()
+        rec.n_lines = self.n_lines
+        rec.wavelength = self.t["wavelength"].data_ptr()
+        rec.gf = self.t["gf"].data_ptr()
+        rec.cgf = self.t["cgf"].data_ptr()
+        rec.gamma_rad = self.t["gamma_rad"].data_ptr()
+        rec.gamma_stark = self.t["gamma_stark"].data_ptr()
+        rec.gamma_vdw = self.t["gamma_vdw"].data_ptr()
+        rec.elo_cm = self.t["excitation_energy"].data_ptr()
+        rec.element_idx = self.t["element_idx"].data_ptr()
+        rec.ion_stage = self.t["ion_stages"].data_ptr()
+        rec.line_type = self.t["line_types"].data_ptr()
+        rec.process_mask = self.t["process_mask"].data_ptr()
+        rec.asynth_mask = self.t["asynth_mask"].data_ptr()
+        rec.sorted_by_wavelength = 1
+        self.rec = rec
+
+    def to_catalog_order(self, per_line: np.ndarray) -> np.ndarray:
+        """Rows in device (sorted) order -> rows in catalog order."""
+        if self.order is None:
+            return per_line
+        out = np.empty_like(per_line)
+        out[self.order] = per_line
+        return out
+
+
+def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", tile_bins=0,
+                 warps_per_tile=0) -> _native.KsOptions:
+    opt = _native.KsOptions()
+    opt.cutoff = float(cutoff)
+    opt.microturb_kms = float(microturb_kms)
+    opt.rhoxj = float(rhoxj)
+    opt.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    opt.tile_bins = int(tile_bins)
+    opt.warps_per_tile = int(warps_per_tile)
+    return opt
+
+
+class Synthesizer:
+    """Fused continuum -> TRANSP -> ASYNTH -> JOSH for one atmosphere.
+
+    Owns the workspace and the outputs (``flux_total``/``flux_cont`` F_nu,
+    ``asynth`` the line opacity).  ``run()`` enqueues the synthesis on the
+    current stream and returns nothing; ``run(stats=True)`` synchronises and
+    returns the counters."""
+
+    def __init__(self, catalog: DeviceCatalog, atmosphere: DeviceAtmosphere, grid: DeviceGrid,
+                 options: Optional[_native.KsOptions] = None, keep_asynth: bool = True):
+        self.lib = _native.load()
+        self.catalog, self.atmosphere, self.grid = catalog, atmosphere, grid
+        self.options = options or make_options()
+        dev = grid.wavelength.device
+        ws = C.c_size_t()
+        _native.check(self.lib.ks_workspace_size(catalog.n_lines, atmosphere.n_layers, grid.n,
+                                                 C.byref(self.options), C.byref(ws)))
+        self.workspace_bytes = int(ws.value)
+        self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=dev)
+        self.flux_total = torch.empty(grid.n, dtype=torch.float64, device=dev)
+        self.flux_cont = torch.empty(grid.n, dtype=torch.float64, device=dev)
+        fp64 = self.options.precision == _native.KS_PREC_FP64
+        self.asynth = (torch.empty((atmosphere.n_layers, grid.n),
+                                   dtype=torch.float64 if fp64 else torch.float32, device=dev)
+                       if keep_asynth else None)
+
+    def run(self, stats: bool = False, stream: Optional[torch.cuda.Stream] = None):
+        st = _native.KsStats()
+        status = self.lib.ks_synthesize(
+            C.byref(self.catalog.rec), C.byref(self.atmosphere.rec), C.byref(self.grid.rec),
+            C.byref(self.options), _ptr(self.workspace), self.workspace_bytes,
+            _ptr(self.flux_total), _ptr(self.flux_cont), _ptr(self.asynth),
+            C.byref(st) if stats else None, stream_handle(stream))
+        _native.check(status)
+        return st.as_dict() if stats else None

@@ -433,8 +433,10 @@ static inline double near_profile(int64_t off, double *tabi, double tabstep,
 /* line_opacity.py:946-1340 compute_asynth_from_transp with its wing kernel
  * (:187-617), for plain lines (line_type 0).  Per depth: centre adds in line
  * order (:1091-1102), then wings in line order (:241-617), then x STIM
- * (:1338).  pair_out, when given, receives per (line, depth) the number of
- * grid points the pair wrote (centre + wings), the unit of work. */
+ * (:1338).  evals_per_depth receives the number of grid points written per
+ * depth (centre + wings, the unit of work); maxstep_out (optional, [nl, L])
+ * the wing reach of each pair, negated when the near-wing cutoff ended it
+ * (no far wing). */
 void kso_asynth(int64_t nl, int64_t L, const uint8_t *valid, const double *transp,
                 const int32_t *line_type, const uint8_t *asynth_mask,
                 const int32_t *ion_stage, const int32_t *element_idx,
@@ -445,7 +447,7 @@ void kso_asynth(int64_t nl, int64_t L, const uint8_t *valid, const double *trans
                 const double *txnxn, const double *temperature,
                 const double *cont_kapmin, const double *grid, int64_t n_wl,
                 double cutoff, const double *h0, const double *h1, const double *h2,
-                double *asynth, int64_t *evals_per_depth) {
+                double *asynth, int64_t *evals_per_depth, int32_t *maxstep_out) {
     double resolu = 300000.0;
     if (n_wl > 1) {
         double ratio = grid[1] / grid[0];
@@ -528,6 +530,7 @@ void kso_asynth(int64_t nl, int64_t L, const uint8_t *valid, const double *trans
                 }
                 if (maxstep > MAX_PROFILE_STEPS) maxstep = MAX_PROFILE_STEPS;
             }
+            if (maxstep_out) maxstep_out[li * L + d] = (int32_t)(use_far ? maxstep : -maxstep);
             int red = 1, blue = 1;
             double tabo = 0.5;
             for (int64_t off = 1; off <= maxstep && (red || blue); off++) {

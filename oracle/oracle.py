@@ -161,6 +161,7 @@ def asynth(cat, route, atm, grid, tr, valid, center_idx, wing_idx, cont_kapmin, 
     nion, nelem = dop.shape[1], dop.shape[2]
     out = np.zeros((L, n))
     evals = np.zeros(L, dtype=np.int64)
+    reach = np.zeros((nl, L), dtype=np.int32)
     lib().kso_asynth(
         C.c_int64(nl), C.c_int64(L), _p(np.ascontiguousarray(valid, np.uint8), P_U8), _p(_d(tr), P_D),
         _p(np.ascontiguousarray(cat["line_type"], np.int32), P_I32), _p(route["asynth_mask"], P_U8),
@@ -172,8 +173,9 @@ def asynth(cat, route, atm, grid, tr, valid, center_idx, wing_idx, cont_kapmin, 
         _p(dop, P_D), C.c_int64(nion), C.c_int64(nelem), _p(_d(atm["electron_density"]), P_D),
         _p(txnxn(atm), P_D), _p(_d(atm["temperature"]), P_D), _p(_d(cont_kapmin), P_D),
         _p(_d(grid), P_D), C.c_int64(n), C.c_double(cutoff),
-        _p(tb["h0tab"], P_D), _p(tb["h1tab"], P_D), _p(tb["h2tab"], P_D), _p(out, P_D), _p(evals, P_I64))
-    return out, evals
+        _p(tb["h0tab"], P_D), _p(tb["h1tab"], P_D), _p(tb["h2tab"], P_D), _p(out, P_D), _p(evals, P_I64),
+        _p(reach, P_I32))
+    return out, evals, reach
 
 
 def line_source(atm, grid):
@@ -218,7 +220,7 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
     t1 = time.perf_counter()
     tr, valid = transp(cat, route, atm, cidx, kapmin, tb, cutoff, microturb)
     t2 = time.perf_counter()
-    asy, evals = asynth(cat, route, atm, grid, tr, valid, cidx, widx, kapmin, tb, cutoff)
+    asy, evals, reach = asynth(cat, route, atm, grid, tr, valid, cidx, widx, kapmin, tb, cutoff)
     t3 = time.perf_counter()
     rhox = np.asarray(atm["depth"], dtype=np.float64)
     fscat = np.exp(-rhox / rhoxj) if rhoxj > 0.0 else np.zeros_like(rhox)
@@ -232,7 +234,7 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
         timings.update(setup=t1 - t0, transp=t2 - t1, asynth=t3 - t2, transfer=t4 - t3)
     return dict(
         wavelength=grid, center_indices=cidx, wing_indices=widx, cont_abs=ca, cont_scat=cs,
-        transp=tr, valid_mask=valid, asynth=asy, evals_per_depth=evals,
+        transp=tr, valid_mask=valid, asynth=asy, evals_per_depth=evals, reach=reach,
         flux_total_hz=ft, flux_cont_hz=fc, flux_total=ft * conv, flux_cont=fc * conv,
         iterations=iters,
     )

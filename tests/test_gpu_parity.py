@@ -1,0 +1,164 @@
+"""CUDA path against the reference goldens and the CPU oracle (needs a GPU).
+
+Tolerances (written here, from the spec contract):
+* bins (centre/wing) and the TRANSP valid mask: bit-exact;
+* FP64 path: TRANSP/ASYNTH/continuum within 1e-12 relative of the reference,
+  fluxes within 1e-10;
+* mixed path: normalised flux within 1e-4 (absolute, F/Fc is O(1)) and
+  continuum flux within 1e-3 relative of the FP64 reference.
+"""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from _cases import (SMALL_CASES, atm_path, available_cases, gfall_path, golden, golden_valid,
+                    window)
+from kurucz_py_joss_submission_gb300 import _native
+from kurucz_py_joss_submission_gb300.device import (DeviceAtmosphere, DeviceCatalog, DeviceGrid,
+                                                     Synthesizer, make_options, stream_handle)
+from kurucz_py_joss_submission_gb300.engine.continuum import build_depth_continuum
+from kurucz_py_joss_submission_gb300.engine.opacity import _nearest_grid_indices
+from kurucz_py_joss_submission_gb300.engine.radiative import solve_lte_spectrum
+from kurucz_py_joss_submission_gb300.io import atmosphere as atm_io
+from kurucz_py_joss_submission_gb300.io.lines import atomic
+from kurucz_py_joss_submission_gb300.physics.line_opacity import (compute_asynth_from_transp,
+                                                                   compute_transp)
+from oracle import gfall, oracle
+
+pytestmark = pytest.mark.gpu
+
+NORM_TOL = 1e-4
+CONT_TOL = 1e-3
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def catalog(name):
+    w0, w1 = window(name)
+    return atomic.load_catalog_window(gfall_path(name), w0, w1)
+
+
+@pytest.mark.parametrize("name", available_cases())
+def test_centre_bins_bit_exact(name):
+    g = golden(name)
+    cat = catalog(name)
+    assert np.array_equal(_nearest_grid_indices(g["wavelength"], cat.wavelength), g["line_indices"])
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_continuum_fp64_and_mixed(name):
+    g = golden(name)
+    atm = atm_io.load_cached(atm_path(name))
+    ca, cs = build_depth_continuum(atm, g["wavelength"], precision="fp64")
+    assert rel(ca, g["cont_abs"]) < 1e-12 and rel(cs, g["cont_scat"]) < 1e-12
+    ca32, cs32 = build_depth_continuum(atm, g["wavelength"], precision="mixed")
+    assert rel(ca32, g["cont_abs"]) < 1e-4 and rel(cs32, g["cont_scat"]) < 1e-4
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_transp_seam(name):
+    g = golden(name)
+    atm = atm_io.load_cached(atm_path(name))
+    tr, valid, cidx = compute_transp(catalog(name), None, atm, 1e-3, g["cont_abs"] + g["cont_scat"],
+                                     g["wavelength"])
+    assert np.array_equal(valid, golden_valid(g))
+    assert np.array_equal(cidx, g["line_indices"])
+    m = golden_valid(g)
+    assert rel(tr[m], g["transp"][m]) < 1e-12
+    assert np.all(tr[~m] == 0.0)
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_asynth_seam(name):
+    g = golden(name)
+    atm = atm_io.load_cached(atm_path(name))
+    st = {}
+    asy = compute_asynth_from_transp(g["transp"], catalog(name), atm, g["wavelength"],
+                                     valid_mask=golden_valid(g), cutoff=1e-3,
+                                     continuum_absorption=g["cont_abs"] + g["cont_scat"],
+                                     grid_origin=float(g["wavelength"][0]), stats=st)
+    assert rel(asy, g["asynth"]) < 1e-12
+    assert st["device_flags"] == 0
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_formal_solution_seam(name):
+    g = golden(name)
+    atm = atm_io.load_cached(atm_path(name))
+    src = oracle.line_source(oracle.load_atmosphere(atm_path(name)), g["wavelength"])
+    ft, fc = solve_lte_spectrum(g["wavelength"], atm.temperature, atm.depth, g["cont_abs"],
+                                g["cont_scat"], g["asynth"], np.zeros_like(g["asynth"]),
+                                line_source=src, precision="fp64")
+    assert rel(ft, g["flux_total_hz"]) < 1e-10
+    assert rel(fc, g["flux_cont_hz"]) < 1e-10
+
+
+def run_fused(name, precision, **kw):
+    g = golden(name)
+    atm = atm_io.load_cached(atm_path(name))
+    syn = Synthesizer(DeviceCatalog(catalog(name)), DeviceAtmosphere(atm),
+                      DeviceGrid(g["wavelength"]), make_options(precision=precision, **kw))
+    st = syn.run(stats=True)
+    torch.cuda.synchronize()
+    return g, syn, st
+
+
+@pytest.mark.parametrize("name", available_cases())
+def test_fused_fp64_matches_reference(name):
+    g, syn, st = run_fused(name, "fp64")
+    assert st["device_flags"] == 0
+    ft, fc = syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy()
+    assert rel(fc, g["flux_cont_hz"]) < 1e-10
+    assert rel(ft, g["flux_total_hz"]) < 1e-9
+    asy = syn.asynth.cpu().numpy()
+    if "asynth" in g and g["asynth"].shape == asy.shape:
+        assert rel(asy, g["asynth"]) < 1e-12
+    else:
+        assert rel(asy[g["asynth_rows"]], g["asynth"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", available_cases())
+def test_fused_mixed_within_contract(name):
+    g, syn, st = run_fused(name, "mixed")
+    assert st["device_flags"] == 0
+    ft, fc = syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy()
+    nf_ref = g["flux_total_hz"] / g["flux_cont_hz"]
+    assert float(np.max(np.abs(ft / fc - nf_ref))) <= NORM_TOL
+    assert rel(fc, g["flux_cont_hz"]) <= CONT_TOL
+
+
+@pytest.mark.parametrize("name", SMALL_CASES)
+def test_evaluation_count_matches_oracle(name):
+    w0, w1 = window(name)
+    tb = oracle.tables()
+    ocat = gfall.filter_window(gfall.parse_gfall(gfall_path(name), tb["potion"]), w0, w1)
+    ref = oracle.synthesize(oracle.load_atmosphere(atm_path(name)), ocat, w0, w1, tb=tb)
+    _, _, st = run_fused(name, "fp64")
+    assert st["evaluations"] == int(ref["evals_per_depth"].sum())
+    assert st["valid_pairs"] == int(ref["valid_mask"].sum())
+    _, _, st32 = run_fused(name, "mixed")
+    # single-precision gates may differ only for pairs at the cutoff
+    assert abs(st32["valid_pairs"] - st["valid_pairs"]) <= max(2, st["valid_pairs"] // 10000)
+
+
+@pytest.mark.parametrize("tile,warps", [(256, 4), (512, 8), (2048, 8), (1024, 16)])
+def test_tiling_does_not_change_fp64_result(tile, warps):
+    name = "uv_300_302"
+    g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps)
+    assert rel(syn.asynth.cpu().numpy(), g["asynth"]) < 1e-12
+
+
+def test_mixed_is_deterministic():
+    name = "uv_300_302"
+    _, s1, _ = run_fused(name, "mixed")
+    a1 = s1.asynth.cpu().numpy().copy()
+    f1 = s1.flux_total.cpu().numpy().copy()
+    s1.run()
+    torch.cuda.synchronize()
+    assert np.array_equal(a1, s1.asynth.cpu().numpy())
+    assert np.array_equal(f1, s1.flux_total.cpu().numpy())
