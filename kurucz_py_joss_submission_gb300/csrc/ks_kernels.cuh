@@ -975,9 +975,15 @@ __global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __g
         }
         m++;
     }
-    if (m == 0) {
+    if (m < 2) {
+        // fewer than two usable layers: no tau scale to interpolate on (the
+        // reference returns 0 for an empty column and cannot map one layer)
         a.flux_total[j] = 0.0;
         a.flux_cont[j] = 0.0;
+        if (a.iters) {
+            a.iters[2 * j] = 0;
+            a.iters[2 * j + 1] = 0;
+        }
         return;
     }
     if (m > 1 && !(mass[0] < mass[m - 1])) {
