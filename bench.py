@@ -1,0 +1,403 @@
+"""Benchmark of the GB300 line-opacity + transfer path (one JSON line).
+
+Workload (``full_300_1800``): one synthetic grey atmosphere (Teff 5800 K,
+log g 4.44, 72 layers, converted by the reference's own converter), the
+300-1800 nm grid at R = 300000 (537,529 points) and 1.5M seeded atomic lines
+(gfall format, log-uniform in wavelength).  A step is one full synthesis --
+continuum, TRANSP, ASYNTH, line source, JOSH flux and continuum flux for
+every grid point -- with inputs resident in HBM.  The metric is
+line.depth.lambda evaluations per second (the exact count of opacity
+contributions accumulated, as the reference's wing loops count them); the
+line also carries spectra/s, ``e2e`` (same metric through the public API
+from pinned host buffers, copies inside the timed region), the live
+roofline of the dominant kernel and the CPU baseline.
+
+``--impl reference`` times the CPU restatement of the reference path
+(``oracle/``, C + OpenMP on every host core) on a bounded sample of the
+same workload; the reference itself is pure Python/Numba and cannot run on
+the GPU host.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(name="full_300_1800", teff=5800.0, logg=4.44, wl_start=300.0, wl_end=1800.0,
+                resolution=300000.0, n_lines=1_500_000, seed=20241, atm="atm_t5800g444.npz")
+METRIC = "line.depth.lambda evaluations/s (spectra/s alongside), <=1e-4 rel flux err vs FP64, 1xGB300"
+# FP32 work per accumulated contribution: the far-wing value X/o^2 shared by
+# the red and blue bin (1 mul + 1 fast divide = 2 flops per 2 contributions)
+# plus the Kahan-compensated add (4 flops): 5 flops per contribution.
+FLOPS_PER_EVAL = 5.0
+# CPU-baseline sample: 12 windows of 40 nm spread log-uniformly over 300-1800 nm
+SAMPLE_WINDOWS = [(float(a), float(a) + 40.0) for a in np.exp(np.linspace(np.log(305.0), np.log(1750.0), 12))]
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload_catalog_path() -> Path:
+    from kurucz_py_joss_submission_gb300 import workloads
+
+    tmp = Path(os.environ.get("TMPDIR", "/tmp"))
+    p = tmp / f"kgb300_{WORKLOAD['name']}_{WORKLOAD['seed']}.gf"
+    if not p.exists():
+        t = time.time()
+        d = workloads.random_atomic_lines(WORKLOAD["n_lines"], WORKLOAD["wl_start"], WORKLOAD["wl_end"],
+                                          WORKLOAD["seed"], log_uniform=True)
+        tmpname = p.with_suffix(f".{os.getpid()}.tmp")
+        workloads.write_gfall(tmpname, d)
+        os.replace(tmpname, p)
+        log(f"generated {p} in {time.time() - t:.1f}s")
+    return p
+
+
+def wavelength_grid(w0=None, w1=None):
+    from kurucz_py_joss_submission_gb300 import _native
+
+    w0 = WORKLOAD["wl_start"] if w0 is None else w0
+    w1 = WORKLOAD["wl_end"] if w1 is None else w1
+    L = _native.load()
+    n = L.ks_wavelength_grid(w0, w1, WORKLOAD["resolution"], None, 0)
+    g = np.zeros(n)
+    L.ks_wavelength_grid(w0, w1, WORKLOAD["resolution"], g.ctypes.data_as(_native.PD), n)
+    return g
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the accumulation kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "accumulate_kernel_full_300_1800.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_full_size"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def cpu_baseline(cat_path: Path, steps: int = 1):
+    """Oracle port on the sample windows with every host thread: evals/s."""
+    from oracle import gfall, oracle
+
+    oracle.build()
+    tb = oracle.tables()
+    atm = oracle.load_atmosphere(ROOT / "tests" / "golden" / WORKLOAD["atm"])
+    full = gfall.parse_gfall  # noqa: F841 (the restated parser is slow; use the native reader)
+    from kurucz_py_joss_submission_gb300.io.lines import atomic
+
+    cats = []
+    for w0, w1 in SAMPLE_WINDOWS:
+        c = atomic.load_catalog_window(cat_path, w0, w1, sort=False)
+        cats.append(dict(wavelength=c.wavelength, log_gf=c.log_gf, code=c.code,
+                         excitation_energy=c.excitation_energy, gamma_rad=c.gamma_rad,
+                         gamma_stark=c.gamma_stark, gamma_vdw=c.gamma_vdw,
+                         nelem=c.element_idx + 1, ion_stage=c.ion_stages, line_type=c.line_types,
+                         n_lower=np.zeros(len(c), np.int32), n_upper=np.zeros(len(c), np.int32),
+                         line_size=np.zeros(len(c), np.int32)))
+    threads = oracle.num_threads()
+    tot_t, tot_e, tot_pts = 0.0, 0, 0
+    for _ in range(steps):
+        for (w0, w1), c in zip(SAMPLE_WINDOWS, cats):
+            t = time.perf_counter()
+            r = oracle.synthesize(atm, c, w0, w1, WORKLOAD["resolution"], tb=tb)
+            tot_t += time.perf_counter() - t
+            tot_e += int(r["evals_per_depth"].sum())
+            tot_pts += r["wavelength"].size
+    return dict(evals_per_s=tot_e / tot_t, seconds=tot_t, evals=tot_e, points=tot_pts,
+                threads=threads)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cat_path = workload_catalog_path()
+    n_full = 537529
+    for _ in range(max(args.warmup, 0)):
+        pass  # the CPU port has no warm-up state; each step is a fresh sample
+    res = cpu_baseline(cat_path, steps=max(1, args.steps))
+    spectra = (res["points"] / n_full) / res["seconds"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": res["evals_per_s"], "unit": "evals/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * res["seconds"] / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], "n_lines": WORKLOAD["n_lines"],
+                   "n_wavelengths": n_full, "n_layers": 72},
+        "spectra_per_s": spectra,
+        "cpu_baseline": {"value": res["evals_per_s"], "unit": "evals/s", "cores": res["threads"],
+                         "kind": "port",
+                         "sample": f"{len(SAMPLE_WINDOWS)} windows x 40 nm of the workload "
+                                   f"({res['points']} grid points, {res['evals']} evaluations) per step"},
+        "e2e": {"value": res["evals_per_s"], "unit": "evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from kurucz_py_joss_submission_gb300 import _native
+    from kurucz_py_joss_submission_gb300.device import (DeviceAtmosphere, DeviceCatalog, DeviceGrid,
+                                                         Synthesizer, make_options)
+    from kurucz_py_joss_submission_gb300.io import atmosphere as atm_io
+    from kurucz_py_joss_submission_gb300.io.lines import atomic
+
+    cat_path = workload_catalog_path()
+    t = time.time()
+    w0, w1 = (args.window if args.window else (WORKLOAD["wl_start"], WORKLOAD["wl_end"]))
+    cat = atomic.load_catalog_window(cat_path, w0, w1, sort=True)
+    atm = atm_io.load_cached(ROOT / "tests" / "golden" / WORKLOAD["atm"])
+    grid = wavelength_grid(w0, w1)
+    log(f"catalog {len(cat)} lines, grid {grid.size} points, setup {time.time() - t:.1f}s")
+    dcat, datm, dgrid = DeviceCatalog(cat, dev), DeviceAtmosphere(atm, dev), DeviceGrid(grid, device=dev)
+    opt = make_options(precision=args.precision, tile_bins=args.tile_bins,
+                       warps_per_tile=args.warps_per_tile)
+    syn = Synthesizer(dcat, datm, dgrid, opt, keep_asynth=False)
+    st = syn.run(stats=True)
+    evals = st["evaluations"]
+    launches = st["kernel_launches"]
+    log(f"stats {st}")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        syn.run()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record()
+        for _ in range(args.steps):
+            syn.run()
+        e1.record()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_step = ms / args.steps
+    value = world * evals * args.steps / (ms / 1e3)
+    spectra = world * args.steps / (ms / 1e3)
+
+    # per-stage device times (CUDA events inside the library), for the roofline
+    prof = Synthesizer(dcat, datm, dgrid, make_options(precision=args.precision, tile_bins=args.tile_bins,
+                                                       warps_per_tile=args.warps_per_tile, profile=True),
+                       keep_asynth=False)
+    stage = {k: [] for k in ("accumulate", "transfer", "pair_setup", "continuum", "partition", "bins_prep", "total")}
+    for _ in range(max(3, min(args.steps, 5))):
+        s = prof.run(stats=True)["stage_ms"]
+        for k in stage:
+            stage[k].append(s[k])
+    stage_ms = {k: statistics.median(v) for k, v in stage.items()}
+    del prof
+
+    # end to end: pinned host inputs -> H2D -> synthesis -> D2H of both fluxes
+    host = {}
+    h2d = 0
+    for name, tns in list(dcat.t.items()) + list(datm.t.items()) + [("grid", dgrid.wavelength)]:
+        hp = torch.empty(tns.shape, dtype=tns.dtype, pin_memory=True)
+        hp.copy_(tns.cpu())
+        host[name] = (hp, tns)
+        h2d += hp.numel() * hp.element_size()
+    out_t = torch.empty(grid.size, dtype=torch.float64, pin_memory=True)
+    out_c = torch.empty(grid.size, dtype=torch.float64, pin_memory=True)
+    d2h = 2 * grid.size * 8
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    e0.record()
+    for _ in range(e2e_steps):
+        for hp, tns in host.values():
+            tns.copy_(hp, non_blocking=True)
+        syn.run()
+        out_t.copy_(syn.flux_total, non_blocking=True)
+        out_c.copy_(syn.flux_cont, non_blocking=True)
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_value = world * evals / (e2e_ms / 1e3)
+
+    line = None
+    if rank == 0:
+        # accuracy of this precision against the all-FP64 path on the same inputs
+        ft = syn.flux_total.cpu().numpy().copy()
+        fc = syn.flux_cont.cpu().numpy().copy()
+        err = None
+        if args.precision != "fp64" and not args.skip_fp64_check:
+            ref = Synthesizer(dcat, datm, dgrid, make_options(precision="fp64"), keep_asynth=False)
+            ref.run()
+            torch.cuda.synchronize()
+            ft64 = ref.flux_total.cpu().numpy()
+            fc64 = ref.flux_cont.cpu().numpy()
+            d = ft / fc - ft64 / fc64
+            err = {"norm_flux_max_abs": float(np.max(np.abs(d))), "norm_flux_rms": float(np.sqrt(np.mean(d * d))),
+                   "cont_flux_max_rel": float(np.max(np.abs(fc / fc64 - 1.0)))}
+            del ref
+        hbm_peak, peak_kind = measured_peaks()
+        acc_ms = stage_ms["accumulate"]
+        L = atm.layers
+        acc_bytes = st["valid_pairs"] * 36.0 + L * grid.size * 4.0   # descriptors + positions in, ASYNTH out
+        achieved_gbs = acc_bytes / (acc_ms / 1e3) / 1e9
+        traffic = ncu_traffic()
+        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        cpu = cpu_baseline(cat_path) if not args.skip_cpu else None
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD["name"] + (f"[{w0}-{w1} nm]" if args.window else ""),
+                       "n_lines": len(cat), "n_wavelengths": int(grid.size),
+                       "n_layers": int(L), "precision": args.precision,
+                       "l2": "inputs larger than L2 (pair descriptors ~2 GB, opacity cubes ~0.3 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "spectra_per_s": spectra,
+            "evaluations_per_step": evals,
+            "valid_pairs": st["valid_pairs"],
+            "stage_ms": stage_ms,
+            "accuracy_vs_fp64": err,
+            "e2e": {"value": e2e_value, "unit": "evals/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches * args.steps),
+            "clocks": clk.summary(),
+            "roofline": {"bound": "hbm", "kernel": "accumulate_kernel", "achieved": achieved_gbs,
+                         "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                         "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": acc_bytes},
+            "roofline_fp32": {"kernel": "accumulate_kernel",
+                              "achieved": evals * FLOPS_PER_EVAL / (acc_ms / 1e3) / 1e12,
+                              "peak": fp32_peak, "unit": "TFLOP/s",
+                              "frac": evals * FLOPS_PER_EVAL / (acc_ms / 1e3) / 1e12 / fp32_peak,
+                              "peak_kind": "nominal (152 SM x 128 lanes x 2 x 2.07 GHz)"},
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = {"value": cpu["evals_per_s"], "unit": "evals/s", "cores": cpu["threads"],
+                                    "kind": "port",
+                                    "sample": f"{len(SAMPLE_WINDOWS)} windows x 40 nm of the workload "
+                                              f"({cpu['points']} points, {cpu['evals']} evaluations, "
+                                              f"{cpu['seconds']:.1f} s)"}
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--tile-bins", type=int, default=0)
+    ap.add_argument("--warps-per-tile", type=int, default=0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64-check", action="store_true")
+    ap.add_argument("--window", type=float, nargs=2, default=None,
+                    help="restrict the workload to a wavelength window (small profiling case)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -108,7 +108,8 @@ typedef struct {
     int32_t precision;      /* ks_precision */
     int32_t tile_bins;      /* accumulation tile width; 0 = autotuned default */
     int32_t warps_per_tile; /* warps per accumulation CTA; 0 = default */
-    int32_t reserved;
+    int32_t profile;        /* 1: time each stage with CUDA events into ks_stats.stage_ms
+                               (only when a ks_stats pointer is given) */
 } ks_options;
 
 /* Counters of one synthesis (filled when a pointer is given). */
@@ -118,7 +119,9 @@ typedef struct {
     int64_t maxj_wavelengths;   /* total-flux solves that took the MAXJ=1 path */
     int64_t iterations;         /* Gauss-Seidel sweeps summed over all solves */
     int32_t device_flags;       /* nonzero when a kernel hit an internal limit */
-    int32_t reserved;
+    int32_t kernel_launches;    /* kernels this call launched */
+    float stage_ms[8];          /* with ks_options.profile: bins+prep, continuum, pair setup,
+                                   partition, accumulation, transfer, (unused), total */
 } ks_stats;
 
 /* ---- library ---------------------------------------------------------- */

@@ -69,7 +69,7 @@ class KsOptions(C.Structure):
     _fields_ = [
         ("cutoff", C.c_double), ("microturb_kms", C.c_double), ("rhoxj", C.c_double),
         ("precision", C.c_int32), ("tile_bins", C.c_int32), ("warps_per_tile", C.c_int32),
-        ("reserved", C.c_int32),
+        ("profile", C.c_int32),
     ]
 
 
@@ -77,11 +77,17 @@ class KsStats(C.Structure):
     _fields_ = [
         ("valid_pairs", C.c_int64), ("evaluations", C.c_int64),
         ("maxj_wavelengths", C.c_int64), ("iterations", C.c_int64),
-        ("device_flags", C.c_int32), ("reserved", C.c_int32),
+        ("device_flags", C.c_int32), ("kernel_launches", C.c_int32),
+        ("stage_ms", C.c_float * 8),
     ]
 
+    STAGES = ("bins_prep", "continuum", "pair_setup", "partition", "accumulate", "transfer",
+              "unused", "total")
+
     def as_dict(self) -> dict:
-        return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "stage_ms"}
+        d["stage_ms"] = {n: float(v) for n, v in zip(self.STAGES, self.stage_ms) if n != "unused"}
+        return d
 
 
 # exported symbol -> (restype, argtypes)

@@ -56,6 +56,7 @@ __device__ float g_h0f[VOIGT_N], g_h1f[VOIGT_N], g_h2f[VOIGT_N];
 __device__ double g_extab[EXP_N], g_extabf[EXP_N];
 __device__ float g_extab_f[EXP_N], g_extabf_f[EXP_N];
 __device__ double g_xtau[NXTAU], g_ch[NXTAU];
+__device__ float g_coefj32[NXTAU * NXTAU];
 
 struct HostTables {
     bool ready = false;
@@ -67,7 +68,7 @@ static std::mutex g_tables_mu;
 
 struct DevTables {
     const double *h0d, *h1d, *h2d, *extab, *extabf, *xtau, *ch;
-    const float *h0f, *h1f, *h2f, *extab_f, *extabf_f;
+    const float *h0f, *h1f, *h2f, *extab_f, *extabf_f, *coefj32;
 };
 static const int kMaxDevices = 64;
 static bool g_dev_ready[kMaxDevices];
@@ -233,6 +234,7 @@ static ks_status device_tables(DevTables* out) {
         KS_CUDA(cudaMemcpyToSymbol(g_extabf_f, eff.data(), sizeof(float) * EXP_N));
         KS_CUDA(cudaMemcpyToSymbol(g_xtau, t.xtau.data(), sizeof(double) * NXTAU));
         KS_CUDA(cudaMemcpyToSymbol(g_ch, t.ch.data(), sizeof(double) * NXTAU));
+        KS_CUDA(cudaMemcpyToSymbol(g_coefj32, t.cj.c, sizeof(float) * NXTAU * NXTAU));
         DevTables d;
         const void* p;
         KS_CUDA(sym_addr(g_h0d, &p)); d.h0d = (const double*)p;
@@ -247,6 +249,7 @@ static ks_status device_tables(DevTables* out) {
         KS_CUDA(sym_addr(g_extabf_f, &p)); d.extabf_f = (const float*)p;
         KS_CUDA(sym_addr(g_xtau, &p)); d.xtau = (const double*)p;
         KS_CUDA(sym_addr(g_ch, &p)); d.ch = (const double*)p;
+        KS_CUDA(sym_addr(g_coefj32, &p)); d.coefj32 = (const float*)p;
         g_dev[dev] = d;
         g_dev_ready[dev] = true;
     }
@@ -728,6 +731,7 @@ static TransferArgs transfer_args(const ks_atmos* atm, const ks_grid* g, const W
     a.depth = w.depth;
     a.xtau = t.xtau;
     a.ch = t.ch;
+    a.coefj32 = t.coefj32;
     a.flux_total = ft;
     a.flux_cont = fc;
     a.iters = w.iters;
@@ -918,11 +922,41 @@ extern "C" ks_status ks_formal_solution(const ks_atmos* atm, const ks_grid* grid
     return KS_OK;
 }
 
+// Optional per-stage CUDA events of one synthesis (ks_options.profile).
+struct StageTimer {
+    bool on = false;
+    cudaEvent_t ev[8];
+    int n = 0;
+    cudaStream_t s = nullptr;
+    void start(cudaStream_t st, bool enable) {
+        on = enable;
+        s = st;
+        if (!on) return;
+        for (int i = 0; i < 8; i++) cudaEventCreate(&ev[i]);
+        cudaEventRecord(ev[0], s);
+        n = 1;
+    }
+    void mark() {
+        if (on && n < 8) cudaEventRecord(ev[n++], s);
+    }
+    void finish(ks_stats* stats) {
+        if (!on) return;
+        cudaEventSynchronize(ev[n - 1]);
+        if (stats) {
+            for (int i = 0; i < 8; i++) stats->stage_ms[i] = 0.f;
+            for (int i = 1; i < n && i <= 6; i++) cudaEventElapsedTime(&stats->stage_ms[i - 1], ev[i - 1], ev[i]);
+            cudaEventElapsedTime(&stats->stage_ms[7], ev[0], ev[n - 1]);
+        }
+        for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
+        on = false;
+    }
+};
+
 template <typename R>
 static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
                                  const ks_options* opt, Workspace& w, const DevTables& t,
                                  double* flux_total, double* flux_cont, R* asynth,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, StageTimer& tm) {
     constexpr bool fp64 = sizeof(R) == 8;
     ks_status st;
     const int L = atm->n_layers;
@@ -934,23 +968,26 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
     ContArgs ca = cont_args(atm, grid);
     R* cabs = (R*)w.cont_abs;
     R* cscat = (R*)w.cont_scat;
-    if constexpr (fp64) {
-        KS_CUDA(launch_prep_f64(pa, s));
-        KS_CUDA(launch_continuum_f64(ca, cabs, cscat, s));
-    } else {
-        KS_CUDA(launch_prep_f32(pa, s));
-        KS_CUDA(launch_continuum_f32(ca, cabs, cscat, s));
-    }
+    if constexpr (fp64) KS_CUDA(launch_prep_f64(pa, s));
+    else KS_CUDA(launch_prep_f32(pa, s));
+    tm.mark();
+    if constexpr (fp64) KS_CUDA(launch_continuum_f64(ca, cabs, cscat, s));
+    else KS_CUDA(launch_continuum_f32(ca, cabs, cscat, s));
+    tm.mark();
     if (lines->n_lines > 0) {
         PairArgs p = pair_args(lines, atm, grid, opt, w, t);
         if constexpr (fp64)
             KS_CUDA(launch_pair_setup_f64(p, true, cabs, cscat, (PairDesc<double>*)w.desc, w.cls, s));
         else
             KS_CUDA(launch_pair_setup_f32(p, true, cabs, cscat, (PairDesc<float>*)w.desc, w.cls, s));
+        tm.mark();
         if ((st = run_partition(w, L, s))) return st;
+        tm.mark();
     } else {
         // no lines: every class list is empty
         KS_CUDA(cudaMemsetAsync(w.class_off, 0, sizeof(int64_t) * L * (N_REACH_CLASSES + 1), s));
+        tm.mark();
+        tm.mark();
     }
     AccArgs a = acc_args(lines, atm, grid, opt, w, t, fp64);
     int warps = default_warps(opt);
@@ -958,11 +995,13 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f64(a, warps, (const PairDesc<double>*)w.desc, asynth, s));
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
+    tm.mark();
     TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, true, fp64);
     if constexpr (fp64)
         KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
     else
         KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
+    tm.mark();
     return KS_OK;
 }
 
@@ -993,9 +1032,16 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     Carve c{(char*)workspace, workspace_bytes, 0, false};
     layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
     void* asy = asynth_out ? asynth_out : w.asynth;
-    if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s);
-    else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s);
+    StageTimer tm;
+    tm.start(s, stats && opt && opt->profile);
+    if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s, tm);
+    else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s, tm);
+    tm.finish(stats);
     if (st) return st;
-    if (stats) return collect_stats(w, grid->n, stats, s);
+    if (stats) {
+        st = collect_stats(w, grid->n, stats, s);
+        stats->kernel_launches = lines->n_lines > 0 ? 10 : 7;
+        return st;
+    }
     return KS_OK;
 }

@@ -440,35 +440,52 @@ __device__ __forceinline__ int64_t lower_bound_pos(const int32_t* __restrict__ p
     return lo;
 }
 
+// Shared-memory accumulator cell of one bin in one warp's copy of the tile:
+// Kahan (sum, compensation) in FP32, a plain sum in FP64.
+template <typename R> struct Cell;
+template <> struct Cell<float> { using T = float2; };
+template <> struct Cell<double> { using T = double; };
+
+__device__ __forceinline__ void cell_add(float2* c, int b, float v) {
+    float2 t = c[b];
+    kahan_add(t.x, t.y, v);
+    c[b] = t;
+}
+__device__ __forceinline__ void cell_add(double* c, int b, double v) { c[b] += v; }
+
 // One CTA per (lambda tile, depth).  For every reach class k it selects the
 // pairs whose wing centre lies within 2^k (+1) bins of the tile -- a
-// contiguous range of that class's centre-sorted list -- and gives them to
-// its warps in a fixed round-robin order.  A warp adds one pair at a time
-// into its own shared-memory copy of the tile (lanes take consecutive wing
-// offsets; each offset's profile value goes to the red bin c+o and the blue
-// bin c-o), so no two lanes ever write the same word and no atomics are
-// needed.  The copies are then summed in a fixed order, multiplied by STIM
-// (line_opacity.py:1338) and written with coalesced stores.
+// contiguous range of that class's centre-sorted list.  Warps take those
+// pairs in batches of 32 (batch b -> warp b mod nwarps, a fixed order): each
+// lane loads one pair's descriptor, then the warp walks the 32 pairs,
+// broadcasting each descriptor by shuffles.  For a pair, lanes take
+// consecutive wing offsets; each offset's profile value goes to the red bin
+// c+o and the blue bin c-o of the warp's own shared-memory copy of the tile,
+// so no two lanes write the same word and no atomics are needed.  Near-wing
+// and far-wing offsets run in separate loops (no divergence between the
+// table/Voigt branch and X/o^2).  The copies are summed in warp order,
+// multiplied by STIM (line_opacity.py:1338) and stored coalesced.
 template <typename R>
-__global__ void __launch_bounds__(256) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
+__global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
                                                          R* __restrict__ out) {
+    using CellT = typename Cell<R>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int W = a.tile_bins;
     const int nwarps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int d = blockIdx.y;
-    const int64_t T0 = (int64_t)blockIdx.x * W;
-    const int64_t T1 = min(T0 + (int64_t)W, a.n_wl);
-    const int span = (int)(T1 - T0);
+    const int T0 = blockIdx.x * W;
+    const int T1 = (int)min((int64_t)T0 + W, a.n_wl);
+    const int span = T1 - T0;
 
-    R* tab = reinterpret_cast<R*>(smem_raw);  // h0[VOIGT_N], h1[VOIGT_N]
-    R* sh0 = tab;
-    R* sh1 = tab + VOIGT_N;
+    R* sh0 = reinterpret_cast<R*>(smem_raw);
+    R* sh1 = sh0 + VOIGT_N;
     size_t tab_bytes = (2 * VOIGT_N * sizeof(R) + 15) & ~size_t(15);
-    R* acc = reinterpret_cast<R*>(smem_raw + tab_bytes);  // [nwarps][2][W] (float) or [nwarps][W]
-    __shared__ int64_t cls_lo[N_REACH_CLASSES], cls_hi[N_REACH_CLASSES];
+    CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
+    __shared__ int64_t cls_lo[N_REACH_CLASSES];
     __shared__ int64_t cls_base[N_REACH_CLASSES + 1];
+    __shared__ int64_t cls_hi_s[N_REACH_CLASSES];
 
     const R* gh0 = sizeof(R) == 8 ? (const R*)a.h0d : (const R*)a.h0f;
     const R* gh1 = sizeof(R) == 8 ? (const R*)a.h1d : (const R*)a.h1f;
@@ -477,73 +494,101 @@ __global__ void __launch_bounds__(256) accumulate_kernel(AccArgs a, const PairDe
         sh0[i] = gh0[i];
         sh1[i] = gh1[i];
     }
-    const int acc_stride = (sizeof(R) == 4) ? 2 * W : W;
-    for (int i = threadIdx.x; i < nwarps * acc_stride; i += blockDim.x) acc[i] = R(0);
+    for (int i = threadIdx.x; i < nwarps * W; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) acc[i] = make_float2(0.f, 0.f);
+        else acc[i] = 0.0;
+    }
     if (threadIdx.x < N_REACH_CLASSES) {
         int k = threadIdx.x;
         const int64_t* off = a.class_off + (int64_t)d * (N_REACH_CLASSES + 1);
         int64_t lo = off[k], hi = off[k + 1];
         int64_t h = class_halo(k) + 1;
-        int64_t s = lower_bound_pos(a.class_pos, lo, hi, a.wing_idx, T0 - h);
-        int64_t t = lower_bound_pos(a.class_pos, s, hi, a.wing_idx, T1 + h);
-        cls_lo[k] = s;
-        cls_hi[k] = t;
+        int64_t s0 = lower_bound_pos(a.class_pos, lo, hi, a.wing_idx, (int64_t)T0 - h);
+        int64_t s1 = lower_bound_pos(a.class_pos, s0, hi, a.wing_idx, (int64_t)T1 + h);
+        cls_lo[k] = s0;
+        cls_hi_s[k] = s1;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         int64_t b = 0;
         for (int k = 0; k < N_REACH_CLASSES; k++) {
             cls_base[k] = b;
-            b += cls_hi[k] - cls_lo[k];
+            b += cls_hi_s[k] - cls_lo[k];
         }
         cls_base[N_REACH_CLASSES] = b;
     }
     __syncthreads();
 
-    R* my_sum = acc + warp * acc_stride;
-    R* my_cmp = (sizeof(R) == 4) ? my_sum + W : nullptr;
+    CellT* my = acc + warp * W;
     const int64_t total = cls_base[N_REACH_CLASSES];
     const PairDesc<R>* drow = desc + (int64_t)d * a.stride;
-    int k = 0;
     int64_t evals = 0;
-    for (int64_t item = warp; item < total; item += nwarps) {
-        while (item >= cls_base[k + 1]) k++;
-        int64_t p = a.class_pos[cls_lo[k] + (item - cls_base[k])];
-        const PairDesc<R> pd = drow[p];
-        const int64_t c = pd.wing_c;
-        // centre contribution
-        int ctr = pd.ctr_n10 & 15;
-        if (ctr) {
-            int64_t cb = c + (ctr - 8);
-            if (cb >= T0 && cb < T1) {
-                if (lane == 0) acc_add<R>(my_sum, my_cmp, (int)(cb - T0), pd.kapcen);
-                evals++;
-            }
+    const int64_t nbatch = (total + 31) >> 5;
+    for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
+        // each lane fetches one descriptor of the batch
+        int64_t item = bt * 32 + lane;
+        PairDesc<R> mine;
+        mine.maxstep_far = 0;
+        mine.ctr_n10 = 0;
+        mine.wing_c = 0;
+        mine.kappa0 = mine.adamp = mine.dvoigt = mine.xfar = mine.kapcen = R(0);
+        if (item < total) {
+            int k = 0;
+            while (item >= cls_base[k + 1]) k++;
+            int64_t p = a.class_pos[cls_lo[k] + (item - cls_base[k])];
+            mine = drow[p];
         }
-        const int reach = pd.maxstep_far & 0x7fffffff;
-        if (reach == 0) continue;
-        const bool far = pd.maxstep_far < 0;
-        const int n10 = pd.ctr_n10 >> 8;
-        // red offsets: c + o in [T0, T1); blue offsets: c - o in [T0, T1)
-        int64_t rlo = max((int64_t)1, T0 - c), rhi = min((int64_t)reach, T1 - 1 - c);
-        int64_t blo = max((int64_t)1, c - (T1 - 1)), bhi = min((int64_t)reach, c - T0);
-        bool rr = rlo <= rhi, bb = blo <= bhi;
-        if (!rr && !bb) continue;
-        int64_t olo = rr ? (bb ? min(rlo, blo) : rlo) : blo;
-        int64_t ohi = rr ? (bb ? max(rhi, bhi) : rhi) : bhi;
-        evals += (rr ? rhi - rlo + 1 : 0) + (bb ? bhi - blo + 1 : 0);
-        const R k0 = pd.kappa0, ad = pd.adamp, dv = pd.dvoigt, xf = pd.xfar;
-        for (int64_t o = olo + lane; o <= ohi; o += 32) {
-            R v;
-            if (far && o > n10) {
-                R oo = (R)o * (R)o;
-                if (sizeof(R) == 4) v = (R)__fdividef((float)xf, (float)oo);
-                else v = xf / oo;
-            } else {
-                v = near_profile<R>((int)o, dv, ad, k0, sh0, sh1, gh2);
+        const int nb = (int)min((int64_t)32, total - bt * 32);
+        for (int i = 0; i < nb; i++) {
+            const int c = __shfl_sync(0xffffffffu, mine.wing_c, i);
+            const int ms = __shfl_sync(0xffffffffu, mine.maxstep_far, i);
+            const int cn = __shfl_sync(0xffffffffu, mine.ctr_n10, i);
+            const int ctr = cn & 15;
+            if (ctr) {
+                const int cb = c + (ctr - 8);
+                if (cb >= T0 && cb < T1) {
+                    const R kc = __shfl_sync(0xffffffffu, mine.kapcen, i);
+                    if (lane == 0) cell_add(my, cb - T0, kc);
+                    evals++;
+                }
             }
-            if (rr && o >= rlo && o <= rhi) acc_add<R>(my_sum, my_cmp, (int)(c + o - T0), v);
-            if (bb && o >= blo && o <= bhi) acc_add<R>(my_sum, my_cmp, (int)(c - o - T0), v);
+            const int reach = ms & 0x7fffffff;
+            if (reach == 0) continue;
+            // red offsets: c + o in [T0, T1); blue offsets: c - o in [T0, T1)
+            const int rlo = max(1, T0 - c), rhi = min(reach, T1 - 1 - c);
+            const int blo = max(1, c - (T1 - 1)), bhi = min(reach, c - T0);
+            const bool rr = rlo <= rhi, bb = blo <= bhi;
+            if (!rr && !bb) continue;
+            const int olo = rr ? (bb ? min(rlo, blo) : rlo) : blo;
+            const int ohi = rr ? (bb ? max(rhi, bhi) : rhi) : bhi;
+            evals += (rr ? rhi - rlo + 1 : 0) + (bb ? bhi - blo + 1 : 0);
+            const bool far = ms < 0;
+            const int n10 = cn >> 8;
+            const int near_hi = far ? min(ohi, n10) : ohi;
+            if (olo <= near_hi) {
+                const R k0 = __shfl_sync(0xffffffffu, mine.kappa0, i);
+                const R ad = __shfl_sync(0xffffffffu, mine.adamp, i);
+                const R dv = __shfl_sync(0xffffffffu, mine.dvoigt, i);
+                for (int o = olo + lane; o <= near_hi; o += 32) {
+                    R v = near_profile<R>(o, dv, ad, k0, sh0, sh1, gh2);
+                    if (rr && o >= rlo && o <= rhi) cell_add(my, c + o - T0, v);
+                    if (bb && o >= blo && o <= bhi) cell_add(my, c - o - T0, v);
+                }
+            }
+            if (far) {
+                const int flo = max(olo, n10 + 1);
+                if (flo <= ohi) {
+                    const R xf = __shfl_sync(0xffffffffu, mine.xfar, i);
+                    for (int o = flo + lane; o <= ohi; o += 32) {
+                        R oo = (R)o * (R)o;
+                        R v;
+                        if constexpr (sizeof(R) == 4) v = __fdividef(xf, oo);
+                        else v = xf / oo;
+                        if (rr && o >= rlo && o <= rhi) cell_add(my, c + o - T0, v);
+                        if (bb && o >= blo && o <= bhi) cell_add(my, c - o - T0, v);
+                    }
+                }
+            }
         }
     }
     __syncthreads();
@@ -551,26 +596,25 @@ __global__ void __launch_bounds__(256) accumulate_kernel(AccArgs a, const PairDe
     const DepthPar dp = a.depth[d];
     for (int b = threadIdx.x; b < span; b += blockDim.x) {
         R v;
-        if (sizeof(R) == 4) {
+        if constexpr (sizeof(R) == 4) {
             float s = 0.f, cp = 0.f;
             for (int w = 0; w < nwarps; w++) {
-                const float* ws = reinterpret_cast<const float*>(acc) + w * acc_stride;
-                kahan_add(s, cp, ws[b]);
-                kahan_add(s, cp, -ws[W + b]);
+                float2 t = acc[w * W + b];
+                kahan_add(s, cp, t.x);
+                kahan_add(s, cp, -t.y);
             }
             float freq = (float)(C_LIGHT_NM / a.grid[T0 + b]);
-            float stim = 1.0f - __expf(-freq * (float)dp.hkt_asynth);
-            v = (R)(s * stim);
+            float stim = -expm1f(-freq * (float)dp.hkt_asynth);
+            v = s * stim;
         } else {
             double s = 0.0;
-            for (int w = 0; w < nwarps; w++) s += (double)acc[w * acc_stride + b];
+            for (int w = 0; w < nwarps; w++) s += acc[w * W + b];
             double freq = C_LIGHT_NM / a.grid[T0 + b];
             double stim = 1.0 - exp(-freq * dp.hkt_asynth);
             v = (R)(s * stim);
         }
         out[(int64_t)d * a.n_wl + T0 + b] = v;
     }
-    // evaluation counter (lane 0 of each warp holds the warp's count)
     if (a.evals && lane == 0 && evals) atomicAdd((unsigned long long*)a.evals, (unsigned long long)evals);
 }
 
@@ -827,7 +871,8 @@ __device__ __forceinline__ int josh_sweeps_fast(const CoefJ32& cj, const float* 
 template <typename R, bool REF_SWEEP>
 __device__ double josh_flux(int n, const R* acont, const R* scont, const R* aline, const R* sline,
                             const R* sigmac, const R* sigmal, const R* rho, const R* xtau,
-                            const double* ch, const CoefJ32& cj, int* iters_out) {
+                            const double* ch, const CoefJ32& cj, const float* coefj_ref,
+                            int* iters_out) {
     R abtot[MAX_LAYERS], alpha[MAX_LAYERS], snubar[MAX_LAYERS], taunu[MAX_LAYERS];
     const R eps = (R)EPS38;
     for (int j = 0; j < n; j++) {
@@ -885,7 +930,7 @@ __device__ double josh_flux(int n, const R* acont, const R* scont, const R* alin
         xm32[l] = (float)(xb * (R(1) - xa));
     }
     int it;
-    if (REF_SWEEP) it = josh_sweeps_ref(cj.c, xs32, xa32, xm32);
+    if (REF_SWEEP) it = josh_sweeps_ref(coefj_ref, xs32, xa32, xm32);
     else it = josh_sweeps_fast(cj, xa32, xm32, xs32);
     *iters_out = it;
     double flux = 0.0;
@@ -1009,8 +1054,8 @@ __global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __g
     R xtau[NXTAU];
     for (int l = 0; l < NXTAU; l++) xtau[l] = (R)a.xtau[l];
     int itc = 0, itt = 0;
-    double fc = josh_flux<R, REF_SWEEP>(m, ca, pl, zero, pl, cs, zero, mass, xtau, a.ch, cj, &itc);
-    double ft = josh_flux<R, REF_SWEEP>(m, ca, pl, la, src, cs, ls, mass, xtau, a.ch, cj, &itt);
+    double fc = josh_flux<R, REF_SWEEP>(m, ca, pl, zero, pl, cs, zero, mass, xtau, a.ch, cj, a.coefj32, &itc);
+    double ft = josh_flux<R, REF_SWEEP>(m, ca, pl, la, src, cs, ls, mass, xtau, a.ch, cj, a.coefj32, &itt);
     a.flux_cont[j] = fc;
     a.flux_total[j] = ft;
     if (a.iters) {

@@ -163,7 +163,7 @@ class DeviceCatalog:
 
 
 def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", tile_bins=0,
-                 warps_per_tile=0) -> _native.KsOptions:
+                 warps_per_tile=0, profile=False) -> _native.KsOptions:
     opt = _native.KsOptions()
     opt.cutoff = float(cutoff)
     opt.microturb_kms = float(microturb_kms)
@@ -171,6 +171,7 @@ def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", t
     opt.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     opt.tile_bins = int(tile_bins)
     opt.warps_per_tile = int(warps_per_tile)
+    opt.profile = 1 if profile else 0
     return opt
 
 
