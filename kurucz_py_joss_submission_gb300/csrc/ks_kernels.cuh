@@ -453,22 +453,63 @@ __device__ __forceinline__ void cell_add(float2* c, int b, float v) {
 }
 __device__ __forceinline__ void cell_add(double* c, int b, double v) { c[b] += v; }
 
+// Near-zone profile with the (H0, H1) table interleaved in shared memory.
+template <typename R, typename R2>
+__device__ __forceinline__ R near_profile_tab(int off, R dv, R tabstep, R ad, R k0,
+                                              const R2* __restrict__ h01, const R* __restrict__ h0g,
+                                              const R* __restrict__ h1g, const R* __restrict__ h2g) {
+    R x = (R)off * dv;
+    if (ad < R(0.2)) {
+        if (x > R(10)) return k0 * (R(0.5642) * ad / (x * x));
+        int idx = (int)(R(0.5) + (R)off * tabstep);
+        idx = idx > VOIGT_N - 1 ? VOIGT_N - 1 : idx;
+        R2 h = h01[idx];
+        return k0 * (h.x + ad * h.y);
+    }
+    return k0 * voigt_hv<R>(x, ad, h0g, h1g, h2g);
+}
+
+template <typename R> struct Vec2;
+template <> struct Vec2<float> { using T = float2; };
+template <> struct Vec2<double> { using T = double2; };
+
+// Accumulates profile values for offsets [lo, hi] into bins base + sgn*o of
+// the warp's copy (lanes take consecutive offsets).
+template <typename R, typename R2, typename CellT, bool FAR>
+__device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, int hi, int lane,
+                                         R k0, R ad, R dv, R tabstep, R xf, const R2* h01,
+                                         const R* h0g, const R* h1g, const R* h2g) {
+    for (int o = lo + lane; o <= hi; o += 32) {
+        R v;
+        if (FAR) {
+            R oo = (R)o * (R)o;
+            if constexpr (sizeof(R) == 4) v = __fdividef(xf, oo);
+            else v = xf / oo;
+        } else {
+            v = near_profile_tab<R, R2>(o, dv, tabstep, ad, k0, h01, h0g, h1g, h2g);
+        }
+        cell_add(my, base + sgn * o, v);
+    }
+}
+
 // One CTA per (lambda tile, depth).  For every reach class k it selects the
 // pairs whose wing centre lies within 2^k (+1) bins of the tile -- a
 // contiguous range of that class's centre-sorted list.  Warps take those
-// pairs in batches of 32 (batch b -> warp b mod nwarps, a fixed order): each
-// lane loads one pair's descriptor, then the warp walks the 32 pairs,
-// broadcasting each descriptor by shuffles.  For a pair, lanes take
-// consecutive wing offsets; each offset's profile value goes to the red bin
-// c+o and the blue bin c-o of the warp's own shared-memory copy of the tile,
-// so no two lanes write the same word and no atomics are needed.  Near-wing
-// and far-wing offsets run in separate loops (no divergence between the
-// table/Voigt branch and X/o^2).  The copies are summed in warp order,
-// multiplied by STIM (line_opacity.py:1338) and stored coalesced.
+// pairs in batches of 32 (batch b -> warp b mod nwarps, a fixed order).
+// Each lane loads one pair's descriptor and works out, for its pair, the
+// offsets whose red bin c+o and blue bin c-o fall in the tile, split at
+// N10DOP into the near (table/Voigt) and far (X/o^2) zones; a ballot drops
+// pairs that miss the tile.  The warp then walks the remaining pairs,
+// broadcasting each pair's ranges by shuffles, and runs up to four
+// branch-free loops (red/blue x near/far) with lanes on consecutive offsets,
+// adding into the warp's own shared-memory copy of the tile -- no two lanes
+// write the same word, so no atomics are needed.  The copies are summed in
+// warp order, multiplied by STIM (line_opacity.py:1338) and stored coalesced.
 template <typename R>
 __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
                                                          R* __restrict__ out) {
     using CellT = typename Cell<R>::T;
+    using R2 = typename Vec2<R>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int W = a.tile_bins;
     const int nwarps = blockDim.x >> 5;
@@ -479,9 +520,8 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const int T1 = (int)min((int64_t)T0 + W, a.n_wl);
     const int span = T1 - T0;
 
-    R* sh0 = reinterpret_cast<R*>(smem_raw);
-    R* sh1 = sh0 + VOIGT_N;
-    size_t tab_bytes = (2 * VOIGT_N * sizeof(R) + 15) & ~size_t(15);
+    R2* h01 = reinterpret_cast<R2*>(smem_raw);  // interleaved (H0, H1)
+    size_t tab_bytes = (VOIGT_N * sizeof(R2) + 15) & ~size_t(15);
     CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
     __shared__ int64_t cls_lo[N_REACH_CLASSES];
     __shared__ int64_t cls_base[N_REACH_CLASSES + 1];
@@ -491,8 +531,10 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const R* gh1 = sizeof(R) == 8 ? (const R*)a.h1d : (const R*)a.h1f;
     const R* gh2 = sizeof(R) == 8 ? (const R*)a.h2d : (const R*)a.h2f;
     for (int i = threadIdx.x; i < VOIGT_N; i += blockDim.x) {
-        sh0[i] = gh0[i];
-        sh1[i] = gh1[i];
+        R2 h;
+        h.x = gh0[i];
+        h.y = gh1[i];
+        h01[i] = h;
     }
     for (int i = threadIdx.x; i < nwarps * W; i += blockDim.x) {
         if constexpr (sizeof(R) == 4) acc[i] = make_float2(0.f, 0.f);
@@ -522,72 +564,73 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     CellT* my = acc + warp * W;
     const int64_t total = cls_base[N_REACH_CLASSES];
     const PairDesc<R>* drow = desc + (int64_t)d * a.stride;
-    int64_t evals = 0;
+    unsigned long long evals = 0;
     const int64_t nbatch = (total + 31) >> 5;
+    int kcur = 0;
     for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
-        // each lane fetches one descriptor of the batch
-        int64_t item = bt * 32 + lane;
-        PairDesc<R> mine;
-        mine.maxstep_far = 0;
-        mine.ctr_n10 = 0;
-        mine.wing_c = 0;
-        mine.kappa0 = mine.adamp = mine.dvoigt = mine.xfar = mine.kapcen = R(0);
+        // ---- per lane: one pair and its in-tile offset ranges ----
+        const int64_t item = bt * 32 + lane;
+        int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
+        R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
+        bool far = false;
         if (item < total) {
-            int k = 0;
-            while (item >= cls_base[k + 1]) k++;
-            int64_t p = a.class_pos[cls_lo[k] + (item - cls_base[k])];
-            mine = drow[p];
-        }
-        const int nb = (int)min((int64_t)32, total - bt * 32);
-        for (int i = 0; i < nb; i++) {
-            const int c = __shfl_sync(0xffffffffu, mine.wing_c, i);
-            const int ms = __shfl_sync(0xffffffffu, mine.maxstep_far, i);
-            const int cn = __shfl_sync(0xffffffffu, mine.ctr_n10, i);
-            const int ctr = cn & 15;
+            while (item >= cls_base[kcur + 1]) kcur++;
+            while (kcur > 0 && item < cls_base[kcur]) kcur--;
+            const int64_t p = a.class_pos[cls_lo[kcur] + (item - cls_base[kcur])];
+            const PairDesc<R> pd = drow[p];
+            c = pd.wing_c;
+            const int ctr = pd.ctr_n10 & 15;
             if (ctr) {
-                const int cb = c + (ctr - 8);
-                if (cb >= T0 && cb < T1) {
-                    const R kc = __shfl_sync(0xffffffffu, mine.kapcen, i);
-                    if (lane == 0) cell_add(my, cb - T0, kc);
+                int cc = c + (ctr - 8);
+                if (cc >= T0 && cc < T1) {
+                    cb = cc - T0;
+                    kc = pd.kapcen;
                     evals++;
                 }
             }
-            const int reach = ms & 0x7fffffff;
-            if (reach == 0) continue;
-            // red offsets: c + o in [T0, T1); blue offsets: c - o in [T0, T1)
-            const int rlo = max(1, T0 - c), rhi = min(reach, T1 - 1 - c);
-            const int blo = max(1, c - (T1 - 1)), bhi = min(reach, c - T0);
-            const bool rr = rlo <= rhi, bb = blo <= bhi;
-            if (!rr && !bb) continue;
-            const int olo = rr ? (bb ? min(rlo, blo) : rlo) : blo;
-            const int ohi = rr ? (bb ? max(rhi, bhi) : rhi) : bhi;
-            evals += (rr ? rhi - rlo + 1 : 0) + (bb ? bhi - blo + 1 : 0);
-            const bool far = ms < 0;
-            const int n10 = cn >> 8;
-            const int near_hi = far ? min(ohi, n10) : ohi;
-            if (olo <= near_hi) {
-                const R k0 = __shfl_sync(0xffffffffu, mine.kappa0, i);
-                const R ad = __shfl_sync(0xffffffffu, mine.adamp, i);
-                const R dv = __shfl_sync(0xffffffffu, mine.dvoigt, i);
-                for (int o = olo + lane; o <= near_hi; o += 32) {
-                    R v = near_profile<R>(o, dv, ad, k0, sh0, sh1, gh2);
-                    if (rr && o >= rlo && o <= rhi) cell_add(my, c + o - T0, v);
-                    if (bb && o >= blo && o <= bhi) cell_add(my, c - o - T0, v);
-                }
+            const int reach = pd.maxstep_far & 0x7fffffff;
+            if (reach > 0) {
+                rlo = max(1, T0 - c);
+                rhi = min(reach, T1 - 1 - c);
+                blo = max(1, c - (T1 - 1));
+                bhi = min(reach, c - T0);
+                if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
+                if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
             }
-            if (far) {
-                const int flo = max(olo, n10 + 1);
-                if (flo <= ohi) {
-                    const R xf = __shfl_sync(0xffffffffu, mine.xfar, i);
-                    for (int o = flo + lane; o <= ohi; o += 32) {
-                        R oo = (R)o * (R)o;
-                        R v;
-                        if constexpr (sizeof(R) == 4) v = __fdividef(xf, oo);
-                        else v = xf / oo;
-                        if (rr && o >= rlo && o <= rhi) cell_add(my, c + o - T0, v);
-                        if (bb && o >= blo && o <= bhi) cell_add(my, c - o - T0, v);
-                    }
-                }
+            far = pd.maxstep_far < 0;
+            nz = far ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
+            k0 = pd.kappa0;
+            ad = pd.adamp;
+            dv = pd.dvoigt;
+            xf = pd.xfar;
+        }
+        const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
+        unsigned mask = __ballot_sync(0xffffffffu, active);
+        while (mask) {
+            const int i = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int ci = __shfl_sync(0xffffffffu, c, i);
+            const int cbi = __shfl_sync(0xffffffffu, cb, i);
+            if (cbi >= 0) {
+                const R kci = __shfl_sync(0xffffffffu, kc, i);
+                if (lane == 0) cell_add(my, cbi, kci);
+            }
+            const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
+            const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
+            if (rl > rh && bl > bh) continue;
+            const int nzi = __shfl_sync(0xffffffffu, nz, i);
+            const R adi = __shfl_sync(0xffffffffu, ad, i);
+            const R dvi = __shfl_sync(0xffffffffu, dv, i);
+            const R k0i = __shfl_sync(0xffffffffu, k0, i);
+            const R xfi = __shfl_sync(0xffffffffu, xf, i);
+            const R ts = R(200) * dvi;
+            const int rbase = ci - T0, bbase = ci - T0;
+            // red: bins rbase + o; blue: bins bbase - o
+            wing_run<R, R2, CellT, false>(my, rbase, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+            wing_run<R, R2, CellT, false>(my, bbase, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+            if (nzi != 0x7fffffff) {
+                wing_run<R, R2, CellT, true>(my, rbase, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                wing_run<R, R2, CellT, true>(my, bbase, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
             }
         }
     }
@@ -615,7 +658,11 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         }
         out[(int64_t)d * a.n_wl + T0 + b] = v;
     }
-    if (a.evals && lane == 0 && evals) atomicAdd((unsigned long long*)a.evals, (unsigned long long)evals);
+    // evaluation counter: warp sum, one atomic per warp
+    if (a.evals) {
+        for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
+        if (lane == 0 && evals) atomicAdd(a.evals, evals);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -805,7 +852,7 @@ __device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew,
 // Gauss-Seidel scattering sweeps of the reference (josh_solver.py:24-92), in
 // single precision as the reference runs them, with the reference's
 // summation order and no fused multiply-add.
-static __device__ __noinline__ int josh_sweeps_ref(const float* __restrict__ coefj, float* xs,
+__device__ __forceinline__ int josh_sweeps_ref(const float* __restrict__ coefj, float* xs,
                                             const float* xalpha, const float* xsbar_mod) {
     float diag[NXTAU];
     for (int k = 0; k < NXTAU; k++) diag[k] = __fsub_rn(1.0f, __fmul_rn(xalpha[k], coefj[k * NXTAU + k]));
@@ -961,14 +1008,12 @@ __device__ __forceinline__ R planck_nu(double freq, double hkt) {
 // corrected line opacity, split by FSCAT into absorption and scattering
 // (opacity.py:2408-2420).
 template <typename R, bool REF_SWEEP>
-__global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __grid_constant__ CoefJ32 cj,
-                                                       const R* __restrict__ cont_abs,
-                                                       const R* __restrict__ cont_scat,
-                                                       const R* __restrict__ line_op,
-                                                       const R* __restrict__ line_sc,
-                                                       const R* __restrict__ line_src) {
-    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.n) return;
+__device__ __forceinline__ void transfer_column(const TransferArgs& a, const CoefJ32& cj,
+                                                const R* __restrict__ cont_abs,
+                                                const R* __restrict__ cont_scat,
+                                                const R* __restrict__ line_op,
+                                                const R* __restrict__ line_sc,
+                                                const R* __restrict__ line_src, int64_t j) {
     const int L = a.n_layers;
     R mass[MAX_LAYERS], ca[MAX_LAYERS], cs[MAX_LAYERS], la[MAX_LAYERS], ls[MAX_LAYERS],
         src[MAX_LAYERS], pl[MAX_LAYERS];
@@ -1062,6 +1107,18 @@ __global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __g
         a.iters[2 * j] = itc;
         a.iters[2 * j + 1] = itt;
     }
+}
+
+template <typename R, bool REF_SWEEP>
+__global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __grid_constant__ CoefJ32 cj,
+                                                       const R* __restrict__ cont_abs,
+                                                       const R* __restrict__ cont_scat,
+                                                       const R* __restrict__ line_op,
+                                                       const R* __restrict__ line_sc,
+                                                       const R* __restrict__ line_src) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    transfer_column<R, REF_SWEEP>(a, cj, cont_abs, cont_scat, line_op, line_sc, line_src, j);
 }
 
 }  // namespace ks
