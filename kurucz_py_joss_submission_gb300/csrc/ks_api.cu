@@ -687,7 +687,7 @@ static ks_status run_partition(const Workspace& w, int L, cudaStream_t s) {
 }
 
 static int default_tile(const ks_options* opt, bool fp64) {
-    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : (fp64 ? 512 : 1024);
+    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : 512;
     return t;
 }
 static int default_warps(const ks_options* opt) {

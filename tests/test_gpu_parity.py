@@ -94,7 +94,7 @@ def test_formal_solution_seam(name):
     ft, fc = solve_lte_spectrum(g["wavelength"], atm.temperature, atm.depth, g["cont_abs"],
                                 g["cont_scat"], g["asynth"], np.zeros_like(g["asynth"]),
                                 line_source=src, precision="fp64")
-    assert rel(ft, g["flux_total_hz"]) < 1e-10
+    assert float(np.max(np.abs(ft - g["flux_total_hz"]) / g["flux_cont_hz"])) < 1e-10
     assert rel(fc, g["flux_cont_hz"]) < 1e-10
 
 
@@ -114,7 +114,8 @@ def test_fused_fp64_matches_reference(name):
     assert st["device_flags"] == 0
     ft, fc = syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy()
     assert rel(fc, g["flux_cont_hz"]) < 1e-10
-    assert rel(ft, g["flux_total_hz"]) < 1e-9
+    # relative to the continuum: saturated MAXJ=1 cores have fluxes ~1e-18
+    assert float(np.max(np.abs(ft - g["flux_total_hz"]) / g["flux_cont_hz"])) < 1e-9
     asy = syn.asynth.cpu().numpy()
     if "asynth" in g and g["asynth"].shape == asy.shape:
         assert rel(asy, g["asynth"]) < 1e-12
