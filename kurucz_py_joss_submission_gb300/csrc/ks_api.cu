@@ -349,7 +349,7 @@ __global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __
         f.gs = (float)gs[i];
         f.gw = (float)gw[i];
         f.gf = (float)gf[i];
-        f.pad = 0.f;
+        f.wl = (float)w;
         linef[i] = f;
     }
 }
@@ -727,6 +727,7 @@ static TransferArgs transfer_args(const ks_atmos* atm, const ks_grid* g, const W
     a.n_layers = atm->n_layers;
     a.asynth_mode = asynth_mode ? 1 : 0;
     a.slinec_mode = fp64 ? 1 : 0;
+    a.line_scat = 0;
     a.grid = g->wavelength;
     a.depth = w.depth;
     a.xtau = t.xtau;
@@ -997,6 +998,7 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
     tm.mark();
     TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, true, fp64);
+    ta.line_scat = (opt && opt->rhoxj > 0.0) ? 1 : 0;
     if constexpr (fp64)
         KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
     else

@@ -17,19 +17,20 @@ struct GridPar {
 // radiative.py:33, opacity.py:2408-2414).
 struct DepthPar {
     double rho, xne, txnxn, hckt, hkt, hkt_asynth, temperature, rhox, fscat;
-    float hckt_hi, hckt_lo, xne_f, txnxn_f;
+    float hckt_hi, hckt_lo, xne_f, txnxn_f, hkt_f, rhox_f, fscat_f, pad;
 };
 
 // Per (depth, ion, element) entry.
 struct IonPar {
     double pop, dop, dop_transp, xnfdop, dvoigt;
-    float xnfdop_f, dop_f, dvoigt_f, pop_over_rho_f;
-    int n10dop, pad;
+    float xnfdop_f, dop_f, dvoigt_f, pop_over_rho_f, dopw_f;
+    int n10dop;
+    int ok;  // bit 0: TRANSP may use it (pop, DOPPLE, rho > 0); bit 1: wings (pop, DOPPLE > 0)
 };
 
 // Per-line single-precision copies for the mixed path.
 struct LineF {
-    float cgf, elo_hi, elo_lo, gr, gs, gw, gf, pad;
+    float cgf, elo_hi, elo_lo, gr, gs, gw, gf, wl;
 };
 
 // Wing descriptor of one valid (line, depth) pair.
@@ -112,6 +113,7 @@ struct TransferArgs {
     int n_layers;
     int asynth_mode;   // line opacity given as ASYNTH (split by FSCAT here)
     int slinec_mode;   // source = SLINEC of the driver's frequency (FP64 path)
+    int line_scat;     // some layer has FSCAT > 0 (RHOXJ > 0): line scattering present
     const double *grid;
     const DepthPar *depth;
     const double *xtau, *ch;

@@ -54,6 +54,10 @@ __global__ void prep_depth_kernel(PrepArgs a) {
         p.hckt_lo = (float)(p.hckt - (double)p.hckt_hi);
         p.xne_f = (float)p.xne;
         p.txnxn_f = (float)p.txnxn;
+        p.hkt_f = (float)p.hkt;
+        p.rhox_f = (float)p.rhox;
+        p.fscat_f = (float)p.fscat;
+        p.pad = 0.f;
         a.depth[d] = p;
     }
     double pop = a.population[i];
@@ -73,7 +77,8 @@ __global__ void prep_depth_kernel(PrepArgs a) {
     q.dop_f = (float)dop_t;
     q.dvoigt_f = (float)q.dvoigt;
     q.pop_over_rho_f = rho > 0.0 ? (float)(pop / rho) : 0.0f;
-    q.pad = 0;
+    q.dopw_f = (float)dop;
+    q.ok = ((pop > 0.0 && dop_t > 0.0 && rho > 0.0) ? 1 : 0) | ((pop > 0.0 && dop > 0.0) ? 2 : 0);
     a.ion[i] = q;
 }
 
@@ -245,10 +250,10 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
     const int c_ctr = a.center_idx[li];
     const int c_wing = a.wing_idx[li];
     const int64_t nwl = a.n_wl;
-    auto kap_at = [&](int c) -> double {
+    auto kap_at = [&](int c) -> R {
         int cc = c < 0 ? 0 : (c > (int)nwl - 1 ? (int)nwl - 1 : c);
-        double v = (double)kap_a[(int64_t)d * nwl + cc];
-        if (kap_b) v += (double)kap_b[(int64_t)d * nwl + cc];
+        R v = kap_a[(int64_t)d * nwl + cc];
+        if (kap_b) v += kap_b[(int64_t)d * nwl + cc];
         return v;
     };
 
@@ -257,10 +262,10 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
     R kappa0_w = R(0);  // kappa0 for the wings
     bool valid = false;
     if (FUSED) {
-        if (a.process_mask[li] && q.pop > 0.0 && q.dop_transp > 0.0 && dp.rho > 0.0) {
+        if (a.process_mask[li] && (q.ok & 1)) {
             if (!F32) {
                 const double lw = a.wavelength[li];
-                double kapmin = kap_at(c_ctr) * a.cutoff;
+                double kapmin = (double)kap_at(c_ctr) * a.cutoff;
                 double k0pre = (lt == 1) ? a.gamma_vdw[li] * a.gf[li] * (q.pop / dp.rho)
                                          : a.cgf[li] * q.xnfdop;
                 if (k0pre >= kapmin) {
@@ -284,7 +289,7 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
                 }
             } else {
                 const LineF lf = a.linef[li];
-                float kapmin = (float)(kap_at(c_ctr) * a.cutoff);
+                float kapmin = (float)kap_at(c_ctr) * (float)a.cutoff;
                 float k0pre = (lt == 1) ? lf.gw * lf.gf * q.pop_over_rho_f : lf.cgf * q.xnfdop_f;
                 if (k0pre >= kapmin) {
                     float boltz = fast_ex_mixed(lf.elo_hi, lf.elo_lo, dp.hckt_hi, dp.hckt_lo,
@@ -334,7 +339,8 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
     out.maxstep_far = 0;
     int reach = 0;
     int n10dop = 0;
-    const bool wings = (lt == 0) && q.dop > 0.0 && q.pop > 0.0 && a.wavelength[li] > 0.0 &&
+    const bool wl_pos = F32 ? a.linef[li].wl > 0.0f : a.wavelength[li] > 0.0;
+    const bool wings = (lt == 0) && (q.ok & 2) && wl_pos &&
                        c_wing >= -MAX_PROFILE_STEPS && c_wing <= nwl - 1 + MAX_PROFILE_STEPS;
     if (wings) {
         R adamp, kappa0, dvoigt;
@@ -352,7 +358,7 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
             dvoigt = (R)(dopple > 0 ? 1.0 / (dopple * resolu) : 1.0);
         } else {
             const LineF lf = a.linef[li];
-            float ad = (lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f) / (float)q.dop;
+            float ad = __fdividef(lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f, q.dopw_f);
             adamp = (R)(ad > 1e-12f ? ad : 1e-12f);
             kappa0 = kappa0_w;
             n10dop = q.n10dop;
@@ -362,7 +368,7 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
             atomicOr(a.flags, FLAG_N10DOP_RANGE);
             return;
         }
-        const R kapmin_ref = (R)(kap_at(c_wing) * a.cutoff);
+        const R kapmin_ref = kap_at(c_wing) * (R)a.cutoff;
         const R* h0 = F32 ? (const R*)a.h0f : (const R*)a.h0d;
         const R* h1 = F32 ? (const R*)a.h1f : (const R*)a.h1d;
         const R* h2 = F32 ? (const R*)a.h2f : (const R*)a.h2d;
@@ -385,8 +391,10 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
             far = true;
             if (n10dop > 0 && prof_n10 > R(0) && kapmin_ref > R(0)) {
                 xfar = prof_n10 * (R)n10dop * (R)n10dop;
-                double ms = sqrt((double)xfar / (double)kapmin_ref) + 1.0;
-                reach = ms > (double)MAX_PROFILE_STEPS ? MAX_PROFILE_STEPS : (int)ms;
+                R ms;
+                if constexpr (F32) ms = sqrtf(__fdividef(xfar, kapmin_ref)) + 1.0f;
+                else ms = sqrt(xfar / kapmin_ref) + 1.0;
+                reach = ms > (R)MAX_PROFILE_STEPS ? MAX_PROFILE_STEPS : (int)ms;
             }
         }
         out.kappa0 = kappa0;
@@ -669,6 +677,12 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
 // transfer (JOSH)
 // ---------------------------------------------------------------------------
 
+// Division of the transfer arithmetic: IEEE in FP64 (the reference's
+// operations), the fast reciprocal-multiply in FP32 (2 ulp; operands here are
+// opacities, optical depths and column masses far below 2^126).
+__device__ __forceinline__ float tdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double tdiv(double a, double b) { return a / b; }
+
 // Parabolic coefficients of PARCOE after its boundary overrides
 // (josh_solver.py:110-152) at index j, before the smoothing pass.
 template <typename R>
@@ -676,24 +690,24 @@ __device__ __forceinline__ void parcoe_raw(const R* f, const R* x, int n, int j,
     if (j == 0 || j == 1 || (j == 2 && n > 3) || j == n - 1) {
         int j0 = (j == n - 1) ? n - 2 : j;
         R den = x[j0 + 1] - x[j0];
-        b = den != R(0) ? (f[j0 + 1] - f[j0]) / den : R(0);
+        b = den != R(0) ? tdiv(f[j0 + 1] - f[j0], den) : R(0);
         a = f[j] - x[j] * b;
         c = R(0);
         return;
     }
     int j1 = j - 1;
     R den = x[j] - x[j1];
-    R dd = den != R(0) ? (f[j] - f[j1]) / den : R(0);
+    R dd = den != R(0) ? tdiv(f[j] - f[j1], den) : R(0);
     R den1 = (x[j + 1] - x[j]) * (x[j + 1] - x[j1]);
-    R term1 = den1 != R(0) ? f[j + 1] / den1 : R(0);
+    R term1 = den1 != R(0) ? tdiv(f[j + 1], den1) : R(0);
     R den2 = x[j + 1] - x[j1];
     R den3 = x[j + 1] - x[j];
     R den4 = x[j] - x[j1];
     R part = R(0);
     if (den4 != R(0)) {
-        R t1 = den2 != R(0) ? f[j1] / den2 : R(0);
-        R t2 = den3 != R(0) ? f[j] / den3 : R(0);
-        part = (t1 - t2) / den4;
+        R t1 = den2 != R(0) ? tdiv(f[j1], den2) : R(0);
+        R t2 = den3 != R(0) ? tdiv(f[j], den3) : R(0);
+        part = tdiv(t1 - t2, den4);
     }
     c = term1 + part;
     b = dd - (x[j] + x[j1]) * c;
@@ -709,7 +723,7 @@ __device__ void integ_tau(const R* x, const R* f, int n, R start, R* fint) {
     if (n == 1) return;
     if (n == 2) {
         R den = x[1] - x[0];
-        R b = den != R(0) ? (f[1] - f[0]) / den : R(0);
+        R b = den != R(0) ? tdiv(f[1] - f[0], den) : R(0);
         R a0 = f[0] - x[0] * b;
         R dx = x[1] - x[0];
         R term = a0 + R(0.5) * b * (x[1] + x[0]);
@@ -727,12 +741,13 @@ __device__ void integ_tau(const R* x, const R* f, int n, R start, R* fint) {
             if (i == n - 2) {
                 // a[n1-1] = a[-1] (josh_solver.py:164-166)
                 R den = x[n - 1] - x[n - 2];
-                b_i = den != R(0) ? (f[n - 1] - f[n - 2]) / den : R(0);
+                b_i = den != R(0) ? tdiv(f[n - 1] - f[n - 2], den) : R(0);
                 a_i = f[n - 1] - x[n - 1] * b_i;
                 c_i = R(0);
             } else if (ci != R(0)) {
-                R den = (cn < R(0) ? -cn : cn) + (ci < R(0) ? -ci : ci);
-                R wt = den > R(0) ? (cn < R(0) ? -cn : cn) / den : R(0);
+                R acn = cn < R(0) ? -cn : cn;
+                R den = acn + (ci < R(0) ? -ci : ci);
+                R wt = den > R(0) ? tdiv(acn, den) : R(0);
                 a_i = an + wt * (ai - an);
                 b_i = bn + wt * (bi - bn);
                 c_i = cn + wt * (ci - cn);
@@ -742,11 +757,8 @@ __device__ void integ_tau(const R* x, const R* f, int n, R start, R* fint) {
         R term = a_i + R(0.5) * b_i * (x[i + 1] + x[i]);
         term += (c_i / R(3)) * ((x[i + 1] + x[i]) * x[i + 1] + x[i] * x[i]);
         R inc = term * dx;
-        if (sizeof(R) == 4) {
-            float sf = (float)s, cf = (float)comp;
-            kahan_add(sf, cf, (float)inc);
-            s = (R)sf;
-            comp = (R)cf;
+        if constexpr (sizeof(R) == 4) {
+            kahan_add(s, comp, inc);
         } else {
             s = s + inc;
         }
@@ -759,8 +771,8 @@ __device__ void integ_tau(const R* x, const R* f, int n, R start, R* fint) {
 // DERIV (josh_solver.py:193-217)
 template <typename R>
 __device__ void deriv(const R* x, const R* f, int n, R* dfdx) {
-    dfdx[0] = (f[1] - f[0]) / (x[1] - x[0]);
-    dfdx[n - 1] = (f[n - 1] - f[n - 2]) / (x[n - 1] - x[n - 2]);
+    dfdx[0] = tdiv(f[1] - f[0], x[1] - x[0]);
+    dfdx[n - 1] = tdiv(f[n - 1] - f[n - 2], x[n - 1] - x[n - 2]);
     if (n == 2) return;
     R s = x[1] != x[0] ? (R)(((x[1] - x[0]) < R(0)) ? -1 : 1) : R(1);
     for (int j = 1; j < n - 1; j++) {
@@ -769,13 +781,13 @@ __device__ void deriv(const R* x, const R* f, int n, R* dfdx) {
         sc = t > sc ? t : sc;
         t = fabs(f[j + 1]);
         sc = t > sc ? t : sc;
-        sc = x[j] != R(0) ? sc / fabs(x[j]) : sc;
+        sc = x[j] != R(0) ? tdiv(sc, (R)fabs(x[j])) : sc;
         if (sc == R(0)) sc = R(1);
-        R d1 = (f[j + 1] - f[j]) / (x[j + 1] - x[j]) / sc;
-        R d0 = (f[j] - f[j - 1]) / (x[j] - x[j - 1]) / sc;
-        R tan1 = d1 / (s * sqrt(R(1) + d1 * d1) + R(1));
-        R tan0 = d0 / (s * sqrt(R(1) + d0 * d0) + R(1));
-        dfdx[j] = (tan1 + tan0) / (R(1) - tan1 * tan0) * sc;
+        R d1 = tdiv(tdiv(f[j + 1] - f[j], x[j + 1] - x[j]), sc);
+        R d0 = tdiv(tdiv(f[j] - f[j - 1], x[j] - x[j - 1]), sc);
+        R tan1 = tdiv(d1, s * sqrt(R(1) + d1 * d1) + R(1));
+        R tan0 = tdiv(d0, s * sqrt(R(1) + d0 * d0) + R(1));
+        dfdx[j] = tdiv(tan1 + tan0, R(1) - tan1 * tan0) * sc;
     }
 }
 
@@ -795,7 +807,7 @@ __device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew,
                 if (l == 2 || l == 3) {
                     l = l < nold ? l : nold;
                     Cc = R(0);
-                    B = (f1[l] - f1[l - 1]) / (x1[l] - x1[l - 1]);
+                    B = tdiv(f1[l] - f1[l - 1], x1[l] - x1[l - 1]);
                     A = f1[l] - x1[l] * B;
                     ll = l;
                     break;
@@ -803,10 +815,10 @@ __device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew,
                 int l1 = l - 1;
                 if (l > ll + 1 || l == 4) {
                     int l2 = l - 2;
-                    R dd = (f1[l1] - f1[l2]) / (x1[l1] - x1[l2]);
-                    cbac = f1[l] / ((x1[l] - x1[l1]) * (x1[l] - x1[l2])) +
-                           (f1[l2] / (x1[l] - x1[l2]) - f1[l1] / (x1[l] - x1[l1])) /
-                               (x1[l1] - x1[l2]);
+                    R dd = tdiv(f1[l1] - f1[l2], x1[l1] - x1[l2]);
+                    cbac = tdiv(f1[l], (x1[l] - x1[l1]) * (x1[l] - x1[l2])) +
+                           tdiv(tdiv(f1[l2], x1[l] - x1[l2]) - tdiv(f1[l1], x1[l] - x1[l1]),
+                                x1[l1] - x1[l2]);
                     bbac = dd - (x1[l1] + x1[l2]) * cbac;
                     abac = f1[l2] - x1[l2] * dd + x1[l1] * x1[l2] * cbac;
                     if (!(l < nold)) {
@@ -820,15 +832,15 @@ __device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew,
                         break;
                     }
                 }
-                R dd = (f1[l] - f1[l1]) / (x1[l] - x1[l1]);
-                cfor = f1[l + 1] / ((x1[l + 1] - x1[l]) * (x1[l + 1] - x1[l1])) +
-                       (f1[l1] / (x1[l + 1] - x1[l1]) - f1[l] / (x1[l + 1] - x1[l])) /
-                           (x1[l] - x1[l1]);
+                R dd = tdiv(f1[l] - f1[l1], x1[l] - x1[l1]);
+                cfor = tdiv(f1[l + 1], (x1[l + 1] - x1[l]) * (x1[l + 1] - x1[l1])) +
+                       tdiv(tdiv(f1[l1], x1[l + 1] - x1[l1]) - tdiv(f1[l], x1[l + 1] - x1[l]),
+                            x1[l] - x1[l1]);
                 bfor = dd - (x1[l] + x1[l1]) * cfor;
                 afor = f1[l1] - x1[l1] * dd + x1[l] * x1[l1] * cfor;
                 R acf = cfor < R(0) ? -cfor : cfor;
                 R acb = cbac < R(0) ? -cbac : cbac;
-                R wt = acf != R(0) ? acf / (acf + acb) : R(0);
+                R wt = acf != R(0) ? tdiv(acf, acf + acb) : R(0);
                 A = afor + wt * (abac - afor);
                 B = bfor + wt * (bbac - bfor);
                 Cc = cfor + wt * (cbac - cfor);
@@ -839,7 +851,7 @@ __device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew,
             if (l > nold) {
                 l = nold;
                 Cc = R(0);
-                B = (f1[l] - f1[l - 1]) / (x1[l] - x1[l - 1]);
+                B = tdiv(f1[l] - f1[l - 1], x1[l] - x1[l - 1]);
                 A = f1[l] - x1[l] * B;
                 ll = l;
                 break;
@@ -853,7 +865,7 @@ __device__ void map1_xtau(const R* xold, const R* fold, int nold, const R* xnew,
 // single precision as the reference runs them, with the reference's
 // summation order and no fused multiply-add.
 __device__ __forceinline__ int josh_sweeps_ref(const float* __restrict__ coefj, float* xs,
-                                            const float* xalpha, const float* xsbar_mod) {
+                                               const float* xalpha, const float* xsbar_mod) {
     float diag[NXTAU];
     for (int k = 0; k < NXTAU; k++) diag[k] = __fsub_rn(1.0f, __fmul_rn(xalpha[k], coefj[k * NXTAU + k]));
     for (int it = 0; it < NXTAU; it++) {
@@ -914,7 +926,9 @@ __device__ __forceinline__ int josh_sweeps_fast(const CoefJ32& cj, const float* 
     return it_done;
 }
 
-// JOSH surface flux for one column (josh_solver.py:367-767).
+// JOSH surface flux for one column (josh_solver.py:367-767).  aline, sline
+// and sigmal may be NULL (no line opacity / source = scont / no line
+// scattering).
 template <typename R, bool REF_SWEEP>
 __device__ double josh_flux(int n, const R* acont, const R* scont, const R* aline, const R* sline,
                             const R* sigmac, const R* sigmal, const R* rho, const R* xtau,
@@ -923,13 +937,16 @@ __device__ double josh_flux(int n, const R* acont, const R* scont, const R* alin
     R abtot[MAX_LAYERS], alpha[MAX_LAYERS], snubar[MAX_LAYERS], taunu[MAX_LAYERS];
     const R eps = (R)EPS38;
     for (int j = 0; j < n; j++) {
-        R ab = acont[j] + aline[j] + sigmac[j] + sigmal[j];
+        const R al_j = aline ? aline[j] : R(0);
+        const R sl_j = sigmal ? sigmal[j] : R(0);
+        R ab = acont[j] + al_j + sigmac[j] + sl_j;
         abtot[j] = ab > eps ? ab : (ab != ab ? ab : eps);
-        R sc = sigmac[j] + sigmal[j];
-        R al = abtot[j] > R(0) ? sc / abtot[j] : R(0);
-        alpha[j] = al < R(0) ? R(0) : (al > R(1) ? R(1) : al);
-        R den = acont[j] + aline[j];
-        snubar[j] = den > R(0) ? (acont[j] * scont[j] + aline[j] * sline[j]) / den : scont[j];
+        R sc = sigmac[j] + sl_j;
+        R alp = abtot[j] > R(0) ? tdiv(sc, abtot[j]) : R(0);
+        alpha[j] = alp < R(0) ? R(0) : (alp > R(1) ? R(1) : alp);
+        R den = acont[j] + al_j;
+        const R sline_j = sline ? sline[j] : scont[j];
+        snubar[j] = den > R(0) ? tdiv(acont[j] * scont[j] + al_j * sline_j, den) : scont[j];
     }
     // rho ascending after solve_lte_frequency's reversal, so needs_reverse
     // (josh_solver.py:465) is false here.
@@ -950,7 +967,7 @@ __device__ double josh_flux(int n, const R* acont, const R* scont, const R* alin
                 R an = snew < R(0) ? -snew : snew;
                 R dn = an > eps ? an : eps;
                 R df = snew - snu[j];
-                err += (df < R(0) ? -df : df) / dn;
+                err += tdiv(df < R(0) ? -df : df, dn);
                 snu[j] = snew;
             }
             it_done = it + 1;
@@ -986,27 +1003,23 @@ __device__ double josh_flux(int n, const R* acont, const R* scont, const R* alin
 }
 
 // Planck function B_nu (radiative.py:20-39).
-template <typename R>
-__device__ __forceinline__ R planck_nu(double freq, double hkt) {
-    if (sizeof(R) == 8) {
-        double freq15 = freq / 1.0e15;
-        double ehvkt = exp(-freq * hkt);
-        double stim = 1.0 - ehvkt;
-        double bnu = 1.47439e-2 * pow(freq15, 3.0) * ehvkt / stim;
-        return (R)(bnu != bnu ? 0.0 : bnu);
-    } else {
-        float freq15 = (float)(freq / 1.0e15);
-        float x = (float)(freq * hkt);
-        float ehvkt = __expf(-x);
-        float bnu = 1.47439e-2f * freq15 * freq15 * freq15 * ehvkt / (-expm1f(-x));
-        return (R)(bnu != bnu ? 0.0f : bnu);
-    }
+__device__ __forceinline__ double planck_nu(double freq, double hkt) {
+    double freq15 = freq / 1.0e15;
+    double ehvkt = exp(-freq * hkt);
+    double stim = 1.0 - ehvkt;
+    double bnu = 1.47439e-2 * pow(freq15, 3.0) * ehvkt / stim;
+    return bnu != bnu ? 0.0 : bnu;
+}
+__device__ __forceinline__ float planck_nu(float freq15, float freq_hkt_x) {
+    // freq15^3 * e^-x / (1 - e^-x), x = h nu / k T
+    float bnu = 1.47439e-2f * freq15 * freq15 * freq15 * __fdividef(__expf(-freq_hkt_x), -expm1f(-freq_hkt_x));
+    return bnu != bnu ? 0.0f : bnu;
 }
 
-// One thread per wavelength (radiative.py:42-218 and the per-lambda loop of
-// :282-494).  Field arrays are [L, n]; asynth is the stimulated-emission-
-// corrected line opacity, split by FSCAT into absorption and scattering
-// (opacity.py:2408-2420).
+// One wavelength's depth column (radiative.py:42-218 and the per-lambda loop
+// of :282-494).  Field arrays are [L, n]; in ASYNTH mode the line opacity is
+// the stimulated-emission-corrected ASYNTH, split by FSCAT into absorption
+// and scattering (opacity.py:2408-2420).
 template <typename R, bool REF_SWEEP>
 __device__ __forceinline__ void transfer_column(const TransferArgs& a, const CoefJ32& cj,
                                                 const R* __restrict__ cont_abs,
@@ -1014,45 +1027,56 @@ __device__ __forceinline__ void transfer_column(const TransferArgs& a, const Coe
                                                 const R* __restrict__ line_op,
                                                 const R* __restrict__ line_sc,
                                                 const R* __restrict__ line_src, int64_t j) {
+    constexpr bool F32 = sizeof(R) == 4;
     const int L = a.n_layers;
     R mass[MAX_LAYERS], ca[MAX_LAYERS], cs[MAX_LAYERS], la[MAX_LAYERS], ls[MAX_LAYERS],
-        src[MAX_LAYERS], pl[MAX_LAYERS];
-    double hkts[MAX_LAYERS];
+        src[MAX_LAYERS], pl[MAX_LAYERS], hk[MAX_LAYERS];
     const double wl = a.grid[j];
     const double freq = C_LIGHT_NM / (wl > 1e-12 ? wl : 1e-12);
+    const float freq15_f = (float)(freq / 1.0e15);
+    const float freq_f = (float)freq;
+    const bool has_ls = (!a.asynth_mode && line_sc != nullptr) || (a.asynth_mode && a.line_scat);
+    const bool own_src = line_src != nullptr || (a.slinec_mode && !F32);
     int m = 0;
     for (int d = 0; d < L; d++) {
-        const DepthPar dp = a.depth[d];
-        double cm = dp.rhox;
+        const DepthPar& dp = a.depth[d];
+        R cm = F32 ? (R)dp.rhox_f : (R)dp.rhox;
         R aa = cont_abs[(int64_t)d * a.n + j];
         R ss = cont_scat[(int64_t)d * a.n + j];
-        R lo, lsg;
+        R lo, lsg = R(0);
         if (a.asynth_mode) {
             R A = line_op[(int64_t)d * a.n + j];
-            R fs = (R)dp.fscat;
-            lo = A * (R(1) - fs);
-            R one_m = R(1) - fs;
-            R alinec = lo / (one_m > R(1e-12) ? one_m : R(1e-12));
-            lsg = alinec * fs;
+            if (a.line_scat) {
+                R fs = F32 ? (R)dp.fscat_f : (R)dp.fscat;
+                lo = A * (R(1) - fs);
+                R one_m = R(1) - fs;
+                R alinec = tdiv(lo, one_m > R(1e-12) ? one_m : R(1e-12));
+                lsg = alinec * fs;
+            } else {
+                lo = A;
+            }
         } else {
             lo = line_op[(int64_t)d * a.n + j];
             lsg = line_sc ? line_sc[(int64_t)d * a.n + j] : R(0);
         }
         const R mx = (R)MAX_OPACITY_REAL4;
-        bool ok = cm >= 0.0 && isfinite(cm) && isfinite((double)aa) && isfinite((double)ss) &&
-                  isfinite((double)lo) && isfinite((double)lsg) && aa < mx && ss < mx && lo < mx &&
-                  lsg < mx;
-        if (!ok || !(cm > 0.0)) continue;
-        mass[m] = (R)cm;
+        bool ok = cm >= R(0) && isfinite(cm) && isfinite(aa) && isfinite(ss) && isfinite(lo) &&
+                  isfinite(lsg) && aa < mx && ss < mx && lo < mx && lsg < mx;
+        if (!ok || !(cm > R(0))) continue;
+        mass[m] = cm;
         ca[m] = aa;
         cs[m] = ss;
         la[m] = lo;
-        ls[m] = lsg;
-        hkts[m] = dp.hkt;
+        if (has_ls) ls[m] = lsg;
+        hk[m] = F32 ? (R)dp.hkt_f : (R)dp.hkt;
         if (line_src) {
             R v = line_src[(int64_t)d * a.n + j];
-            src[m] = isfinite((double)v) ? v : planck_nu<R>(freq, dp.hkt);
-        } else if (a.slinec_mode && sizeof(R) == 8) {
+            if (!isfinite(v)) {
+                if constexpr (F32) v = planck_nu(freq15_f, freq_f * dp.hkt_f);
+                else v = planck_nu(freq, dp.hkt);
+            }
+            src[m] = v;
+        } else if (own_src) {
             // SLINEC = BNU*STIM/(1-EHVKT) with the driver's frequency
             // (opacity.py:2215-2227, bfudge.py:144-145)
             double fr = C_LIGHT_CM / (wl * 1.0e-7);
@@ -1061,7 +1085,7 @@ __device__ __forceinline__ void transfer_column(const TransferArgs& a, const Coe
             double st = 1.0 - eh;
             double bnu = 1.47439e-02 * pow(f15, 3.0) * eh / st;
             double v = (bnu * st) / (1.0 - eh);
-            src[m] = isfinite(v) ? (R)v : planck_nu<R>(freq, dp.hkt);
+            src[m] = isfinite(v) ? (R)v : (R)planck_nu(freq, dp.hkt);
         }
         m++;
     }
@@ -1084,23 +1108,22 @@ __device__ __forceinline__ void transfer_column(const TransferArgs& a, const Coe
             t = ca[q]; ca[q] = ca[r]; ca[r] = t;
             t = cs[q]; cs[q] = cs[r]; cs[r] = t;
             t = la[q]; la[q] = la[r]; la[r] = t;
-            t = ls[q]; ls[q] = ls[r]; ls[r] = t;
-            t = src[q]; src[q] = src[r]; src[r] = t;
-            double h = hkts[q]; hkts[q] = hkts[r]; hkts[r] = h;
+            if (has_ls) { t = ls[q]; ls[q] = ls[r]; ls[r] = t; }
+            if (own_src) { t = src[q]; src[q] = src[r]; src[r] = t; }
+            t = hk[q]; hk[q] = hk[r]; hk[r] = t;
         }
     }
-    const bool src_is_planck = !line_src && !(a.slinec_mode && sizeof(R) == 8);
     for (int q = 0; q < m; q++) {
-        pl[q] = planck_nu<R>(freq, hkts[q]);
-        if (src_is_planck) src[q] = pl[q];
+        if constexpr (F32) pl[q] = planck_nu(freq15_f, freq_f * hk[q]);
+        else pl[q] = planck_nu(freq, hk[q]);
     }
-    R zero[MAX_LAYERS];
-    for (int q = 0; q < m; q++) zero[q] = R(0);
     R xtau[NXTAU];
     for (int l = 0; l < NXTAU; l++) xtau[l] = (R)a.xtau[l];
     int itc = 0, itt = 0;
-    double fc = josh_flux<R, REF_SWEEP>(m, ca, pl, zero, pl, cs, zero, mass, xtau, a.ch, cj, a.coefj32, &itc);
-    double ft = josh_flux<R, REF_SWEEP>(m, ca, pl, la, src, cs, ls, mass, xtau, a.ch, cj, a.coefj32, &itt);
+    double fc = josh_flux<R, REF_SWEEP>(m, ca, pl, nullptr, nullptr, cs, nullptr, mass, xtau, a.ch, cj,
+                                        a.coefj32, &itc);
+    double ft = josh_flux<R, REF_SWEEP>(m, ca, pl, la, own_src ? src : pl, cs, has_ls ? ls : nullptr, mass,
+                                        xtau, a.ch, cj, a.coefj32, &itt);
     a.flux_cont[j] = fc;
     a.flux_total[j] = ft;
     if (a.iters) {
