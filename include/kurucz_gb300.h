@@ -220,6 +220,25 @@ ks_status ks_synthesize(const ks_lines *lines, const ks_atmos *atm, const ks_gri
                         double *flux_total, double *flux_cont, void *asynth_out,
                         ks_stats *stats, void *stream);
 
+/* The fused synthesis of ks_synthesize for callers that cannot allocate
+ * device memory: a plug-in running inside a host application that owns all
+ * device memory, or a runtime reached through an FFI with no CUDA allocator,
+ * cannot hand over a workspace.  This entry point allocates nothing (no
+ * cudaMalloc, no cudaFree, no allocating library routine): its scratch is a
+ * fixed 64 MiB array inside the library, so sizes whose ks_workspace_size
+ * exceeds 64 MiB are rejected with KS_ERR_NOMEM (on a 72-layer atmosphere
+ * and a 6,000-point grid about 20,000 lines fit in KS_PREC_MIXED, 8,000 in
+ * KS_PREC_FP64).  The caller still passes
+ * inputs and outputs.  All calls on a device share the array: calls that
+ * overlap on the GPU race and must be serialised.  The first call on each
+ * device looks up the array's device address (and, like every entry point,
+ * copies the constant tables), so make it before any stream capture on that
+ * device.  No stats are returned.  This entry point has no counterpart in the
+ * reference. */
+ks_status ks_synthesize_noalloc(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                                const ks_options *opt, double *flux_total, double *flux_cont,
+                                void *asynth_out, void *stream);
+
 /* ---- gfall reader ---------------------------------------------------------- */
 
 /* Native reader of gfall line lists (synthe_py/io/lines/atomic.py:299

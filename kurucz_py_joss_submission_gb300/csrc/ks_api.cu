@@ -1047,3 +1047,72 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     }
     return KS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// synthesis without any device allocation
+// ---------------------------------------------------------------------------
+
+// Scratch of ks_synthesize_noalloc: a fixed 64 MiB array in the library's own
+// device image.  Every GPU that loads the library holds it until the process
+// exits.  All calls on a device share it, so calls that overlap on the GPU
+// (concurrent streams, or threads) race on it and must be serialised by the
+// caller.  Host code must not use the symbol itself as a device address: the
+// address comes from cudaGetSymbolAddress, per device.
+static const size_t kNoAllocScratchBytes = (size_t)64 << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static void* g_noalloc_ptr[kMaxDevices];
+static std::mutex g_noalloc_mu;
+
+extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos* atm,
+                                           const ks_grid* grid, const ks_options* opt,
+                                           double* flux_total, double* flux_cont, void* asynth_out,
+                                           void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_lines(lines);
+    if (!st) st = check_cont(atm);
+    if (st) return st;
+    if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize_noalloc: NULL flux output");
+    if (opt && (opt->tile_bins < 0 || opt->tile_bins > 8192 || (opt->tile_bins % 32) != 0))
+        return fail(KS_ERR_INVALID, "tile_bins must be a multiple of 32 in [32, 8192] (0 = default)");
+    if (opt && (opt->warps_per_tile < 0 || opt->warps_per_tile > 16))
+        return fail(KS_ERR_INVALID, "warps_per_tile must be in [1, 16] (0 = default)");
+    bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    bool need_asynth = asynth_out == nullptr;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    if (dry.used > kNoAllocScratchBytes)
+        return fail(KS_ERR_NOMEM,
+                    "ks_synthesize_noalloc: these sizes need " + std::to_string(dry.used) +
+                        " bytes of scratch, more than the 64 MiB (67108864 bytes) the no-allocation "
+                        "entry point holds; use ks_synthesize with a caller workspace");
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    int dev = 0;
+    KS_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(KS_ERR_UNSUPPORTED, "device index out of range");
+    void* scratch = nullptr;
+    {
+        // set-up, once per device (this device is current): the device
+        // address of the scratch array
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    Carve c{(char*)scratch, kNoAllocScratchBytes, 0, false};
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    void* asy = asynth_out ? asynth_out : w.asynth;
+    StageTimer tm;  // off: no profiling in this entry point
+    // synthesize_impl clears the counters, flags and reach classes in the
+    // scratch before use; everything else is written before it is read.
+    if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s, tm);
+    else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s, tm);
+    return st;
+}
