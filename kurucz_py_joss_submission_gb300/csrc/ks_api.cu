@@ -686,6 +686,18 @@ static ks_status run_partition(const Workspace& w, int L, cudaStream_t s) {
     return KS_OK;
 }
 
+// The accumulation tile: each warp owns tile_bins / warps_per_tile bins, a
+// multiple of 32 and at most 4 per lane.
+static ks_status check_tiling(const ks_options* opt) {
+    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : 512;
+    int w = opt && opt->warps_per_tile > 0 ? opt->warps_per_tile : 8;
+    if ((opt && (opt->tile_bins < 0 || opt->warps_per_tile < 0)) || w > 16 || t % (32 * w) != 0 ||
+        t / (32 * w) > 4)
+        return fail(KS_ERR_INVALID,
+                    "tile_bins must be 32 * warps_per_tile * (1..4), warps_per_tile <= 16 (0 = defaults 512, 8)");
+    return KS_OK;
+}
+
 static int default_tile(const ks_options* opt, bool fp64) {
     int t = opt && opt->tile_bins > 0 ? opt->tile_bins : 512;
     return t;
@@ -1017,10 +1029,7 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     if (!st) st = check_cont(atm);
     if (st) return st;
     if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize: NULL flux output");
-    if (opt && (opt->tile_bins < 0 || opt->tile_bins > 8192 || (opt->tile_bins % 32) != 0))
-        return fail(KS_ERR_INVALID, "tile_bins must be a multiple of 32 in [32, 8192] (0 = default)");
-    if (opt && (opt->warps_per_tile < 0 || opt->warps_per_tile > 16))
-        return fail(KS_ERR_INVALID, "warps_per_tile must be in [1, 16] (0 = default)");
+    if ((st = check_tiling(opt))) return st;
     DevTables t;
     if ((st = device_tables(&t))) return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1073,10 +1082,7 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     if (!st) st = check_cont(atm);
     if (st) return st;
     if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize_noalloc: NULL flux output");
-    if (opt && (opt->tile_bins < 0 || opt->tile_bins > 8192 || (opt->tile_bins % 32) != 0))
-        return fail(KS_ERR_INVALID, "tile_bins must be a multiple of 32 in [32, 8192] (0 = default)");
-    if (opt && (opt->warps_per_tile < 0 || opt->warps_per_tile > 16))
-        return fail(KS_ERR_INVALID, "warps_per_tile must be in [1, 16] (0 = default)");
+    if ((st = check_tiling(opt))) return st;
     bool fp64 = opt && opt->precision == KS_PREC_FP64;
     bool need_asynth = asynth_out == nullptr;
     Carve dry{nullptr, 0, 0, true};

@@ -3,6 +3,7 @@
 // (synthe_py/physics/line_opacity.py:39-49, engine/radiative.py:14-17).
 #pragma once
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 

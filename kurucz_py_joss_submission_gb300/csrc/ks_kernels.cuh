@@ -454,6 +454,9 @@ template <typename R> struct Cell;
 template <> struct Cell<float> { using T = float2; };
 template <> struct Cell<double> { using T = double; };
 
+__device__ __forceinline__ void kahan_acc(float& s, float& c, float v) { kahan_add(s, c, v); }
+__device__ __forceinline__ void kahan_acc(double& s, double& c, double v) { (void)c; s += v; }
+
 __device__ __forceinline__ void cell_add(float2* c, int b, float v) {
     float2 t = c[b];
     kahan_add(t.x, t.y, v);
@@ -500,19 +503,32 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
     }
 }
 
-// One CTA per (lambda tile, depth).  For every reach class k it selects the
-// pairs whose wing centre lies within 2^k (+1) bins of the tile -- a
-// contiguous range of that class's centre-sorted list.  Warps take those
-// pairs in batches of 32 (batch b -> warp b mod nwarps, a fixed order).
-// Each lane loads one pair's descriptor and works out, for its pair, the
-// offsets whose red bin c+o and blue bin c-o fall in the tile, split at
-// N10DOP into the near (table/Voigt) and far (X/o^2) zones; a ballot drops
-// pairs that miss the tile.  The warp then walks the remaining pairs,
-// broadcasting each pair's ranges by shuffles, and runs up to four
-// branch-free loops (red/blue x near/far) with lanes on consecutive offsets,
-// adding into the warp's own shared-memory copy of the tile -- no two lanes
-// write the same word, so no atomics are needed.  The copies are summed in
-// warp order, multiplied by STIM (line_opacity.py:1338) and stored coalesced.
+// First reach class handled by the bin-owner pass (reach > 2^(LONG_CLASS-1)).
+constexpr int LONG_CLASS = 8;
+constexpr int LONG_CHUNK = 256;   // long pairs staged in shared memory at a time
+constexpr int MAX_BPL = 4;        // tile bins owned per lane in the bin-owner pass
+
+// One CTA per (lambda tile, depth).  For every reach class k the contributing
+// pairs are those whose wing centre lies within 2^k (+1) bins of the tile --
+// a contiguous range of that class's centre-sorted list.  Two passes:
+//
+// * Short and medium pairs (reach <= 2^(LONG_CLASS-1)), pair-major: warps
+//   take batches of 32 pairs (batch b -> warp b mod nwarps).  Each lane loads
+//   one pair's descriptor and works out its in-tile red/blue x near/far
+//   offset ranges; a ballot drops pairs that miss the tile; the warp walks the
+//   rest, broadcasting each pair by shuffles, with lanes on consecutive
+//   offsets, adding into the warp's own shared-memory copy of the tile as
+//   Kahan pairs -- no two lanes write the same word, no atomics.
+// * Long pairs (most of the evaluations), bin-owner: they are staged in shared
+//   memory LONG_CHUNK at a time and every warp walks all of them over the
+//   tile bins it owns (each lane owns bins warp*W/nwarps + lane + 32*i),
+//   accumulating Kahan pairs in registers -- every warp does the same number
+//   of pairs, so the passes stay balanced and no shared-memory word is
+//   read-modified-written.
+//
+// Each owned bin is then the Kahan sum of the warp copies (in warp order) and
+// the register sum, times STIM (line_opacity.py:1338), stored coalesced.  The
+// order of every sum is fixed, so results are bit-identical across runs.
 template <typename R>
 __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
                                                          R* __restrict__ out) {
@@ -526,11 +542,11 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const int d = blockIdx.y;
     const int T0 = blockIdx.x * W;
     const int T1 = (int)min((int64_t)T0 + W, a.n_wl);
-    const int span = T1 - T0;
 
     R2* h01 = reinterpret_cast<R2*>(smem_raw);  // interleaved (H0, H1)
     size_t tab_bytes = (VOIGT_N * sizeof(R2) + 15) & ~size_t(15);
     CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
+    PairDesc<R>* lng = reinterpret_cast<PairDesc<R>*>(smem_raw + tab_bytes + sizeof(CellT) * nwarps * W);
     __shared__ int64_t cls_lo[N_REACH_CLASSES];
     __shared__ int64_t cls_base[N_REACH_CLASSES + 1];
     __shared__ int64_t cls_hi_s[N_REACH_CLASSES];
@@ -569,102 +585,174 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     }
     __syncthreads();
 
-    CellT* my = acc + warp * W;
-    const int64_t total = cls_base[N_REACH_CLASSES];
     const PairDesc<R>* drow = desc + (int64_t)d * a.stride;
     unsigned long long evals = 0;
-    const int64_t nbatch = (total + 31) >> 5;
-    int kcur = 0;
-    for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
-        // ---- per lane: one pair and its in-tile offset ranges ----
-        const int64_t item = bt * 32 + lane;
-        int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
-        R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
-        bool far = false;
-        if (item < total) {
-            while (item >= cls_base[kcur + 1]) kcur++;
-            while (kcur > 0 && item < cls_base[kcur]) kcur--;
-            const int64_t p = a.class_pos[cls_lo[kcur] + (item - cls_base[kcur])];
-            const PairDesc<R> pd = drow[p];
-            c = pd.wing_c;
-            const int ctr = pd.ctr_n10 & 15;
-            if (ctr) {
-                int cc = c + (ctr - 8);
-                if (cc >= T0 && cc < T1) {
-                    cb = cc - T0;
-                    kc = pd.kapcen;
-                    evals++;
+
+    // ------------------------------------------------ short/medium, pair-major
+    {
+        CellT* my = acc + warp * W;
+        const int64_t total = cls_base[LONG_CLASS];
+        const int64_t nbatch = (total + 31) >> 5;
+        int kcur = 0;
+        for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
+            const int64_t item = bt * 32 + lane;
+            int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
+            R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
+            if (item < total) {
+                while (item >= cls_base[kcur + 1]) kcur++;
+                const int64_t p = a.class_pos[cls_lo[kcur] + (item - cls_base[kcur])];
+                const PairDesc<R> pd = drow[p];
+                c = pd.wing_c;
+                const int ctr = pd.ctr_n10 & 15;
+                if (ctr) {
+                    int cc = c + (ctr - 8);
+                    if (cc >= T0 && cc < T1) {
+                        cb = cc - T0;
+                        kc = pd.kapcen;
+                        evals++;
+                    }
+                }
+                const int reach = pd.maxstep_far & 0x7fffffff;
+                if (reach > 0) {
+                    rlo = max(1, T0 - c);
+                    rhi = min(reach, T1 - 1 - c);
+                    blo = max(1, c - (T1 - 1));
+                    bhi = min(reach, c - T0);
+                    if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
+                    if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
+                }
+                nz = pd.maxstep_far < 0 ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
+                k0 = pd.kappa0;
+                ad = pd.adamp;
+                dv = pd.dvoigt;
+                xf = pd.xfar;
+            }
+            const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
+            unsigned mask = __ballot_sync(0xffffffffu, active);
+            while (mask) {
+                const int i = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int ci = __shfl_sync(0xffffffffu, c, i);
+                const int cbi = __shfl_sync(0xffffffffu, cb, i);
+                if (cbi >= 0) {
+                    const R kci = __shfl_sync(0xffffffffu, kc, i);
+                    if (lane == 0) cell_add(my, cbi, kci);
+                }
+                const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
+                const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
+                if (rl > rh && bl > bh) continue;
+                const int nzi = __shfl_sync(0xffffffffu, nz, i);
+                const R adi = __shfl_sync(0xffffffffu, ad, i);
+                const R dvi = __shfl_sync(0xffffffffu, dv, i);
+                const R k0i = __shfl_sync(0xffffffffu, k0, i);
+                const R xfi = __shfl_sync(0xffffffffu, xf, i);
+                const R ts = R(200) * dvi;
+                const int base = ci - T0;
+                wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                if (nzi != 0x7fffffff) {
+                    wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                 }
             }
-            const int reach = pd.maxstep_far & 0x7fffffff;
-            if (reach > 0) {
-                rlo = max(1, T0 - c);
-                rhi = min(reach, T1 - 1 - c);
-                blo = max(1, c - (T1 - 1));
-                bhi = min(reach, c - T0);
-                if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
-                if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
-            }
-            far = pd.maxstep_far < 0;
-            nz = far ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
-            k0 = pd.kappa0;
-            ad = pd.adamp;
-            dv = pd.dvoigt;
-            xf = pd.xfar;
         }
-        const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
-        unsigned mask = __ballot_sync(0xffffffffu, active);
-        while (mask) {
-            const int i = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int ci = __shfl_sync(0xffffffffu, c, i);
-            const int cbi = __shfl_sync(0xffffffffu, cb, i);
-            if (cbi >= 0) {
-                const R kci = __shfl_sync(0xffffffffu, kc, i);
-                if (lane == 0) cell_add(my, cbi, kci);
+    }
+
+    // ------------------------------------------------ long pairs, bin-owner
+    const int per_warp = W / nwarps;           // bins owned by a warp (multiple of 32)
+    const int bpl = per_warp >> 5;             // bins per lane (<= MAX_BPL)
+    const int wb0 = T0 + warp * per_warp;      // first owned bin (absolute)
+    R ls[MAX_BPL], lc[MAX_BPL];
+#pragma unroll
+    for (int q = 0; q < MAX_BPL; q++) ls[q] = lc[q] = R(0);
+    {
+        const int64_t lbase = cls_base[LONG_CLASS];
+        const int64_t ltotal = cls_base[N_REACH_CLASSES] - lbase;
+        int kcur = LONG_CLASS;
+        for (int64_t c0 = 0; c0 < ltotal; c0 += LONG_CHUNK) {
+            const int cnt = (int)min((int64_t)LONG_CHUNK, ltotal - c0);
+            __syncthreads();  // previous chunk fully consumed
+            for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+                const int64_t item = lbase + c0 + t;
+                int k = kcur;
+                while (item >= cls_base[k + 1]) k++;
+                const int64_t p = a.class_pos[cls_lo[k] + (item - cls_base[k])];
+                lng[t] = drow[p];
             }
-            const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
-            const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
-            if (rl > rh && bl > bh) continue;
-            const int nzi = __shfl_sync(0xffffffffu, nz, i);
-            const R adi = __shfl_sync(0xffffffffu, ad, i);
-            const R dvi = __shfl_sync(0xffffffffu, dv, i);
-            const R k0i = __shfl_sync(0xffffffffu, k0, i);
-            const R xfi = __shfl_sync(0xffffffffu, xf, i);
-            const R ts = R(200) * dvi;
-            const int rbase = ci - T0, bbase = ci - T0;
-            // red: bins rbase + o; blue: bins bbase - o
-            wing_run<R, R2, CellT, false>(my, rbase, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-            wing_run<R, R2, CellT, false>(my, bbase, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-            if (nzi != 0x7fffffff) {
-                wing_run<R, R2, CellT, true>(my, rbase, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                wing_run<R, R2, CellT, true>(my, bbase, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+            {
+                const int64_t last = lbase + c0 + cnt - 1;
+                while (last >= cls_base[kcur + 1]) kcur++;
+            }
+            __syncthreads();
+            for (int t = 0; t < cnt; t++) {
+                const PairDesc<R> pd = lng[t];
+                const int c = pd.wing_c;
+                const int reach = pd.maxstep_far & 0x7fffffff;
+                const int ctr = pd.ctr_n10 & 15;
+                const int cb = ctr ? c + (ctr - 8) : INT_MIN;
+                // does the pair touch this warp's bins [wb0, wb0 + per_warp)?
+                const int lo = ctr ? min(c - reach, cb) : c - reach;
+                const int hi = ctr ? max(c + reach, cb) : c + reach;
+                if (hi < wb0 || lo >= wb0 + per_warp) continue;
+                const bool far = pd.maxstep_far < 0;
+                const int nzi = far ? (pd.ctr_n10 >> 8) : 0x7fffffff;
+                const R ts = R(200) * pd.dvoigt;
+#pragma unroll
+                for (int q = 0; q < MAX_BPL; q++) {
+                    if (q >= bpl) break;
+                    const int b = wb0 + lane + 32 * q;
+                    if (b >= T1) continue;
+                    if (b == cb) {
+                        kahan_acc(ls[q], lc[q], pd.kapcen);
+                        evals++;
+                    }
+                    const int o = b > c ? b - c : c - b;
+                    if (o == 0 || o > reach) continue;
+                    R v;
+                    if (o > nzi) {
+                        R oo = (R)o * (R)o;
+                        if constexpr (sizeof(R) == 4) v = __fdividef(pd.xfar, oo);
+                        else v = pd.xfar / oo;
+                    } else {
+                        v = near_profile_tab<R, R2>(o, pd.dvoigt, ts, pd.adamp, pd.kappa0, h01, gh0, gh1, gh2);
+                    }
+                    kahan_acc(ls[q], lc[q], v);
+                    evals++;
+                }
             }
         }
     }
     __syncthreads();
-    // combine the warp copies in warp order, apply STIM and store
+    // ------------------------------------------------ combine, STIM, store
     const DepthPar dp = a.depth[d];
-    for (int b = threadIdx.x; b < span; b += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < MAX_BPL; q++) {
+        if (q >= bpl) break;
+        const int b = wb0 + lane + 32 * q;
+        if (b >= T1) continue;
+        const int bl = b - T0;
         R v;
         if constexpr (sizeof(R) == 4) {
             float s = 0.f, cp = 0.f;
             for (int w = 0; w < nwarps; w++) {
-                float2 t = acc[w * W + b];
+                float2 t = acc[w * W + bl];
                 kahan_add(s, cp, t.x);
                 kahan_add(s, cp, -t.y);
             }
-            float freq = (float)(C_LIGHT_NM / a.grid[T0 + b]);
+            kahan_add(s, cp, ls[q]);
+            kahan_add(s, cp, -lc[q]);
+            float freq = (float)(C_LIGHT_NM / a.grid[b]);
             float stim = -expm1f(-freq * (float)dp.hkt_asynth);
             v = s * stim;
         } else {
             double s = 0.0;
-            for (int w = 0; w < nwarps; w++) s += acc[w * W + b];
-            double freq = C_LIGHT_NM / a.grid[T0 + b];
+            for (int w = 0; w < nwarps; w++) s += acc[w * W + bl];
+            s += ls[q];
+            double freq = C_LIGHT_NM / a.grid[b];
             double stim = 1.0 - exp(-freq * dp.hkt_asynth);
             v = (R)(s * stim);
         }
-        out[(int64_t)d * a.n_wl + T0 + b] = v;
+        out[(int64_t)d * a.n_wl + b] = v;
     }
     // evaluation counter: warp sum, one atomic per warp
     if (a.evals) {

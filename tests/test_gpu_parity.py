@@ -147,7 +147,7 @@ def test_evaluation_count_matches_oracle(name):
     assert abs(st32["valid_pairs"] - st["valid_pairs"]) <= max(2, st["valid_pairs"] // 10000)
 
 
-@pytest.mark.parametrize("tile,warps", [(256, 4), (512, 8), (2048, 8), (1024, 16)])
+@pytest.mark.parametrize("tile,warps", [(256, 4), (512, 8), (1024, 8), (512, 16), (2048, 16)])
 def test_tiling_does_not_change_fp64_result(tile, warps):
     name = "uv_300_302"
     g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps)
