@@ -503,7 +503,7 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
     }
 }
 
-// First reach class handled by the bin-owner pass (reach > 2^(LONG_CLASS-1)).
+// Default first reach class of the bin-owner pass (reach > 2^(class-1)).
 constexpr int LONG_CLASS = 8;
 constexpr int LONG_CHUNK = 256;   // long pairs staged in shared memory at a time
 constexpr int MAX_BPL = 4;        // tile bins owned per lane in the bin-owner pass
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     // ------------------------------------------------ short/medium, pair-major
     {
         CellT* my = acc + warp * W;
-        const int64_t total = cls_base[LONG_CLASS];
+        const int64_t total = cls_base[a.long_class];
         const int64_t nbatch = (total + 31) >> 5;
         int kcur = 0;
         for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
@@ -666,9 +666,9 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
 #pragma unroll
     for (int q = 0; q < MAX_BPL; q++) ls[q] = lc[q] = R(0);
     {
-        const int64_t lbase = cls_base[LONG_CLASS];
+        const int64_t lbase = cls_base[a.long_class];
         const int64_t ltotal = cls_base[N_REACH_CLASSES] - lbase;
-        int kcur = LONG_CLASS;
+        int kcur = a.long_class;
         for (int64_t c0 = 0; c0 < ltotal; c0 += LONG_CHUNK) {
             const int cnt = (int)min((int64_t)LONG_CHUNK, ltotal - c0);
             __syncthreads();  // previous chunk fully consumed
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
             }
             {
                 const int64_t last = lbase + c0 + cnt - 1;
-                while (last >= cls_base[kcur + 1]) kcur++;
+                while (kcur < N_REACH_CLASSES - 1 && last >= cls_base[kcur + 1]) kcur++;
             }
             __syncthreads();
             for (int t = 0; t < cnt; t++) {

@@ -147,10 +147,11 @@ def test_evaluation_count_matches_oracle(name):
     assert abs(st32["valid_pairs"] - st["valid_pairs"]) <= max(2, st["valid_pairs"] // 10000)
 
 
-@pytest.mark.parametrize("tile,warps", [(256, 4), (512, 8), (1024, 8), (512, 16), (2048, 16)])
-def test_tiling_does_not_change_fp64_result(tile, warps):
+@pytest.mark.parametrize("tile,warps,long_class", [(256, 4, 0), (512, 8, 0), (1024, 8, 0), (512, 16, 0),
+                                                   (512, 8, 22), (512, 8, 4), (1024, 16, 6)])
+def test_tiling_does_not_change_fp64_result(tile, warps, long_class):
     name = "uv_300_302"
-    g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps)
+    g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps, long_class=long_class)
     assert rel(syn.asynth.cpu().numpy(), g["asynth"]) < 1e-12
 
 
