@@ -503,8 +503,6 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
     }
 }
 
-// Default first reach class of the bin-owner pass (reach > 2^(class-1)).
-constexpr int LONG_CLASS = 8;
 constexpr int LONG_CHUNK = 256;   // long pairs staged in shared memory at a time
 constexpr int MAX_BPL = 4;        // tile bins owned per lane in the bin-owner pass
 
