@@ -686,15 +686,18 @@ static ks_status run_partition(const Workspace& w, int L, cudaStream_t s) {
     return KS_OK;
 }
 
-// The accumulation tile: each warp owns tile_bins / warps_per_tile bins, a
-// multiple of 32 and at most 4 per lane.
+// The accumulation tile: a multiple of 32 bins, at most 8192, with 1-16
+// warps, whose per-warp copies must fit the 227 KB of shared memory.
 static ks_status check_tiling(const ks_options* opt) {
     int t = opt && opt->tile_bins > 0 ? opt->tile_bins : 512;
     int w = opt && opt->warps_per_tile > 0 ? opt->warps_per_tile : 8;
-    if ((opt && (opt->tile_bins < 0 || opt->warps_per_tile < 0)) || w > 16 || t % (32 * w) != 0 ||
-        t / (32 * w) > 4)
+    bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    if ((opt && (opt->tile_bins < 0 || opt->warps_per_tile < 0)) || w > 16 || t % 32 != 0 || t > 8192)
         return fail(KS_ERR_INVALID,
-                    "tile_bins must be 32 * warps_per_tile * (1..4), warps_per_tile <= 16 (0 = defaults 512, 8)");
+                    "tile_bins must be a multiple of 32 up to 8192 and warps_per_tile 1..16 (0 = defaults 512, 8)");
+    size_t smem = fp64 ? accumulate_smem_bytes_f64(t, w) : accumulate_smem_bytes_f32(t, w);
+    if (smem > 227 * 1024)
+        return fail(KS_ERR_INVALID, "tile_bins x warps_per_tile needs more than 227 KB of shared memory");
     return KS_OK;
 }
 

@@ -503,30 +503,21 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
     }
 }
 
-constexpr int LONG_CHUNK = 256;   // long pairs staged in shared memory at a time
-constexpr int MAX_BPL = 4;        // tile bins owned per lane in the bin-owner pass
-
 // One CTA per (lambda tile, depth).  For every reach class k the contributing
 // pairs are those whose wing centre lies within 2^k (+1) bins of the tile --
-// a contiguous range of that class's centre-sorted list.  Two passes:
-//
-// * Short and medium pairs (reach <= 2^(LONG_CLASS-1)), pair-major: warps
-//   take batches of 32 pairs (batch b -> warp b mod nwarps).  Each lane loads
-//   one pair's descriptor and works out its in-tile red/blue x near/far
-//   offset ranges; a ballot drops pairs that miss the tile; the warp walks the
-//   rest, broadcasting each pair by shuffles, with lanes on consecutive
-//   offsets, adding into the warp's own shared-memory copy of the tile as
-//   Kahan pairs -- no two lanes write the same word, no atomics.
-// * Long pairs (most of the evaluations), bin-owner: they are staged in shared
-//   memory LONG_CHUNK at a time and every warp walks all of them over the
-//   tile bins it owns (each lane owns bins warp*W/nwarps + lane + 32*i),
-//   accumulating Kahan pairs in registers -- every warp does the same number
-//   of pairs, so the passes stay balanced and no shared-memory word is
-//   read-modified-written.
-//
-// Each owned bin is then the Kahan sum of the warp copies (in warp order) and
-// the register sum, times STIM (line_opacity.py:1338), stored coalesced.  The
-// order of every sum is fixed, so results are bit-identical across runs.
+// a contiguous range of that class's centre-sorted list.  The pairs are dealt
+// to the warps in batches, round-robin in a fixed order: 32 pairs per batch
+// below class long_class (many short pairs, each a little work) and one pair
+// per batch from long_class up (few long pairs, each a lot of work), so the
+// long pairs spread over all warps instead of landing on one.  In a batch
+// each lane loads one pair's descriptor and works out its in-tile red/blue x
+// near/far offset ranges; a ballot drops pairs that miss the tile; the warp
+// walks the rest, broadcasting each pair by shuffles, and runs up to four
+// branch-free loops with lanes on consecutive offsets, adding into the warp's
+// own shared-memory copy of the tile as Kahan pairs -- no two lanes write the
+// same word, so no atomics.  The copies are then summed in warp order,
+// multiplied by STIM (line_opacity.py:1338) and stored coalesced.  Every sum
+// has a fixed order, so results are bit-identical across runs.
 template <typename R>
 __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
                                                          R* __restrict__ out) {
@@ -540,14 +531,15 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const int d = blockIdx.y;
     const int T0 = blockIdx.x * W;
     const int T1 = (int)min((int64_t)T0 + W, a.n_wl);
+    const int span = T1 - T0;
 
     R2* h01 = reinterpret_cast<R2*>(smem_raw);  // interleaved (H0, H1)
     size_t tab_bytes = (VOIGT_N * sizeof(R2) + 15) & ~size_t(15);
     CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
-    PairDesc<R>* lng = reinterpret_cast<PairDesc<R>*>(smem_raw + tab_bytes + sizeof(CellT) * nwarps * W);
     __shared__ int64_t cls_lo[N_REACH_CLASSES];
     __shared__ int64_t cls_base[N_REACH_CLASSES + 1];
     __shared__ int64_t cls_hi_s[N_REACH_CLASSES];
+    __shared__ int64_t bat_base[N_REACH_CLASSES + 1];  // first batch of each class
 
     const R* gh0 = sizeof(R) == 8 ? (const R*)a.h0d : (const R*)a.h0f;
     const R* gh1 = sizeof(R) == 8 ? (const R*)a.h1d : (const R*)a.h1f;
@@ -574,183 +566,113 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        int64_t b = 0;
+        int64_t b = 0, nb = 0;
         for (int k = 0; k < N_REACH_CLASSES; k++) {
+            const int64_t n = cls_hi_s[k] - cls_lo[k];
             cls_base[k] = b;
-            b += cls_hi_s[k] - cls_lo[k];
+            bat_base[k] = nb;
+            b += n;
+            nb += k < a.long_class ? (n + 31) >> 5 : n;
         }
         cls_base[N_REACH_CLASSES] = b;
+        bat_base[N_REACH_CLASSES] = nb;
     }
     __syncthreads();
 
+    CellT* my = acc + warp * W;
     const PairDesc<R>* drow = desc + (int64_t)d * a.stride;
     unsigned long long evals = 0;
-
-    // ------------------------------------------------ short/medium, pair-major
-    {
-        CellT* my = acc + warp * W;
-        const int64_t total = cls_base[a.long_class];
-        const int64_t nbatch = (total + 31) >> 5;
-        int kcur = 0;
-        for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
-            const int64_t item = bt * 32 + lane;
-            int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
-            R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
-            if (item < total) {
-                while (item >= cls_base[kcur + 1]) kcur++;
-                const int64_t p = a.class_pos[cls_lo[kcur] + (item - cls_base[kcur])];
-                const PairDesc<R> pd = drow[p];
-                c = pd.wing_c;
-                const int ctr = pd.ctr_n10 & 15;
-                if (ctr) {
-                    int cc = c + (ctr - 8);
-                    if (cc >= T0 && cc < T1) {
-                        cb = cc - T0;
-                        kc = pd.kapcen;
-                        evals++;
-                    }
-                }
-                const int reach = pd.maxstep_far & 0x7fffffff;
-                if (reach > 0) {
-                    rlo = max(1, T0 - c);
-                    rhi = min(reach, T1 - 1 - c);
-                    blo = max(1, c - (T1 - 1));
-                    bhi = min(reach, c - T0);
-                    if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
-                    if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
-                }
-                nz = pd.maxstep_far < 0 ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
-                k0 = pd.kappa0;
-                ad = pd.adamp;
-                dv = pd.dvoigt;
-                xf = pd.xfar;
-            }
-            const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
-            unsigned mask = __ballot_sync(0xffffffffu, active);
-            while (mask) {
-                const int i = __ffs(mask) - 1;
-                mask &= mask - 1;
-                const int ci = __shfl_sync(0xffffffffu, c, i);
-                const int cbi = __shfl_sync(0xffffffffu, cb, i);
-                if (cbi >= 0) {
-                    const R kci = __shfl_sync(0xffffffffu, kc, i);
-                    if (lane == 0) cell_add(my, cbi, kci);
-                }
-                const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
-                const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
-                if (rl > rh && bl > bh) continue;
-                const int nzi = __shfl_sync(0xffffffffu, nz, i);
-                const R adi = __shfl_sync(0xffffffffu, ad, i);
-                const R dvi = __shfl_sync(0xffffffffu, dv, i);
-                const R k0i = __shfl_sync(0xffffffffu, k0, i);
-                const R xfi = __shfl_sync(0xffffffffu, xf, i);
-                const R ts = R(200) * dvi;
-                const int base = ci - T0;
-                wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                if (nzi != 0x7fffffff) {
-                    wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                    wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                }
-            }
-        }
-    }
-
-    // ------------------------------------------------ long pairs, bin-owner
-    const int per_warp = W / nwarps;           // bins owned by a warp (multiple of 32)
-    const int bpl = per_warp >> 5;             // bins per lane (<= MAX_BPL)
-    const int wb0 = T0 + warp * per_warp;      // first owned bin (absolute)
-    R ls[MAX_BPL], lc[MAX_BPL];
-#pragma unroll
-    for (int q = 0; q < MAX_BPL; q++) ls[q] = lc[q] = R(0);
-    {
-        const int64_t lbase = cls_base[a.long_class];
-        const int64_t ltotal = cls_base[N_REACH_CLASSES] - lbase;
-        int kcur = a.long_class;
-        for (int64_t c0 = 0; c0 < ltotal; c0 += LONG_CHUNK) {
-            const int cnt = (int)min((int64_t)LONG_CHUNK, ltotal - c0);
-            __syncthreads();  // previous chunk fully consumed
-            for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-                const int64_t item = lbase + c0 + t;
-                int k = kcur;
-                while (item >= cls_base[k + 1]) k++;
-                const int64_t p = a.class_pos[cls_lo[k] + (item - cls_base[k])];
-                lng[t] = drow[p];
-            }
-            {
-                const int64_t last = lbase + c0 + cnt - 1;
-                while (kcur < N_REACH_CLASSES - 1 && last >= cls_base[kcur + 1]) kcur++;
-            }
-            __syncthreads();
-            for (int t = 0; t < cnt; t++) {
-                const PairDesc<R> pd = lng[t];
-                const int c = pd.wing_c;
-                const int reach = pd.maxstep_far & 0x7fffffff;
-                const int ctr = pd.ctr_n10 & 15;
-                const int cb = ctr ? c + (ctr - 8) : INT_MIN;
-                // does the pair touch this warp's bins [wb0, wb0 + per_warp)?
-                const int lo = ctr ? min(c - reach, cb) : c - reach;
-                const int hi = ctr ? max(c + reach, cb) : c + reach;
-                if (hi < wb0 || lo >= wb0 + per_warp) continue;
-                const bool far = pd.maxstep_far < 0;
-                const int nzi = far ? (pd.ctr_n10 >> 8) : 0x7fffffff;
-                const R ts = R(200) * pd.dvoigt;
-#pragma unroll
-                for (int q = 0; q < MAX_BPL; q++) {
-                    if (q >= bpl) break;
-                    const int b = wb0 + lane + 32 * q;
-                    if (b >= T1) continue;
-                    if (b == cb) {
-                        kahan_acc(ls[q], lc[q], pd.kapcen);
-                        evals++;
-                    }
-                    const int o = b > c ? b - c : c - b;
-                    if (o == 0 || o > reach) continue;
-                    R v;
-                    if (o > nzi) {
-                        R oo = (R)o * (R)o;
-                        if constexpr (sizeof(R) == 4) v = __fdividef(pd.xfar, oo);
-                        else v = pd.xfar / oo;
-                    } else {
-                        v = near_profile_tab<R, R2>(o, pd.dvoigt, ts, pd.adamp, pd.kappa0, h01, gh0, gh1, gh2);
-                    }
-                    kahan_acc(ls[q], lc[q], v);
+    const int64_t nbatch = bat_base[N_REACH_CLASSES];
+    int kb = 0;
+    for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
+        while (bt >= bat_base[kb + 1]) kb++;
+        const bool wide = kb < a.long_class;
+        const int64_t first = cls_base[kb] + (wide ? (bt - bat_base[kb]) * 32 : (bt - bat_base[kb]));
+        const int cnt = wide ? (int)min((int64_t)32, cls_base[kb + 1] - first) : 1;
+        // ---- per lane: one pair and its in-tile offset ranges ----
+        int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
+        R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
+        if (lane < cnt) {
+            const int64_t p = a.class_pos[cls_lo[kb] + (first + lane - cls_base[kb])];
+            const PairDesc<R> pd = drow[p];
+            c = pd.wing_c;
+            const int ctr = pd.ctr_n10 & 15;
+            if (ctr) {
+                int cc = c + (ctr - 8);
+                if (cc >= T0 && cc < T1) {
+                    cb = cc - T0;
+                    kc = pd.kapcen;
                     evals++;
                 }
             }
+            const int reach = pd.maxstep_far & 0x7fffffff;
+            if (reach > 0) {
+                rlo = max(1, T0 - c);
+                rhi = min(reach, T1 - 1 - c);
+                blo = max(1, c - (T1 - 1));
+                bhi = min(reach, c - T0);
+                if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
+                if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
+            }
+            nz = pd.maxstep_far < 0 ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
+            k0 = pd.kappa0;
+            ad = pd.adamp;
+            dv = pd.dvoigt;
+            xf = pd.xfar;
+        }
+        const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
+        unsigned mask = __ballot_sync(0xffffffffu, active);
+        while (mask) {
+            const int i = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int ci = __shfl_sync(0xffffffffu, c, i);
+            const int cbi = __shfl_sync(0xffffffffu, cb, i);
+            if (cbi >= 0) {
+                const R kci = __shfl_sync(0xffffffffu, kc, i);
+                if (lane == 0) cell_add(my, cbi, kci);
+            }
+            const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
+            const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
+            if (rl > rh && bl > bh) continue;
+            const int nzi = __shfl_sync(0xffffffffu, nz, i);
+            const R adi = __shfl_sync(0xffffffffu, ad, i);
+            const R dvi = __shfl_sync(0xffffffffu, dv, i);
+            const R k0i = __shfl_sync(0xffffffffu, k0, i);
+            const R xfi = __shfl_sync(0xffffffffu, xf, i);
+            const R ts = R(200) * dvi;
+            const int base = ci - T0;
+            // red: bins base + o; blue: bins base - o
+            wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+            wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+            if (nzi != 0x7fffffff) {
+                wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+            }
         }
     }
     __syncthreads();
-    // ------------------------------------------------ combine, STIM, store
+    // combine the warp copies in warp order, apply STIM and store
     const DepthPar dp = a.depth[d];
-#pragma unroll
-    for (int q = 0; q < MAX_BPL; q++) {
-        if (q >= bpl) break;
-        const int b = wb0 + lane + 32 * q;
-        if (b >= T1) continue;
-        const int bl = b - T0;
+    for (int b = threadIdx.x; b < span; b += blockDim.x) {
         R v;
         if constexpr (sizeof(R) == 4) {
             float s = 0.f, cp = 0.f;
             for (int w = 0; w < nwarps; w++) {
-                float2 t = acc[w * W + bl];
+                float2 t = acc[w * W + b];
                 kahan_add(s, cp, t.x);
                 kahan_add(s, cp, -t.y);
             }
-            kahan_add(s, cp, ls[q]);
-            kahan_add(s, cp, -lc[q]);
-            float freq = (float)(C_LIGHT_NM / a.grid[b]);
+            float freq = (float)(C_LIGHT_NM / a.grid[T0 + b]);
             float stim = -expm1f(-freq * (float)dp.hkt_asynth);
             v = s * stim;
         } else {
             double s = 0.0;
-            for (int w = 0; w < nwarps; w++) s += acc[w * W + bl];
-            s += ls[q];
-            double freq = C_LIGHT_NM / a.grid[b];
+            for (int w = 0; w < nwarps; w++) s += acc[w * W + b];
+            double freq = C_LIGHT_NM / a.grid[T0 + b];
             double stim = 1.0 - exp(-freq * dp.hkt_asynth);
             v = (R)(s * stim);
         }
-        out[(int64_t)d * a.n_wl + b] = v;
+        out[(int64_t)d * a.n_wl + T0 + b] = v;
     }
     // evaluation counter: warp sum, one atomic per warp
     if (a.evals) {

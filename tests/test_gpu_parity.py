@@ -148,7 +148,7 @@ def test_evaluation_count_matches_oracle(name):
 
 
 @pytest.mark.parametrize("tile,warps,long_class", [(256, 4, 0), (512, 8, 0), (1024, 8, 0), (512, 16, 0),
-                                                   (512, 8, 22), (512, 8, 4), (1024, 16, 6)])
+                                                   (512, 8, 22), (512, 8, 1), (1024, 12, 6), (96, 3, 0)])
 def test_tiling_does_not_change_fp64_result(tile, warps, long_class):
     name = "uv_300_302"
     g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps, long_class=long_class)
