@@ -110,9 +110,9 @@ typedef struct {
     int32_t warps_per_tile; /* warps per accumulation CTA; 0 = default */
     int32_t profile;        /* 1: time each stage with CUDA events into ks_stats.stage_ms
                                (only when a ks_stats pointer is given) */
-    int32_t long_class;     /* pairs of wing reach > 2^(long_class-1) bins are dealt to the
-                               accumulation warps one at a time (shorter ones 32 at a time);
-                               0 = default (22 = never) */
+    int32_t short_class;    /* reach classes 0..short_class-1 (wing reach <= 2^(short_class-1)
+                               bins) are accumulated one lane per pair; 0 = default (6),
+                               negative = none */
     int32_t reserved;
 } ks_options;
 

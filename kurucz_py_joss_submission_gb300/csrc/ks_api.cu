@@ -718,8 +718,8 @@ static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g
     a.stride = w.stride;
     a.n_layers = atm->n_layers;
     a.tile_bins = default_tile(opt, fp64);
-    a.long_class = (opt && opt->long_class > 0 && opt->long_class <= N_REACH_CLASSES) ? opt->long_class
-                                                                                       : LONG_CLASS;
+    a.short_class = !opt || opt->short_class == 0 ? SHORT_CLASS
+                    : opt->short_class < 0 ? 0 : min(opt->short_class, N_REACH_CLASSES);
     a.grid = g->wavelength;
     a.wing_idx = w.wing;
     a.class_pos = w.class_pos;

@@ -98,7 +98,7 @@ struct PairArgs {
 struct AccArgs {
     int64_t n_lines, n_wl, stride;
     int n_layers, tile_bins;
-    int long_class;             // first reach class of the bin-owner pass (N_REACH_CLASSES: none)
+    int short_class;            // reach classes below it are accumulated one lane per pair
     const double *grid;
     const int32_t *wing_idx;
     const int32_t *class_pos;   // per depth, per class: line positions, ascending

@@ -503,21 +503,31 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
     }
 }
 
+// Adds v to a bin of the warp's own copy with a shared-memory atomic: to the
+// sum word of the Kahan pair in FP32 (uncompensated; used for the short
+// pairs, whose contributions are small), to the cell in FP64.  Only lanes of
+// one warp touch a copy, and a warp's atomics to one word are applied in a
+// fixed order, so the result does not vary between runs.
+__device__ __forceinline__ void cell_atomic(float2* c, int b, float v) { atomicAdd(&c[b].x, v); }
+__device__ __forceinline__ void cell_atomic(double* c, int b, double v) { atomicAdd(&c[b], v); }
+
 // One CTA per (lambda tile, depth).  For every reach class k the contributing
 // pairs are those whose wing centre lies within 2^k (+1) bins of the tile --
 // a contiguous range of that class's centre-sorted list.  The pairs are dealt
-// to the warps in batches, round-robin in a fixed order: 32 pairs per batch
-// below class long_class (many short pairs, each a little work) and one pair
-// per batch from long_class up (few long pairs, each a lot of work), so the
-// long pairs spread over all warps instead of landing on one.  In a batch
-// each lane loads one pair's descriptor and works out its in-tile red/blue x
-// near/far offset ranges; a ballot drops pairs that miss the tile; the warp
-// walks the rest, broadcasting each pair by shuffles, and runs up to four
-// branch-free loops with lanes on consecutive offsets, adding into the warp's
-// own shared-memory copy of the tile as Kahan pairs -- no two lanes write the
-// same word, so no atomics.  The copies are then summed in warp order,
-// multiplied by STIM (line_opacity.py:1338) and stored coalesced.  Every sum
-// has a fixed order, so results are bit-identical across runs.
+// to the warps in batches of 32, round-robin in a fixed order, each lane
+// loading one pair's descriptor.
+//  * Classes below short_class (reach <= 2^(short_class-1) bins: most pairs,
+//    each a few evaluations): every lane walks its own pair, offset by
+//    offset in lockstep with the others, and adds the red and blue values
+//    with shared-memory atomics -- two lanes may hit the same bin.
+//  * Longer classes: each lane works out its pair's in-tile red/blue x
+//    near/far offset ranges, a ballot drops pairs that miss the tile, and
+//    the warp walks the rest, broadcasting each pair by shuffles, running up
+//    to four branch-free loops with lanes on consecutive offsets and adding
+//    into the warp's copy as Kahan pairs (no two lanes write the same word).
+// The copies are then summed in warp order, multiplied by STIM
+// (line_opacity.py:1338) and stored coalesced.  Every sum has a fixed order,
+// so results are bit-identical across runs.
 template <typename R>
 __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
                                                          R* __restrict__ out) {
@@ -572,7 +582,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
             cls_base[k] = b;
             bat_base[k] = nb;
             b += n;
-            nb += k < a.long_class ? (n + 31) >> 5 : n;
+            nb += (n + 31) >> 5;
         }
         cls_base[N_REACH_CLASSES] = b;
         bat_base[N_REACH_CLASSES] = nb;
@@ -586,9 +596,56 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     int kb = 0;
     for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
         while (bt >= bat_base[kb + 1]) kb++;
-        const bool wide = kb < a.long_class;
-        const int64_t first = cls_base[kb] + (wide ? (bt - bat_base[kb]) * 32 : (bt - bat_base[kb]));
-        const int cnt = wide ? (int)min((int64_t)32, cls_base[kb + 1] - first) : 1;
+        const int64_t first = cls_base[kb] + (bt - bat_base[kb]) * 32;
+        const int cnt = (int)min((int64_t)32, cls_base[kb + 1] - first);
+        if (kb < a.short_class) {
+            // ---- short pairs: one lane per pair ----
+            int cb = 0, reach = 0, nz = 0;
+            R k0 = R(0), ad = R(0), dv = R(0), xf = R(0);
+            if (lane < cnt) {
+                const int64_t p = a.class_pos[cls_lo[kb] + (first + lane - cls_base[kb])];
+                const PairDesc<R> pd = drow[p];
+                cb = pd.wing_c - T0;
+                const int ctr = pd.ctr_n10 & 15;
+                if (ctr) {
+                    const int cc = cb + (ctr - 8);
+                    if ((unsigned)cc < (unsigned)span) {
+                        cell_atomic(my, cc, pd.kapcen);
+                        evals++;
+                    }
+                }
+                reach = pd.maxstep_far & 0x7fffffff;
+                nz = pd.maxstep_far < 0 ? (pd.ctr_n10 >> 8) : 0x7fffffff;
+                k0 = pd.kappa0;
+                ad = pd.adamp;
+                dv = pd.dvoigt;
+                xf = pd.xfar;
+                if (reach > 0) {
+                    const int rlo = max(1, -cb), rhi = min(reach, span - 1 - cb);
+                    const int blo = max(1, cb - (span - 1)), bhi = min(reach, cb);
+                    if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
+                    if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
+                }
+            }
+            const R ts = R(200) * dv;
+            const int maxr = __reduce_max_sync(0xffffffffu, reach);
+            for (int o = 1; o <= maxr; o++) {
+                if (o <= reach) {
+                    R v;
+                    if (o <= nz) {
+                        v = near_profile_tab<R, R2>(o, dv, ts, ad, k0, h01, gh0, gh1, gh2);
+                    } else {
+                        const R oo = (R)o * (R)o;
+                        if constexpr (sizeof(R) == 4) v = __fdividef(xf, oo);
+                        else v = xf / oo;
+                    }
+                    if ((unsigned)(cb + o) < (unsigned)span) cell_atomic(my, cb + o, v);
+                    if ((unsigned)(cb - o) < (unsigned)span) cell_atomic(my, cb - o, v);
+                }
+            }
+            __syncwarp();
+            continue;
+        }
         // ---- per lane: one pair and its in-tile offset ranges ----
         int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
         R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);

@@ -124,8 +124,9 @@ def test_fused_fp64_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", available_cases())
-def test_fused_mixed_within_contract(name):
-    g, syn, st = run_fused(name, "mixed")
+@pytest.mark.parametrize("short_class", [0, -1, 22])
+def test_fused_mixed_within_contract(name, short_class):
+    g, syn, st = run_fused(name, "mixed", short_class=short_class)
     assert st["device_flags"] == 0
     ft, fc = syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy()
     nf_ref = g["flux_total_hz"] / g["flux_cont_hz"]
@@ -147,11 +148,11 @@ def test_evaluation_count_matches_oracle(name):
     assert abs(st32["valid_pairs"] - st["valid_pairs"]) <= max(2, st["valid_pairs"] // 10000)
 
 
-@pytest.mark.parametrize("tile,warps,long_class", [(256, 4, 0), (512, 8, 0), (1024, 8, 0), (512, 16, 0),
-                                                   (512, 8, 22), (512, 8, 1), (1024, 12, 6), (96, 3, 0)])
-def test_tiling_does_not_change_fp64_result(tile, warps, long_class):
+@pytest.mark.parametrize("tile,warps,short_class", [(256, 4, 0), (512, 8, 0), (1024, 8, 0), (512, 16, 0),
+                                                    (512, 8, -1), (512, 8, 1), (1024, 12, 7), (96, 3, 22)])
+def test_tiling_does_not_change_fp64_result(tile, warps, short_class):
     name = "uv_300_302"
-    g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps, long_class=long_class)
+    g, syn, _ = run_fused(name, "fp64", tile_bins=tile, warps_per_tile=warps, short_class=short_class)
     assert rel(syn.asynth.cpu().numpy(), g["asynth"]) < 1e-12
 
 
