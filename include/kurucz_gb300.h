@@ -113,7 +113,8 @@ typedef struct {
     int32_t short_class;    /* reach classes 0..short_class-1 (wing reach <= 2^(short_class-1)
                                bins) are accumulated one lane per pair; 0 = default (6),
                                negative = none */
-    int32_t reserved;
+    int32_t transfer_path;  /* single precision, fused: 0 = streaming pass (columns it cannot
+                               take go to the per-column kernel), 1 = per-column kernel only */
 } ks_options;
 
 /* Counters of one synthesis (filled when a pointer is given). */

@@ -176,6 +176,10 @@ extern "C" ks_status ks_init_tables(const double* tabvi, const double* tabh1, in
     t.ch.assign(ch, ch + NXTAU);
     t.coefj.assign(coefj, coefj + NXTAU * NXTAU);
     for (int i = 0; i < NXTAU * NXTAU; i++) t.cj.c[i] = (float)coefj[i];
+    for (int i = 0; i < NXTAU; i++) {
+        t.cj.ch[i] = (float)ch[i];
+        t.cj.xtau[i] = (float)xtau[i];
+    }
     t.ready = true;
     g_tables = std::move(t);
     for (int i = 0; i < kMaxDevices; i++) g_dev_ready[i] = false;
@@ -487,6 +491,7 @@ struct Workspace {
     int32_t* class_pos;
     unsigned long long* counters;  // [0] valid pairs, [1] evaluations
     int32_t* iters;
+    int32_t* tlist;  // wavelengths left to the general transfer kernel
     int* flags;
     int64_t stride;
     int nchunks;
@@ -516,6 +521,7 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.class_pos = c.take<int32_t>((size_t)L * w.stride);
     w.counters = c.take<unsigned long long>(4);
     w.iters = c.take<int32_t>(2 * (size_t)(n_wl > 0 ? n_wl : 1));
+    w.tlist = c.take<int32_t>(n_wl > 0 ? n_wl : 1);
     w.flags = c.take<int>(1);
 }
 
@@ -1018,8 +1024,10 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
     ta.line_scat = (opt && opt->rhoxj > 0.0) ? 1 : 0;
     if constexpr (fp64)
         KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
-    else
+    else if (opt && opt->transfer_path == 1)
         KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
+    else
+        KS_CUDA(launch_transfer_stream_f32(ta, &g_tables.cj, cabs, cscat, asynth, w.tlist, w.counters + 2, s));
     tm.mark();
     return KS_OK;
 }
@@ -1035,6 +1043,8 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     if (st) return st;
     if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize: NULL flux output");
     if ((st = check_tiling(opt))) return st;
+    if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))
+        return fail(KS_ERR_INVALID, "transfer_path must be 0 (streaming) or 1 (per-column)");
     DevTables t;
     if ((st = device_tables(&t))) return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1056,7 +1066,12 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     if (st) return st;
     if (stats) {
         st = collect_stats(w, grid->n, stats, s);
-        stats->kernel_launches = lines->n_lines > 0 ? 10 : 7;
+        // grid parameters, line bins, prep, continuum, pair setup, three
+        // partition passes, accumulation, transfer (FP32: streaming pass +
+        // list pass)
+        const bool has_lines = lines->n_lines > 0;
+        const bool stream_pass = !fp64 && !(opt && opt->transfer_path == 1);
+        stats->kernel_launches = 4 + (has_lines ? 5 : 0) + (stream_pass ? 2 : 1);
         return st;
     }
     return KS_OK;
@@ -1088,6 +1103,8 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     if (st) return st;
     if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize_noalloc: NULL flux output");
     if ((st = check_tiling(opt))) return st;
+    if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))
+        return fail(KS_ERR_INVALID, "transfer_path must be 0 (streaming) or 1 (per-column)");
     bool fp64 = opt && opt->precision == KS_PREC_FP64;
     bool need_asynth = asynth_out == nullptr;
     Carve dry{nullptr, 0, 0, true};

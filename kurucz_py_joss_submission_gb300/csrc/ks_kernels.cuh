@@ -1209,4 +1209,389 @@ __global__ void __launch_bounds__(128) transfer_kernel(TransferArgs a, const __g
     transfer_column<R, REF_SWEEP>(a, cj, cont_abs, cont_scat, line_op, line_sc, line_src, j);
 }
 
+// ---------------------------------------------------------------------------
+// Streaming single-precision transfer (fused ASYNTH mode)
+// ---------------------------------------------------------------------------
+//
+// The same per-wavelength JOSH solution as transfer_column<float, false>, in
+// one pass over the layers with nothing per layer kept in memory: layer i+3
+// is read while INTEG (PARCOE with its smoothing) closes tau[i+1], and MAP1
+// onto the 51-point JOSH grid consumes each new tau together with S-bar and
+// alpha through a four-layer window, writing the mapped (S-bar, alpha) pairs
+// to shared memory.  The sweeps then run with XS in registers.  Columns the
+// pass does not cover -- a non-finite or out-of-range input, fewer than three
+// layers, column masses that do not increase, or the MAXJ = 1 branch -- are
+// appended to a list for transfer_column.
+
+constexpr int TS_THREADS = 128;
+
+// Shared-memory load the compiler may not hoist out of the sweep loop (the
+// 51 loop-invariant pairs would otherwise be held in registers).
+__device__ __forceinline__ float2 ts_ld(const float2* p) {
+    float2 v;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+    return v;
+}
+
+// One layer of one solve: total opacity, albedo and S-bar (radiative.py
+// solve_lte_frequency, josh_solver.py:367-420); false when an input is not
+// usable.
+template <bool TOTAL>
+__device__ __forceinline__ bool ts_layer(const float* __restrict__ cab, const float* __restrict__ csc,
+                                         const float* __restrict__ lop, int line_scat, int64_t off,
+                                         float fscat, float hkt, float freq15, float freq, float& ab,
+                                         float& al, float& sn) {
+    const float mx = (float)MAX_OPACITY_REAL4;
+    const float eps = (float)EPS38;
+    const float ca = cab[off], cs = csc[off];
+    float lo = 0.f, lsg = 0.f;
+    bool ok = isfinite(ca) && isfinite(cs) && ca < mx && cs < mx;
+    if (TOTAL) {
+        const float A = lop[off];
+        if (line_scat) {
+            lo = A * (1.f - fscat);
+            const float one_m = 1.f - fscat;
+            lsg = tdiv(lo, one_m > 1e-12f ? one_m : 1e-12f) * fscat;
+        } else {
+            lo = A;
+        }
+        ok = ok && isfinite(lo) && isfinite(lsg) && lo < mx && lsg < mx;
+    }
+    const float pl = planck_nu(freq15, freq * hkt);
+    const float t = ((ca + lo) + cs) + lsg;
+    ab = t > eps ? t : (t != t ? t : eps);
+    const float alp = ab > 0.f ? tdiv(cs + lsg, ab) : 0.f;
+    al = alp < 0.f ? 0.f : (alp > 1.f ? 1.f : alp);
+    const float den = ca + lo;
+    sn = den > 0.f ? tdiv(ca * pl + lo * pl, den) : pl;
+    return ok;
+}
+
+// Quadratic coefficients through three points, the MAP1 "back"/"forward"
+// parabola (josh_solver.py:220-353).
+__device__ __forceinline__ void ts_parab(float xa, float xb, float xc, float fa, float fb, float fc,
+                                         float& A, float& B, float& C) {
+    const float dd = tdiv(fb - fa, xb - xa);
+    C = tdiv(fc, (xc - xb) * (xc - xa)) + tdiv(tdiv(fa, xc - xa) - tdiv(fb, xc - xb), xb - xa);
+    B = dd - (xb + xa) * C;
+    A = fa - xa * dd + xb * xa * C;
+}
+__device__ __forceinline__ void ts_line(float xa, float xb, float fa, float fb, float& A, float& B, float& C) {
+    B = tdiv(fb - fa, xb - xa);
+    A = fb - xb * B;
+    C = 0.f;
+}
+__device__ __forceinline__ void ts_blend(float xa, float xb, float xc, float xd, float fa, float fb, float fc,
+                                         float fd, float& A, float& B, float& C) {
+    float ab, bb, cb, af, bf, cf;
+    ts_parab(xa, xb, xc, fa, fb, fc, ab, bb, cb);
+    ts_parab(xb, xc, xd, fb, fc, fd, af, bf, cf);
+    const float acf = fabsf(cf), acb = fabsf(cb);
+    const float wt = acf != 0.f ? tdiv(acf, acf + acb) : 0.f;
+    A = af + wt * (ab - af);
+    B = bf + wt * (bb - bf);
+    C = cf + wt * (cb - cf);
+}
+
+// MAP1 of (S-bar, alpha) onto the JOSH grid, fed one layer at a time.
+struct TsMap {
+    float x0, x1, x2, x3, f0, f1, f2, f3, g0, g1, g2, g3;  // the newest four layers
+    int avail, k;
+    float tau0, s0, a0;
+    float2* out;         // this thread's column of the [NXTAU][TS_THREADS] array
+    const float* xtau;   // JOSH grid in shared memory
+
+    __device__ __forceinline__ void emit(float xk, float As, float Bs, float Cs, float Aa, float Ba, float Ca) {
+        const float vs = As + (Bs + Cs * xk) * xk;
+        const float va = Aa + (Ba + Ca * xk) * xk;
+        const float eps = (float)EPS38;
+        float xb = vs > eps ? vs : eps;
+        float xa = va < 0.f ? 0.f : (va > 1.f ? 1.f : va);
+        if (xk < tau0) {
+            xb = s0;
+            xa = a0;
+        }
+        out[k * TS_THREADS] = make_float2(xb, xa);
+    }
+    // Grid points below x1[l] = x2, with l = avail - 1 (1-based) and the
+    // window x0..x3 = x1[l-2..l+1].
+    __device__ __forceinline__ void step() {
+        if (k >= NXTAU) return;
+        float xk = xtau[k];
+        if (!(xk < x2)) return;
+        const int l = avail - 1;
+        float As, Bs, Cs, Aa, Ba, Ca;
+        if (l <= 3) {
+            ts_line(x1, x2, f1, f2, As, Bs, Cs);
+            ts_line(x1, x2, g1, g2, Aa, Ba, Ca);
+        } else {
+            ts_blend(x0, x1, x2, x3, f0, f1, f2, f3, As, Bs, Cs);
+            ts_blend(x0, x1, x2, x3, g0, g1, g2, g3, Aa, Ba, Ca);
+        }
+        do {
+            emit(xk, As, Bs, Cs, Aa, Ba, Ca);
+            if (++k >= NXTAU) break;
+            xk = xtau[k];
+        } while (xk < x2);
+    }
+    __device__ __forceinline__ void push(float x, float f, float g) {
+        x0 = x1; x1 = x2; x2 = x3; x3 = x;
+        f0 = f1; f1 = f2; f2 = f3; f3 = f;
+        g0 = g1; g1 = g2; g2 = g3; g3 = g;
+        if (++avail >= 3) step();
+    }
+    // After the last layer (avail = n, window x1[n-3..n]): the last interval
+    // and the linear extrapolation beyond it.
+    __device__ __forceinline__ void finish() {
+        if (k >= NXTAU) return;
+        float xk = xtau[k];
+        float As, Bs, Cs, Aa, Ba, Ca;
+        if (xk < x3) {
+            if (avail <= 3) {
+                ts_line(x2, x3, f2, f3, As, Bs, Cs);
+                ts_line(x2, x3, g2, g3, Aa, Ba, Ca);
+            } else {
+                ts_parab(x1, x2, x3, f1, f2, f3, As, Bs, Cs);
+                ts_parab(x1, x2, x3, g1, g2, g3, Aa, Ba, Ca);
+            }
+            do {
+                emit(xk, As, Bs, Cs, Aa, Ba, Ca);
+                if (++k >= NXTAU) return;
+                xk = xtau[k];
+            } while (xk < x3);
+        }
+        ts_line(x2, x3, f2, f3, As, Bs, Cs);
+        ts_line(x2, x3, g2, g3, Aa, Ba, Ca);
+        for (; k < NXTAU; k++) emit(xtau[k], As, Bs, Cs, Aa, Ba, Ca);
+    }
+};
+
+// PARCOE coefficients at layer j from f[j-1], f[j], f[j+1] (fm, f0, fp),
+// the cases of parcoe_raw for j >= 2.
+__device__ __forceinline__ void ts_parcoe(const float* x, int n, int j, float fm, float f0, float fp,
+                                          float& a, float& b, float& c) {
+    if (j == 2 && n > 3) {
+        const float den = x[j + 1] - x[j];
+        b = den != 0.f ? tdiv(fp - f0, den) : 0.f;
+        a = f0 - x[j] * b;
+        c = 0.f;
+        return;
+    }
+    if (j == n - 1) {
+        const float den = x[j] - x[j - 1];
+        b = den != 0.f ? tdiv(f0 - fm, den) : 0.f;
+        a = f0 - x[j] * b;
+        c = 0.f;
+        return;
+    }
+    const int j1 = j - 1;
+    const float den = x[j] - x[j1];
+    const float dd = den != 0.f ? tdiv(f0 - fm, den) : 0.f;
+    const float den1 = (x[j + 1] - x[j]) * (x[j + 1] - x[j1]);
+    const float term1 = den1 != 0.f ? tdiv(fp, den1) : 0.f;
+    const float den2 = x[j + 1] - x[j1];
+    const float den3 = x[j + 1] - x[j];
+    const float den4 = x[j] - x[j1];
+    float part = 0.f;
+    if (den4 != 0.f) {
+        const float t1 = den2 != 0.f ? tdiv(fm, den2) : 0.f;
+        const float t2 = den3 != 0.f ? tdiv(f0, den3) : 0.f;
+        part = tdiv(t1 - t2, den4);
+    }
+    c = term1 + part;
+    b = dd - (x[j] + x[j1]) * c;
+    a = fm - x[j1] * dd + x[j] * x[j1] * c;
+}
+
+// One JOSH solve of one column, streamed; returns the sweep count, or 0 when
+// the column needs transfer_column.
+template <bool TOTAL>
+__device__ __forceinline__ int ts_solve(const TransferArgs& a, const CoefJ32& cj, const float* __restrict__ cab,
+                                        const float* __restrict__ csc, const float* __restrict__ lop,
+                                        int64_t j, int n, const float* s_x, const float* s_hkt,
+                                        const float* s_fs, const float* s_xtau, float freq15, float freq,
+                                        float2* col, double& flux) {
+    const int64_t N = a.n;
+    const int ls = a.line_scat;
+    // window f[i..i+3] of abtot, S-bar and alpha
+    float F0, F1, F2, F3 = 0.f, N0, N1, N2, N3 = 0.f, G0, G1, G2, G3 = 0.f;
+    bool ok = ts_layer<TOTAL>(cab, csc, lop, ls, j, s_fs[0], s_hkt[0], freq15, freq, F0, G0, N0);
+    ok &= ts_layer<TOTAL>(cab, csc, lop, ls, N + j, s_fs[1], s_hkt[1], freq15, freq, F1, G1, N1);
+    ok &= ts_layer<TOTAL>(cab, csc, lop, ls, 2 * N + j, s_fs[2], s_hkt[2], freq15, freq, F2, G2, N2);
+    if (n > 3) ok &= ts_layer<TOTAL>(cab, csc, lop, ls, 3 * N + j, s_fs[3], s_hkt[3], freq15, freq, F3, G3, N3);
+    const float tau0 = F0 * s_x[0];
+    if (!ok || !(tau0 <= s_xtau[NXTAU - 1])) return 0;
+    const float eps = (float)EPS38;
+    TsMap m;
+    m.x0 = m.x1 = m.x2 = m.x3 = 0.f;
+    m.f0 = m.f1 = m.f2 = m.f3 = 0.f;
+    m.g0 = m.g1 = m.g2 = m.g3 = 0.f;
+    m.avail = 0;
+    m.k = 0;
+    m.tau0 = tau0;
+    m.s0 = N0 > eps ? N0 : eps;
+    m.a0 = G0;
+    m.out = col;
+    m.xtau = s_xtau;
+    m.push(tau0, N0, G0);
+    // INTEG (josh_solver.py:171-189) with PARCOE's smoothing folded in
+    const float* x = s_x;
+    float ai, bi, ci, an, bn, cn;
+    {
+        const float d0 = x[1] - x[0];
+        bi = d0 != 0.f ? tdiv(F1 - F0, d0) : 0.f;
+        ai = F0 - x[0] * bi;
+        ci = 0.f;
+        const float d1 = x[2] - x[1];
+        bn = d1 != 0.f ? tdiv(F2 - F1, d1) : 0.f;
+        an = F1 - x[1] * bn;
+        cn = 0.f;
+    }
+    float s = tau0, comp = 0.f;
+    for (int i = 0; i < n - 1; i++) {
+        float a_i = ai, b_i = bi, c_i = ci;
+        if (i >= 1) {
+            if (i == n - 2) {
+                const float den = x[n - 1] - x[n - 2];
+                b_i = den != 0.f ? tdiv(F1 - F0, den) : 0.f;
+                a_i = F1 - x[n - 1] * b_i;
+                c_i = 0.f;
+            } else if (ci != 0.f) {
+                const float acn = fabsf(cn);
+                const float den = acn + fabsf(ci);
+                const float wt = den > 0.f ? tdiv(acn, den) : 0.f;
+                a_i = an + wt * (ai - an);
+                b_i = bn + wt * (bi - bn);
+                c_i = cn + wt * (ci - cn);
+            }
+        }
+        const float xa = x[i], xb = x[i + 1];
+        const float dx = xb - xa;
+        float term = a_i + 0.5f * b_i * (xb + xa);
+        term += (c_i / 3.f) * ((xb + xa) * xb + xa * xa);
+        kahan_add(s, comp, term * dx);
+        m.push(s, N1, G1);
+        ai = an; bi = bn; ci = cn;
+        if (i + 2 <= n - 1) ts_parcoe(x, n, i + 2, F1, F2, F3, an, bn, cn);
+        F0 = F1; F1 = F2; F2 = F3;
+        N0 = N1; N1 = N2; N2 = N3;
+        G0 = G1; G1 = G2; G2 = G3;
+        if (i + 4 <= n - 1) {
+            const int d = i + 4;
+            ok &= ts_layer<TOTAL>(cab, csc, lop, ls, (int64_t)d * N + j, s_fs[d], s_hkt[d], freq15, freq, F3, G3, N3);
+        } else {
+            F3 = G3 = N3 = 0.f;
+        }
+    }
+    if (!ok) return 0;
+    m.finish();
+    // Gauss-Seidel sweeps (josh_solver.py:24-92), XS in registers, the
+    // operator in the constant bank
+    float xs[NXTAU];
+#pragma unroll
+    for (int l = 0; l < NXTAU; l++) xs[l] = col[l * TS_THREADS].x;
+    int it_done = NXTAU;
+    for (int it = 0; it < NXTAU; it++) {
+        bool err = false;
+#pragma unroll
+        for (int k = NXTAU - 1; k >= 0; k--) {
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+            for (int q = 0; q + 3 < NXTAU; q += 4) {
+                s0 = fmaf(cj.c[k * NXTAU + q], xs[q], s0);
+                s1 = fmaf(cj.c[k * NXTAU + q + 1], xs[q + 1], s1);
+                s2 = fmaf(cj.c[k * NXTAU + q + 2], xs[q + 2], s2);
+                s3 = fmaf(cj.c[k * NXTAU + q + 3], xs[q + 3], s3);
+            }
+#pragma unroll
+            for (int q = (NXTAU / 4) * 4; q < NXTAU; q++) s0 = fmaf(cj.c[k * NXTAU + q], xs[q], s0);
+            const float sum = (s0 + s1) + (s2 + s3);
+            const float2 ba = ts_ld(col + k * TS_THREADS);
+            const float xak = ba.y;
+            const float xm = ba.x * (1.f - ba.y);
+            const float diag = 1.0f - xak * cj.c[k * NXTAU + k];
+            const float dl = __fdividef(fmaf(sum, xak, xm) - xs[k], diag);
+            const float xk = xs[k];
+            err |= (xk == 0.0f) || (fabsf(dl) > 1.0e-5f * fabsf(xk));
+            const float nv = xk + dl;
+            xs[k] = nv > 1.0e-38f ? nv : 1.0e-38f;
+        }
+        if (!err) {
+            it_done = it + 1;
+            break;
+        }
+    }
+    // surface flux, compensated single-precision sum
+    float fs = 0.f, fc = 0.f;
+#pragma unroll
+    for (int l = 0; l < NXTAU; l++) kahan_add(fs, fc, cj.ch[l] * xs[l]);
+    flux = (double)fs - (double)fc;
+    return it_done;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TS_THREADS, 4) transfer_stream_kernel(
+    TransferArgs a, const __grid_constant__ CoefJ32 cj, const float* __restrict__ cab,
+    const float* __restrict__ csc, const float* __restrict__ lop, int32_t* __restrict__ list,
+    unsigned long long* __restrict__ count) {
+    extern __shared__ float2 ts_cols[];  // [NXTAU][TS_THREADS]
+    __shared__ float s_x[MAX_LAYERS], s_hkt[MAX_LAYERS], s_fs[MAX_LAYERS], s_xtau[NXTAU];
+    __shared__ int s_ok;
+    const int L = a.n_layers;
+    for (int d = threadIdx.x; d < L; d += blockDim.x) {
+        s_x[d] = a.depth[d].rhox_f;
+        s_hkt[d] = a.depth[d].hkt_f;
+        s_fs[d] = a.depth[d].fscat_f;
+    }
+    for (int l = threadIdx.x; l < NXTAU; l += blockDim.x) s_xtau[l] = cj.xtau[l];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bool ok = L >= 3 && L <= MAX_LAYERS;
+        for (int d = 0; ok && d < L; d++) {
+            const float v = s_x[d];
+            ok = isfinite(v) && v > 0.f && (d == 0 || v > s_x[d - 1]);
+        }
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    const int64_t j = (int64_t)blockIdx.x * TS_THREADS + threadIdx.x;
+    if (j >= a.n) return;
+    bool done = false;
+    if (s_ok) {
+        const double wl = a.grid[j];
+        const double freq = C_LIGHT_NM / (wl > 1e-12 ? wl : 1e-12);
+        const float freq15 = (float)(freq / 1.0e15);
+        const float freq_f = (float)freq;
+        float2* col = ts_cols + threadIdx.x;
+        double ft = 0.0, fc = 0.0;
+        const int itt = ts_solve<true>(a, cj, cab, csc, lop, j, L, s_x, s_hkt, s_fs, s_xtau, freq15, freq_f, col, ft);
+        if (itt > 0) {
+            const int itc = ts_solve<false>(a, cj, cab, csc, lop, j, L, s_x, s_hkt, s_fs, s_xtau, freq15, freq_f, col, fc);
+            if (itc > 0) {
+                a.flux_total[j] = ft;
+                a.flux_cont[j] = fc;
+                if (a.iters) {
+                    a.iters[2 * j] = itc;
+                    a.iters[2 * j + 1] = itt;
+                }
+                done = true;
+            }
+        }
+    }
+    if (!done) list[atomicAdd(count, 1ull)] = (int32_t)j;
+}
+
+// transfer_column for the wavelengths the streaming pass listed.
+template <typename R>
+__global__ void __launch_bounds__(128) transfer_list_kernel(TransferArgs a, const __grid_constant__ CoefJ32 cj,
+                                                            const R* __restrict__ cab, const R* __restrict__ csc,
+                                                            const R* __restrict__ lop,
+                                                            const int32_t* __restrict__ list,
+                                                            const unsigned long long* __restrict__ count) {
+    const int64_t nl = (int64_t)*count;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x)
+        transfer_column<R, false>(a, cj, cab, csc, lop, nullptr, nullptr, list[i]);
+}
+
 }  // namespace ks

@@ -7,10 +7,13 @@
 
 namespace ks {
 
-// JOSH mean-intensity operator in single precision, passed to the fast
-// sweep kernel by value so it lives in the kernel's constant bank.
+// JOSH constants in single precision -- the mean-intensity operator, the
+// flux weights and the optical-depth grid -- passed to the transfer kernels
+// by value so they live in the kernel's constant bank.
 struct CoefJ32 {
     float c[51 * 51];
+    float ch[51];
+    float xtau[51];
 };
 
 #define KS_DECLARE_LAUNCHERS(R, SUF)                                                              \
@@ -24,6 +27,10 @@ struct CoefJ32 {
     cudaError_t launch_transfer_##SUF(const TransferArgs& a, const CoefJ32* cj, const R* ca,     \
                                       const R* cs, const R* lo, const R* lsc, const R* src,      \
                                       cudaStream_t s);                                            \
+    cudaError_t launch_transfer_stream_##SUF(const TransferArgs& a, const CoefJ32* cj,           \
+                                             const R* ca, const R* cs, const R* lo,               \
+                                             int32_t* list, unsigned long long* count,            \
+                                             cudaStream_t s);                                     \
     size_t accumulate_smem_bytes_##SUF(int tile_bins, int warps);
 
 KS_DECLARE_LAUNCHERS(float, f32)

@@ -163,7 +163,8 @@ class DeviceCatalog:
 
 
 def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", tile_bins=0,
-                 warps_per_tile=0, profile=False, short_class=0) -> _native.KsOptions:
+                 warps_per_tile=0, profile=False, short_class=0,
+                 transfer_path=0) -> _native.KsOptions:
     opt = _native.KsOptions()
     opt.cutoff = float(cutoff)
     opt.microturb_kms = float(microturb_kms)
@@ -173,6 +174,7 @@ def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", t
     opt.warps_per_tile = int(warps_per_tile)
     opt.profile = 1 if profile else 0
     opt.short_class = int(short_class)
+    opt.transfer_path = int(transfer_path)
     return opt
 
 

@@ -156,6 +156,25 @@ def test_tiling_does_not_change_fp64_result(tile, warps, short_class):
     assert rel(syn.asynth.cpu().numpy(), g["asynth"]) < 1e-12
 
 
+@pytest.mark.parametrize("name", available_cases())
+def test_streaming_transfer_matches_per_column_kernel(name):
+    """The single-pass transfer against the per-column kernel, both FP32, on
+    the same opacities; columns the pass hands over (MAXJ = 1 cores of the
+    strong-line case) go through the per-column kernel in both runs."""
+    _, s0, st0 = run_fused(name, "mixed")
+    _, s1, st1 = run_fused(name, "mixed", transfer_path=1)
+    f0, c0 = s0.flux_total.cpu().numpy(), s0.flux_cont.cpu().numpy()
+    f1, c1 = s1.flux_total.cpu().numpy(), s1.flux_cont.cpu().numpy()
+    assert np.array_equal(s0.asynth.cpu().numpy(), s1.asynth.cpu().numpy())
+    assert float(np.max(np.abs(f0 - f1) / c1)) <= 2e-6
+    assert rel(c0, c1) <= 2e-6
+    assert st0["maxj_wavelengths"] == st1["maxj_wavelengths"]
+    assert abs(st0["iterations"] - st1["iterations"]) <= max(2, st1["iterations"] // 1000)
+    assert (st0["kernel_launches"], st1["kernel_launches"]) == (11, 10)
+    if name == "strong_600_601":
+        assert st0["maxj_wavelengths"] > 0
+
+
 def test_mixed_is_deterministic():
     name = "uv_300_302"
     _, s1, _ = run_fused(name, "mixed")
