@@ -461,6 +461,36 @@ __global__ void __launch_bounds__(kPartThreads) class_scatter_kernel(
     }
 }
 
+// For every (depth, tile, class): the range of the class's centre-sorted
+// list whose wing centres lie within the class's maximum reach (+1 bin) of
+// the tile, as offsets from the class start.  One thread per (tile, class),
+// two binary searches over wing bins.
+__device__ __forceinline__ int64_t lower_bound_wing(const int32_t* __restrict__ pos, int64_t lo, int64_t hi,
+                                                    const int32_t* __restrict__ wing, int64_t key) {
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)wing[pos[mid]] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void tile_ranges_kernel(const int64_t* __restrict__ class_off, const int32_t* __restrict__ class_pos,
+                                   const int32_t* __restrict__ wing, int64_t n_wl, int tile_bins, int ntiles,
+                                   int2* __restrict__ rng) {
+    const int d = blockIdx.y;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)ntiles * N_REACH_CLASSES) return;
+    const int t = (int)(idx / N_REACH_CLASSES), k = (int)(idx % N_REACH_CLASSES);
+    const int64_t* off = class_off + (int64_t)d * (N_REACH_CLASSES + 1);
+    const int64_t lo = off[k], hi = off[k + 1];
+    const int64_t T0 = (int64_t)t * tile_bins;
+    const int64_t T1 = min(T0 + tile_bins, n_wl);
+    const int64_t h = class_halo(k) + 1;
+    const int64_t s0 = lower_bound_wing(class_pos, lo, hi, wing, T0 - h);
+    const int64_t s1 = lower_bound_wing(class_pos, s0, hi, wing, T1 + h);
+    rng[((int64_t)d * ntiles + t) * N_REACH_CLASSES + k] = make_int2((int)(s0 - lo), (int)(s1 - lo));
+}
+
 // ---------------------------------------------------------------------------
 // workspace
 // ---------------------------------------------------------------------------
@@ -492,13 +522,15 @@ struct Workspace {
     unsigned long long* counters;  // [0] valid pairs, [1] evaluations
     int32_t* iters;
     int32_t* tlist;  // wavelengths left to the general transfer kernel
+    int2* tile_rng;  // per (depth, tile, class) contributing range
+    int ntiles;
     int* flags;
     int64_t stride;
     int nchunks;
 };
 
 static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl, int n_ion,
-                   int n_elem, bool fp64, bool need_cont, bool need_asynth) {
+                   int n_elem, bool fp64, bool need_cont, bool need_asynth, int tile_bins = 0) {
     size_t rs = fp64 ? 8 : 4;
     w.stride = ((n_lines + kChunk - 1) / kChunk) * kChunk;
     if (w.stride == 0) w.stride = kChunk;
@@ -522,6 +554,8 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.counters = c.take<unsigned long long>(4);
     w.iters = c.take<int32_t>(2 * (size_t)(n_wl > 0 ? n_wl : 1));
     w.tlist = c.take<int32_t>(n_wl > 0 ? n_wl : 1);
+    w.ntiles = tile_bins > 0 ? (int)((n_wl + tile_bins - 1) / tile_bins) : 0;
+    w.tile_rng = c.take<int2>((size_t)L * (w.ntiles > 0 ? w.ntiles : 1) * N_REACH_CLASSES);
     w.flags = c.take<int>(1);
 }
 
@@ -532,7 +566,8 @@ extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_
     bool fp64 = opt && opt->precision == KS_PREC_FP64;
     Carve c{nullptr, 0, 0, true};
     Workspace w;
-    layout(c, w, n_lines, n_layers, n_wavelengths, 6, 139, fp64, true, true);
+    layout(c, w, n_lines, n_layers, n_wavelengths, 6, 139, fp64, true, true,
+           opt && opt->tile_bins > 0 ? opt->tile_bins : 512);
     *bytes = c.used + 256;
     return KS_OK;
 }
@@ -679,7 +714,7 @@ static ks_status run_bins(const ks_lines* l, const ks_grid* g, const Workspace& 
     return KS_OK;
 }
 
-static ks_status run_partition(const Workspace& w, int L, cudaStream_t s) {
+static ks_status run_partition(const Workspace& w, int L, int64_t n_wl, int tile_bins, cudaStream_t s) {
     dim3 grid(w.nchunks, L);
     class_count_kernel<<<grid, kPartThreads, 0, s>>>(w.cls, w.stride, w.nchunks, w.counts);
     KS_CUDA(cudaGetLastError());
@@ -689,6 +724,13 @@ static ks_status run_partition(const Workspace& w, int L, cudaStream_t s) {
     class_scatter_kernel<<<grid, kPartThreads, 0, s>>>(w.cls, w.stride, w.nchunks, w.chunk_base,
                                                        w.class_pos);
     KS_CUDA(cudaGetLastError());
+    if (w.ntiles > 0) {
+        const int64_t work = (int64_t)w.ntiles * N_REACH_CLASSES;
+        dim3 rg((unsigned)((work + 255) / 256), (unsigned)L);
+        tile_ranges_kernel<<<rg, 256, 0, s>>>(w.class_off, w.class_pos, w.wing, n_wl, tile_bins, w.ntiles,
+                                              w.tile_rng);
+        KS_CUDA(cudaGetLastError());
+    }
     return KS_OK;
 }
 
@@ -730,6 +772,7 @@ static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g
     a.wing_idx = w.wing;
     a.class_pos = w.class_pos;
     a.class_off = w.class_off;
+    a.tile_rng = w.tile_rng;
     a.depth = w.depth;
     a.h0d = t.h0d;
     a.h1d = t.h1d;
@@ -881,11 +924,13 @@ extern "C" ks_status ks_asynth(const ks_lines* lines, const ks_atmos* atm, const
     cudaStream_t s = (cudaStream_t)stream;
     Carve dry{nullptr, 0, 0, true};
     Workspace w;
-    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false);
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false,
+           default_tile(opt, true));
     if (!workspace || workspace_bytes < dry.used)
         return fail(KS_ERR_NOMEM, "ks_asynth: workspace too small (see ks_workspace_size)");
     Carve c{(char*)workspace, workspace_bytes, 0, false};
-    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false);
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, true, false, false,
+           default_tile(opt, true));
     KS_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int), s));
     KS_CUDA(cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned long long), s));
     KS_CUDA(cudaMemsetAsync(w.cls, 0xff, (size_t)atm->n_layers * w.stride, s));
@@ -895,7 +940,7 @@ extern "C" ks_status ks_asynth(const ks_lines* lines, const ks_atmos* atm, const
     p.transp_in = transp;
     p.valid_in = valid;
     KS_CUDA(launch_pair_setup_f64(p, false, cont_kapmin, nullptr, (PairDesc<double>*)w.desc, w.cls, s));
-    if ((st = run_partition(w, atm->n_layers, s))) return st;
+    if ((st = run_partition(w, atm->n_layers, grid->n, default_tile(opt, true), s))) return st;
     AccArgs a = acc_args(lines, atm, grid, opt, w, t, true);
     KS_CUDA(launch_accumulate_f64(a, default_warps(opt), (const PairDesc<double>*)w.desc, asynth_out, s));
     if (stats) return collect_stats(w, 0, stats, s);
@@ -1005,11 +1050,12 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         else
             KS_CUDA(launch_pair_setup_f32(p, true, cabs, cscat, (PairDesc<float>*)w.desc, w.cls, s));
         tm.mark();
-        if ((st = run_partition(w, L, s))) return st;
+        if ((st = run_partition(w, L, grid->n, default_tile(opt, fp64), s))) return st;
         tm.mark();
     } else {
         // no lines: every class list is empty
         KS_CUDA(cudaMemsetAsync(w.class_off, 0, sizeof(int64_t) * L * (N_REACH_CLASSES + 1), s));
+        KS_CUDA(cudaMemsetAsync(w.tile_rng, 0, sizeof(int2) * L * w.ntiles * N_REACH_CLASSES, s));
         tm.mark();
         tm.mark();
     }
@@ -1052,11 +1098,13 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     bool need_asynth = asynth_out == nullptr;
     Carve dry{nullptr, 0, 0, true};
     Workspace w;
-    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth,
+           default_tile(opt, fp64));
     if (!workspace || workspace_bytes < dry.used)
         return fail(KS_ERR_NOMEM, "ks_synthesize: workspace too small (see ks_workspace_size)");
     Carve c{(char*)workspace, workspace_bytes, 0, false};
-    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth,
+           default_tile(opt, fp64));
     void* asy = asynth_out ? asynth_out : w.asynth;
     StageTimer tm;
     tm.start(s, stats && opt && opt->profile);
@@ -1109,7 +1157,8 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     bool need_asynth = asynth_out == nullptr;
     Carve dry{nullptr, 0, 0, true};
     Workspace w;
-    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth,
+           default_tile(opt, fp64));
     if (dry.used > kNoAllocScratchBytes)
         return fail(KS_ERR_NOMEM,
                     "ks_synthesize_noalloc: these sizes need " + std::to_string(dry.used) +
@@ -1135,7 +1184,8 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     }
     cudaStream_t s = (cudaStream_t)stream;
     Carve c{(char*)scratch, kNoAllocScratchBytes, 0, false};
-    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth);
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, true, need_asynth,
+           default_tile(opt, fp64));
     void* asy = asynth_out ? asynth_out : w.asynth;
     StageTimer tm;  // off: no profiling in this entry point
     // synthesize_impl clears the counters, flags and reach classes in the

@@ -103,6 +103,7 @@ struct AccArgs {
     const int32_t *wing_idx;
     const int32_t *class_pos;   // per depth, per class: line positions, ascending
     const int64_t *class_off;   // [L][N_REACH_CLASSES + 1] absolute offsets into class_pos
+    const int2 *tile_rng;       // [L][tiles][N_REACH_CLASSES] contributing range within each class
     const DepthPar *depth;
     const double *h0d, *h1d, *h2d;
     const float *h0f, *h1f, *h2f;

@@ -546,14 +546,19 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     R2* h01 = reinterpret_cast<R2*>(smem_raw);  // interleaved (H0, H1)
     size_t tab_bytes = (VOIGT_N * sizeof(R2) + 15) & ~size_t(15);
     CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
-    __shared__ int64_t cls_lo[N_REACH_CLASSES];
-    __shared__ int64_t cls_base[N_REACH_CLASSES + 1];
-    __shared__ int64_t cls_hi_s[N_REACH_CLASSES];
+    __shared__ int64_t cls_lo[N_REACH_CLASSES];        // absolute index of the class's first contributing pair
+    __shared__ int64_t cls_n[N_REACH_CLASSES];         // contributing pairs of the class
     __shared__ int64_t bat_base[N_REACH_CLASSES + 1];  // first batch of each class
 
     const R* gh0 = sizeof(R) == 8 ? (const R*)a.h0d : (const R*)a.h0f;
     const R* gh1 = sizeof(R) == 8 ? (const R*)a.h1d : (const R*)a.h1f;
     const R* gh2 = sizeof(R) == 8 ? (const R*)a.h2d : (const R*)a.h2f;
+    if (threadIdx.x < N_REACH_CLASSES) {
+        const int k = threadIdx.x;
+        const int2 r = a.tile_rng[((int64_t)d * gridDim.x + blockIdx.x) * N_REACH_CLASSES + k];
+        cls_lo[k] = a.class_off[(int64_t)d * (N_REACH_CLASSES + 1) + k] + r.x;
+        cls_n[k] = r.y - r.x;
+    }
     for (int i = threadIdx.x; i < VOIGT_N; i += blockDim.x) {
         R2 h;
         h.x = gh0[i];
@@ -564,27 +569,13 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         if constexpr (sizeof(R) == 4) acc[i] = make_float2(0.f, 0.f);
         else acc[i] = 0.0;
     }
-    if (threadIdx.x < N_REACH_CLASSES) {
-        int k = threadIdx.x;
-        const int64_t* off = a.class_off + (int64_t)d * (N_REACH_CLASSES + 1);
-        int64_t lo = off[k], hi = off[k + 1];
-        int64_t h = class_halo(k) + 1;
-        int64_t s0 = lower_bound_pos(a.class_pos, lo, hi, a.wing_idx, (int64_t)T0 - h);
-        int64_t s1 = lower_bound_pos(a.class_pos, s0, hi, a.wing_idx, (int64_t)T1 + h);
-        cls_lo[k] = s0;
-        cls_hi_s[k] = s1;
-    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        int64_t b = 0, nb = 0;
+        int64_t nb = 0;
         for (int k = 0; k < N_REACH_CLASSES; k++) {
-            const int64_t n = cls_hi_s[k] - cls_lo[k];
-            cls_base[k] = b;
             bat_base[k] = nb;
-            b += n;
-            nb += (n + 31) >> 5;
+            nb += (cls_n[k] + 31) >> 5;
         }
-        cls_base[N_REACH_CLASSES] = b;
         bat_base[N_REACH_CLASSES] = nb;
     }
     __syncthreads();
@@ -593,18 +584,47 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const PairDesc<R>* drow = desc + (int64_t)d * a.stride;
     unsigned long long evals = 0;
     const int64_t nbatch = bat_base[N_REACH_CLASSES];
-    int kb = 0;
-    for (int64_t bt = warp; bt < nbatch; bt += nwarps) {
-        while (bt >= bat_base[kb + 1]) kb++;
-        const int64_t first = cls_base[kb] + (bt - bat_base[kb]) * 32;
-        const int cnt = (int)min((int64_t)32, cls_base[kb + 1] - first);
+    // Batches are software-pipelined: the descriptors of the warp's next
+    // batch and the positions of the one after it are in flight while the
+    // current batch is processed.
+    int kcur = 0;  // class of the furthest batch looked up (batches ascend)
+    auto batch_class = [&](int64_t bt) {
+        while (bt >= bat_base[kcur + 1]) kcur++;
+        return kcur;
+    };
+    int64_t bt = warp;
+    int kb = 0, cnt = 0, kb_n = 0, cnt_n = 0;
+    int32_t pos_n = 0;
+    PairDesc<R> pd{};
+    if (bt < nbatch) {
+        kb = batch_class(bt);
+        const int64_t f = (bt - bat_base[kb]) * 32;
+        cnt = (int)min((int64_t)32, cls_n[kb] - f);
+        if (lane < cnt) pd = drow[a.class_pos[cls_lo[kb] + f + lane]];
+    }
+    if (bt + nwarps < nbatch) {
+        kb_n = batch_class(bt + nwarps);
+        const int64_t f = (bt + nwarps - bat_base[kb_n]) * 32;
+        cnt_n = (int)min((int64_t)32, cls_n[kb_n] - f);
+        if (lane < cnt_n) pos_n = a.class_pos[cls_lo[kb_n] + f + lane];
+    }
+    for (; bt < nbatch; bt += nwarps) {
+        PairDesc<R> pd_n{};
+        if (lane < cnt_n && bt + nwarps < nbatch) pd_n = drow[pos_n];
+        int kb_nn = 0, cnt_nn = 0;
+        int32_t pos_nn = 0;
+        if (bt + 2 * nwarps < nbatch) {
+            kb_nn = batch_class(bt + 2 * nwarps);
+            const int64_t f = (bt + 2 * nwarps - bat_base[kb_nn]) * 32;
+            cnt_nn = (int)min((int64_t)32, cls_n[kb_nn] - f);
+            if (lane < cnt_nn) pos_nn = a.class_pos[cls_lo[kb_nn] + f + lane];
+        }
+        const bool valid = lane < cnt;
         if (kb < a.short_class) {
             // ---- short pairs: one lane per pair ----
             int cb = 0, reach = 0, nz = 0;
             R k0 = R(0), ad = R(0), dv = R(0), xf = R(0);
-            if (lane < cnt) {
-                const int64_t p = a.class_pos[cls_lo[kb] + (first + lane - cls_base[kb])];
-                const PairDesc<R> pd = drow[p];
+            if (valid) {
                 cb = pd.wing_c - T0;
                 const int ctr = pd.ctr_n10 & 15;
                 if (ctr) {
@@ -644,68 +664,72 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
                 }
             }
             __syncwarp();
-            continue;
-        }
-        // ---- per lane: one pair and its in-tile offset ranges ----
-        int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
-        R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
-        if (lane < cnt) {
-            const int64_t p = a.class_pos[cls_lo[kb] + (first + lane - cls_base[kb])];
-            const PairDesc<R> pd = drow[p];
-            c = pd.wing_c;
-            const int ctr = pd.ctr_n10 & 15;
-            if (ctr) {
-                int cc = c + (ctr - 8);
-                if (cc >= T0 && cc < T1) {
-                    cb = cc - T0;
-                    kc = pd.kapcen;
-                    evals++;
+        } else {
+            // ---- per lane: one pair and its in-tile offset ranges ----
+            int c = 0, cb = -1, rlo = 1, rhi = 0, blo = 1, bhi = 0, nz = 0;
+            R k0 = R(0), ad = R(0), dv = R(0), xf = R(0), kc = R(0);
+            if (valid) {
+                c = pd.wing_c;
+                const int ctr = pd.ctr_n10 & 15;
+                if (ctr) {
+                    int cc = c + (ctr - 8);
+                    if (cc >= T0 && cc < T1) {
+                        cb = cc - T0;
+                        kc = pd.kapcen;
+                        evals++;
+                    }
+                }
+                const int reach = pd.maxstep_far & 0x7fffffff;
+                if (reach > 0) {
+                    rlo = max(1, T0 - c);
+                    rhi = min(reach, T1 - 1 - c);
+                    blo = max(1, c - (T1 - 1));
+                    bhi = min(reach, c - T0);
+                    if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
+                    if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
+                }
+                nz = pd.maxstep_far < 0 ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
+                k0 = pd.kappa0;
+                ad = pd.adamp;
+                dv = pd.dvoigt;
+                xf = pd.xfar;
+            }
+            const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
+            unsigned mask = __ballot_sync(0xffffffffu, active);
+            while (mask) {
+                const int i = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int ci = __shfl_sync(0xffffffffu, c, i);
+                const int cbi = __shfl_sync(0xffffffffu, cb, i);
+                if (cbi >= 0) {
+                    const R kci = __shfl_sync(0xffffffffu, kc, i);
+                    if (lane == 0) cell_add(my, cbi, kci);
+                }
+                const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
+                const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
+                if (rl > rh && bl > bh) continue;
+                const int nzi = __shfl_sync(0xffffffffu, nz, i);
+                const R adi = __shfl_sync(0xffffffffu, ad, i);
+                const R dvi = __shfl_sync(0xffffffffu, dv, i);
+                const R k0i = __shfl_sync(0xffffffffu, k0, i);
+                const R xfi = __shfl_sync(0xffffffffu, xf, i);
+                const R ts = R(200) * dvi;
+                const int base = ci - T0;
+                // red: bins base + o; blue: bins base - o
+                wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                if (nzi != 0x7fffffff) {
+                    wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                 }
             }
-            const int reach = pd.maxstep_far & 0x7fffffff;
-            if (reach > 0) {
-                rlo = max(1, T0 - c);
-                rhi = min(reach, T1 - 1 - c);
-                blo = max(1, c - (T1 - 1));
-                bhi = min(reach, c - T0);
-                if (rlo <= rhi) evals += (unsigned long long)(rhi - rlo + 1);
-                if (blo <= bhi) evals += (unsigned long long)(bhi - blo + 1);
-            }
-            nz = pd.maxstep_far < 0 ? (pd.ctr_n10 >> 8) : 0x7fffffff;  // last near-zone offset
-            k0 = pd.kappa0;
-            ad = pd.adamp;
-            dv = pd.dvoigt;
-            xf = pd.xfar;
         }
-        const bool active = cb >= 0 || rlo <= rhi || blo <= bhi;
-        unsigned mask = __ballot_sync(0xffffffffu, active);
-        while (mask) {
-            const int i = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int ci = __shfl_sync(0xffffffffu, c, i);
-            const int cbi = __shfl_sync(0xffffffffu, cb, i);
-            if (cbi >= 0) {
-                const R kci = __shfl_sync(0xffffffffu, kc, i);
-                if (lane == 0) cell_add(my, cbi, kci);
-            }
-            const int rl = __shfl_sync(0xffffffffu, rlo, i), rh = __shfl_sync(0xffffffffu, rhi, i);
-            const int bl = __shfl_sync(0xffffffffu, blo, i), bh = __shfl_sync(0xffffffffu, bhi, i);
-            if (rl > rh && bl > bh) continue;
-            const int nzi = __shfl_sync(0xffffffffu, nz, i);
-            const R adi = __shfl_sync(0xffffffffu, ad, i);
-            const R dvi = __shfl_sync(0xffffffffu, dv, i);
-            const R k0i = __shfl_sync(0xffffffffu, k0, i);
-            const R xfi = __shfl_sync(0xffffffffu, xf, i);
-            const R ts = R(200) * dvi;
-            const int base = ci - T0;
-            // red: bins base + o; blue: bins base - o
-            wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-            wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-            if (nzi != 0x7fffffff) {
-                wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-            }
-        }
+        pd = pd_n;
+        kb = kb_n;
+        cnt = cnt_n;
+        pos_n = pos_nn;
+        kb_n = kb_nn;
+        cnt_n = cnt_nn;
     }
     __syncthreads();
     // combine the warp copies in warp order, apply STIM and store
