@@ -115,6 +115,8 @@ typedef struct {
                                negative = none */
     int32_t transfer_path;  /* single precision, fused: 0 = streaming pass (columns it cannot
                                take go to the per-column kernel), 1 = per-column kernel only */
+    int32_t long_class;     /* reach classes >= long_class are dealt to the accumulation warps in
+                               batches of 8 pairs instead of 32; 0 = default (22 = never) */
 } ks_options;
 
 /* Counters of one synthesis (filled when a pointer is given). */

@@ -768,6 +768,7 @@ static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g
     a.tile_bins = default_tile(opt, fp64);
     a.short_class = !opt || opt->short_class == 0 ? SHORT_CLASS
                     : opt->short_class < 0 ? 0 : min(opt->short_class, N_REACH_CLASSES);
+    a.long_class = !opt || opt->long_class <= 0 ? LONG_CLASS : min(opt->long_class, N_REACH_CLASSES);
     a.grid = g->wavelength;
     a.wing_idx = w.wing;
     a.class_pos = w.class_pos;

@@ -99,6 +99,7 @@ struct AccArgs {
     int64_t n_lines, n_wl, stride;
     int n_layers, tile_bins;
     int short_class;            // reach classes below it are accumulated one lane per pair
+    int long_class;             // reach classes from it are dealt in batches of 8 pairs
     const double *grid;
     const int32_t *wing_idx;
     const int32_t *class_pos;   // per depth, per class: line positions, ascending

@@ -372,15 +372,50 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
         const R* h0 = F32 ? (const R*)a.h0f : (const R*)a.h0d;
         const R* h1 = F32 ? (const R*)a.h1f : (const R*)a.h1d;
         const R* h2 = F32 ? (const R*)a.h2f : (const R*)a.h2d;
-        // near-wing KAPMIN scan (line_opacity.py:474-537)
+        // near-wing KAPMIN scan (line_opacity.py:474-537): the first offset
+        // whose profile falls below KAPMIN
         int cut = -1;
         R prof_n10 = R(0);
-        for (int ns = 1; ns <= n10dop; ns++) {
+        int ns = 1;
+        // FP32 with ADAMP < 0.2: from table index 5 on, H0 + a*H1 does not
+        // increase with the offset for any a in [0, 0.2] (the tabulated
+        // differences satisfy dH0 + 0.2*dH1 <= 0 there; only the first
+        // four steps near v = 0 rise), nor does the x > 10 asymptote, which
+        // also lies below the last table value.  Offsets mapping below
+        // index 5 are scanned one by one, the rest by a galloping search.
+        const bool monotone = F32 && adamp < R(0.2);
+        for (; ns <= n10dop; ns++) {
+            if (monotone && (int)(R(0.5) + (R)ns * (R(200) * dvoigt)) >= 5) break;
             R p = near_profile<R>(ns, dvoigt, adamp, kappa0, h0, h1, h2);
             if (ns == n10dop) prof_n10 = p;
             if (p < kapmin_ref) {
                 cut = ns;
                 break;
+            }
+        }
+        if (monotone && cut == -1 && ns <= n10dop) {
+            int lo = ns - 1, probe = ns, step = 1, hi = -1;
+            for (;;) {
+                const R p = near_profile<R>(probe, dvoigt, adamp, kappa0, h0, h1, h2);
+                if (p < kapmin_ref) {
+                    hi = probe;
+                    break;
+                }
+                lo = probe;
+                if (probe == n10dop) {
+                    prof_n10 = p;
+                    break;
+                }
+                probe = min(probe + step, n10dop);
+                step <<= 1;
+            }
+            if (hi > 0) {
+                while (hi - lo > 1) {
+                    const int mid = lo + ((hi - lo) >> 1);
+                    if (near_profile<R>(mid, dvoigt, adamp, kappa0, h0, h1, h2) < kapmin_ref) hi = mid;
+                    else lo = mid;
+                }
+                cut = hi;
             }
         }
         bool far = false;
@@ -574,7 +609,8 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         int64_t nb = 0;
         for (int k = 0; k < N_REACH_CLASSES; k++) {
             bat_base[k] = nb;
-            nb += (cls_n[k] + 31) >> 5;
+            const int bs = k < a.long_class ? 32 : 8;
+            nb += (cls_n[k] + bs - 1) / bs;
         }
         bat_base[N_REACH_CLASSES] = nb;
     }
@@ -598,14 +634,16 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     PairDesc<R> pd{};
     if (bt < nbatch) {
         kb = batch_class(bt);
-        const int64_t f = (bt - bat_base[kb]) * 32;
-        cnt = (int)min((int64_t)32, cls_n[kb] - f);
+        const int bs = kb < a.long_class ? 32 : 8;
+        const int64_t f = (bt - bat_base[kb]) * bs;
+        cnt = (int)min((int64_t)bs, cls_n[kb] - f);
         if (lane < cnt) pd = drow[a.class_pos[cls_lo[kb] + f + lane]];
     }
     if (bt + nwarps < nbatch) {
         kb_n = batch_class(bt + nwarps);
-        const int64_t f = (bt + nwarps - bat_base[kb_n]) * 32;
-        cnt_n = (int)min((int64_t)32, cls_n[kb_n] - f);
+        const int bs = kb_n < a.long_class ? 32 : 8;
+        const int64_t f = (bt + nwarps - bat_base[kb_n]) * bs;
+        cnt_n = (int)min((int64_t)bs, cls_n[kb_n] - f);
         if (lane < cnt_n) pos_n = a.class_pos[cls_lo[kb_n] + f + lane];
     }
     for (; bt < nbatch; bt += nwarps) {
@@ -615,8 +653,9 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         int32_t pos_nn = 0;
         if (bt + 2 * nwarps < nbatch) {
             kb_nn = batch_class(bt + 2 * nwarps);
-            const int64_t f = (bt + 2 * nwarps - bat_base[kb_nn]) * 32;
-            cnt_nn = (int)min((int64_t)32, cls_n[kb_nn] - f);
+            const int bs = kb_nn < a.long_class ? 32 : 8;
+            const int64_t f = (bt + 2 * nwarps - bat_base[kb_nn]) * bs;
+            cnt_nn = (int)min((int64_t)bs, cls_n[kb_nn] - f);
             if (lane < cnt_nn) pos_nn = a.class_pos[cls_lo[kb_nn] + f + lane];
         }
         const bool valid = lane < cnt;
