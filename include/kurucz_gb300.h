@@ -106,8 +106,8 @@ typedef struct {
     double microturb_kms;   /* synthesis microturbulence (default 0) */
     double rhoxj;           /* scattering scale height (0 = LTE, fscat = 0) */
     int32_t precision;      /* ks_precision */
-    int32_t tile_bins;      /* accumulation tile width; 0 = autotuned default */
-    int32_t warps_per_tile; /* warps per accumulation CTA; 0 = default */
+    int32_t tile_bins;      /* accumulation tile width in bins, a multiple of 32; 0 = 1024 */
+    int32_t warps_per_tile; /* warps per accumulation CTA, 1..16; 0 = 8 */
     int32_t profile;        /* 1: time each stage with CUDA events into ks_stats.stage_ms
                                (only when a ks_stats pointer is given) */
     int32_t short_class;    /* reach classes 0..short_class-1 (wing reach <= 2^(short_class-1)

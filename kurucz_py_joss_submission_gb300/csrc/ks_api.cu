@@ -364,6 +364,7 @@ __global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __
 // scatter that keeps line order inside every class (warp ballots give each
 // lane its rank among equal classes).
 static const int kChunk = 4096;
+static const int kDefaultTile = 1024;  // accumulation tile (bins) unless ks_options.tile_bins says otherwise
 static const int kPartThreads = 256;
 
 __global__ void class_count_kernel(const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
@@ -567,7 +568,7 @@ extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_
     Carve c{nullptr, 0, 0, true};
     Workspace w;
     layout(c, w, n_lines, n_layers, n_wavelengths, 6, 139, fp64, true, true,
-           opt && opt->tile_bins > 0 ? opt->tile_bins : 512);
+           opt && opt->tile_bins > 0 ? opt->tile_bins : kDefaultTile);
     *bytes = c.used + 256;
     return KS_OK;
 }
@@ -737,12 +738,12 @@ static ks_status run_partition(const Workspace& w, int L, int64_t n_wl, int tile
 // The accumulation tile: a multiple of 32 bins, at most 8192, with 1-16
 // warps, whose per-warp copies must fit the 227 KB of shared memory.
 static ks_status check_tiling(const ks_options* opt) {
-    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : 512;
+    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : kDefaultTile;
     int w = opt && opt->warps_per_tile > 0 ? opt->warps_per_tile : 8;
     bool fp64 = opt && opt->precision == KS_PREC_FP64;
     if ((opt && (opt->tile_bins < 0 || opt->warps_per_tile < 0)) || w > 16 || t % 32 != 0 || t > 8192)
         return fail(KS_ERR_INVALID,
-                    "tile_bins must be a multiple of 32 up to 8192 and warps_per_tile 1..16 (0 = defaults 512, 8)");
+                    "tile_bins must be a multiple of 32 up to 8192 and warps_per_tile 1..16 (0 = defaults 1024, 8)");
     size_t smem = fp64 ? accumulate_smem_bytes_f64(t, w) : accumulate_smem_bytes_f32(t, w);
     if (smem > 227 * 1024)
         return fail(KS_ERR_INVALID, "tile_bins x warps_per_tile needs more than 227 KB of shared memory");
@@ -750,7 +751,7 @@ static ks_status check_tiling(const ks_options* opt) {
 }
 
 static int default_tile(const ks_options* opt, bool fp64) {
-    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : 512;
+    int t = opt && opt->tile_bins > 0 ? opt->tile_bins : kDefaultTile;
     return t;
 }
 static int default_warps(const ks_options* opt) {
