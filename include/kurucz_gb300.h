@@ -227,6 +227,32 @@ ks_status ks_synthesize(const ks_lines *lines, const ks_atmos *atm, const ks_gri
                         double *flux_total, double *flux_cont, void *asynth_out,
                         ks_stats *stats, void *stream);
 
+/* ks_synthesize in two halves, for runs sharded over GPUs by layer: each
+ * stage before the transfer works layer by layer (the same split as the
+ * reference's depth loops in line_opacity.py:56-184 and :946-1340), and the
+ * transfer wavelength by wavelength (radiative.py:282-494).
+ *
+ * ks_opacity: continuum -> TRANSP -> ASYNTH on the layers of `atm` (any
+ * contiguous block of an atmosphere's layers), writing the ASYNTH and
+ * continuum (absorption, scattering) cubes, device, [n_layers, n], float for
+ * MIXED / double for FP64.  Workspace as ks_synthesize.  No reference
+ * counterpart: the reference runs the whole path in one process. */
+ks_status ks_opacity(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                     const ks_options *opt, void *workspace, size_t workspace_bytes,
+                     void *asynth_out, void *cont_abs_out, void *cont_scat_out,
+                     ks_stats *stats, void *stream);
+
+/* ks_transfer_opacity: the transfer of ks_synthesize (line source, FSCAT
+ * split, two JOSH solves) on cubes [n_layers, n] holding every layer of
+ * `atm` for the wavelengths of `grid` (a slice of the full grid is allowed):
+ * a spectrum stitched from slices is identical to the unsharded one.
+ * Allocates its small scratch on the stream.  Replaces the tail of
+ * opacity.py:2084 run_synthesis from :3788 (solve_lte_spectrum). */
+ks_status ks_transfer_opacity(const ks_atmos *atm, const ks_grid *grid, const ks_options *opt,
+                              const void *cont_abs, const void *cont_scat, const void *asynth,
+                              double *flux_total, double *flux_cont, ks_stats *stats,
+                              void *stream);
+
 /* The fused synthesis of ks_synthesize for callers that cannot allocate
  * device memory: a plug-in running inside a host application that owns all
  * device memory, or a runtime reached through an FFI with no CUDA allocator,

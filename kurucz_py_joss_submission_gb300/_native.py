@@ -111,6 +111,10 @@ SIGNATURES = {
     "ks_synthesize": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                   C.POINTER(KsOptions), P, C.c_size_t, P, P, P,
                                   C.POINTER(KsStats), P]),
+    "ks_opacity": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
+                               C.POINTER(KsOptions), P, C.c_size_t, P, P, P, C.POINTER(KsStats), P]),
+    "ks_transfer_opacity": (C.c_int32, [C.POINTER(KsAtmos), C.POINTER(KsGrid), C.POINTER(KsOptions),
+                                        P, P, P, P, P, C.POINTER(KsStats), P]),
     "ks_synthesize_noalloc": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                           C.POINTER(KsOptions), P, P, P, P]),
     "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,

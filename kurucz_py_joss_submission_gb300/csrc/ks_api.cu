@@ -807,11 +807,13 @@ static TransferArgs transfer_args(const ks_atmos* atm, const ks_grid* g, const W
     return a;
 }
 
-static ks_status collect_stats(const Workspace& w, int64_t n_wl, ks_stats* stats, cudaStream_t s) {
+static ks_status collect_stats(const Workspace& w, int64_t n_wl, ks_stats* stats, cudaStream_t s,
+                               bool with_iters = true) {
     unsigned long long ctr[2];
     int flags = 0;
     KS_CUDA(cudaMemcpyAsync(ctr, w.counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
     KS_CUDA(cudaMemcpyAsync(&flags, w.flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!with_iters) n_wl = 0;
     std::vector<int32_t> it(2 * (size_t)n_wl);
     if (n_wl > 0)
         KS_CUDA(cudaMemcpyAsync(it.data(), w.iters, sizeof(int32_t) * 2 * n_wl,
@@ -1023,11 +1025,38 @@ struct StageTimer {
     }
 };
 
+// The JOSH stage of the fused path (radiative.py:282-494 over ASYNTH split
+// by FSCAT, opacity.py:2408-2420): FP64 per-column kernel, or the FP32
+// streaming pass (per-column kernel on request).
+template <typename R>
+static ks_status run_transfer(const ks_atmos* atm, const ks_grid* grid, const ks_options* opt,
+                              const Workspace& w, const DevTables& t, const R* cabs, const R* cscat,
+                              const R* asynth, double* flux_total, double* flux_cont, cudaStream_t s) {
+    constexpr bool fp64 = sizeof(R) == 8;
+    TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, true, fp64);
+    ta.line_scat = (opt && opt->rhoxj > 0.0) ? 1 : 0;
+    if constexpr (fp64)
+        KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
+    else if (opt && opt->transfer_path == 1)
+        KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
+    else
+        KS_CUDA(launch_transfer_stream_f32(ta, &g_tables.cj, cabs, cscat, asynth, w.tlist, w.counters + 2, s));
+    return KS_OK;
+}
+
+static int fused_launches(bool has_lines, bool fp64, const ks_options* opt, bool with_transfer) {
+    // grid parameters, prep, continuum, accumulation; line bins, pair setup,
+    // three partition passes and the tile ranges; the transfer (FP32:
+    // streaming pass + list pass)
+    const bool stream_pass = !fp64 && !(opt && opt->transfer_path == 1);
+    return 4 + (has_lines ? 6 : 0) + (with_transfer ? (stream_pass ? 2 : 1) : 0);
+}
+
 template <typename R>
 static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
                                  const ks_options* opt, Workspace& w, const DevTables& t,
                                  double* flux_total, double* flux_cont, R* asynth,
-                                 cudaStream_t s, StageTimer& tm) {
+                                 cudaStream_t s, StageTimer& tm, bool do_transfer = true) {
     constexpr bool fp64 = sizeof(R) == 8;
     ks_status st;
     const int L = atm->n_layers;
@@ -1068,14 +1097,8 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
     tm.mark();
-    TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, true, fp64);
-    ta.line_scat = (opt && opt->rhoxj > 0.0) ? 1 : 0;
-    if constexpr (fp64)
-        KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
-    else if (opt && opt->transfer_path == 1)
-        KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
-    else
-        KS_CUDA(launch_transfer_stream_f32(ta, &g_tables.cj, cabs, cscat, asynth, w.tlist, w.counters + 2, s));
+    if (!do_transfer) return KS_OK;
+    if ((st = run_transfer<R>(atm, grid, opt, w, t, cabs, cscat, asynth, flux_total, flux_cont, s))) return st;
     tm.mark();
     return KS_OK;
 }
@@ -1116,15 +1139,112 @@ extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, c
     if (st) return st;
     if (stats) {
         st = collect_stats(w, grid->n, stats, s);
-        // grid parameters, line bins, prep, continuum, pair setup, three
-        // partition passes, accumulation, transfer (FP32: streaming pass +
-        // list pass)
-        const bool has_lines = lines->n_lines > 0;
-        const bool stream_pass = !fp64 && !(opt && opt->transfer_path == 1);
-        stats->kernel_launches = 4 + (has_lines ? 5 : 0) + (stream_pass ? 2 : 1);
+        stats->kernel_launches = fused_launches(lines->n_lines > 0, fp64, opt, true);
         return st;
     }
     return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the fused path in two halves, for depth-sharded runs
+// ---------------------------------------------------------------------------
+
+// Everything of ks_synthesize before the transfer, on the layers given
+// (any contiguous block of an atmosphere: each stage is per layer), with the
+// ASYNTH and continuum cubes [n_layers, n] written to the caller's buffers.
+extern "C" ks_status ks_opacity(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                                const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                void* asynth_out, void* cont_abs_out, void* cont_scat_out,
+                                ks_stats* stats, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_lines(lines);
+    if (!st) st = check_cont(atm);
+    if (st) return st;
+    if (!asynth_out || !cont_abs_out || !cont_scat_out)
+        return fail(KS_ERR_INVALID, "ks_opacity: NULL output cube");
+    if ((st = check_tiling(opt))) return st;
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, false, false,
+           default_tile(opt, fp64));
+    if (!workspace || workspace_bytes < dry.used)
+        return fail(KS_ERR_NOMEM, "ks_opacity: workspace too small (see ks_workspace_size)");
+    Carve c{(char*)workspace, workspace_bytes, 0, false};
+    layout(c, w, lines->n_lines, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, false, false,
+           default_tile(opt, fp64));
+    w.cont_abs = cont_abs_out;
+    w.cont_scat = cont_scat_out;
+    StageTimer tm;
+    tm.start(s, stats && opt && opt->profile);
+    if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, nullptr, nullptr, (double*)asynth_out, s, tm, false);
+    else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, nullptr, nullptr, (float*)asynth_out, s, tm, false);
+    tm.finish(stats);
+    if (st) return st;
+    if (stats) {
+        st = collect_stats(w, grid->n, stats, s, false);
+        stats->kernel_launches = fused_launches(lines->n_lines > 0, fp64, opt, false);
+        return st;
+    }
+    return KS_OK;
+}
+
+// The transfer of ks_synthesize on opacity cubes [n_layers, n] that
+// ks_opacity produced (possibly layer block by layer block, regathered for
+// a wavelength slice of the grid): the same arithmetic, so a spectrum
+// assembled from slices equals the unsharded one.  Allocates its small
+// workspace on the stream.
+extern "C" ks_status ks_transfer_opacity(const ks_atmos* atm, const ks_grid* grid, const ks_options* opt,
+                                         const void* cont_abs, const void* cont_scat, const void* asynth,
+                                         double* flux_total, double* flux_cont, ks_stats* stats,
+                                         void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (st) return st;
+    if (!cont_abs || !cont_scat || !asynth || !flux_total || !flux_cont)
+        return fail(KS_ERR_INVALID, "ks_transfer_opacity: NULL input/output");
+    if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))
+        return fail(KS_ERR_INVALID, "transfer_path must be 0 (streaming) or 1 (per-column)");
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, 0, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, false, false);
+    char* buf = nullptr;
+    KS_CUDA(cudaMallocAsync((void**)&buf, dry.used + 256, s));
+    Carve c{buf, dry.used + 256, 0, false};
+    layout(c, w, 0, atm->n_layers, grid->n, atm->n_ion, atm->n_elem, fp64, false, false);
+    st = KS_OK;
+    if (cudaMemsetAsync(w.flags, 0, sizeof(int), s) != cudaSuccess ||
+        cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned long long), s) != cudaSuccess)
+        st = fail(KS_ERR_CUDA, "ks_transfer_opacity: memset failed");
+    if (!st) st = run_bins(nullptr, grid, w, false, s);
+    if (!st) {
+        PrepArgs pa = prep_args(atm, opt, w);
+        cudaError_t e = fp64 ? launch_prep_f64(pa, s) : launch_prep_f32(pa, s);
+        if (e != cudaSuccess) st = fail(KS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (!st) {
+        if (fp64)
+            st = run_transfer<double>(atm, grid, opt, w, t, (const double*)cont_abs, (const double*)cont_scat,
+                                      (const double*)asynth, flux_total, flux_cont, s);
+        else
+            st = run_transfer<float>(atm, grid, opt, w, t, (const float*)cont_abs, (const float*)cont_scat,
+                                     (const float*)asynth, flux_total, flux_cont, s);
+    }
+    if (!st && stats) {
+        st = collect_stats(w, grid->n, stats, s);
+        const bool stream_pass = !fp64 && !(opt && opt->transfer_path == 1);
+        stats->kernel_launches = 2 + (stream_pass ? 2 : 1);
+    }
+    cudaFreeAsync(buf, s);
+    return st;
 }
 
 // ---------------------------------------------------------------------------

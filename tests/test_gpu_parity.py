@@ -170,7 +170,7 @@ def test_streaming_transfer_matches_per_column_kernel(name):
     assert rel(c0, c1) <= 2e-6
     assert st0["maxj_wavelengths"] == st1["maxj_wavelengths"]
     assert abs(st0["iterations"] - st1["iterations"]) <= max(2, st1["iterations"] // 1000)
-    assert (st0["kernel_launches"], st1["kernel_launches"]) == (11, 10)
+    assert (st0["kernel_launches"], st1["kernel_launches"]) == (12, 11)
     if name == "strong_600_601":
         assert st0["maxj_wavelengths"] > 0
 
