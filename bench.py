@@ -245,10 +245,22 @@ def run_ours(args):
     dcat, datm, dgrid = DeviceCatalog(cat, dev), DeviceAtmosphere(atm, dev), DeviceGrid(grid, device=dev)
     opt = make_options(precision=args.precision, tile_bins=args.tile_bins,
                        warps_per_tile=args.warps_per_tile)
-    syn = Synthesizer(dcat, datm, dgrid, opt, keep_asynth=False)
-    st = syn.run(stats=True)
-    evals = st["evaluations"]
-    launches = st["kernel_launches"]
+    shard = None
+    if world > 1:
+        # one spectrum over `world` GPUs: layer blocks -> all-to-all -> wavelength slices
+        from kurucz_py_joss_submission_gb300 import sharding
+
+        shard = sharding.ShardRank(dcat, atm, grid, None, rank, world, opt, device=dev)
+        st = shard.run(stats=True)
+        step = shard.run
+        outputs = (shard.flux_total, shard.flux_cont)
+    else:
+        syn = Synthesizer(dcat, datm, dgrid, opt, keep_asynth=False)
+        st = syn.run(stats=True)
+        step = syn.run
+        outputs = (syn.flux_total, syn.flux_cont)
+    evals = st["evaluations"]          # one whole spectrum (summed over ranks)
+    launches = st["kernel_launches"]   # this rank's
     log(f"stats {st}")
 
     def barrier():
@@ -257,14 +269,14 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        syn.run()
+        step()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
         e0.record()
         for _ in range(args.steps):
-            syn.run()
+            step()
         e1.record()
         barrier()
     ms = e0.elapsed_time(e1)
@@ -273,53 +285,72 @@ def run_ours(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     ms_step = ms / args.steps
-    value = world * evals * args.steps / (ms / 1e3)
-    spectra = world * args.steps / (ms / 1e3)
+    value = evals * args.steps / (ms / 1e3)
+    spectra = args.steps / (ms / 1e3)
 
     # per-stage device times (CUDA events inside the library), for the roofline
-    prof = Synthesizer(dcat, datm, dgrid, make_options(precision=args.precision, tile_bins=args.tile_bins,
-                                                       warps_per_tile=args.warps_per_tile, profile=True),
-                       keep_asynth=False)
+    # (N > 1: this rank's opacity half, i.e. its block of layers)
+    popt = make_options(precision=args.precision, tile_bins=args.tile_bins,
+                        warps_per_tile=args.warps_per_tile, profile=True)
+    if shard is not None:
+        prof = sharding.ShardRank(dcat, atm, grid, None, rank, world, popt, device=dev)
+        prof_run = lambda: prof.opacity(stats=True)
+    else:
+        prof = Synthesizer(dcat, datm, dgrid, popt, keep_asynth=False)
+        prof_run = lambda: prof.run(stats=True)
     stage = {k: [] for k in ("accumulate", "transfer", "pair_setup", "continuum", "partition", "bins_prep", "total")}
+    prof_stats = None
     for _ in range(max(3, min(args.steps, 5))):
-        s = prof.run(stats=True)["stage_ms"]
+        prof_stats = prof_run()
         for k in stage:
-            stage[k].append(s[k])
+            stage[k].append(prof_stats["stage_ms"][k])
     stage_ms = {k: statistics.median(v) for k, v in stage.items()}
     del prof
 
     # end to end: pinned host inputs -> H2D -> synthesis -> D2H of both fluxes
-    host = {}
+    host = []
     h2d = 0
-    for name, tns in list(dcat.t.items()) + list(datm.t.items()) + [("grid", dgrid.wavelength)]:
+    dev_inputs = list(dcat.t.values())
+    if shard is not None:
+        dev_inputs += list(shard.atm_block.t.values()) + list(shard.atm_full.t.values())
+        dev_inputs += [shard.grid.wavelength, shard.grid_slice.wavelength]
+    else:
+        dev_inputs += list(datm.t.values()) + [dgrid.wavelength]
+    for tns in dev_inputs:
         hp = torch.empty(tns.shape, dtype=tns.dtype, pin_memory=True)
         hp.copy_(tns.cpu())
-        host[name] = (hp, tns)
+        host.append((hp, tns))
         h2d += hp.numel() * hp.element_size()
-    out_t = torch.empty(grid.size, dtype=torch.float64, pin_memory=True)
-    out_c = torch.empty(grid.size, dtype=torch.float64, pin_memory=True)
-    d2h = 2 * grid.size * 8
+    out_t = torch.empty(outputs[0].numel(), dtype=torch.float64, pin_memory=True)
+    out_c = torch.empty(outputs[1].numel(), dtype=torch.float64, pin_memory=True)
+    d2h = 2 * outputs[0].numel() * 8
     e2e_steps = max(1, min(args.steps, 5))
     barrier()
     e0.record()
     for _ in range(e2e_steps):
-        for hp, tns in host.values():
+        for hp, tns in host:
             tns.copy_(hp, non_blocking=True)
-        syn.run()
-        out_t.copy_(syn.flux_total, non_blocking=True)
-        out_c.copy_(syn.flux_cont, non_blocking=True)
+        step()
+        out_t.copy_(outputs[0], non_blocking=True)
+        out_c.copy_(outputs[1], non_blocking=True)
     e1.record()
     barrier()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    e2e_value = world * evals / (e2e_ms / 1e3)
+    if world > 1:
+        v = torch.tensor([e2e_ms, float(h2d), float(d2h)], dtype=torch.float64, device=dev)
+        mx = v[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(v)
+        e2e_ms, h2d, d2h = float(mx.item()), float(v[1].item()), float(v[2].item())
+    e2e_value = evals / (e2e_ms / 1e3)
 
     line = None
     if rank == 0:
         # accuracy of this precision against the all-FP64 path on the same inputs
-        ft = syn.flux_total.cpu().numpy().copy()
-        fc = syn.flux_cont.cpu().numpy().copy()
+        ft = outputs[0].cpu().numpy().copy()
+        fc = outputs[1].cpu().numpy().copy()
         err = None
-        if args.precision != "fp64" and not args.skip_fp64_check:
+        if args.precision != "fp64" and not args.skip_fp64_check and world == 1:
             ref = Synthesizer(dcat, datm, dgrid, make_options(precision="fp64"), keep_asynth=False)
             ref.run()
             torch.cuda.synchronize()
@@ -332,21 +363,26 @@ def run_ours(args):
         hbm_peak, peak_kind = measured_peaks()
         acc_ms = stage_ms["accumulate"]
         L = atm.layers
-        acc_bytes = st["valid_pairs"] * 36.0 + L * grid.size * 4.0   # descriptors + positions in, ASYNTH out
+        # descriptors + positions in, ASYNTH out (N > 1: rank 0's block of layers)
+        acc_pairs = prof_stats["valid_pairs"] if shard is not None else st["valid_pairs"]
+        acc_layers = (shard.depth_blocks[0][1] - shard.depth_blocks[0][0]) if shard is not None else L
+        acc_bytes = acc_pairs * 36.0 + acc_layers * grid.size * 4.0
+        acc_evals = prof_stats["evaluations"] if shard is not None else evals
         achieved_gbs = acc_bytes / (acc_ms / 1e3) / 1e9
         traffic = ncu_traffic()
         fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
-        cpu = cpu_baseline(cat_path) if not args.skip_cpu else None
+        cpu = cpu_baseline(cat_path) if (not args.skip_cpu and world == 1) else None
         line = {
             "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
             "dtype": "fp32" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD["name"] + (f"[{w0}-{w1} nm]" if args.window else ""),
                        "n_lines": len(cat), "n_wavelengths": int(grid.size),
                        "n_layers": int(L), "precision": args.precision,
                        "l2": "inputs larger than L2 (pair descriptors ~2 GB, opacity cubes ~0.3 GB)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": "1 GPU" if world == 1 else
+                       f"{world} GPUs: layer blocks, one all-to-all, wavelength slices"},
             "spectra_per_s": spectra,
             "evaluations_per_step": evals,
             "valid_pairs": st["valid_pairs"],
@@ -361,11 +397,12 @@ def run_ours(args):
                          "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": acc_bytes},
             "roofline_fp32": {"kernel": "accumulate_kernel",
-                              "achieved": evals * FLOPS_PER_EVAL / (acc_ms / 1e3) / 1e12,
+                              "achieved": acc_evals * FLOPS_PER_EVAL / (acc_ms / 1e3) / 1e12,
                               "peak": fp32_peak, "unit": "TFLOP/s",
-                              "frac": evals * FLOPS_PER_EVAL / (acc_ms / 1e3) / 1e12 / fp32_peak,
+                              "frac": acc_evals * FLOPS_PER_EVAL / (acc_ms / 1e3) / 1e12 / fp32_peak,
                               "peak_kind": "nominal (152 SM x 128 lanes x 2 x 2.07 GHz)"},
         }
+        line["cpu_baseline"] = None  # timed on rank 0 at N = 1 only
         if cpu is not None:
             line["cpu_baseline"] = {"value": cpu["evals_per_s"], "unit": "evals/s", "cores": cpu["threads"],
                                     "kind": "port",
