@@ -226,14 +226,16 @@ __device__ __forceinline__ R near_profile(int off, R dvoigt, R adamp, R kappa0,
 // writes the pair's descriptor and reach class (0xff: no contribution).
 // FP64 instantiation: the reference's arithmetic operation by operation.
 // FP32 instantiation: single precision after exact FASTEX table indices.
+// First half of one (line, depth) pair: the TRANSP gates and the centre
+// add.  Returns true when the pair still needs its wings (pair_wings), with
+// KAPCEN, the wing kappa0 and the centre code; otherwise the pair is
+// finished (no contribution, or a centre-only descriptor written here).
 template <typename R, bool FUSED>
-__global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
-                                  const R* __restrict__ kap_b, PairDesc<R>* __restrict__ desc,
-                                  uint8_t* __restrict__ cls) {
+__device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict__ kap_a,
+                                          const R* __restrict__ kap_b, PairDesc<R>* __restrict__ desc,
+                                          uint8_t* __restrict__ cls, int64_t li, int d, R& kc_out,
+                                          R& k0_out, int& code_out) {
     constexpr bool F32 = sizeof(R) == 4;
-    int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int d = blockIdx.y;
-    if (li >= a.n_lines) return;
     const int L = a.n_layers;
     int64_t slot = (int64_t)d * a.stride + li;
     cls[slot] = 0xff;
@@ -244,7 +246,7 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
     const int e = a.element_idx[li];
     const int ion = a.ion_stage[li];
     const int lt = a.line_type[li];
-    if (e < 0 || e >= a.n_elem || ion <= 0 || ion > a.n_ion) return;
+    if (e < 0 || e >= a.n_elem || ion <= 0 || ion > a.n_ion) return false;
     const DepthPar& dp = a.depth[d];
     const IonPar& q = a.ion[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
     const int c_ctr = a.center_idx[li];
@@ -317,7 +319,7 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
         valid = a.valid_in[li * L + d] != 0;
         kapcen = (R)a.transp_in[li * L + d];
     }
-    if (!valid || !(kapcen > R(0))) return;
+    if (!valid || !(kapcen > R(0))) return false;
 
     // ---------------- ASYNTH parameters (line_opacity.py:1161-1272) ----------------
     int ctr_code = 0;  // centre add, line_opacity.py:1091-1102
@@ -325,10 +327,57 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
         int dlt = c_ctr - c_wing;
         if (dlt < -7 || dlt > 7) {
             atomicOr(a.flags, FLAG_N10DOP_RANGE);
-            return;
+            return false;
         }
         ctr_code = dlt + 8;
     }
+    const bool wl_pos = F32 ? a.linef[li].wl > 0.0f : a.wavelength[li] > 0.0;
+    const bool wings = (lt == 0) && (q.ok & 2) && wl_pos &&
+                       c_wing >= -MAX_PROFILE_STEPS && c_wing <= nwl - 1 + MAX_PROFILE_STEPS;
+    if (wings) {
+        kc_out = kapcen;
+        k0_out = kappa0_w;
+        code_out = ctr_code;
+        return true;
+    }
+    if (ctr_code != 0) {
+        PairDesc<R> out;
+        out.wing_c = c_wing;
+        out.kapcen = kapcen;
+        out.kappa0 = R(0);
+        out.adamp = R(0);
+        out.dvoigt = R(0);
+        out.xfar = R(0);
+        out.maxstep_far = 0;
+        out.ctr_n10 = ctr_code;
+        desc[slot] = out;
+        cls[slot] = 0;
+    }
+    return false;
+}
+
+// Second half: the wing parameters (line_opacity.py:1161-1272), the
+// near-wing KAPMIN crossing (:474-537), MAXSTEP and X_far, the descriptor and
+// the reach class.
+template <typename R>
+__device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restrict__ kap_a,
+                                           const R* __restrict__ kap_b, PairDesc<R>* __restrict__ desc,
+                                           uint8_t* __restrict__ cls, int64_t li, int d, R kapcen,
+                                           R kappa0_w, int ctr_code) {
+    constexpr bool F32 = sizeof(R) == 4;
+    const int64_t slot = (int64_t)d * a.stride + li;
+    const int e = a.element_idx[li];
+    const int ion = a.ion_stage[li];
+    const DepthPar& dp = a.depth[d];
+    const IonPar& q = a.ion[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
+    const int c_wing = a.wing_idx[li];
+    const int64_t nwl = a.n_wl;
+    auto kap_at = [&](int c) -> R {
+        int cc = c < 0 ? 0 : (c > (int)nwl - 1 ? (int)nwl - 1 : c);
+        R v = kap_a[(int64_t)d * nwl + cc];
+        if (kap_b) v += kap_b[(int64_t)d * nwl + cc];
+        return v;
+    };
     PairDesc<R> out;
     out.wing_c = c_wing;
     out.kapcen = kapcen;
@@ -339,10 +388,7 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
     out.maxstep_far = 0;
     int reach = 0;
     int n10dop = 0;
-    const bool wl_pos = F32 ? a.linef[li].wl > 0.0f : a.wavelength[li] > 0.0;
-    const bool wings = (lt == 0) && (q.ok & 2) && wl_pos &&
-                       c_wing >= -MAX_PROFILE_STEPS && c_wing <= nwl - 1 + MAX_PROFILE_STEPS;
-    if (wings) {
+    {
         R adamp, kappa0, dvoigt;
         if (!F32) {
             const double lw = a.wavelength[li];
@@ -442,6 +488,40 @@ __global__ void pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
     out.ctr_n10 = ctr_code | (n10dop << 8);
     desc[slot] = out;
     cls[slot] = (uint8_t)reach_class(reach);
+}
+
+// One CTA per (128 consecutive lines, depth): every thread runs the gates of
+// its pair and queues it in shared memory if it needs wings; the queue is
+// then worked by the CTA's first threads, so the wing code and its variable
+// scan run on packed lanes instead of on the lanes whose pairs passed the
+// gates.  Each pair writes only its own descriptor slot and class byte, so
+// the queue order does not change the result.
+template <typename R, bool FUSED>
+__global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
+                                                         const R* __restrict__ kap_b,
+                                                         PairDesc<R>* __restrict__ desc,
+                                                         uint8_t* __restrict__ cls) {
+    __shared__ int q_n;
+    __shared__ int q_li[128], q_code[128];
+    __shared__ R q_kc[128], q_k0[128];
+    if (threadIdx.x == 0) q_n = 0;
+    __syncthreads();
+    const int d = blockIdx.y;
+    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li < a.n_lines) {
+        R kc, k0;
+        int code;
+        if (pair_gate<R, FUSED>(a, kap_a, kap_b, desc, cls, li, d, kc, k0, code)) {
+            const int i = atomicAdd(&q_n, 1);
+            q_li[i] = (int)li;
+            q_kc[i] = kc;
+            q_k0[i] = k0;
+            q_code[i] = code;
+        }
+    }
+    __syncthreads();
+    const int i = threadIdx.x;
+    if (i < q_n) pair_wings<R>(a, kap_a, kap_b, desc, cls, q_li[i], d, q_kc[i], q_k0[i], q_code[i]);
 }
 
 // ---------------------------------------------------------------------------
