@@ -1,9 +1,12 @@
 """Benchmark of the GB300 line-opacity + transfer path (one JSON line).
 
-Workload (``full_300_1800``): one synthetic grey atmosphere (Teff 5800 K,
-log g 4.44, 72 layers, converted by the reference's own converter), the
-300-1800 nm grid at R = 300000 (537,529 points) and 1.5M seeded atomic lines
-(gfall format, log-uniform in wavelength).  A step is one full synthesis --
+Workload (``--workload``, default ``full_300_1800``): one synthetic grey
+atmosphere (Teff 5800 K, log g 4.44, 72 layers, converted by the reference's
+own converter), the 300-1800 nm grid at R = 300000 (537,529 points) and 1.5M
+seeded atomic lines (gfall format, log-uniform in wavelength).
+``window_500_510`` is the 20,000-line 500-510 nm case (5,941 points) the
+reference itself runs on a CPU; ``dense_10m`` the stress case: Teff 2500 K,
+log g -1.0, 300-1800 nm, 1.5M atomic + 8.5M molecular-band-like lines.  A step is one full synthesis --
 continuum, TRANSP, ASYNTH, line source, JOSH flux and continuum flux for
 every grid point -- with inputs resident in HBM.  The metric is
 line.depth.lambda evaluations per second (the exact count of opacity
@@ -35,15 +38,38 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-WORKLOAD = dict(name="full_300_1800", teff=5800.0, logg=4.44, wl_start=300.0, wl_end=1800.0,
-                resolution=300000.0, n_lines=1_500_000, seed=20241, atm="atm_t5800g444.npz")
+# Workloads: line draws from kurucz_py_joss_submission_gb300.workloads.WORKLOADS, plus the
+# converted atmosphere and the CPU-baseline sample windows.
+_SAMPLE_40NM = [(float(a), float(a) + 40.0) for a in np.exp(np.linspace(np.log(305.0), np.log(1750.0), 12))]
+_SAMPLE_10NM = [(float(a), float(a) + 10.0) for a in np.exp(np.linspace(np.log(305.0), np.log(1780.0), 12))]
+BENCH_WORKLOADS = {
+    "full_300_1800": dict(atm="atm_t5800g444.npz", sample=_SAMPLE_40NM),
+    "window_500_510": dict(atm="atm_t5800g444.npz", sample=[(500.0, 510.0)]),
+    "dense_10m": dict(atm="atm_t2500gm10.npz", sample=_SAMPLE_10NM),
+}
+
+
+def workload_spec(name: str) -> dict:
+    from kurucz_py_joss_submission_gb300 import workloads
+
+    spec = dict(workloads.WORKLOADS[name])
+    spec.update(BENCH_WORKLOADS[name])
+    spec["name"] = name
+    spec.setdefault("resolution", 300000.0)
+    return spec
+
+
+WORKLOAD = workload_spec("full_300_1800")
 METRIC = "line.depth.lambda evaluations/s (spectra/s alongside), <=1e-4 rel flux err vs FP64, 1xGB300"
 # FP32 work per accumulated contribution: the far-wing value X/o^2 shared by
 # the red and blue bin (1 mul + 1 fast divide = 2 flops per 2 contributions)
 # plus the Kahan-compensated add (4 flops): 5 flops per contribution.
 FLOPS_PER_EVAL = 5.0
-# CPU-baseline sample: 12 windows of 40 nm spread log-uniformly over 300-1800 nm
-SAMPLE_WINDOWS = [(float(a), float(a) + 40.0) for a in np.exp(np.linspace(np.log(305.0), np.log(1750.0), 12))]
+
+
+def sample_text() -> str:
+    w = WORKLOAD["sample"]
+    return f"{len(w)} window(s) x {w[0][1] - w[0][0]:g} nm of the workload"
 
 
 def log(*a):
@@ -58,7 +84,11 @@ def workload_catalog_path() -> Path:
     if not p.exists():
         t = time.time()
         d = workloads.random_atomic_lines(WORKLOAD["n_lines"], WORKLOAD["wl_start"], WORKLOAD["wl_end"],
-                                          WORKLOAD["seed"], log_uniform=True)
+                                          WORKLOAD["seed"], log_uniform=WORKLOAD["log_uniform"])
+        if WORKLOAD.get("n_band_lines"):
+            bands = workloads.random_band_lines(WORKLOAD["n_band_lines"], WORKLOAD["wl_start"],
+                                                WORKLOAD["wl_end"], WORKLOAD["band_seed"])
+            d = workloads.merge_lines(d, bands)
         tmpname = p.with_suffix(f".{os.getpid()}.tmp")
         workloads.write_gfall(tmpname, d)
         os.replace(tmpname, p)
@@ -167,7 +197,7 @@ def cpu_baseline(cat_path: Path, steps: int = 1):
     from kurucz_py_joss_submission_gb300.io.lines import atomic
 
     cats = []
-    for w0, w1 in SAMPLE_WINDOWS:
+    for w0, w1 in WORKLOAD["sample"]:
         c = atomic.load_catalog_window(cat_path, w0, w1, sort=False)
         cats.append(dict(wavelength=c.wavelength, log_gf=c.log_gf, code=c.code,
                          excitation_energy=c.excitation_energy, gamma_rad=c.gamma_rad,
@@ -177,15 +207,18 @@ def cpu_baseline(cat_path: Path, steps: int = 1):
                          line_size=np.zeros(len(c), np.int32)))
     threads = oracle.num_threads()
     tot_t, tot_e, tot_pts = 0.0, 0, 0
-    for _ in range(steps):
-        for (w0, w1), c in zip(SAMPLE_WINDOWS, cats):
+    rep = 0
+    # at least `steps` passes over the sample, and at least 10 s of CPU time
+    while rep < steps or (tot_t < 10.0 and rep < 1000):
+        rep += 1
+        for (w0, w1), c in zip(WORKLOAD["sample"], cats):
             t = time.perf_counter()
             r = oracle.synthesize(atm, c, w0, w1, WORKLOAD["resolution"], tb=tb)
             tot_t += time.perf_counter() - t
             tot_e += int(r["evals_per_depth"].sum())
             tot_pts += r["wavelength"].size
     return dict(evals_per_s=tot_e / tot_t, seconds=tot_t, evals=tot_e, points=tot_pts,
-                threads=threads)
+                threads=threads, passes=rep)
 
 
 def run_reference(args):
@@ -193,7 +226,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     cat_path = workload_catalog_path()
-    n_full = 537529
+    n_full = int(wavelength_grid().size)
     for _ in range(max(args.warmup, 0)):
         pass  # the CPU port has no warm-up state; each step is a fresh sample
     res = cpu_baseline(cat_path, steps=max(1, args.steps))
@@ -203,13 +236,14 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * res["seconds"] / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD["name"], "n_lines": WORKLOAD["n_lines"],
+        "config": {"workload": WORKLOAD["name"],
+                   "n_lines": WORKLOAD["n_lines"] + WORKLOAD.get("n_band_lines", 0),
                    "n_wavelengths": n_full, "n_layers": 72},
         "spectra_per_s": spectra,
         "cpu_baseline": {"value": res["evals_per_s"], "unit": "evals/s", "cores": res["threads"],
                          "kind": "port",
-                         "sample": f"{len(SAMPLE_WINDOWS)} windows x 40 nm of the workload "
-                                   f"({res['points']} grid points, {res['evals']} evaluations) per step"},
+                         "sample": f"{sample_text()}, {res['passes']} pass(es) ({res['points']} grid "
+                                   f"points, {res['evals']} evaluations) per step"},
         "e2e": {"value": res["evals_per_s"], "unit": "evals/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -272,14 +306,30 @@ def run_ours(args):
         step()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # Small workloads fit in L2 (129 MB): flush it (write 256 MB) before every
+    # timed step, outside the timed interval; the large ones stream more than
+    # L2 per step by themselves.
+    small = WORKLOAD["n_lines"] + WORKLOAD.get("n_band_lines", 0) < 200_000 or args.window is not None
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if small else None
     with ClockSampler(local) as clk:
         barrier()
-        e0.record()
-        for _ in range(args.steps):
-            step()
-        e1.record()
-        barrier()
-    ms = e0.elapsed_time(e1)
+        if flush_buf is None:
+            e0.record()
+            for _ in range(args.steps):
+                step()
+            e1.record()
+            barrier()
+            ms = e0.elapsed_time(e1)
+        else:
+            ms = 0.0
+            for _ in range(args.steps):
+                flush_buf.fill_(1)
+                e0.record()
+                step()
+                e1.record()
+                e1.synchronize()
+                ms += e0.elapsed_time(e1)
+            barrier()
     if world > 1:
         tt = torch.tensor([ms], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -380,7 +430,9 @@ def run_ours(args):
             "config": {"workload": WORKLOAD["name"] + (f"[{w0}-{w1} nm]" if args.window else ""),
                        "n_lines": len(cat), "n_wavelengths": int(grid.size),
                        "n_layers": int(L), "precision": args.precision,
-                       "l2": "inputs larger than L2 (pair descriptors ~2 GB, opacity cubes ~0.3 GB)",
+                       "l2": ("L2 flushed (256 MB written) before every timed step" if flush_buf is not None
+                              else f"inputs larger than L2 (pair descriptors {st['valid_pairs'] * 32 / 1e9:.1f} GB, "
+                                   f"opacity cubes {3 * L * grid.size * 4 / 1e9:.2f} GB per step)"),
                        "parallelism": "1 GPU" if world == 1 else
                        f"{world} GPUs: layer blocks, one all-to-all, wavelength slices"},
             "spectra_per_s": spectra,
@@ -406,9 +458,8 @@ def run_ours(args):
         if cpu is not None:
             line["cpu_baseline"] = {"value": cpu["evals_per_s"], "unit": "evals/s", "cores": cpu["threads"],
                                     "kind": "port",
-                                    "sample": f"{len(SAMPLE_WINDOWS)} windows x 40 nm of the workload "
-                                              f"({cpu['points']} points, {cpu['evals']} evaluations, "
-                                              f"{cpu['seconds']:.1f} s)"}
+                                    "sample": f"{sample_text()}, {cpu['passes']} pass(es) ({cpu['points']} "
+                                              f"points, {cpu['evals']} evaluations, {cpu['seconds']:.1f} s)"}
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -430,7 +481,12 @@ def main():
     ap.add_argument("--skip-fp64-check", action="store_true")
     ap.add_argument("--window", type=float, nargs=2, default=None,
                     help="restrict the workload to a wavelength window (small profiling case)")
+    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS), default="full_300_1800",
+                    help="full_300_1800 (headline: 1.5M lines, Teff 5800 K), window_500_510 (20k lines, "
+                         "the CPU-runnable reference case), dense_10m (10M lines, Teff 2500 K, log g -1)")
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = workload_spec(args.workload)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -254,6 +254,64 @@ def random_atomic_lines(
     )
 
 
+# Band lines carry an atomic species code: the synthesis path takes
+# populations for Z <= 99 only (line_opacity.py:758-763 maps a record's
+# element to its atomic number; records with a molecular code are dropped),
+# so molecular-band-like lines are written as Ti I (22.00).
+BAND_CODE = 22.00
+
+
+def random_band_lines(n_lines: int, wl_min: float, wl_max: float, seed: int,
+                      j_max: int = 150) -> LineDraw:
+    """Draw ``n_lines`` lines in molecular-band-like sequences.
+
+    Each band has a head wavelength ~ U(wl_min, wl_max) nm, a rotational
+    constant B ~ U(0.3, 2) cm^-1 and lines J = 0..j_max at wavenumber
+    sigma_J = sigma_head - dB J^2 (spacing growing as J^2, dB = 0.02 B),
+    lower-level energy E = B J (J + 1), log gf ~ N(-4, 1), damping drawn as
+    for the atomic lines, species code :data:`BAND_CODE`.  Lines outside
+    [wl_min, wl_max] are dropped; bands are drawn until ``n_lines`` lines
+    are kept.  Returned sorted by wavelength.
+    """
+    rng = np.random.default_rng(seed)
+    j = np.arange(j_max + 1, dtype=np.float64)
+    parts, kept = [], 0
+    while kept < n_lines:
+        nb = max(64, int(1.3 * (n_lines - kept) / (j_max + 1)) + 1)
+        head = rng.uniform(wl_min, wl_max, nb)
+        b = rng.uniform(0.3, 2.0, nb)
+        sigma = (1.0e7 / head)[:, None] - (0.02 * b)[:, None] * j[None, :] ** 2
+        with np.errstate(divide="ignore"):
+            wl = np.where(sigma > 0, 1.0e7 / np.where(sigma > 0, sigma, 1.0), np.inf)
+        e = b[:, None] * j[None, :] * (j[None, :] + 1.0)
+        ok = (wl >= wl_min) & (wl <= wl_max)
+        wl, e = wl[ok], e[ok]
+        parts.append((wl, e))
+        kept += wl.size
+    wl = np.concatenate([p[0] for p in parts])[:n_lines]
+    elo = np.concatenate([p[1] for p in parts])[:n_lines]
+    n = wl.size
+    loggf = np.clip(rng.normal(-4.0, 1.0, n), -8.0, 1.0)
+    gr = rng.normal(8.0, 0.5, n)
+    gs = rng.normal(-5.5, 0.5, n)
+    gw = rng.normal(-7.5, 0.3, n)
+    order = np.argsort(wl, kind="stable")
+    return LineDraw(
+        wavelength_nm=wl[order], log_gf=loggf[order], code=np.full(n, BAND_CODE)[order],
+        e_lower_cm=elo[order], log_gamma_rad=gr[order], log_gamma_stark=gs[order],
+        log_gamma_vdw=gw[order],
+    )
+
+
+def merge_lines(*draws: LineDraw) -> LineDraw:
+    """Concatenate line draws, sorted by wavelength (stable)."""
+    cat = {f: np.concatenate([getattr(d, f) for d in draws]) for f in
+           ("wavelength_nm", "log_gf", "code", "e_lower_cm", "log_gamma_rad", "log_gamma_stark",
+            "log_gamma_vdw")}
+    order = np.argsort(cat["wavelength_nm"], kind="stable")
+    return LineDraw(**{k: v[order] for k, v in cat.items()})
+
+
 def _nonzero_f62(x: np.ndarray) -> np.ndarray:
     """Keep damping logs away from the F6.2 value 0.00, which gfall reads as 'absent'."""
     r = np.round(x, 2)
@@ -291,4 +349,8 @@ WORKLOADS: Dict[str, Dict[str, object]] = {
     # full 300-1800 nm, 1.5M lines, same atmosphere (single-GPU headline case)
     "full_300_1800": dict(teff=5800.0, logg=4.44, wl_start=300.0, wl_end=1800.0,
                           n_lines=1_500_000, log_uniform=True, seed=20241),
+    # dense stress: Teff 2500 log g -1.0, 300-1800 nm, 1.5M atomic + 8.5M band lines
+    "dense_10m": dict(teff=2500.0, logg=-1.0, wl_start=300.0, wl_end=1800.0,
+                      n_lines=1_500_000, log_uniform=True, seed=20242,
+                      n_band_lines=8_500_000, band_seed=20243),
 }

@@ -52,6 +52,7 @@ ATM_FIELDS = (
 ATMOSPHERES = {
     "t5800g444": dict(teff=5800.0, logg=4.44, metallicity=0.0),
     "t6000g430": dict(teff=6000.0, logg=4.30, metallicity=0.0),
+    "t2500gm10": dict(teff=2500.0, logg=-1.0, metallicity=0.0),
 }
 
 # name: atmosphere, window, line draw.  Line windows extend 0.15 nm past the
@@ -67,6 +68,10 @@ CASES = {
                            strong=True),
     "window_500_510": dict(atm="t5800g444", wl_start=500.0, wl_end=510.0,
                            n_lines=20_000, draw=(500.0, 510.0), log_uniform=False, seed=20240),
+    # cool giant with molecular-band-like lines (the dense stress case's physics)
+    "cool_600_601": dict(atm="t2500gm10", wl_start=600.0, wl_end=601.0,
+                         n_lines=200, draw=(599.85, 601.15), log_uniform=False, seed=14,
+                         band_lines=800, band_seed=15),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -85,6 +90,10 @@ def case_lines(case: dict) -> workloads.LineDraw:
         case["n_lines"], case["draw"][0], case["draw"][1], case["seed"],
         log_uniform=case["log_uniform"],
     )
+    if case.get("band_lines"):
+        bands = workloads.random_band_lines(case["band_lines"], case["draw"][0], case["draw"][1],
+                                            case["band_seed"])
+        lines = workloads.merge_lines(lines, bands)
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth
         # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)
