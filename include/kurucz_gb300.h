@@ -111,12 +111,12 @@ typedef struct {
     int32_t profile;        /* 1: time each stage with CUDA events into ks_stats.stage_ms
                                (only when a ks_stats pointer is given) */
     int32_t short_class;    /* reach classes 0..short_class-1 (wing reach <= 2^(short_class-1)
-                               bins) are accumulated one lane per pair; 0 = default (6),
+                               bins) are accumulated one lane per pair; 0 = default (7),
                                negative = none */
     int32_t transfer_path;  /* single precision, fused: 0 = streaming pass (columns it cannot
                                take go to the per-column kernel), 1 = per-column kernel only */
     int32_t long_class;     /* reach classes >= long_class are dealt to the accumulation warps in
-                               batches of 8 pairs instead of 32; 0 = default (22 = never) */
+                               batches of 8 pairs instead of 32; 0 = default (8) */
 } ks_options;
 
 /* Counters of one synthesis (filled when a pointer is given). */

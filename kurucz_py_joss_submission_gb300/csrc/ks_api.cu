@@ -1062,12 +1062,16 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
     const int L = atm->n_layers;
     KS_CUDA(cudaMemsetAsync(w.flags, 0, sizeof(int), s));
     KS_CUDA(cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned long long), s));
-    KS_CUDA(cudaMemsetAsync(w.cls, 0xff, (size_t)L * w.stride, s));
-    if ((st = run_bins(lines, grid, w, !fp64, s))) return st;
+    // class bytes of the padding slots [n_lines, stride) of every depth (the
+    // pair setup writes the others)
+    if (w.stride > lines->n_lines)
+        KS_CUDA(cudaMemset2DAsync(w.cls + lines->n_lines, (size_t)w.stride, 0xff,
+                                  (size_t)(w.stride - lines->n_lines), (size_t)L, s));
     PrepArgs pa = prep_args(atm, opt, w);
     ContArgs ca = cont_args(atm, grid);
     R* cabs = (R*)w.cont_abs;
     R* cscat = (R*)w.cont_scat;
+    if ((st = run_bins(lines, grid, w, !fp64, s))) return st;
     if constexpr (fp64) KS_CUDA(launch_prep_f64(pa, s));
     else KS_CUDA(launch_prep_f32(pa, s));
     tm.mark();

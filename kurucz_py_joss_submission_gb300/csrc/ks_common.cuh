@@ -20,8 +20,8 @@ constexpr int EXP_N = 1001;                 // EXTAB/EXTABF length
 constexpr int NXTAU = 51;                   // JOSH optical-depth grid
 constexpr int MAX_LAYERS = 128;             // per-wavelength column bound
 constexpr int N_REACH_CLASSES = 22;         // reach classes 0..21 (2^20 > MAXPROF)
-constexpr int LONG_CLASS = 22;              // default: every class in batches of 32 pairs
-constexpr int SHORT_CLASS = 6;              // default: classes 0-5 (reach <= 32 bins) one lane per pair
+constexpr int LONG_CLASS = 8;               // default: classes 8+ (reach > 128 bins) in batches of 8 pairs
+constexpr int SHORT_CLASS = 7;              // default: classes 0-6 (reach <= 64 bins) one lane per pair
 constexpr double EPS38 = 1.0e-38;
 constexpr double MAX_OPACITY_REAL4 = 3.4e38;
 

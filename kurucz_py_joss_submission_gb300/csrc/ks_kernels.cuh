@@ -592,8 +592,45 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // read-modify-write; a bin at either end without its partner is added by
 // lane 0 / lane 1.  Each bin gets the same additions in the same order as
 // with one bin per lane.
+// Long far runs (>= 64 bins): aligned quads of bins (4q .. 4q+3), one per
+// lane, four values from packed FP32x2 arithmetic and one 16-byte
+// read-modify-write; the up to three bins at each end outside whole quads
+// are added by lanes 0-2 (low end) and 4-6 (high end).
+__device__ __forceinline__ void far_run_x4(float* my, int b_lo, int b_hi, int base, int sgn, int lane,
+                                           float xf) {
+    const int e_lo = (4 - (b_lo & 3)) & 3;  // bins before the first whole quad
+    const int e_hi = (b_hi + 1) & 3;        // bins after the last whole quad
+    int eb = -1;
+    if (lane < e_lo) eb = b_lo + lane;
+    else if (lane >= 4 && lane < 4 + e_hi) eb = b_hi - e_hi + 1 + (lane - 4);
+    if (eb >= 0) {
+        const float o = (float)(sgn * (eb - base));
+        my[eb] += __fdividef(xf, o * o);
+    }
+    float4* my4 = reinterpret_cast<float4*>(my);
+    const int q0 = (b_lo + e_lo) >> 2, q1 = ((b_hi - e_hi + 1) >> 2) - 1;
+    const float2 xf2 = make_float2(xf, xf);
+    const float2 d2 = make_float2(2.0f * (float)sgn, 2.0f * (float)sgn);
+    for (int q = q0 + lane; q <= q1; q += 32) {
+        const int o0 = sgn * (4 * q - base);
+        const float2 oa = make_float2((float)o0, (float)(o0 + sgn));
+        const float2 ob = __fadd2_rn(oa, d2);
+        const float2 sa = __fmul2_rn(oa, oa), sb = __fmul2_rn(ob, ob);
+        const float2 va = __fmul2_rn(xf2, make_float2(rcp_approx(sa.x), rcp_approx(sa.y)));
+        const float2 vb = __fmul2_rn(xf2, make_float2(rcp_approx(sb.x), rcp_approx(sb.y)));
+        float4 c = my4[q];
+        const float2 ca = __fadd2_rn(make_float2(c.x, c.y), va);
+        const float2 cb = __fadd2_rn(make_float2(c.z, c.w), vb);
+        my4[q] = make_float4(ca.x, ca.y, cb.x, cb.y);
+    }
+}
+
 __device__ __forceinline__ void far_run_x2(float* my, int base, int sgn, int lo, int hi, int lane, float xf) {
     if (lo > hi) return;
+    if (hi - lo >= 63) {
+        far_run_x4(my, sgn > 0 ? base + lo : base - hi, sgn > 0 ? base + hi : base - lo, base, sgn, lane, xf);
+        return;
+    }
     const int b_lo = sgn > 0 ? base + lo : base - hi;
     const int b_hi = sgn > 0 ? base + hi : base - lo;
     int eb = -1;
