@@ -525,6 +525,8 @@ struct Workspace {
     int32_t* tlist;  // wavelengths left to the general transfer kernel
     int2* tile_rng;  // per (depth, tile, class) contributing range
     int ntiles;
+    float* coef_f;   // continuum coefficient tables in FP32: absorption, then scattering
+    float* freq_f;   // c / lambda per grid point in FP32
     int* flags;
     int64_t stride;
     int nchunks;
@@ -557,6 +559,8 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.tlist = c.take<int32_t>(n_wl > 0 ? n_wl : 1);
     w.ntiles = tile_bins > 0 ? (int)((n_wl + tile_bins - 1) / tile_bins) : 0;
     w.tile_rng = c.take<int2>((size_t)L * (w.ntiles > 0 ? w.ntiles : 1) * N_REACH_CLASSES);
+    w.coef_f = c.take<float>(2 * (size_t)L * (MAX_EDGES - 1) * 3);
+    w.freq_f = c.take<float>(n_wl > 0 ? n_wl : 1);
     w.flags = c.take<int>(1);
 }
 
@@ -593,6 +597,7 @@ static ks_status check_cont(const ks_atmos* a) {
     if (!a->wledge || !a->cont_abs_coeff || !a->cont_scat_coeff || a->n_edge < 2)
         return fail(KS_ERR_INVALID,
                     "continuum coefficients are missing (wledge, cont_abs_coeff, cont_scat_coeff)");
+    if (a->n_edge > MAX_EDGES) return fail(KS_ERR_UNSUPPORTED, "more than 1024 continuum edges");
     return KS_OK;
 }
 
@@ -641,6 +646,9 @@ static PrepArgs prep_args(const ks_atmos* atm, const ks_options* opt, const Work
     p.gp = w.gp;
     p.depth = w.depth;
     p.ion = w.ion;
+    p.n_coeff = 0;
+    p.abs_coeff = p.scat_coeff = nullptr;
+    p.abs_coeff_f = p.scat_coeff_f = nullptr;
     return p;
 }
 
@@ -656,6 +664,8 @@ static ContArgs cont_args(const ks_atmos* atm, const ks_grid* g) {
     c.delta_edge = atm->delta_edge;
     c.abs_coeff = atm->cont_abs_coeff;
     c.scat_coeff = atm->cont_scat_coeff;
+    c.abs_coeff_f = c.scat_coeff_f = nullptr;
+    c.freq_f = nullptr;
     return c;
 }
 
@@ -670,6 +680,7 @@ static PairArgs pair_args(const ks_lines* l, const ks_atmos* atm, const ks_grid*
     p.n_ion = atm->n_ion;
     p.n_elem = atm->n_elem;
     p.cutoff = opt ? opt->cutoff : 1e-3;
+    p.cutoff_f = (float)p.cutoff;
     p.gp = w.gp;
     p.wavelength = l->wavelength;
     p.gf = l->gf;
@@ -775,6 +786,7 @@ static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g
     a.class_pos = w.class_pos;
     a.class_off = w.class_off;
     a.tile_rng = w.tile_rng;
+    a.freq_f = w.freq_f;
     a.depth = w.depth;
     a.h0d = t.h0d;
     a.h1d = t.h1d;
@@ -1069,6 +1081,20 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
                                   (size_t)(w.stride - lines->n_lines), (size_t)L, s));
     PrepArgs pa = prep_args(atm, opt, w);
     ContArgs ca = cont_args(atm, grid);
+    if constexpr (!fp64) {
+        // the prep kernel converts the continuum tables once; the continuum
+        // kernel then reads them in FP32 and leaves c/lambda for the
+        // accumulation epilogue
+        const int64_t nc = (int64_t)L * (atm->n_edge - 1) * 3;
+        pa.n_coeff = nc;
+        pa.abs_coeff = atm->cont_abs_coeff;
+        pa.scat_coeff = atm->cont_scat_coeff;
+        pa.abs_coeff_f = w.coef_f;
+        pa.scat_coeff_f = w.coef_f + (size_t)L * (MAX_EDGES - 1) * 3;
+        ca.abs_coeff_f = pa.abs_coeff_f;
+        ca.scat_coeff_f = pa.scat_coeff_f;
+        ca.freq_f = w.freq_f;
+    }
     R* cabs = (R*)w.cont_abs;
     R* cscat = (R*)w.cont_scat;
     if ((st = run_bins(lines, grid, w, !fp64, s))) return st;

@@ -19,6 +19,7 @@ constexpr int VOIGT_N = 2001;               // H0/H1/H2TAB length, step 1/200
 constexpr int EXP_N = 1001;                 // EXTAB/EXTABF length
 constexpr int NXTAU = 51;                   // JOSH optical-depth grid
 constexpr int MAX_LAYERS = 128;             // per-wavelength column bound
+constexpr int MAX_EDGES = 1024;             // continuum edges (the reference's tables have 341)
 constexpr int N_REACH_CLASSES = 22;         // reach classes 0..21 (2^20 > MAXPROF)
 constexpr int LONG_CLASS = 8;               // default: classes 8+ (reach > 128 bins) in batches of 8 pairs
 constexpr int SHORT_CLASS = 7;              // default: classes 0-6 (reach <= 64 bins) one lane per pair

@@ -51,12 +51,18 @@ struct PrepArgs {
     const GridPar *gp;
     DepthPar *depth;
     IonPar *ion;
+    // single-precision copies of the continuum coefficient tables (optional)
+    int64_t n_coeff;
+    const double *abs_coeff, *scat_coeff;
+    float *abs_coeff_f, *scat_coeff_f;
 };
 
 struct ContArgs {
     int n_layers, n_edge, coeff_log10;
     int64_t n;
     const double *grid, *wledge, *half_edge, *delta_edge, *abs_coeff, *scat_coeff;
+    const float *abs_coeff_f, *scat_coeff_f;  // FP32 path: the same tables in single precision
+    float *freq_f;                            // optional out: c / lambda per grid point, FP32
 };
 
 struct LineBinArgs {
@@ -74,6 +80,7 @@ struct PairArgs {
     int64_t n_lines, n_wl, stride;
     int n_layers, n_ion, n_elem;
     double cutoff;
+    float cutoff_f;  // the same in single precision (mixed path)
     const GridPar *gp;
     const double *wavelength, *gf, *cgf, *gamma_rad, *gamma_stark, *gamma_vdw, *elo_cm;
     const int32_t *element_idx, *ion_stage, *line_type;
@@ -105,6 +112,7 @@ struct AccArgs {
     const int32_t *class_pos;   // per depth, per class: line positions, ascending
     const int64_t *class_off;   // [L][N_REACH_CLASSES + 1] absolute offsets into class_pos
     const int2 *tile_rng;       // [L][tiles][N_REACH_CLASSES] contributing range within each class
+    const float *freq_f;        // c / lambda per grid point (FP32 path)
     const DepthPar *depth;
     const double *h0d, *h1d, *h2d;
     const float *h0f, *h1f, *h2f;

@@ -31,6 +31,13 @@ template <typename R>
 __global__ void prep_depth_kernel(PrepArgs a) {
     int64_t per_depth = (int64_t)a.n_ion * a.n_elem;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.abs_coeff_f) {
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t k = i; k < a.n_coeff; k += stride) {
+            a.abs_coeff_f[k] = (float)a.abs_coeff[k];
+            a.scat_coeff_f[k] = (float)a.scat_coeff[k];
+        }
+    }
     if (i >= (int64_t)a.n_layers * per_depth) return;
     int d = (int)(i / per_depth);
     double temp_raw = a.temperature[d];
@@ -109,6 +116,7 @@ __global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __rest
     double c1 = (w - half) * (w - right) / delta;
     double c2 = (left - w) * (w - right) * 2.0 / delta;
     double c3 = (w - left) * (w - half) / delta;
+    if (a.freq_f) a.freq_f[j] = (float)(C_LIGHT_NM / w);
     const int nseg = a.n_edge - 1;
     for (int d = 0; d < a.n_layers; d++) {
         const double* ca = a.abs_coeff + ((int64_t)d * nseg + e) * 3;
@@ -119,8 +127,15 @@ __global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __rest
             ls = (R)(cs[0] * c1 + cs[1] * c2 + cs[2] * c3);
         } else {
             float fc1 = (float)c1, fc2 = (float)c2, fc3 = (float)c3;
-            la = (R)((float)ca[0] * fc1 + (float)ca[1] * fc2 + (float)ca[2] * fc3);
-            ls = (R)((float)cs[0] * fc1 + (float)cs[1] * fc2 + (float)cs[2] * fc3);
+            if (a.abs_coeff_f) {  // tables already in single precision
+                const float* fa = a.abs_coeff_f + ((int64_t)d * nseg + e) * 3;
+                const float* fs = a.scat_coeff_f + ((int64_t)d * nseg + e) * 3;
+                la = (R)(fa[0] * fc1 + fa[1] * fc2 + fa[2] * fc3);
+                ls = (R)(fs[0] * fc1 + fs[1] * fc2 + fs[2] * fc3);
+            } else {
+                la = (R)((float)ca[0] * fc1 + (float)ca[1] * fc2 + (float)ca[2] * fc3);
+                ls = (R)((float)cs[0] * fc1 + (float)cs[1] * fc2 + (float)cs[2] * fc3);
+            }
         }
         if (a.coeff_log10) {
             la = la > R(38) ? R(38) : la;
@@ -135,8 +150,8 @@ __global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __rest
             const R mx = (R)MAX_OPACITY_REAL4;
             la = la < R(0) ? R(0) : (la > mx ? mx : la);
             ls = ls < R(0) ? R(0) : (ls > mx ? mx : ls);
-            if (!isfinite((double)la)) la = mx;
-            if (!isfinite((double)ls)) ls = mx;
+            if (!isfinite(la)) la = mx;
+            if (!isfinite(ls)) ls = mx;
         }
         cont_abs[(int64_t)d * a.n + j] = la;
         cont_scat[(int64_t)d * a.n + j] = ls;
@@ -291,7 +306,7 @@ __device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict
                 }
             } else {
                 const LineF lf = a.linef[li];
-                float kapmin = (float)kap_at(c_ctr) * (float)a.cutoff;
+                float kapmin = (float)kap_at(c_ctr) * a.cutoff_f;
                 float k0pre = (lt == 1) ? lf.gw * lf.gf * q.pop_over_rho_f : lf.cgf * q.xnfdop_f;
                 if (k0pre >= kapmin) {
                     float boltz = fast_ex_mixed(lf.elo_hi, lf.elo_lo, dp.hckt_hi, dp.hckt_lo,
@@ -414,7 +429,7 @@ __device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restric
             atomicOr(a.flags, FLAG_N10DOP_RANGE);
             return;
         }
-        const R kapmin_ref = kap_at(c_wing) * (R)a.cutoff;
+        const R kapmin_ref = kap_at(c_wing) * (F32 ? (R)a.cutoff_f : (R)a.cutoff);
         const R* h0 = F32 ? (const R*)a.h0f : (const R*)a.h0d;
         const R* h1 = F32 ? (const R*)a.h1f : (const R*)a.h1d;
         const R* h2 = F32 ? (const R*)a.h2f : (const R*)a.h2d;
@@ -577,6 +592,20 @@ __device__ __forceinline__ void wing_run(CellT* my, int base, int sgn, int lo, i
             v = near_profile_tab<R, R2>(o, dv, tabstep, ad, k0, h01, h0g, h1g, h2g);
         }
         cell_add(my, base + sgn * o, v);
+    }
+}
+
+// Near wings on both sides at once, offsets [1, m] (both sides inside the
+// tile): one profile value per offset, added to bins base + o and base - o.
+// Each bin receives the same single addition as with two one-sided runs.
+template <typename R, typename R2, typename CellT>
+__device__ __forceinline__ void near_both(CellT* my, int base, int m, int lane, R k0, R ad, R dv,
+                                          R tabstep, const R2* h01, const R* h0g, const R* h1g,
+                                          const R* h2g) {
+    for (int o = 1 + lane; o <= m; o += 32) {
+        const R v = near_profile_tab<R, R2>(o, dv, tabstep, ad, k0, h01, h0g, h1g, h2g);
+        cell_add(my, base + o, v);
+        cell_add(my, base - o, v);
     }
 }
 
@@ -868,9 +897,16 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
                 const int base = ci - T0;
                 // red: bins base + o; blue: bins base - o
                 if constexpr (sizeof(R) == 4) {
-                    // near runs are short: one bin per lane; far runs: bin pairs
-                    wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
-                    wing_run<R, R2, CellT, false>(my, base, -1, bl, min(bh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    // near wings: both sides together where both are in the tile,
+                    // one bin per lane; far wings: bin pairs / quads
+                    const int nr = min(rh, nzi), nb = min(bh, nzi);
+                    int m = 0;
+                    if (rl == 1 && bl == 1) {
+                        m = min(nr, nb);
+                        near_both<R, R2, CellT>(my, base, m, lane, k0i, adi, dvi, ts, h01, gh0, gh1, gh2);
+                    }
+                    wing_run<R, R2, CellT, false>(my, base, 1, max(rl, m + 1), nr, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
+                    wing_run<R, R2, CellT, false>(my, base, -1, max(bl, m + 1), nb, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                     if (nzi != 0x7fffffff) {
                         far_run_x2(my, base, 1, max(rl, nzi + 1), rh, lane, xfi);
                         far_run_x2(my, base, -1, max(bl, nzi + 1), bh, lane, xfi);
@@ -902,7 +938,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
             for (int w = 0; w < nwarps; w++) {
                 kahan_add(s, cp, acc[w * W + b]);
             }
-            float freq = (float)(C_LIGHT_NM / a.grid[T0 + b]);
+            const float freq = a.freq_f[T0 + b];
             float stim = -expm1f(-freq * (float)dp.hkt_asynth);
             v = s * stim;
         } else {
