@@ -47,6 +47,8 @@ BENCH_WORKLOADS = {
     "window_500_510": dict(atm="atm_t5800g444.npz", sample=[(500.0, 510.0)]),
     "dense_10m": dict(atm="atm_t2500gm10.npz", sample=_SAMPLE_10NM),
 }
+# Batched workload: 256 jobs (atmosphere, window) over the full_300_1800 line list
+BATCH_JOBS, BATCH_SEED = 256, 304
 
 
 def workload_spec(name: str) -> dict:
@@ -468,6 +470,142 @@ def run_ours(args):
     return 0
 
 
+def batch_jobs(n_atm: int):
+    from kurucz_py_joss_submission_gb300.batch import Job
+
+    rng = np.random.default_rng(BATCH_SEED)
+    jobs = []
+    for _ in range(BATCH_JOBS):
+        a = int(rng.integers(n_atm))
+        width = float(rng.uniform(1.0, 50.0))
+        start = float(rng.uniform(300.0, 1800.0 - width))
+        jobs.append(Job(a, start, start + width))
+    return jobs
+
+
+def run_batch(args):
+    """256 syntheses (uneven layer counts and windows, shared 1.5M lines) as
+    one captured CUDA graph per step; spectra/s and evaluations/s."""
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from kurucz_py_joss_submission_gb300 import autotune
+    from kurucz_py_joss_submission_gb300.batch import BatchSynthesizer
+    from kurucz_py_joss_submission_gb300.device import DeviceCatalog
+    from kurucz_py_joss_submission_gb300.io import atmosphere as atm_io
+    from kurucz_py_joss_submission_gb300.io.lines import atomic
+
+    global WORKLOAD
+    WORKLOAD = workload_spec("full_300_1800")
+    cat = atomic.load_catalog_window(workload_catalog_path(), 300.0, 1800.0, sort=True)
+    man = json.loads((ROOT / "tests" / "golden" / "batch_atmospheres.json").read_text())
+    atms = [atm_io.load_cached(ROOT / "tests" / "golden" / k["file"]) for k in man["kept"]]
+    jobs_all = batch_jobs(len(atms))
+    jobs = jobs_all[rank::world]          # jobs are independent: shard them across ranks
+    dcat = DeviceCatalog(cat, dev)
+    probe = BatchSynthesizer(dcat, atms, jobs, precision=args.precision, device=dev)
+    tuned = autotune.tune(probe)
+    del probe
+    bs = BatchSynthesizer(dcat, atms, jobs, precision=args.precision, tuned=tuned, device=dev)
+    evals = bs.evaluations()
+    bs.capture()
+    for _ in range(args.warmup):
+        bs.replay()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            bs.replay()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    tot = torch.tensor([ms, float(evals), float(len(jobs))], dtype=torch.float64, device=dev)
+    if world > 1:
+        mx = tot[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot)
+        ms, evals = float(mx.item()), int(tot[1].item())
+    ms_step = ms / args.steps
+    # end to end: pinned host copies of the shared lines, atmospheres and grids in, fluxes out
+    host, h2d = [], 0
+    dev_in = list(dcat.t.values()) + [t for a in bs.atm for t in a.t.values()] + [g.wavelength for g in bs.grids]
+    for t in dev_in:
+        hp = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        hp.copy_(t.cpu())
+        host.append((hp, t))
+        h2d += hp.numel() * hp.element_size()
+    outs = [(torch.empty(f.numel(), dtype=torch.float64, pin_memory=True), f) for f in bs.flux_total + bs.flux_cont]
+    d2h = sum(o.numel() * 8 for o, _ in outs)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(e2e_steps):
+        for hp, t in host:
+            t.copy_(hp, non_blocking=True)
+        bs.replay()
+        for o, f in outs:
+            o.copy_(f, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    line = None
+    if rank == 0:
+        err = None
+        if args.precision != "fp64" and not args.skip_fp64_check:
+            ref = BatchSynthesizer(dcat, atms, jobs, precision="fp64", device=dev)
+            ref.run()
+            torch.cuda.synchronize()
+            per = []
+            cmax = 0.0
+            for i in range(len(jobs)):
+                ft, fc = bs.flux_total[i].cpu().numpy(), bs.flux_cont[i].cpu().numpy()
+                rt, rc = ref.flux_total[i].cpu().numpy(), ref.flux_cont[i].cpu().numpy()
+                per.append(float(np.max(np.abs(ft / fc - rt / rc))))
+                cmax = max(cmax, float(np.max(np.abs(fc / rc - 1.0))))
+            err = {"norm_flux_max_abs_worst_spectrum": max(per), "norm_flux_max_abs_median_spectrum":
+                   float(np.median(per)), "cont_flux_max_rel": cmax, "spectra_checked": len(per)}
+            del ref
+        npts = [g.n for g in bs.grids]
+        line = {
+            "metric": "spectra/s (batched: 256 atmospheres x windows, one CUDA graph per step)",
+            "value": len(jobs_all) * args.steps / (ms / 1e3), "unit": "spectra/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+            "dtype": "fp32" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": "batch_256", "jobs": len(jobs_all), "atmospheres": len(atms),
+                       "layers": sorted({a.layers for a in atms}), "grid_points_min": int(min(npts)),
+                       "grid_points_max": int(max(npts)), "grid_points_total": int(sum(npts)),
+                       "n_lines_shared": len(cat), "tuned": {str(k): v for k, v in tuned.items()},
+                       "streams": bs.n_streams, "precision": args.precision,
+                       "l2": "inputs larger than L2 (shared lines 111 MB + per-job descriptors)",
+                       "parallelism": "1 GPU" if world == 1 else f"{world} GPUs, jobs split across ranks"},
+            "evaluations_per_s": evals * args.steps / (ms / 1e3),
+            "evaluations_per_step": evals,
+            "accuracy_vs_fp64": err,
+            "e2e": {"value": len(jobs_all) / (e2e_ms / 1e3), "unit": "spectra/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "clocks": clk.summary(),
+            "roofline": None,
+            "cpu_baseline": None,
+        }
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -481,11 +619,16 @@ def main():
     ap.add_argument("--skip-fp64-check", action="store_true")
     ap.add_argument("--window", type=float, nargs=2, default=None,
                     help="restrict the workload to a wavelength window (small profiling case)")
-    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS), default="full_300_1800",
+    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS) + ["batch_256"], default="full_300_1800",
                     help="full_300_1800 (headline: 1.5M lines, Teff 5800 K), window_500_510 (20k lines, "
                          "the CPU-runnable reference case), dense_10m (10M lines, Teff 2500 K, log g -1)")
     args = ap.parse_args()
     global WORKLOAD
+    if args.workload == "batch_256":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "batched workload: timed on the GPU path only"}))
+            return 0
+        return run_batch(args)
     WORKLOAD = workload_spec(args.workload)
     if args.impl == "reference":
         return run_reference(args)

@@ -189,8 +189,11 @@ def format_atm(atm: GreyAtmosphere, metallicity: float = 0.0) -> str:
 
 
 def grey_atmosphere_atm(path: Path, teff: float, logg: float, metallicity: float = 0.0,
-                        vturb_kms: float = 2.0) -> GreyAtmosphere:
-    atm = grey_atmosphere(teff, logg, vturb_kms=vturb_kms, metallicity=metallicity)
+                        vturb_kms: float = 2.0, n_layers: int = 72) -> GreyAtmosphere:
+    """Write the ``.atm`` of a grey model with ``n_layers`` layers spread evenly
+    in log tau over [-6.875, 2.0] (72 layers: the 0.125 step)."""
+    step = (2.0 - (-6.875)) / (n_layers - 1)
+    atm = grey_atmosphere(teff, logg, step=step, vturb_kms=vturb_kms, metallicity=metallicity)
     Path(path).write_text(format_atm(atm, metallicity))
     return atm
 
