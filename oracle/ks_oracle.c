@@ -767,8 +767,8 @@ static double solve_josh(const josh_tables_t *T, int n, const double *acont,
                          const double *scont, const double *aline, const double *sline,
                          const double *sigmac, const double *sigmal, const double *rho,
                          int *iters_out) {
-    double abtot[256], alpha[256], snubar[256], taunu[256];
-    if (n == 0) return 0.0;
+    double abtot[256] = {0}, alpha[256] = {0}, snubar[256] = {0}, taunu[256] = {0};
+    if (n <= 0 || n > 256) return 0.0;
     for (int j = 0; j < n; j++) {
         double ab = acont[j] + aline[j] + sigmac[j] + sigmal[j];
         abtot[j] = ab > EPS ? ab : EPS;
@@ -780,7 +780,7 @@ static double solve_josh(const josh_tables_t *T, int n, const double *acont,
         snubar[j] = den > 0 ? (acont[j] * scont[j] + aline[j] * sline[j]) / den : scont[j];
     }
     int rev = n > 1 && rho[0] > rho[n - 1];
-    double rhoi[256], abi[256];
+    double rhoi[256] = {0}, abi[256] = {0};
     double start;
     for (int j = 0; j < n; j++) {
         rhoi[j] = rev ? rho[n - 1 - j] : rho[j];
