@@ -117,6 +117,9 @@ typedef struct {
                                take go to the per-column kernel), 1 = per-column kernel only */
     int32_t long_class;     /* reach classes >= long_class are dealt to the accumulation warps in
                                batches of 8 pairs instead of 32; 0 = default (8) */
+    int32_t exact_sweeps;   /* FP64 precision only: 1 = solve the JOSH Gauss-Seidel system in FP64
+                               to 1e-13 instead of the reference's FP32 sweep at 1e-5 (the
+                               forward of the differentiable form, smooth in the inputs) */
 } ks_options;
 
 /* Counters of one synthesis (filled when a pointer is given). */
@@ -252,6 +255,24 @@ ks_status ks_transfer_opacity(const ks_atmos *atm, const ks_grid *grid, const ks
                               const void *cont_abs, const void *cont_scat, const void *asynth,
                               double *flux_total, double *flux_cont, ks_stats *stats,
                               void *stream);
+
+/* The differentiable form: the FP64 fused synthesis (precision must be
+ * KS_PREC_FP64; the JOSH system is solved in FP64 to 1e-13 so the fluxes are
+ * smooth in the inputs), then hand-written adjoints of the transfer and of
+ * the line accumulation.  g_flux_total (device, double, [n]) is
+ * dLoss/dF_total of the caller's loss (F_nu; the continuum flux does not
+ * depend on the lines); the outputs are dLoss/dlog10(gf) and
+ * dLoss/dlog10(gamma_rad, gamma_stark, gamma_vdw) per line (device, double,
+ * [n_lines], sorted order).  The TRANSP gates and the wing reach are held
+ * fixed (they are step functions of the parameters).  Wavelengths that take
+ * the MAXJ = 1 branch contribute no gradient; their count is returned in
+ * stats->maxj_wavelengths.  Not covered: line scattering (rhoxj > 0),
+ * microturbulence.  No counterpart in the reference (it has no gradients). */
+ks_status ks_synthesize_adjoint(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                                const ks_options *opt, void *workspace, size_t workspace_bytes,
+                                const double *g_flux_total, double *flux_total, double *flux_cont,
+                                double *d_log_gf, double *d_log_gamma_rad, double *d_log_gamma_stark,
+                                double *d_log_gamma_vdw, ks_stats *stats, void *stream);
 
 /* The fused synthesis of ks_synthesize for callers that cannot allocate
  * device memory: a plug-in running inside a host application that owns all

@@ -69,7 +69,7 @@ class KsOptions(C.Structure):
     _fields_ = [
         ("cutoff", C.c_double), ("microturb_kms", C.c_double), ("rhoxj", C.c_double),
         ("precision", C.c_int32), ("tile_bins", C.c_int32), ("warps_per_tile", C.c_int32),
-        ("profile", C.c_int32), ("short_class", C.c_int32), ("transfer_path", C.c_int32), ("long_class", C.c_int32),
+        ("profile", C.c_int32), ("short_class", C.c_int32), ("transfer_path", C.c_int32), ("long_class", C.c_int32), ("exact_sweeps", C.c_int32),
     ]
 
 
@@ -115,6 +115,9 @@ SIGNATURES = {
                                C.POINTER(KsOptions), P, C.c_size_t, P, P, P, C.POINTER(KsStats), P]),
     "ks_transfer_opacity": (C.c_int32, [C.POINTER(KsAtmos), C.POINTER(KsGrid), C.POINTER(KsOptions),
                                         P, P, P, P, P, C.POINTER(KsStats), P]),
+    "ks_synthesize_adjoint": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
+                                          C.POINTER(KsOptions), P, C.c_size_t, P, P, P, P, P, P, P,
+                                          C.POINTER(KsStats), P]),
     "ks_synthesize_noalloc": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                           C.POINTER(KsOptions), P, P, P, P]),
     "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,

@@ -57,6 +57,7 @@ __device__ double g_extab[EXP_N], g_extabf[EXP_N];
 __device__ float g_extab_f[EXP_N], g_extabf_f[EXP_N];
 __device__ double g_xtau[NXTAU], g_ch[NXTAU];
 __device__ float g_coefj32[NXTAU * NXTAU];
+__device__ double g_coefj64[NXTAU * NXTAU];
 
 struct HostTables {
     bool ready = false;
@@ -69,6 +70,7 @@ static std::mutex g_tables_mu;
 struct DevTables {
     const double *h0d, *h1d, *h2d, *extab, *extabf, *xtau, *ch;
     const float *h0f, *h1f, *h2f, *extab_f, *extabf_f, *coefj32;
+    const double *coefj64;
 };
 static const int kMaxDevices = 64;
 static bool g_dev_ready[kMaxDevices];
@@ -239,6 +241,7 @@ static ks_status device_tables(DevTables* out) {
         KS_CUDA(cudaMemcpyToSymbol(g_xtau, t.xtau.data(), sizeof(double) * NXTAU));
         KS_CUDA(cudaMemcpyToSymbol(g_ch, t.ch.data(), sizeof(double) * NXTAU));
         KS_CUDA(cudaMemcpyToSymbol(g_coefj32, t.cj.c, sizeof(float) * NXTAU * NXTAU));
+        KS_CUDA(cudaMemcpyToSymbol(g_coefj64, t.coefj.data(), sizeof(double) * NXTAU * NXTAU));
         DevTables d;
         const void* p;
         KS_CUDA(sym_addr(g_h0d, &p)); d.h0d = (const double*)p;
@@ -254,6 +257,7 @@ static ks_status device_tables(DevTables* out) {
         KS_CUDA(sym_addr(g_xtau, &p)); d.xtau = (const double*)p;
         KS_CUDA(sym_addr(g_ch, &p)); d.ch = (const double*)p;
         KS_CUDA(sym_addr(g_coefj32, &p)); d.coefj32 = (const float*)p;
+        KS_CUDA(sym_addr(g_coefj64, &p)); d.coefj64 = (const double*)p;
         g_dev[dev] = d;
         g_dev_ready[dev] = true;
     }
@@ -813,6 +817,7 @@ static TransferArgs transfer_args(const ks_atmos* atm, const ks_grid* g, const W
     a.xtau = t.xtau;
     a.ch = t.ch;
     a.coefj32 = t.coefj32;
+    a.coefj64 = nullptr;
     a.flux_total = ft;
     a.flux_cont = fc;
     a.iters = w.iters;
@@ -1047,6 +1052,7 @@ static ks_status run_transfer(const ks_atmos* atm, const ks_grid* grid, const ks
     constexpr bool fp64 = sizeof(R) == 8;
     TransferArgs ta = transfer_args(atm, grid, w, t, flux_total, flux_cont, true, fp64);
     ta.line_scat = (opt && opt->rhoxj > 0.0) ? 1 : 0;
+    if (fp64 && opt && opt->exact_sweeps) ta.coefj64 = t.coefj64;
     if constexpr (fp64)
         KS_CUDA(launch_transfer_f64(ta, &g_tables.cj, cabs, cscat, asynth, nullptr, nullptr, s));
     else if (opt && opt->transfer_path == 1)
@@ -1275,6 +1281,123 @@ extern "C" ks_status ks_transfer_opacity(const ks_atmos* atm, const ks_grid* gri
     }
     cudaFreeAsync(buf, s);
     return st;
+}
+
+// ---------------------------------------------------------------------------
+// gradients (the differentiable form)
+// ---------------------------------------------------------------------------
+
+// The FP64 fused synthesis with the JOSH system solved to 1e-13, then the
+// adjoints of the transfer and of the accumulation for a loss whose
+// derivative with respect to F_total is g_flux_total: gradients with respect
+// to log10 gf and the three log10 damping constants of every line.
+extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                                           const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                           const double* g_flux_total, double* flux_total, double* flux_cont,
+                                           double* d_log_gf, double* d_log_gamma_rad, double* d_log_gamma_stark,
+                                           double* d_log_gamma_vdw, ks_stats* stats, void* stream) {
+    ks_status st = check_atmos(atm);
+    if (!st) st = check_grid(grid);
+    if (!st) st = check_lines(lines);
+    if (!st) st = check_cont(atm);
+    if (st) return st;
+    if (!opt || opt->precision != KS_PREC_FP64)
+        return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: options with precision KS_PREC_FP64 are required");
+    if (opt->rhoxj > 0.0 || opt->microturb_kms > 0.0)
+        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: line scattering and microturbulence are not covered");
+    if (!g_flux_total || !flux_total || !flux_cont || !d_log_gf || !d_log_gamma_rad || !d_log_gamma_stark ||
+        !d_log_gamma_vdw)
+        return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: NULL input/output");
+    if ((st = check_tiling(opt))) return st;
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    ks_options o = *opt;
+    o.exact_sweeps = 1;
+    o.profile = 0;
+    const int L = atm->n_layers;
+    Carve dry{nullptr, 0, 0, true};
+    Workspace w;
+    layout(dry, w, lines->n_lines, L, grid->n, atm->n_ion, atm->n_elem, true, true, true, default_tile(&o, true));
+    if (!workspace || workspace_bytes < dry.used)
+        return fail(KS_ERR_NOMEM, "ks_synthesize_adjoint: workspace too small (see ks_workspace_size, FP64)");
+    Carve c{(char*)workspace, workspace_bytes, 0, false};
+    layout(c, w, lines->n_lines, L, grid->n, atm->n_ion, atm->n_elem, true, true, true, default_tile(&o, true));
+    StageTimer tm;
+    st = synthesize_impl<double>(lines, atm, grid, &o, w, t, flux_total, flux_cont, (double*)w.asynth, s, tm);
+    if (st) return st;
+    // adjoint scratch
+    const size_t n_asy = (size_t)L * grid->n, n_slot = (size_t)L * w.stride;
+    char* buf = nullptr;
+    const size_t bytes = sizeof(double) * (n_asy + 2 * n_slot) + 256;
+    KS_CUDA(cudaMallocAsync((void**)&buf, bytes, s));
+    double* g_asy = (double*)buf;
+    double* g_gf = g_asy + n_asy;
+    double* g_a = g_gf + n_slot;
+    unsigned long long* skipped = w.counters + 3;
+    AdjArgs aa;
+    aa.n = grid->n;
+    aa.n_layers = L;
+    aa.grid = grid->wavelength;
+    aa.depth = w.depth;
+    aa.xtau = t.xtau;
+    aa.ch = t.ch;
+    aa.coefj64 = t.coefj64;
+    aa.cont_abs = (const double*)w.cont_abs;
+    aa.cont_scat = (const double*)w.cont_scat;
+    aa.asynth = (const double*)w.asynth;
+    aa.g_flux = g_flux_total;
+    aa.g_asy = g_asy;
+    aa.skipped = skipped;
+    LineAdjArgs la;
+    la.n_lines = lines->n_lines;
+    la.n_wl = grid->n;
+    la.stride = w.stride;
+    la.n_layers = L;
+    la.desc = (const PairDesc<double>*)w.desc;
+    la.cls = w.cls;
+    la.g_asy = g_asy;
+    la.h0 = t.h0d;
+    la.h1 = t.h1d;
+    la.h2 = t.h2d;
+    la.g_gf = g_gf;
+    la.g_a = g_a;
+    LineGradArgs lg;
+    lg.n_lines = lines->n_lines;
+    lg.stride = w.stride;
+    lg.n_layers = L;
+    lg.n_ion = atm->n_ion;
+    lg.n_elem = atm->n_elem;
+    lg.cls = w.cls;
+    lg.g_gf = g_gf;
+    lg.g_a = g_a;
+    lg.depth = w.depth;
+    lg.ion = w.ion;
+    lg.desc = (const PairDesc<double>*)w.desc;
+    lg.element_idx = lines->element_idx;
+    lg.ion_stage = lines->ion_stage;
+    lg.gamma_rad = lines->gamma_rad;
+    lg.gamma_stark = lines->gamma_stark;
+    lg.gamma_vdw = lines->gamma_vdw;
+    lg.d_loggf = d_log_gf;
+    lg.d_loggr = d_log_gamma_rad;
+    lg.d_loggs = d_log_gamma_stark;
+    lg.d_loggw = d_log_gamma_vdw;
+    cudaError_t e = launch_transfer_adjoint(aa, s);
+    if (e == cudaSuccess) e = launch_line_adjoint(la, s);
+    if (e == cudaSuccess) e = launch_line_grad(lg, s);
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return fail(KS_ERR_CUDA, cudaGetErrorString(e));
+    if (stats) {
+        st = collect_stats(w, grid->n, stats, s);
+        unsigned long long sk = 0;
+        KS_CUDA(cudaMemcpyAsync(&sk, skipped, sizeof(sk), cudaMemcpyDeviceToHost, s));
+        KS_CUDA(cudaStreamSynchronize(s));
+        stats->maxj_wavelengths = (int64_t)sk;  // columns given zero gradient (MAXJ = 1 or masked layers)
+        stats->kernel_launches = fused_launches(lines->n_lines > 0, true, &o, true) + 3;
+        return st;
+    }
+    return KS_OK;
 }
 
 // ---------------------------------------------------------------------------

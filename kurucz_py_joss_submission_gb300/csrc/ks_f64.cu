@@ -4,3 +4,28 @@
 #define KS_R double
 #define KS_SUF f64
 #include "ks_unit.inc"
+
+// adjoint kernels of the differentiable form (FP64 only)
+#include "ks_adjoint.cuh"
+
+namespace ks {
+
+cudaError_t launch_transfer_adjoint(const AdjArgs& a, cudaStream_t s) {
+    if (a.n == 0) return cudaSuccess;
+    transfer_adjoint_kernel<<<(unsigned)((a.n + 63) / 64), 64, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_line_adjoint(const LineAdjArgs& a, cudaStream_t s) {
+    if (a.n_lines == 0) return cudaSuccess;
+    line_adjoint_kernel<<<152 * 16, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_line_grad(const LineGradArgs& a, cudaStream_t s) {
+    if (a.n_lines == 0) return cudaSuccess;
+    line_grad_kernel<<<(unsigned)((a.n_lines + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace ks

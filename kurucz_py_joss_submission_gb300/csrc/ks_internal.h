@@ -129,8 +129,48 @@ struct TransferArgs {
     const DepthPar *depth;
     const double *xtau, *ch;
     const float *coefj32;
+    const double *coefj64;  // non-null: FP64 path solves Gauss-Seidel in FP64 to 1e-13 (differentiable form)
     double *flux_total, *flux_cont;
     int32_t *iters;
+};
+
+// Adjoint of the transfer (differentiable form, FP64).
+struct AdjArgs {
+    int64_t n;
+    int n_layers;
+    const double *grid;
+    const DepthPar *depth;
+    const double *xtau, *ch, *coefj64;
+    const double *cont_abs, *cont_scat, *asynth;  // [L, n]
+    const double *g_flux;                         // [n] dLoss/dF_total
+    double *g_asy;                                // [L, n] out: dLoss/dASYNTH * STIM
+    unsigned long long *skipped;                  // columns given zero
+};
+
+// Adjoint of the accumulation, per (line, depth) pair.
+struct LineAdjArgs {
+    int64_t n_lines, n_wl, stride;
+    int n_layers;
+    const PairDesc<double>* desc;
+    const uint8_t* cls;
+    const double* g_asy;  // [L, n] dLoss/dASYNTH * STIM
+    const double *h0, *h1, *h2;
+    double* g_gf;  // [L, stride] out: sum G c
+    double* g_a;   // [L, stride] out: sum G dc/da (wings, and the centre through KAPCEN)
+};
+
+// Per-line gradients from the per-pair sums.
+struct LineGradArgs {
+    int64_t n_lines, stride;
+    int n_layers, n_ion, n_elem;
+    const uint8_t* cls;
+    const double *g_gf, *g_a;
+    const DepthPar* depth;
+    const IonPar* ion;
+    const PairDesc<double>* desc;
+    const int32_t *element_idx, *ion_stage;
+    const double *gamma_rad, *gamma_stark, *gamma_vdw;
+    double *d_loggf, *d_loggr, *d_loggs, *d_loggw;  // [n_lines] out
 };
 
 }  // namespace ks

@@ -1217,7 +1217,7 @@ template <typename R, bool REF_SWEEP>
 __device__ double josh_flux(int n, const R* acont, const R* scont, const R* aline, const R* sline,
                             const R* sigmac, const R* sigmal, const R* rho, const R* xtau,
                             const double* ch, const CoefJ32& cj, const float* coefj_ref,
-                            int* iters_out) {
+                            int* iters_out, const double* coefj64 = nullptr) {
     R abtot[MAX_LAYERS], alpha[MAX_LAYERS], snubar[MAX_LAYERS], taunu[MAX_LAYERS];
     const R eps = (R)EPS38;
     for (int j = 0; j < n; j++) {
@@ -1276,6 +1276,39 @@ __device__ double josh_flux(int n, const R* acont, const R* scont, const R* alin
         xs32[l] = (float)xb;
         xa32[l] = (float)xa;
         xm32[l] = (float)(xb * (R(1) - xa));
+    }
+    if (sizeof(R) == 8 && coefj64) {
+        // Gauss-Seidel in FP64 to a tight tolerance: the converged solution of
+        // (I - diag(xa) C) xs = xb (1 - xa), smooth in the inputs
+        double xs[NXTAU], xa[NXTAU], xm[NXTAU];
+        for (int l = 0; l < NXTAU; l++) {
+            R xb = xsbar[l] > eps ? xsbar[l] : eps;
+            R xl = xalpha[l] < R(0) ? R(0) : (xalpha[l] > R(1) ? R(1) : xalpha[l]);
+            if (xtau[l] < taunu[0]) {
+                xb = s0;
+                xl = a0;
+            }
+            xs[l] = (double)xb;
+            xa[l] = (double)xl;
+            xm[l] = (double)(xb * (R(1) - xl));
+        }
+        int it = 0;
+        for (; it < 2000; it++) {
+            double dmax = 0.0;
+            for (int k = NXTAU - 1; k >= 0; k--) {
+                double sum = 0.0;
+                for (int q = 0; q < NXTAU; q++) sum += coefj64[k * NXTAU + q] * xs[q];
+                const double nv = sum * xa[k] + xm[k];
+                const double dl = fabs(nv - xs[k]) / fmax(fabs(nv), 1e-300);
+                dmax = dl > dmax ? dl : dmax;
+                xs[k] = nv;
+            }
+            if (dmax < 1e-13) break;
+        }
+        *iters_out = it + 1;
+        double flux = 0.0;
+        for (int l = 0; l < NXTAU; l++) flux += ch[l] * xs[l];
+        return flux;
     }
     int it;
     if (REF_SWEEP) it = josh_sweeps_ref(coefj_ref, xs32, xa32, xm32);
@@ -1405,9 +1438,9 @@ __device__ __forceinline__ void transfer_column(const TransferArgs& a, const Coe
     for (int l = 0; l < NXTAU; l++) xtau[l] = (R)a.xtau[l];
     int itc = 0, itt = 0;
     double fc = josh_flux<R, REF_SWEEP>(m, ca, pl, nullptr, nullptr, cs, nullptr, mass, xtau, a.ch, cj,
-                                        a.coefj32, &itc);
+                                        a.coefj32, &itc, a.coefj64);
     double ft = josh_flux<R, REF_SWEEP>(m, ca, pl, la, own_src ? src : pl, cs, has_ls ? ls : nullptr, mass,
-                                        xtau, a.ch, cj, a.coefj32, &itt);
+                                        xtau, a.ch, cj, a.coefj32, &itt, a.coefj64);
     a.flux_cont[j] = fc;
     a.flux_total[j] = ft;
     if (a.iters) {

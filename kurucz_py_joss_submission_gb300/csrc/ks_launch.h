@@ -36,4 +36,9 @@ struct CoefJ32 {
 KS_DECLARE_LAUNCHERS(float, f32)
 KS_DECLARE_LAUNCHERS(double, f64)
 
+// adjoint kernels (FP64 unit)
+cudaError_t launch_transfer_adjoint(const AdjArgs& a, cudaStream_t s);
+cudaError_t launch_line_adjoint(const LineAdjArgs& a, cudaStream_t s);
+cudaError_t launch_line_grad(const LineGradArgs& a, cudaStream_t s);
+
 }  // namespace ks

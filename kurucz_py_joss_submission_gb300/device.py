@@ -164,7 +164,7 @@ class DeviceCatalog:
 
 def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", tile_bins=0,
                  warps_per_tile=0, profile=False, short_class=0,
-                 transfer_path=0, long_class=0) -> _native.KsOptions:
+                 transfer_path=0, long_class=0, exact_sweeps=0) -> _native.KsOptions:
     opt = _native.KsOptions()
     opt.cutoff = float(cutoff)
     opt.microturb_kms = float(microturb_kms)
@@ -176,6 +176,7 @@ def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", t
     opt.short_class = int(short_class)
     opt.transfer_path = int(transfer_path)
     opt.long_class = int(long_class)
+    opt.exact_sweeps = int(exact_sweeps)
     return opt
 
 
