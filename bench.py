@@ -683,10 +683,12 @@ def run_diff(args):
             g_fd = (vals[0] - vals[1]) / (2 * h)
             g_ad = float(grads[par][i])
             scale = max(abs(g_fd), abs(g_ad))
-            if scale > 1e-14 * max(abs(float(loss.item())), 1e-300):
+            # compare where the central difference resolves the gradient:
+            # a loss change of at least 1e-11 of the loss over +-h
+            if scale * h > 1e-11 * max(abs(float(loss.item())), 1e-300):
                 errs[names[par]].append(abs(g_fd - g_ad) / scale)
         allerr = np.array([e for v in errs.values() for e in v])
-        fd = {"params_checked": 200, "params_with_nonzero_gradient": int(allerr.size), "h_dex": h,
+        fd = {"params_checked": 200, "params_resolved_by_fd": int(allerr.size), "h_dex": h,
               "rel_err_median": float(np.median(allerr)) if allerr.size else None,
               "rel_err_p90": float(np.percentile(allerr, 90)) if allerr.size else None,
               "frac_within_5pct": float(np.mean(allerr < 0.05)) if allerr.size else None,
