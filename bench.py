@@ -237,7 +237,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": res["evals_per_s"], "unit": "evals/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * res["seconds"] / max(1, args.steps), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD["name"],
                    "n_lines": WORKLOAD["n_lines"] + WORKLOAD.get("n_band_lines", 0),
                    "n_wavelengths": n_full, "n_layers": 72},

@@ -84,7 +84,7 @@ class BatchSynthesizer:
     """Fused syntheses of ``jobs`` over shared lines, on ``n_streams`` streams."""
 
     def __init__(self, catalog: DeviceCatalog, atmospheres: Sequence[AtmosphereModel], jobs: Sequence[Job],
-                 precision: str = "mixed", resolution: float = 300000.0, n_streams: int = 8,
+                 precision: str = "mixed", resolution: float = 300000.0, n_streams: int = 32,
                  tuned: Optional[Dict[int, dict]] = None, device="cuda"):
         host = catalog.host
         if np.any((np.abs(host.code - 1.0) < 1e-6) | np.isin(host.line_types, [-1, -2]) |
