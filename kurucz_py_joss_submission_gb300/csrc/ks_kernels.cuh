@@ -640,13 +640,17 @@ __device__ __forceinline__ void far_run_x4(float* my, int b_lo, int b_hi, int ba
     const int q0 = (b_lo + e_lo) >> 2, q1 = ((b_hi - e_hi + 1) >> 2) - 1;
     const float2 xf2 = make_float2(xf, xf);
     const float2 d2 = make_float2(2.0f * (float)sgn, 2.0f * (float)sgn);
-    for (int q = q0 + lane; q <= q1; q += 32) {
-        const int o0 = sgn * (4 * q - base);
-        const float2 oa = make_float2((float)o0, (float)(o0 + sgn));
+    // offsets as floats, stepped by 128 per iteration (exact: |o| < 2^24)
+    const int qs = q0 + lane;
+    const int o0s = sgn * (4 * qs - base);
+    float2 oa = make_float2((float)o0s, (float)(o0s + sgn));
+    const float2 step = make_float2(128.0f * (float)sgn, 128.0f * (float)sgn);
+    for (int q = qs; q <= q1; q += 32) {
         const float2 ob = __fadd2_rn(oa, d2);
         const float2 sa = __fmul2_rn(oa, oa), sb = __fmul2_rn(ob, ob);
         const float2 va = __fmul2_rn(xf2, make_float2(rcp_approx(sa.x), rcp_approx(sa.y)));
         const float2 vb = __fmul2_rn(xf2, make_float2(rcp_approx(sb.x), rcp_approx(sb.y)));
+        oa = __fadd2_rn(oa, step);
         float4 c = my4[q];
         const float2 ca = __fadd2_rn(make_float2(c.x, c.y), va);
         const float2 cb = __fadd2_rn(make_float2(c.z, c.w), vb);
@@ -672,11 +676,14 @@ __device__ __forceinline__ void far_run_x2(float* my, int base, int sgn, int lo,
     float2* my2 = reinterpret_cast<float2*>(my);
     const int j1 = (b_hi - 1) >> 1;
     const float2 xf2 = make_float2(xf, xf);
-    for (int j = ((b_lo + 1) >> 1) + lane; j <= j1; j += 32) {
-        const int o0 = sgn * (2 * j - base);
-        const float2 of = make_float2((float)o0, (float)(o0 + sgn));
+    const int js = ((b_lo + 1) >> 1) + lane;
+    const int o0s = sgn * (2 * js - base);
+    float2 of = make_float2((float)o0s, (float)(o0s + sgn));
+    const float2 step = make_float2(64.0f * (float)sgn, 64.0f * (float)sgn);
+    for (int j = js; j <= j1; j += 32) {
         const float2 oo = __fmul2_rn(of, of);
         my2[j] = __fadd2_rn(my2[j], __fmul2_rn(xf2, make_float2(rcp_approx(oo.x), rcp_approx(oo.y))));
+        of = __fadd2_rn(of, step);
     }
 }
 
