@@ -1,6 +1,6 @@
 /*
  * ks_oracle.c -- CPU restatement of the synthe_py line-opacity and transfer
- * path, used ONLY as test infrastructure: the parity checker for the CUDA
+ * path, used ONLY as test infrastructure: the parity reference for the CUDA
  * library and the timed CPU baseline ("port") in bench.py.  Nothing in the
  * product links or calls this file.
  *

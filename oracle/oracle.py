@@ -1,7 +1,7 @@
 """ctypes driver for the CPU oracle (``ks_oracle.c``) -- test infrastructure.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use this module, always as the checker or the timed CPU
+``bench.py`` use this module, always to verify results or as the timed CPU
 reference, never as part of the product.
 
 :func:`synthesize` follows the data flow of the reference driver
