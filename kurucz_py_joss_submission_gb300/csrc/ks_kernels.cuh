@@ -249,7 +249,7 @@ template <typename R, bool FUSED>
 __device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict__ kap_a,
                                           const R* __restrict__ kap_b, PairDesc<R>* __restrict__ desc,
                                           uint8_t* __restrict__ cls, int64_t li, int d, R& kc_out,
-                                          R& k0_out, int& code_out) {
+                                          R& k0_out, int& code_out, float& num_out, int& qi_out) {
     constexpr bool F32 = sizeof(R) == 4;
     const int L = a.n_layers;
     int64_t slot = (int64_t)d * a.stride + li;
@@ -263,7 +263,8 @@ __device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict
     const int lt = a.line_type[li];
     if (e < 0 || e >= a.n_elem || ion <= 0 || ion > a.n_ion) return false;
     const DepthPar& dp = a.depth[d];
-    const IonPar& q = a.ion[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
+    const int qi = (d * a.n_ion + (ion - 1)) * a.n_elem + e;
+    const IonPar& q = a.ion[qi];
     const int c_ctr = a.center_idx[li];
     const int c_wing = a.wing_idx[li];
     const int64_t nwl = a.n_wl;
@@ -275,6 +276,7 @@ __device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict
     };
 
     // ---------------- TRANSP (line_opacity.py:101-184) ----------------
+    float num = 0.0f;  // FP32: GAMRF + GAMSF*XNE + GAMWF*TXNXN, reused by the wings
     R kapcen = R(0);
     R kappa0_w = R(0);  // kappa0 for the wings
     bool valid = false;
@@ -313,7 +315,8 @@ __device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict
                                                 a.elo_cm[li], dp.hckt, a.extab_f, a.extabf_f);
                     float post = k0pre * boltz;
                     if (post >= kapmin && post > 0.0f) {
-                        float adamp = (lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f) / q.dop_f;
+                        num = lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f;
+                        float adamp = num / q.dop_f;
                         if (adamp >= 0.0f) {
                             float vc = (lt == 1) ? 1.0f
                                      : (adamp < 0.2f ? 1.0f - 1.128f * adamp
@@ -350,9 +353,15 @@ __device__ __forceinline__ bool pair_gate(const PairArgs& a, const R* __restrict
     const bool wings = (lt == 0) && (q.ok & 2) && wl_pos &&
                        c_wing >= -MAX_PROFILE_STEPS && c_wing <= nwl - 1 + MAX_PROFILE_STEPS;
     if (wings) {
+        if (F32 && !FUSED) {
+            const LineF lf = a.linef[li];
+            num = lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f;
+        }
         kc_out = kapcen;
         k0_out = kappa0_w;
         code_out = ctr_code;
+        num_out = num;
+        qi_out = qi;
         return true;
     }
     if (ctr_code != 0) {
@@ -378,13 +387,11 @@ template <typename R>
 __device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restrict__ kap_a,
                                            const R* __restrict__ kap_b, PairDesc<R>* __restrict__ desc,
                                            uint8_t* __restrict__ cls, int64_t li, int d, R kapcen,
-                                           R kappa0_w, int ctr_code) {
+                                           R kappa0_w, int ctr_code, float num, int qi) {
     constexpr bool F32 = sizeof(R) == 4;
     const int64_t slot = (int64_t)d * a.stride + li;
-    const int e = a.element_idx[li];
-    const int ion = a.ion_stage[li];
     const DepthPar& dp = a.depth[d];
-    const IonPar& q = a.ion[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
+    const IonPar& q = a.ion[qi];
     const int c_wing = a.wing_idx[li];
     const int64_t nwl = a.n_wl;
     auto kap_at = [&](int c) -> R {
@@ -418,8 +425,7 @@ __device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restric
             n10dop = (int)(int64_t)(10.0 * dopple * resolu);
             dvoigt = (R)(dopple > 0 ? 1.0 / (dopple * resolu) : 1.0);
         } else {
-            const LineF lf = a.linef[li];
-            float ad = __fdividef(lf.gr + lf.gs * dp.xne_f + lf.gw * dp.txnxn_f, q.dopw_f);
+            float ad = __fdividef(num, q.dopw_f);
             adamp = (R)(ad > 1e-12f ? ad : 1e-12f);
             kappa0 = kappa0_w;
             n10dop = q.n10dop;
@@ -455,20 +461,53 @@ __device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restric
             }
         }
         if (monotone && cut == -1 && ns <= n10dop) {
-            int lo = ns - 1, probe = ns, step = 1, hi = -1;
-            for (;;) {
-                const R p = near_profile<R>(probe, dvoigt, adamp, kappa0, h0, h1, h2);
-                if (p < kapmin_ref) {
-                    hi = probe;
-                    break;
+            // The search starts at the offset where kappa0 (exp(-v^2) +
+            // 0.5642 a / v^2) meets KAPMIN and gallops down or up from it;
+            // with the profile non-increasing on [ns, n10dop] it returns the
+            // first offset below KAPMIN whatever the start.
+            int g = n10dop;
+            const float r = (float)kapmin_ref / (float)kappa0;
+            if (r > 0.0f && r < 1.0f) {
+                const float v = fmaxf(sqrtf(-__logf(r)), sqrtf(0.5642f * (float)adamp / r));
+                const float og = v / (float)dvoigt;
+                if (og < (float)n10dop) g = max(ns, (int)og);
+            } else if (r >= 1.0f) {
+                g = ns;
+            }
+            int lo = ns - 1, hi = -1;
+            const R pg = near_profile<R>(g, dvoigt, adamp, kappa0, h0, h1, h2);
+            if (pg < kapmin_ref) {
+                hi = g;
+                int step = 1;
+                while (hi - lo > 1) {
+                    const int probe = max(hi - step, lo + 1);
+                    if (near_profile<R>(probe, dvoigt, adamp, kappa0, h0, h1, h2) < kapmin_ref) {
+                        hi = probe;
+                        step <<= 1;
+                    } else {
+                        lo = probe;
+                    }
+                    if (lo == probe) break;
                 }
-                lo = probe;
-                if (probe == n10dop) {
-                    prof_n10 = p;
-                    break;
+            } else if (g == n10dop) {
+                prof_n10 = pg;
+            } else {
+                lo = g;
+                int probe = g + 1, step = 1;
+                for (;;) {
+                    const R p = near_profile<R>(probe, dvoigt, adamp, kappa0, h0, h1, h2);
+                    if (p < kapmin_ref) {
+                        hi = probe;
+                        break;
+                    }
+                    lo = probe;
+                    if (probe == n10dop) {
+                        prof_n10 = p;
+                        break;
+                    }
+                    probe = min(probe + step, n10dop);
+                    step <<= 1;
                 }
-                probe = min(probe + step, n10dop);
-                step <<= 1;
             }
             if (hi > 0) {
                 while (hi - lo > 1) {
@@ -517,7 +556,8 @@ __global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __
                                                          PairDesc<R>* __restrict__ desc,
                                                          uint8_t* __restrict__ cls) {
     __shared__ int q_n;
-    __shared__ int q_li[128], q_code[128];
+    __shared__ int q_li[128], q_code[128], q_qi[128];
+    __shared__ float q_num[128];
     __shared__ R q_kc[128], q_k0[128];
     if (threadIdx.x == 0) q_n = 0;
     __syncthreads();
@@ -525,18 +565,22 @@ __global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __
     const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (li < a.n_lines) {
         R kc, k0;
-        int code;
-        if (pair_gate<R, FUSED>(a, kap_a, kap_b, desc, cls, li, d, kc, k0, code)) {
+        int code, qi;
+        float num;
+        if (pair_gate<R, FUSED>(a, kap_a, kap_b, desc, cls, li, d, kc, k0, code, num, qi)) {
             const int i = atomicAdd(&q_n, 1);
             q_li[i] = (int)li;
             q_kc[i] = kc;
             q_k0[i] = k0;
             q_code[i] = code;
+            q_num[i] = num;
+            q_qi[i] = qi;
         }
     }
     __syncthreads();
     const int i = threadIdx.x;
-    if (i < q_n) pair_wings<R>(a, kap_a, kap_b, desc, cls, q_li[i], d, q_kc[i], q_k0[i], q_code[i]);
+    if (i < q_n)
+        pair_wings<R>(a, kap_a, kap_b, desc, cls, q_li[i], d, q_kc[i], q_k0[i], q_code[i], q_num[i], q_qi[i]);
 }
 
 // ---------------------------------------------------------------------------
