@@ -207,6 +207,8 @@ def cpu_baseline(cat_path: Path, steps: int = 1):
                          nelem=c.element_idx + 1, ion_stage=c.ion_stages, line_type=c.line_types,
                          n_lower=np.zeros(len(c), np.int32), n_upper=np.zeros(len(c), np.int32),
                          line_size=np.zeros(len(c), np.int32)))
+    # every host core this process may run on (torchrun sets OMP_NUM_THREADS=1)
+    oracle.set_threads(len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count())
     threads = oracle.num_threads()
     tot_t, tot_e, tot_pts = 0.0, 0, 0
     rep = 0
