@@ -34,6 +34,11 @@ logger = logging.getLogger(__name__)
 C_LIGHT_NM_PER_S = 2.99792458e17
 
 
+def flux_nu_to_lambda(wavelength: np.ndarray, flux_hz: np.ndarray) -> np.ndarray:
+    """F_lambda = F_nu * c / lambda^2 with c in nm/s (opacity.py:3855-3861)."""
+    return flux_hz * (C_LIGHT_NM_PER_S / np.maximum(wavelength ** 2, 1e-40))
+
+
 def _build_wavelength_grid(cfg: SynthesisConfig) -> np.ndarray:
     """Geometric grid of opacity.py:526 (native: sequential multiplication)."""
     g = cfg.wavelength_grid
@@ -111,9 +116,8 @@ def run_synthesis(cfg: SynthesisConfig) -> SynthResult:
 
     flux_total_hz = syn.flux_total.cpu().numpy()
     flux_cont_hz = syn.flux_cont.cpu().numpy()
-    conversion = C_LIGHT_NM_PER_S / np.maximum(wavelength ** 2, 1e-40)
-    flux_total = flux_total_hz * conversion
-    flux_cont = flux_cont_hz * conversion
+    flux_total = flux_nu_to_lambda(wavelength, flux_total_hz)
+    flux_cont = flux_nu_to_lambda(wavelength, flux_cont_hz)
 
     dump_dir = os.environ.get("SYNTHE_PY_STAGE_DUMPS")
     if dump_dir:
