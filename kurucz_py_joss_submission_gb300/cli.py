@@ -19,27 +19,27 @@ from .engine.opacity import run_synthesis
 
 def build_parser() -> argparse.ArgumentParser:
     p = argparse.ArgumentParser(description="GB300 SYNTHE line-opacity and transfer synthesis")
-    p.add_argument("model", type=Path, help="Path to the model atmosphere file (.atm or .npz)")
-    p.add_argument("atomic", type=Path, help="Atomic line catalog (gfall format)")
-    p.add_argument("--npz", type=Path, default=None, help="Explicit .npz atmosphere path")
-    p.add_argument("--spec", type=Path, default=Path("spectrum.spec"), help="Output spectrum")
-    p.add_argument("--wl-start", type=float, default=300.0, help="Start wavelength (nm)")
-    p.add_argument("--wl-end", type=float, default=1800.0, help="End wavelength (nm)")
-    p.add_argument("--resolution", type=float, default=300_000.0, help="Resolving power")
-    p.add_argument("--no-vacuum", action="store_true", help="Treat wavelengths as air")
-    p.add_argument("--cutoff", type=float, default=1e-3, help="Opacity cutoff factor")
-    p.add_argument("--linout", type=int, default=30, help="Line output control flag")
+    p.add_argument("model", type=Path, help="model atmosphere: an ATLAS .atm deck or its converted .npz")
+    p.add_argument("atomic", type=Path, help="line list in gfall fixed-width format")
+    p.add_argument("--npz", type=Path, default=None, help="converted atmosphere to read instead of MODEL")
+    p.add_argument("--spec", type=Path, default=Path("spectrum.spec"), help="where to write the three-column .spec")
+    p.add_argument("--wl-start", type=float, default=300.0, help="first wavelength of the grid, nm")
+    p.add_argument("--wl-end", type=float, default=1800.0, help="last wavelength of the grid, nm")
+    p.add_argument("--resolution", type=float, default=300_000.0, help="lambda / delta-lambda of the log grid")
+    p.add_argument("--no-vacuum", action="store_true", help="line wavelengths are in air, not vacuum")
+    p.add_argument("--cutoff", type=float, default=1e-3, help="KAPMIN as a fraction of the continuum")
+    p.add_argument("--linout", type=int, default=30, help="LINOUT switch of SYNTHE")
     p.add_argument("--cache", type=Path, default=None, help="Line cache directory (unused)")
     p.add_argument("--allow-tfort-runtime", action="store_true", help="Accepted, unused")
     p.add_argument("--n-workers", type=int, default=None, help="Accepted, unused (GPU)")
     p.add_argument("--nlte", action="store_true", help="Accepted; LTE source only")
     p.add_argument("--scat-iterations", type=int, default=8)
     p.add_argument("--scat-tol", type=float, default=1e-3)
-    p.add_argument("--rhoxj", type=float, default=0.0, help="Scattering scale height RHOXJ")
+    p.add_argument("--rhoxj", type=float, default=0.0, help="RHOXJ of the line scattering fraction (0: none)")
     p.add_argument("--log-level", type=str, default="INFO",
                    choices=["DEBUG", "INFO", "WARNING", "ERROR"])
     p.add_argument("--diagnostics", type=Path, default=None)
-    p.add_argument("--microturb", type=float, default=0.0, help="Microturbulence (km/s)")
+    p.add_argument("--microturb", type=float, default=0.0, help="extra microturbulent velocity, km/s")
     p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     p.add_argument("--tile-bins", type=int, default=0)
     p.add_argument("--warps-per-tile", type=int, default=0)
@@ -60,7 +60,7 @@ def main(argv: Optional[list] = None) -> int:
     )
     cfg.log_level = args.log_level
     logging.basicConfig(level=getattr(logging, args.log_level),
-                        format="%(asctime)s %(levelname)s %(name)s: %(message)s")
+                        format="%(asctime)s [%(levelname)s] %(name)s - %(message)s")
     run_synthesis(cfg)
     return 0
 

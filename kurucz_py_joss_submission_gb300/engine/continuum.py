@@ -19,7 +19,7 @@ from ..device import DeviceAtmosphere, DeviceGrid, stream_handle
 def build_depth_continuum(atmosphere, wavelength_grid, precision: str = "fp64", device="cuda"):
     if (atmosphere.continuum_wledge is None or atmosphere.continuum_abs_coeff is None
             or atmosphere.continuum_scat_coeff is None):
-        raise ValueError("Continuum coefficients are missing from atmosphere model.")
+        raise ValueError("the atmosphere carries no continuum coefficient tables (edges, absorption, scattering)")
     lib = _native.load()
     datm = DeviceAtmosphere(atmosphere, device)
     dgrid = DeviceGrid(wavelength_grid, device=device)

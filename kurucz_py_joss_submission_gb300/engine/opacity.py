@@ -43,7 +43,7 @@ def _build_wavelength_grid(cfg: SynthesisConfig) -> np.ndarray:
     """Geometric grid of opacity.py:526 (native: sequential multiplication)."""
     g = cfg.wavelength_grid
     if g.resolution <= 0.0:
-        raise ValueError("Resolution must be positive for geometric wavelength grid")
+        raise ValueError("the log-lambda grid needs a resolving power above zero")
     L = _native.load()
     n = L.ks_wavelength_grid(g.start, g.end, g.resolution, None, 0)
     if n < 0:

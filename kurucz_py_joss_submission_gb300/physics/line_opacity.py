@@ -36,8 +36,8 @@ def compute_transp(
     """Line-centre opacity TRANSP[n_lines, L], valid mask and centre bins."""
     if continuum_absorption is None or wavelength_grid is None:
         raise ValueError(
-            "continuum_absorption and wavelength_grid are required for compute_transp. "
-            "Fortran always uses KAPMIN = CONTINUUM * CUTOFF with no fallback."
+            "compute_transp needs continuum_absorption and wavelength_grid: KAPMIN is the "
+            "continuum at each line centre times the cutoff, with nothing to fall back on"
         )
     if continuum_absorption_full is not None or wavelength_grid_full is not None:
         raise NotImplementedError("full-range KAPMIN tables are not used on the default path")
