@@ -4,6 +4,7 @@ config.  Runs on the CPU (the small 500-510 nm workload, about 10 s each)."""
 
 import json
 import os
+import socket
 import subprocess
 import sys
 from pathlib import Path
@@ -45,9 +46,16 @@ def test_reference_arm_single_process():
     _check_line(json.loads(lines[0]), 1)
 
 
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
 def test_reference_arm_under_torchrun_prints_once():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
-           "--master-addr", "127.0.0.1", "--master-port", "29533", "bench.py", "--gpus", "2", *ARGS]
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--gpus", "2",
+           *ARGS]
     out = subprocess.run(cmd, cwd=ROOT, env=_env(), capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
