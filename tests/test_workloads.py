@@ -28,3 +28,28 @@ def test_line_draw_distributions():
     assert d.log_gf.min() >= -8 and d.log_gf.max() <= 1
     assert abs(np.median(np.log(d.wavelength_nm)) - 0.5 * np.log(300 * 1800)) < 0.02
     assert set(np.unique(d.code)) <= set(workloads.SPECIES_CODES)
+
+
+def test_band_line_draw():
+    n = 120_000
+    d = workloads.random_band_lines(n, 300.0, 1800.0, seed=11)
+    assert d.wavelength_nm.size == n
+    assert np.all(np.diff(d.wavelength_nm) >= 0)
+    assert d.wavelength_nm.min() >= 300.0 and d.wavelength_nm.max() <= 1800.0
+    assert np.all(d.code == workloads.BAND_CODE)
+    assert d.log_gf.min() >= -8 and d.log_gf.max() <= 1
+    assert abs(np.mean(d.log_gf) + 4.0) < 0.02 and abs(np.std(d.log_gf) - 1.0) < 0.02
+    # E = B J (J + 1) with B in [0.3, 2] cm^-1 and J <= 150: J = 0 gives E = 0, the rest lie between
+    # 2 * 0.3 and 150 * 151 * 2
+    e = d.e_lower_cm
+    assert e.min() >= 0.0 and e.max() <= 2.0 * 150 * 151
+    assert np.all((e == 0.0) | (e >= 0.6 - 1e-12))
+    # same seed, same lines
+    again = workloads.random_band_lines(n, 300.0, 1800.0, seed=11)
+    assert np.array_equal(again.wavelength_nm, d.wavelength_nm) and np.array_equal(again.e_lower_cm, e)
+
+
+def test_dense_workload_composition():
+    w = workloads.WORKLOADS["dense_10m"]
+    assert w["n_lines"] + w["n_band_lines"] == 10_000_000
+    assert (w["teff"], w["logg"], w["wl_start"], w["wl_end"]) == (2500.0, -1.0, 300.0, 1800.0)
