@@ -16,7 +16,12 @@
  * Errors: every call returns KS_OK or an error code; ks_last_error() returns
  * the message of the last failure on the calling thread.  Numerical
  * problems inside the data (NaN/Inf opacities) are masked as the reference
- * masks them, not raised.
+ * masks them, not raised.  Internal limits that a kernel meets (a packed
+ * descriptor field overflowing, wing bins out of order) raise a device flag:
+ * a call given a ks_stats pointer returns KS_ERR_DEVICE for its own flags;
+ * every call also ORs its flags into a per-device sticky word, which
+ * ks_check_flags reads and clears, so calls without stats (and CUDA-graph
+ * replays of them) lose no error.
  *
  * Threading: calls are thread-safe; each call only touches the buffers and
  * stream it is given.
@@ -141,6 +146,15 @@ ks_status ks_version(int32_t *major, int32_t *minor);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *ks_last_error(void);
+
+/* Synchronises `stream` (the current device's stream), then takes and clears
+ * the device's sticky flag word: the OR of the internal-limit flags raised by
+ * every call on this device since the last ks_check_flags.  Returns
+ * KS_ERR_DEVICE (message names the limit) when it was nonzero; *flags_out
+ * (may be NULL) receives the word.  Call it after a batch of asynchronous
+ * calls or graph replays.  No reference counterpart: the reference raises
+ * Python exceptions synchronously. */
+ks_status ks_check_flags(void *stream, int32_t *flags_out);
 
 /* Builds the constant tables from the SYNTHE source tables (host memory):
  * the 81-point H1 Voigt table tabvi/tabh1 (synthe_py/physics/tables.py:249,
@@ -279,10 +293,14 @@ ks_status ks_synthesize_adjoint(const ks_lines *lines, const ks_atmos *atm, cons
  * device memory, or a runtime reached through an FFI with no CUDA allocator,
  * cannot hand over a workspace.  This entry point allocates nothing (no
  * cudaMalloc, no cudaFree, no allocating library routine): its scratch is a
- * fixed 64 MiB array inside the library, so sizes whose ks_workspace_size
- * exceeds 64 MiB are rejected with KS_ERR_NOMEM (on a 72-layer atmosphere
- * and a 6,000-point grid about 20,000 lines fit in KS_PREC_MIXED, 8,000 in
- * KS_PREC_FP64).  The caller still passes
+ * fixed 64 MiB array inside the library.  A call is rejected with
+ * KS_ERR_NOMEM when the scratch it needs exceeds 64 MiB; that need is never
+ * more than ks_workspace_size for the same sizes (which assumes the full
+ * 6 x 139 population table, room for the ASYNTH cube even when asynth_out is
+ * given, and 256 bytes of slack), so a problem whose ks_workspace_size is at
+ * most 64 MiB always runs (on a 72-layer atmosphere and a 6,000-point grid
+ * about 20,000 lines fit in KS_PREC_MIXED, 8,000 in KS_PREC_FP64).  The
+ * caller still passes
  * inputs and outputs.  All calls on a device share the array: calls that
  * overlap on the GPU race and must be serialised.  The first call on each
  * device looks up the array's device address (and, like every entry point,

@@ -120,6 +120,7 @@ SIGNATURES = {
                                           C.POINTER(KsStats), P]),
     "ks_synthesize_noalloc": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                           C.POINTER(KsOptions), P, P, P, P]),
+    "ks_check_flags": (C.c_int32, [P, C.POINTER(C.c_int32)]),
     "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,
                                   C.POINTER(P)]),
     "ks_gfall_sort": (C.c_int32, [P]),
@@ -177,3 +178,16 @@ def check(status: int) -> None:
 
 def exported_symbols() -> list:
     return sorted(SIGNATURES)
+
+
+def check_device_flags(stream: Optional[int] = None) -> int:
+    """Synchronise ``stream`` (a cudaStream_t as an int; None = the legacy
+    default stream) and raise :class:`KsError` when any call on the current
+    device has flagged an internal limit since the last check
+    (``ks_check_flags``: the flags are sticky per device and cleared here)."""
+    L = load()
+    f = C.c_int32(0)
+    st = L.ks_check_flags(C.c_void_p(stream) if stream else None, C.byref(f))
+    if st != KS_OK:
+        raise KsError(st, L.ks_last_error().decode())
+    return int(f.value)

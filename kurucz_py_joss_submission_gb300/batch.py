@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .device import DeviceAtmosphere, DeviceCatalog, DeviceGrid, _ptr, make_options
+from .device import DeviceAtmosphere, DeviceCatalog, DeviceGrid, _ptr, check_flags, make_options
 from .io.atmosphere import AtmosphereModel
 from .io.lines.atomic import DELLIM
 
@@ -159,10 +159,15 @@ class BatchSynthesizer:
         self.graph = g
         return g
 
-    def replay(self):
+    def replay(self, check: bool = False):
+        """Launch the captured batch; with ``check`` wait for it and raise if
+        any job flagged an internal limit (the flags stay on the device
+        otherwise, until :func:`device.check_flags`)."""
         if self.graph is None:
             raise RuntimeError("capture() first")
         self.graph.replay()
+        if check:
+            check_flags()
 
     def evaluations(self) -> int:
         """Total line.depth.lambda evaluations of the batch (one synchronous pass)."""

@@ -29,10 +29,15 @@ def build_parser() -> argparse.ArgumentParser:
     p.add_argument("--no-vacuum", action="store_true", help="line wavelengths are in air, not vacuum")
     p.add_argument("--cutoff", type=float, default=1e-3, help="KAPMIN as a fraction of the continuum")
     p.add_argument("--linout", type=int, default=30, help="LINOUT switch of SYNTHE")
-    p.add_argument("--cache", type=Path, default=None, help="Line cache directory (unused)")
+    p.add_argument("--cache", type=Path, default=None,
+                   help="line cache directory of the reference; not used here (the native reader parses "
+                        "1.5M lines in well under a second), a warning is logged")
     p.add_argument("--allow-tfort-runtime", action="store_true", help="Accepted, unused")
-    p.add_argument("--n-workers", type=int, default=None, help="Accepted, unused (GPU)")
-    p.add_argument("--nlte", action="store_true", help="Accepted; LTE source only")
+    p.add_argument("--n-workers", type=int, default=None,
+                   help="host worker threads of the reference; not used (the path runs on the GPU), "
+                        "a warning is logged")
+    p.add_argument("--nlte", action="store_true",
+                   help="NLTE line source of the reference: not supported (LTE only), rejected")
     p.add_argument("--scat-iterations", type=int, default=8)
     p.add_argument("--scat-tol", type=float, default=1e-3)
     p.add_argument("--rhoxj", type=float, default=0.0, help="RHOXJ of the line scattering fraction (0: none)")
@@ -46,8 +51,17 @@ def build_parser() -> argparse.ArgumentParser:
     return p
 
 
+log = logging.getLogger(__name__)
+
+
 def main(argv: Optional[list] = None) -> int:
-    args = build_parser().parse_args(argv)
+    parser = build_parser()
+    args = parser.parse_args(argv)
+    if args.nlte:
+        # the reference's --nlte switches the line source to departure
+        # coefficients (physics/bfudge_tables.py); this path computes the
+        # LTE source only, so running would give a different spectrum
+        parser.error("--nlte is not supported: this GPU path computes the LTE line source only")
     cfg = config.SynthesisConfig.from_cli(
         spec_path=args.spec, diagnostics_path=args.diagnostics, atmosphere_path=args.model,
         atomic_catalog=args.atomic, wl_start=args.wl_start, wl_end=args.wl_end,
@@ -61,6 +75,10 @@ def main(argv: Optional[list] = None) -> int:
     cfg.log_level = args.log_level
     logging.basicConfig(level=getattr(logging, args.log_level),
                         format="%(asctime)s [%(levelname)s] %(name)s - %(message)s")
+    if args.cache is not None:
+        log.warning("--cache %s ignored: line lists are parsed by the native reader on every run", args.cache)
+    if args.n_workers is not None:
+        log.warning("--n-workers %d ignored: the synthesis runs on the GPU", args.n_workers)
     run_synthesis(cfg)
     return 0
 

@@ -446,8 +446,7 @@ __device__ __forceinline__ double near_profile_da(int o, double dvg, double ad, 
     const double x = (double)o * dvg;
     if (ad < 0.2) {
         if (x > 10.0) return k0 * (0.5642 / (x * x));
-        double tabi = 0.5 + (double)o * (200.0 * dvg);
-        int idx = (int)tabi;
+        int idx = tabi_index<double>(o, 200.0 * dvg);
         idx = idx < 0 ? 0 : (idx > VOIGT_N - 1 ? VOIGT_N - 1 : idx);
         return k0 * h1[idx];
     }

@@ -294,6 +294,45 @@ extern "C" int64_t ks_wavelength_grid(double start, double end, double resolutio
 // precision-independent kernels
 // ---------------------------------------------------------------------------
 
+// Internal-limit flags raised on this device since the last ks_check_flags.
+// Every entry point ends by OR-ing its call's flag word into it on the call's
+// stream (flag_sink_kernel), so an overflow in a call that reads no counters
+// is kept until the caller asks; ks_check_flags takes and clears it.
+static __device__ int g_sticky_flags;
+static __device__ int g_taken_flags;
+
+__global__ void flag_sink_kernel(const int* __restrict__ flags) {
+    const int f = *flags;
+    if (f) atomicOr(&g_sticky_flags, f);
+}
+
+__global__ void flag_take_kernel() { g_taken_flags = atomicExch(&g_sticky_flags, 0); }
+
+static ks_status sink_flags(const int* flags, cudaStream_t s) {
+    flag_sink_kernel<<<1, 1, 0, s>>>(flags);
+    KS_CUDA(cudaGetLastError());
+    return KS_OK;
+}
+
+static ks_status flags_status(int flags) {
+    if (flags & 8) return fail(KS_ERR_DEVICE, "wing bins are not monotone in the line order");
+    if (flags & FLAG_N10DOP_RANGE)
+        return fail(KS_ERR_DEVICE, "a pair exceeded a packed descriptor field (N10DOP or centre offset)");
+    if (flags) return fail(KS_ERR_DEVICE, "a kernel raised device flag " + std::to_string(flags));
+    return KS_OK;
+}
+
+extern "C" ks_status ks_check_flags(void* stream, int32_t* flags_out) {
+    cudaStream_t s = (cudaStream_t)stream;
+    int f = 0;
+    flag_take_kernel<<<1, 1, 0, s>>>();
+    KS_CUDA(cudaGetLastError());
+    KS_CUDA(cudaMemcpyFromSymbolAsync(&f, g_taken_flags, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+    KS_CUDA(cudaStreamSynchronize(s));
+    if (flags_out) *flags_out = f;
+    return flags_status(f);
+}
+
 // Grid scalars (opacity.py:570-574; line_opacity.py:235-239 RESOLU and
 // :1035-1058 WBEGIN / grid offset of the wing bins).
 __global__ void grid_params_kernel(const double* g, int64_t n, double grid_origin, GridPar* gp) {
@@ -849,10 +888,7 @@ static ks_status collect_stats(const Workspace& w, int64_t n_wl, ks_stats* stats
         stats->iterations = iters;
         stats->device_flags = flags;
     }
-    if (flags & 8) return fail(KS_ERR_DEVICE, "wing bins are not monotone in the line order");
-    if (flags & FLAG_N10DOP_RANGE)
-        return fail(KS_ERR_DEVICE, "a pair exceeded a packed descriptor field (N10DOP or centre offset)");
-    return KS_OK;
+    return flags_status(flags);
 }
 
 // ---------------------------------------------------------------------------
@@ -878,8 +914,9 @@ extern "C" ks_status ks_line_bins(const ks_grid* grid, const double* wavelength,
             nullptr, nullptr, nullptr, nullptr, flags);
         KS_CUDA(cudaGetLastError());
     }
+    ks_status fs = sink_flags(flags, s);
     KS_CUDA(cudaFreeAsync(gp, s));
-    return KS_OK;
+    return fs;
 }
 
 extern "C" ks_status ks_continuum(const ks_atmos* atm, const ks_grid* grid, int32_t precision,
@@ -926,6 +963,7 @@ extern "C" ks_status ks_transp(const ks_lines* lines, const ks_atmos* atm, const
     if (center_out && lines->n_lines > 0)
         KS_CUDA(cudaMemcpyAsync(center_out, w.center, sizeof(int32_t) * lines->n_lines,
                                 cudaMemcpyDeviceToDevice, s));
+    if ((st = sink_flags(w.flags, s))) return st;
     KS_CUDA(cudaFreeAsync(buf, s));
     return KS_OK;
 }
@@ -964,6 +1002,7 @@ extern "C" ks_status ks_asynth(const ks_lines* lines, const ks_atmos* atm, const
     if ((st = run_partition(w, atm->n_layers, grid->n, default_tile(opt, true), s))) return st;
     AccArgs a = acc_args(lines, atm, grid, opt, w, t, true);
     KS_CUDA(launch_accumulate_f64(a, default_warps(opt), (const PairDesc<double>*)w.desc, asynth_out, s));
+    if ((st = sink_flags(w.flags, s))) return st;
     if (stats) return collect_stats(w, 0, stats, s);
     return KS_OK;
 }
@@ -1003,6 +1042,7 @@ extern "C" ks_status ks_formal_solution(const ks_atmos* atm, const ks_grid* grid
         KS_CUDA(launch_transfer_f32(ta, &g_tables.cj, (const float*)cont_abs, (const float*)cont_scat,
                                     (const float*)line_opacity, (const float*)line_scattering,
                                     (const float*)line_source, s));
+    if ((st = sink_flags(w.flags, s))) return st;
     if (stats) {
         st = collect_stats(w, grid->n, stats, s);
         cudaFreeAsync(buf, s);
@@ -1063,11 +1103,11 @@ static ks_status run_transfer(const ks_atmos* atm, const ks_grid* grid, const ks
 }
 
 static int fused_launches(bool has_lines, bool fp64, const ks_options* opt, bool with_transfer) {
-    // grid parameters, prep, continuum, accumulation; line bins, pair setup,
-    // three partition passes and the tile ranges; the transfer (FP32:
-    // streaming pass + list pass)
+    // grid parameters, prep, continuum, accumulation, the flag sink; line
+    // bins, pair setup, three partition passes and the tile ranges; the
+    // transfer (FP32: streaming pass + list pass)
     const bool stream_pass = !fp64 && !(opt && opt->transfer_path == 1);
-    return 4 + (has_lines ? 6 : 0) + (with_transfer ? (stream_pass ? 2 : 1) : 0);
+    return 5 + (has_lines ? 6 : 0) + (with_transfer ? (stream_pass ? 2 : 1) : 0);
 }
 
 template <typename R>
@@ -1133,10 +1173,12 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
     tm.mark();
-    if (!do_transfer) return KS_OK;
-    if ((st = run_transfer<R>(atm, grid, opt, w, t, cabs, cscat, asynth, flux_total, flux_cont, s))) return st;
-    tm.mark();
-    return KS_OK;
+    if (do_transfer) {
+        if ((st = run_transfer<R>(atm, grid, opt, w, t, cabs, cscat, asynth, flux_total, flux_cont, s)))
+            return st;
+        tm.mark();
+    }
+    return sink_flags(w.flags, s);
 }
 
 extern "C" ks_status ks_synthesize(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
@@ -1274,10 +1316,11 @@ extern "C" ks_status ks_transfer_opacity(const ks_atmos* atm, const ks_grid* gri
             st = run_transfer<float>(atm, grid, opt, w, t, (const float*)cont_abs, (const float*)cont_scat,
                                      (const float*)asynth, flux_total, flux_cont, s);
     }
+    if (!st) st = sink_flags(w.flags, s);
     if (!st && stats) {
         st = collect_stats(w, grid->n, stats, s);
         const bool stream_pass = !fp64 && !(opt && opt->transfer_path == 1);
-        stats->kernel_launches = 2 + (stream_pass ? 2 : 1);
+        stats->kernel_launches = 3 + (stream_pass ? 2 : 1);
     }
     cudaFreeAsync(buf, s);
     return st;

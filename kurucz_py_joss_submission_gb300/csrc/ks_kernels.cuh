@@ -213,10 +213,33 @@ __device__ __forceinline__ float fast_ex_mixed(float e_hi, float e_lo, float h_h
     return extab[i] * extabf[j];
 }
 
+// Voigt table index of near-wing step `off` (ADAMP < 0.2).  The reference
+// carries TABI incrementally, TABI = 0.5, then TABI += TABSTEP per step
+// (line_opacity.py:474-480, :546-552), and takes int(TABI).  The closed form
+// 0.5 + off*TABSTEP has the same integer part unless the sum lies within its
+// accumulated rounding of an integer: each of the `off` additions rounds by
+// at most half an ulp of a value <= TABI, the closed form by about one ulp.
+// FP64: inside that band the incremental sum is replayed, so the index is
+// the reference's; outside it (all but ~1e-10 of the steps) the closed form
+// is used.  FP32 (mixed path): the closed form; an index one off at a tie is
+// within the mixed contract.
+template <typename R>
+__device__ __forceinline__ int tabi_index(int off, R tabstep) {
+    if constexpr (sizeof(R) == 8) {
+        const double t = __dadd_rn(0.5, __dmul_rn((double)off, tabstep));
+        const double fl = floor(t);
+        const double ulp = t >= 1.0 ? ldexp(1.0, ilogb(t) - 52) : 0x1p-53;
+        const double band = (0.5 * (double)off + 2.0) * ulp;
+        if (t - fl > band && fl + 1.0 - t > band) return (int)t;
+        double s = 0.5;
+        for (int k = 0; k < off; k++) s = __dadd_rn(s, tabstep);
+        return (int)s;
+    } else {
+        return (int)(R(0.5) + (R)off * tabstep);
+    }
+}
+
 // Near-zone wing profile at step `off` (line_opacity.py:474-491, :546-565).
-// The reference carries TABI incrementally; here it is 0.5 + off*tabstep,
-// which equals the incremental sum except when that sum lies within a few
-// ulps of an integer.
 template <typename R>
 __device__ __forceinline__ R near_profile(int off, R dvoigt, R adamp, R kappa0,
                                           const R* __restrict__ h0, const R* __restrict__ h1,
@@ -224,8 +247,7 @@ __device__ __forceinline__ R near_profile(int off, R dvoigt, R adamp, R kappa0,
     R x = (R)off * dvoigt;
     if (adamp < R(0.2)) {
         if (x > R(10)) return kappa0 * (R(0.5642) * adamp / (x * x));
-        R tabi = R(0.5) + (R)off * (R(200) * dvoigt);
-        int idx = (int)tabi;
+        int idx = tabi_index<R>(off, R(200) * dvoigt);
         idx = idx < 0 ? 0 : (idx > VOIGT_N - 1 ? VOIGT_N - 1 : idx);
         return kappa0 * (h0[idx] + adamp * h1[idx]);
     }
@@ -608,7 +630,7 @@ __device__ __forceinline__ R near_profile_tab(int off, R dv, R tabstep, R ad, R 
     R x = (R)off * dv;
     if (ad < R(0.2)) {
         if (x > R(10)) return k0 * (R(0.5642) * ad / (x * x));
-        int idx = (int)(R(0.5) + (R)off * tabstep);
+        int idx = tabi_index<R>(off, tabstep);
         idx = idx > VOIGT_N - 1 ? VOIGT_N - 1 : idx;
         R2 h = h01[idx];
         return k0 * (h.x + ad * h.y);

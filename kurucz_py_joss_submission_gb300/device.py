@@ -162,6 +162,15 @@ class DeviceCatalog:
         return out
 
 
+def check_flags(stream: Optional[torch.cuda.Stream] = None) -> None:
+    """Synchronise the stream (default: the current one) and raise
+    ``KsError`` (KS_ERR_DEVICE) if any synthesis on this device flagged an
+    internal limit since the last check.  The calls themselves stay
+    asynchronous; their flags are kept on the device until this is called."""
+    s = stream if stream is not None else torch.cuda.current_stream()
+    _native.check_device_flags(s.cuda_stream)
+
+
 def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", tile_bins=0,
                  warps_per_tile=0, profile=False, short_class=0,
                  transfer_path=0, long_class=0, exact_sweeps=0) -> _native.KsOptions:
@@ -215,3 +224,8 @@ class Synthesizer:
             C.byref(st) if stats else None, stream_handle(stream))
         _native.check(status)
         return st.as_dict() if stats else None
+
+    def check(self, stream: Optional[torch.cuda.Stream] = None) -> None:
+        """Raise if this or any earlier call on the device flagged an internal
+        limit (see :func:`check_flags`)."""
+        check_flags(stream)

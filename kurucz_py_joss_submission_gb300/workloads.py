@@ -264,17 +264,29 @@ def random_atomic_lines(
 BAND_CODE = 22.00
 
 
+# sigma_J = sigma_head - BAND_SPACING * B * J^3 (cm^-1): the gap between
+# lines J and J + 1 is BAND_SPACING * B * (3 J^2 + 3 J + 1), growing
+# quadratically with J (about 0.6 B cm^-1 at J = 30, 13.5 B at J = 150).
+BAND_SPACING = 2.0e-4
+
+
+def band_wavenumbers(sigma_head, b, j):
+    """Wavenumbers (cm^-1) of lines J of bands with head ``sigma_head`` and
+    rotational constant ``b`` (broadcasting): line spacing quadratic in J."""
+    return sigma_head - BAND_SPACING * b * j ** 3
+
+
 def random_band_lines(n_lines: int, wl_min: float, wl_max: float, seed: int,
                       j_max: int = 150) -> LineDraw:
     """Draw ``n_lines`` lines in molecular-band-like sequences.
 
     Each band has a head wavelength ~ U(wl_min, wl_max) nm, a rotational
-    constant B ~ U(0.3, 2) cm^-1 and lines J = 0..j_max at wavenumber
-    sigma_J = sigma_head - dB J^2 (spacing growing as J^2, dB = 0.02 B),
-    lower-level energy E = B J (J + 1), log gf ~ N(-4, 1), damping drawn as
-    for the atomic lines, species code :data:`BAND_CODE`.  Lines outside
-    [wl_min, wl_max] are dropped; bands are drawn until ``n_lines`` lines
-    are kept.  Returned sorted by wavelength.
+    constant B ~ U(0.3, 2) cm^-1 and lines J = 0..j_max at the wavenumbers
+    of :func:`band_wavenumbers` (spacing growing as J^2), lower-level energy
+    E = B J (J + 1), log gf ~ N(-4, 1), damping drawn as for the atomic
+    lines, species code :data:`BAND_CODE`.  Lines outside [wl_min, wl_max]
+    are dropped; bands are drawn until ``n_lines`` lines are kept.  Returned
+    sorted by wavelength.
     """
     rng = np.random.default_rng(seed)
     j = np.arange(j_max + 1, dtype=np.float64)
@@ -283,7 +295,7 @@ def random_band_lines(n_lines: int, wl_min: float, wl_max: float, seed: int,
         nb = max(64, int(1.3 * (n_lines - kept) / (j_max + 1)) + 1)
         head = rng.uniform(wl_min, wl_max, nb)
         b = rng.uniform(0.3, 2.0, nb)
-        sigma = (1.0e7 / head)[:, None] - (0.02 * b)[:, None] * j[None, :] ** 2
+        sigma = band_wavenumbers((1.0e7 / head)[:, None], b[:, None], j[None, :])
         with np.errstate(divide="ignore"):
             wl = np.where(sigma > 0, 1.0e7 / np.where(sigma > 0, sigma, 1.0), np.inf)
         e = b[:, None] * j[None, :] * (j[None, :] + 1.0)

@@ -52,3 +52,16 @@ def atm_path(name: str) -> Path:
 def window(name: str):
     c = MG.CASES[name]
     return c["wl_start"], c["wl_end"]
+
+
+def case_options(name: str) -> dict:
+    """Synthesis options of a case besides the window: line scattering scale
+    (``--rhoxj``) and microturbulence (``--microturb``, km/s)."""
+    c = MG.CASES[name]
+    return {"rhoxj": float(c.get("rhoxj", 0.0)), "microturb": float(c.get("microturb", 0.0))}
+
+
+def device_options(name: str) -> dict:
+    """The same options as ``make_options`` keywords."""
+    o = case_options(name)
+    return {"rhoxj": o["rhoxj"], "microturb_kms": o["microturb"]}

@@ -1,7 +1,8 @@
 """Generate the golden fixtures by running the reference pipeline itself.
 
-Test infrastructure, run in a container that has the reference checkout at
-``/root/reference`` (it is never read at test time).  Numba is not
+Test infrastructure, run in a container that has the reference checkout
+(``--reference DIR`` or ``$SYNTHE_PY_REFERENCE``, default
+``/root/reference``; it is never read at test time).  Numba is not
 installed there, so ``numba_shim/`` (identity ``jit``, ``prange = range``) is
 put first on ``PYTHONPATH`` and the reference executes as plain Python with
 NumPy semantics.
@@ -17,7 +18,7 @@ stage arrays (``case_<name>.npz``): TRANSP + valid mask + centre bins
 columns, and the sha256 of the gfall text so a test can confirm that
 regenerating the line list from its seed gives the same file.
 
-Usage: ``python tests/golden/make_golden.py [case ...]``
+Usage: ``python tests/golden/make_golden.py [--reference DIR] [case ...]``
 """
 
 from __future__ import annotations
@@ -33,7 +34,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REFERENCE = Path("/root/reference")
+REFERENCE = Path(os.environ.get("SYNTHE_PY_REFERENCE", "/root/reference"))
 sys.path.insert(0, str(REPO))
 
 from kurucz_py_joss_submission_gb300 import workloads  # noqa: E402
@@ -53,6 +54,15 @@ ATMOSPHERES = {
     "t5800g444": dict(teff=5800.0, logg=4.44, metallicity=0.0),
     "t6000g430": dict(teff=6000.0, logg=4.30, metallicity=0.0),
     "t2500gm10": dict(teff=2500.0, logg=-1.0, metallicity=0.0),
+    # t5800g444 with the Doppler widths of Fe and Ti set so that the Voigt
+    # table step TABSTEP = 200 / (DOPPLE * RESOLU) is 0.7 (Fe) and 1.1 (Ti):
+    # for such steps the reference's incremental TABI (line_opacity.py:540-548)
+    # and the closed form 0.5 + n*TABSTEP fall on different sides of an
+    # integer at about a hundred offsets of the near wing.  The populations
+    # are scaled by the same factor, so XNFDOP = pop / (rho dop) and the
+    # TRANSP gates are those of the unmodified atmosphere.
+    "t5800g444_tabi": dict(teff=5800.0, logg=4.44, metallicity=0.0, tabstep={26: 0.7, 22: 1.1},
+                           tabi_window=(500.0, 501.0)),
 }
 
 # name: atmosphere, window, line draw.  Line windows extend 0.15 nm past the
@@ -72,6 +82,19 @@ CASES = {
     "cool_600_601": dict(atm="t2500gm10", wl_start=600.0, wl_end=601.0,
                          n_lines=200, draw=(599.85, 601.15), log_uniform=False, seed=14,
                          band_lines=800, band_seed=15),
+    # line scattering: FSCAT = exp(-RHOX / RHOXJ) splits ASYNTH into
+    # absorption and scattering (engine/opacity.py:2408-2440)
+    "scat_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
+                         n_lines=200, draw=(499.85, 501.15), log_uniform=False, seed=16,
+                         rhoxj=0.3),
+    # synthesis microturbulence added to the TRANSP Doppler width
+    # (physics/line_opacity.py:629)
+    "micro_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
+                          n_lines=200, draw=(499.85, 501.15), log_uniform=False, seed=17,
+                          microturb=2.0),
+    # near-wing Voigt table index at rounding ties of TABI (see t5800g444_tabi)
+    "tabi_500_501": dict(atm="t5800g444_tabi", wl_start=500.0, wl_end=501.0,
+                         n_lines=200, draw=(499.85, 501.15), log_uniform=False, seed=18),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -115,6 +138,28 @@ def build_atmosphere(name: str, work: Path) -> Path:
          "--atlas-tables", str(REFERENCE / "synthe_py/data/atlas_tables.npz")],
         check=True, env=_env(), cwd=work, stdout=subprocess.DEVNULL,
     )
+    if spec.get("tabstep"):
+        # RESOLU = 1 / (ratio - 1) of the window's grid (line_opacity.py:235-239),
+        # then a Doppler width whose TABSTEP = 200 * (1 / (DOPPLE * RESOLU)) is
+        # the double nearest the chosen step (searched ulp by ulp)
+        sys.path.insert(0, str(REPO))
+        from oracle import oracle
+
+        grid = oracle.wavelength_grid(*spec["tabi_window"], 300000.0)
+        resolu = 1.0 / (grid[1] / grid[0] - 1.0)
+        with np.load(full_npz, allow_pickle=False) as d:
+            full = {k: np.asarray(d[k]) for k in d.files}
+        for z, step in spec["tabstep"].items():
+            dop = 200.0 / (step * resolu)
+            for _ in range(256):
+                ts = 200.0 * (1.0 / (dop * resolu))
+                if ts == step:
+                    break
+                dop = float(np.nextafter(dop, np.inf if ts > step else -np.inf))
+            scale = dop / full["doppler_per_ion"][:, :, z - 1]
+            full["doppler_per_ion"][:, :, z - 1] = dop
+            full["population_per_ion"][:, :, z - 1] *= scale
+        np.savez(full_npz, **full)
     with np.load(full_npz) as d:
         kept = {k: np.asarray(d[k]) for k in ATM_FIELDS if k in d}
     out = HERE / f"atm_{name}.npz"
@@ -138,7 +183,9 @@ def run_case(name: str, full_npz: Path, work: Path) -> None:
          "--npz", str(full_npz), "--spec", str(spec),
          "--wl-start", repr(case["wl_start"]), "--wl-end", repr(case["wl_end"]),
          "--resolution", "300000", "--n-workers", "1",
-         "--cache", str(work / "cache"), "--log-level", "WARNING"],
+         "--cache", str(work / "cache"), "--log-level", "WARNING",
+         "--rhoxj", repr(float(case.get("rhoxj", 0.0))),
+         "--microturb", repr(float(case.get("microturb", 0.0)))],
         check=True, env=env, cwd=work,
     )
     s3 = np.load(dumps / "stage_3_transp.npz")
@@ -149,6 +196,7 @@ def run_case(name: str, full_npz: Path, work: Path) -> None:
         gfall_sha256=np.array(hashlib.sha256(text.encode()).hexdigest()),
         wl_start=np.float64(case["wl_start"]), wl_end=np.float64(case["wl_end"]),
         resolution=np.float64(300000.0),
+        rhoxj=np.float64(case.get("rhoxj", 0.0)), microturb=np.float64(case.get("microturb", 0.0)),
         wavelength=s5["wavelength"],
         line_indices=np.asarray(s3["line_indices"], dtype=np.int64),
         valid_mask=np.packbits(np.asarray(s3["valid_mask"], dtype=bool), axis=None),
@@ -180,6 +228,10 @@ def run_case(name: str, full_npz: Path, work: Path) -> None:
 
 
 def main(argv: list[str]) -> int:
+    global REFERENCE
+    if argv[:1] == ["--reference"]:
+        REFERENCE = Path(argv[1])
+        argv = argv[2:]
     wanted = argv or list(CASES)
     with tempfile.TemporaryDirectory(prefix="kgold_") as tmp:
         work = Path(tmp)

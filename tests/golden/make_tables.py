@@ -12,20 +12,24 @@ exactly, so they are carried over as numbers, not re-derived:
   van der Waals damping defaults (``synthe_py/io/lines/atomic.py:22``,
   ``synthe_py/data/fortran_data.npz``).
 
-Run once where the reference checkout exists:
-``python kurucz_py_joss_submission_gb300/data/make_tables.py``.
+Run once where the reference checkout exists (``--reference DIR`` or
+``$SYNTHE_PY_REFERENCE``, default ``/root/reference``):
+``python tests/golden/make_tables.py [--reference DIR]``.  Writes the package's
+``data/synthe_tables.npz`` and the test fixture ``tests/golden/tables_ref.npz``.
 """
 
 from __future__ import annotations
 
 import importlib.util
+import os
 import sys
 from pathlib import Path
 
 import numpy as np
 
-REFERENCE = Path("/root/reference")
-OUT = Path(__file__).resolve().parent / "synthe_tables.npz"
+REFERENCE = Path(os.environ.get("SYNTHE_PY_REFERENCE", "/root/reference"))
+HERE = Path(__file__).resolve().parent
+OUT = HERE.parents[1] / "kurucz_py_joss_submission_gb300" / "data" / "synthe_tables.npz"
 
 
 def _load_module(path: Path, name: str):
@@ -37,7 +41,10 @@ def _load_module(path: Path, name: str):
     return mod
 
 
-def main() -> int:
+def main(argv: list) -> int:
+    global REFERENCE
+    if argv[:1] == ["--reference"]:
+        REFERENCE = Path(argv[1])
     josh = _load_module(REFERENCE / "synthe_py/physics/josh_tables.py", "_josh_tables")
     # tables.py imports nothing from the package, so it loads standalone
     tables = _load_module(REFERENCE / "synthe_py/physics/tables.py", "_synthe_tables")
@@ -57,7 +64,7 @@ def main() -> int:
     vt = tables.VoigtTables.build()
     et = tables.ExpTables.build()
     np.savez_compressed(
-        Path(__file__).resolve().parents[2] / "tests/golden/tables_ref.npz",
+        HERE / "tables_ref.npz",
         h0tab=vt.h0tab, h1tab=vt.h1tab, h2tab=vt.h2tab,
         extab=et.extab, extabf=et.extabf,
     )
@@ -66,4 +73,4 @@ def main() -> int:
 
 
 if __name__ == "__main__":
-    raise SystemExit(main())
+    raise SystemExit(main(sys.argv[1:]))

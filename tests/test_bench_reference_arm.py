@@ -64,3 +64,27 @@ def test_reference_arm_under_torchrun_prints_once():
     _check_line(line, 2)
     # the port runs on every host core even though torchrun sets OMP_NUM_THREADS=1
     assert line["cpu_baseline"]["cores"] == len(os.sched_getaffinity(0))
+
+
+def test_reference_arm_loads_nothing_of_the_product():
+    """The CPU arm runs the oracle only: the product's native library is never
+    mapped and its ctypes loader is never imported (lines come from the
+    restated gfall reader, the grid from the restated grid routine)."""
+    code = (
+        "import sys, json\n"
+        f"sys.argv = ['bench.py', *{ARGS!r}]\n"
+        "import bench\n"
+        "rc = bench.main()\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'rc': rc, 'mapped': 'libkurucz_gb300' in maps,\n"
+        "                  'native_imported': 'kurucz_py_joss_submission_gb300._native' in sys.modules,\n"
+        "                  'oracle_mapped': 'libks_oracle' in maps}))\n"
+    )
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, env=_env(), capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    assert res["rc"] == 0
+    assert res["oracle_mapped"]
+    assert not res["mapped"], "the reference arm mapped the product library"
+    assert not res["native_imported"], "the reference arm imported the product's ctypes loader"

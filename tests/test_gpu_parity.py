@@ -4,8 +4,11 @@ Tolerances (written here, from the spec contract):
 * bins (centre/wing) and the TRANSP valid mask: bit-exact;
 * FP64 path: TRANSP/ASYNTH/continuum within 1e-12 relative of the reference,
   fluxes within 1e-10;
-* mixed path: normalised flux within 1e-4 (absolute, F/Fc is O(1)) and
-  continuum flux within 1e-3 relative of the FP64 reference.
+* mixed path: normalised flux F/Fc within 1e-4 relative of the reference's
+  (relative to max(F/Fc, 1e-3): the saturated MAXJ = 1 cores of the
+  strong-line case have F/Fc ~ 1e-18, zero to the reference's own
+  precision, and are held to 1e-7 absolute through that floor), also within
+  1e-4 absolute, and continuum flux within 1e-3 relative.
 """
 
 import ctypes as C
@@ -14,8 +17,8 @@ import numpy as np
 import pytest
 import torch
 
-from _cases import (SMALL_CASES, atm_path, available_cases, gfall_path, golden, golden_valid,
-                    window)
+from _cases import (SMALL_CASES, atm_path, available_cases, case_options, device_options, gfall_path,
+                    golden, golden_valid, window)
 from kurucz_py_joss_submission_gb300 import _native
 from kurucz_py_joss_submission_gb300.device import (DeviceAtmosphere, DeviceCatalog, DeviceGrid,
                                                      Synthesizer, make_options, stream_handle)
@@ -31,7 +34,13 @@ from oracle import gfall, oracle
 pytestmark = pytest.mark.gpu
 
 NORM_TOL = 1e-4
+NORM_FLOOR = 1e-3
 CONT_TOL = 1e-3
+
+
+def norm_rel(nf, nf_ref):
+    """Relative error of the normalised flux, against max(F/Fc, NORM_FLOOR)."""
+    return float(np.max(np.abs(nf - nf_ref) / np.maximum(np.abs(nf_ref), NORM_FLOOR)))
 
 
 def rel(a, b):
@@ -100,6 +109,7 @@ def test_formal_solution_seam(name):
 
 def run_fused(name, precision, **kw):
     g = golden(name)
+    kw = {**device_options(name), **kw}
     atm = atm_io.load_cached(atm_path(name))
     syn = Synthesizer(DeviceCatalog(catalog(name)), DeviceAtmosphere(atm),
                       DeviceGrid(g["wavelength"]), make_options(precision=precision, **kw))
@@ -130,6 +140,7 @@ def test_fused_mixed_within_contract(name, short_class):
     assert st["device_flags"] == 0
     ft, fc = syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy()
     nf_ref = g["flux_total_hz"] / g["flux_cont_hz"]
+    assert norm_rel(ft / fc, nf_ref) <= NORM_TOL
     assert float(np.max(np.abs(ft / fc - nf_ref))) <= NORM_TOL
     assert rel(fc, g["flux_cont_hz"]) <= CONT_TOL
 
@@ -170,7 +181,7 @@ def test_streaming_transfer_matches_per_column_kernel(name):
     assert rel(c0, c1) <= 2e-6
     assert st0["maxj_wavelengths"] == st1["maxj_wavelengths"]
     assert abs(st0["iterations"] - st1["iterations"]) <= max(2, st1["iterations"] // 1000)
-    assert (st0["kernel_launches"], st1["kernel_launches"]) == (12, 11)
+    assert (st0["kernel_launches"], st1["kernel_launches"]) == (13, 12)
     if name == "strong_600_601":
         assert st0["maxj_wavelengths"] > 0
 

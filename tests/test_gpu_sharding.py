@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 import torch
 
-from _cases import atm_path, available_cases, golden, gfall_path, window
+from _cases import atm_path, available_cases, device_options, golden, gfall_path, window
 from kurucz_py_joss_submission_gb300 import sharding
 from kurucz_py_joss_submission_gb300.device import (DeviceAtmosphere, DeviceCatalog, DeviceGrid,
                                                      Synthesizer, make_options)
@@ -30,11 +30,12 @@ def test_sharded_spectrum_is_bit_identical(name, precision, world):
     g = golden(name)
     atm = atm_io.load_cached(atm_path(name))
     dc = DeviceCatalog(_catalog(name))
-    opt = make_options(precision=precision)
+    opt = make_options(precision=precision, **device_options(name))
     syn = Synthesizer(dc, DeviceAtmosphere(atm), DeviceGrid(g["wavelength"]), opt, keep_asynth=False)
     st = syn.run(stats=True)
     torch.cuda.synchronize()
-    ft, fc, evals = sharding.emulate(dc, atm, g["wavelength"], None, world, make_options(precision=precision))
+    ft, fc, evals = sharding.emulate(dc, atm, g["wavelength"], None, world,
+                                     make_options(precision=precision, **device_options(name)))
     torch.cuda.synchronize()
     assert evals == st["evaluations"]
     assert torch.equal(ft, syn.flux_total)

@@ -49,6 +49,20 @@ def test_band_line_draw():
     assert np.array_equal(again.wavelength_nm, d.wavelength_nm) and np.array_equal(again.e_lower_cm, e)
 
 
+def test_band_spacing_grows_quadratically_with_j():
+    """Within a band the gap between lines J and J + 1 is quadratic in J
+    (third differences of the wavenumbers constant, fourth zero), as the
+    dense stress case specifies -- not the linear gap of a Fortrat parabola."""
+    j = np.arange(151, dtype=np.float64)
+    for b in (0.3, 1.0, 2.0):
+        sigma = workloads.band_wavenumbers(20000.0, b, j)
+        gap = -np.diff(sigma)
+        assert np.all(gap > 0) and np.all(np.diff(gap) > 0)
+        assert np.allclose(np.diff(sigma, 3), -6.0 * workloads.BAND_SPACING * b, rtol=1e-6, atol=1e-9)
+        # gap(J) / J^2 tends to a constant, 3 * BAND_SPACING * B (gap[149]: lines 149 -> 150)
+        assert abs(gap[149] / 149.0 ** 2 / (3 * workloads.BAND_SPACING * b) - 1.0) < 0.01
+
+
 def test_dense_workload_composition():
     w = workloads.WORKLOADS["dense_10m"]
     assert w["n_lines"] + w["n_band_lines"] == 10_000_000

@@ -6,9 +6,12 @@ through an FFI with no CUDA allocator): it runs the same fused synthesis as
 ks_synthesize, but in a fixed 64 MiB scratch array inside the library.  This
 test calls it twice in a row through the C ABI and compares both results
 with ks_synthesize on the same inputs; the kernels are deterministic, so the
-fluxes must agree to 1e-12 (relative).  It also checks that sizes beyond the
-scratch are rejected.  This file is collected last so that a run stopping at
-the first failure has already run every other test.
+fluxes must agree to 1e-12 (relative).  It also checks that the call takes
+no device memory -- the device's free memory, and the used and reserved bytes
+of the stream-ordered pool that cudaMallocAsync draws from, are the same
+before and after it -- and that sizes beyond the scratch are rejected.  This
+file is collected last so that a run stopping at the first failure has
+already run every other test.
 """
 
 import ctypes as C
@@ -64,6 +67,49 @@ def test_noalloc_matches_workspace_entry_point_twice(precision):
         assert np.all(np.isfinite(ft)) and np.all(np.isfinite(fc))
         assert float(np.max(np.abs(ft - ft_ref) / fc_ref)) <= TOL
         assert float(np.max(np.abs(fc / fc_ref - 1.0))) <= TOL
+
+
+def _pool_bytes():
+    """(reserved, used) bytes of the current device's default stream-ordered
+    memory pool, read through the driver API (CU_MEMPOOL_ATTR_RESERVED_MEM_CURRENT
+    = 5, CU_MEMPOOL_ATTR_USED_MEM_CURRENT = 7 in cuda.h)."""
+    cu = C.CDLL("libcuda.so.1")
+    dev = C.c_int()
+    assert cu.cuCtxGetDevice(C.byref(dev)) == 0
+    pool = C.c_void_p()
+    assert cu.cuDeviceGetDefaultMemPool(C.byref(pool), dev) == 0
+    out = []
+    for attr in (5, 7):
+        v = C.c_uint64()
+        assert cu.cuMemPoolGetAttribute(pool, C.c_int(attr), C.byref(v)) == 0
+        out.append(int(v.value))
+    return tuple(out)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_noalloc_takes_no_device_memory(precision):
+    lib = _native.load()
+    _, dcat, datm, dgrid = _inputs("uv_300_302")
+    opt = make_options(precision=precision)
+    n = dgrid.n
+    ft = torch.empty(n, dtype=torch.float64, device="cuda")
+    fc = torch.empty(n, dtype=torch.float64, device="cuda")
+    args = (C.byref(dcat.rec), C.byref(datm.rec), C.byref(dgrid.rec), C.byref(opt),
+            C.c_void_p(ft.data_ptr()), C.c_void_p(fc.data_ptr()), None, stream_handle())
+    # warm-up: the one-time set-up (tables, scratch address) and the lazy
+    # loading of the kernels happen here
+    _native.check(lib.ks_synthesize_noalloc(*args))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    pool0 = _pool_bytes()
+    torch_reserved0 = torch.cuda.memory_reserved()
+    for _ in range(3):
+        _native.check(lib.ks_synthesize_noalloc(*args))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, f"device free memory fell by {free0 - free1} bytes"
+    assert _pool_bytes() == pool0
+    assert torch.cuda.memory_reserved() == torch_reserved0
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
