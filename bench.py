@@ -334,14 +334,15 @@ def accuracy_vs_port(cat_path: Path, datm, cpu: dict, dev) -> dict:
         for prec in res:
             syn = Synthesizer(dcat, datm, dgrid, make_options(precision=prec), keep_asynth=False)
             st = syn.run(stats=True)
-            evals_equal &= int(st["evaluations"]) == oev
+            if prec == "fp64":  # the FP64 gates are the reference's; FP32 ones may differ at the cutoff
+                evals_equal &= int(st["evaluations"]) == oev
             res[prec].append(flux_errors(syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy(), oft, ofc))
             del syn
         del dcat, dgrid
     torch.cuda.synchronize()
     out = {k: merge_errors(v) for k, v in res.items()}
     out["windows"] = f"{sample_text()} (oracle: C restatement of the reference path, FP64)"
-    out["evaluations_equal_oracle"] = bool(evals_equal)
+    out["fp64_evaluations_equal_oracle"] = bool(evals_equal)
     return out
 
 

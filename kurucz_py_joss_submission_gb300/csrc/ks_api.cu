@@ -824,6 +824,8 @@ static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g
     a.short_class = !opt || opt->short_class == 0 ? SHORT_CLASS
                     : opt->short_class < 0 ? 0 : min(opt->short_class, N_REACH_CLASSES);
     a.long_class = !opt || opt->long_class <= 0 ? LONG_CLASS : min(opt->long_class, N_REACH_CLASSES);
+    a.far_series = !fp64 && (opt && opt->far_series > 0) && a.tile_bins % MOM_SEG == 0 &&
+                   a.tile_bins <= MOM_SEG * MOM_NSEG;
     a.grid = g->wavelength;
     a.wing_idx = w.wing;
     a.class_pos = w.class_pos;

@@ -448,8 +448,17 @@ __device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restric
             dvoigt = (R)(dopple > 0 ? 1.0 / (dopple * resolu) : 1.0);
         } else {
             float ad = __fdividef(num, q.dopw_f);
-            adamp = (R)(ad > 1e-12f ? ad : 1e-12f);
+            ad = ad > 1e-12f ? ad : 1e-12f;
+            adamp = (R)ad;
             kappa0 = kappa0_w;
+            if (q.dop_f != q.dopw_f) {
+                // microturbulence broadens the TRANSP Doppler width only
+                // (line_opacity.py:629): KAPCEN carries H(0, a) of the
+                // broadened width, and the wing kappa0 is KAPCEN / H(0, a)
+                // of the wing's own width (:1161-1190), not the gate's kappa0
+                const float vc = ad < 0.2f ? 1.0f - 1.128f * ad : voigt_hv<float>(0.0f, ad, a.h0f, a.h1f, a.h2f);
+                kappa0 = vc > 0.0f ? (R)((float)kapcen / vc) : kapcen;
+            }
             n10dop = q.n10dop;
             dvoigt = (R)q.dvoigt_f;
         }
@@ -753,6 +762,31 @@ __device__ __forceinline__ void far_run_x2(float* my, int base, int sgn, int lo,
     }
 }
 
+// Far-wing series of one segment (FP32 accumulation).  A far run adds X / o^2
+// to every bin b it covers, o = |b - c| (line_opacity.py:577-579).  For a
+// 128-bin segment with centre m that lies whole inside the run, with
+// D = m - c and t = b - m (|t / D| < 0.2 from the segment's distance),
+//   X / (D + t)^2 = sum_k (k + 1) (X / D^2) (-64 / D)^k (t / 64)^k,
+// so the segment needs only M_k = sum over its runs of (k + 1) (X / D^2)
+// (-64 / D)^k, k < MOM_K (truncation below 1e-7 relative).  Lane 4 s + j of
+// a warp keeps M_j, M_{j+4}, M_{j+8} of segment s in registers; this adds
+// one run at distance `dist` = D.
+static_assert(MOM_SEG == 128 && MOM_K == 12 && MOM_NSEG * 4 == 32, "series layout: 8 segments x 4 lanes x 3 terms");
+__device__ __forceinline__ void far_series_add(float& m0, float& m1, float& m2, int part, float dist, float xf) {
+    const float inv = __frcp_rn(dist);
+    const float rho = -64.0f * inv;
+    const float amp = xf * inv * inv;
+    const float r2 = rho * rho, r4 = r2 * r2;
+    const float pj = part == 0 ? 1.0f : (part == 1 ? rho : (part == 2 ? r2 : r2 * rho));
+    const float t0 = amp * pj;
+    const float t1 = t0 * r4;
+    const float t2 = t1 * r4;
+    const float c = (float)(part + 1);
+    m0 = fmaf(c, t0, m0);
+    m1 = fmaf(c + 4.0f, t1, m1);
+    m2 = fmaf(c + 8.0f, t2, m2);
+}
+
 // Adds v to a bin of the warp's own copy with a shared-memory atomic (the
 // short pairs, where two lanes may hit one bin).  Only lanes of one warp
 // touch a copy, and a warp's atomics to one word are applied in a fixed
@@ -796,6 +830,13 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     R2* h01 = reinterpret_cast<R2*>(smem_raw);  // interleaved (H0, H1)
     size_t tab_bytes = (VOIGT_N * sizeof(R2) + 15) & ~size_t(15);
     CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
+    // far-wing series (FP32): per warp [MOM_NSEG][MOM_K], then their sum
+    float* mom_w = reinterpret_cast<float*>(acc + (size_t)nwarps * W);
+    float* mom_sum = mom_w + nwarps * MOM_NSEG * MOM_K;
+    const bool mom_on = sizeof(R) == 4 && a.far_series != 0;
+    const int nseg = W / MOM_SEG;
+    const int mseg = lane >> 2, mpart = lane & 3;  // this lane's segment and series terms
+    float mg0 = 0.f, mg1 = 0.f, mg2 = 0.f;
     __shared__ int64_t cls_lo[N_REACH_CLASSES];        // absolute index of the class's first contributing pair
     __shared__ int64_t cls_n[N_REACH_CLASSES];         // contributing pairs of the class
     __shared__ int64_t bat_base[N_REACH_CLASSES + 1];  // first batch of each class
@@ -981,8 +1022,40 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
                     wing_run<R, R2, CellT, false>(my, base, 1, max(rl, m + 1), nr, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                     wing_run<R, R2, CellT, false>(my, base, -1, max(bl, m + 1), nb, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                     if (nzi != 0x7fffffff) {
-                        far_run_x2(my, base, 1, max(rl, nzi + 1), rh, lane, xfi);
-                        far_run_x2(my, base, -1, max(bl, nzi + 1), bh, lane, xfi);
+                        const int r_lo = max(rl, nzi + 1), b_lo = max(bl, nzi + 1);
+                        if (mom_on) {
+                            // segments whole inside the red / blue far run and at least
+                            // MOM_DMIN bins from the centre go to the series, the rest of
+                            // the run bin by bin
+                            int ra = 1, rb = 0, ba = 1, bb = 0;
+                            if (r_lo <= rh) {
+                                ra = max(max((base + r_lo + MOM_SEG - 1) >> 7, (base + MOM_DMIN + MOM_SEG - 1) >> 7), 0);
+                                rb = min(((base + rh + 1) >> 7) - 1, nseg - 1);
+                            }
+                            if (b_lo <= bh) {
+                                ba = max((base - bh + MOM_SEG - 1) >> 7, 0);
+                                bb = min(min(((base - b_lo + 1) >> 7) - 1, (base - MOM_DMIN - (MOM_SEG - 1)) >> 7),
+                                         nseg - 1);
+                            }
+                            if ((ra <= mseg && mseg <= rb) || (ba <= mseg && mseg <= bb))
+                                far_series_add(mg0, mg1, mg2, mpart, (float)(mseg * MOM_SEG - base) + 63.5f,
+                                               (float)xfi);
+                            if (ra <= rb) {
+                                far_run_x2(my, base, 1, r_lo, ra * MOM_SEG - base - 1, lane, xfi);
+                                far_run_x2(my, base, 1, rb * MOM_SEG + MOM_SEG - base, rh, lane, xfi);
+                            } else {
+                                far_run_x2(my, base, 1, r_lo, rh, lane, xfi);
+                            }
+                            if (ba <= bb) {
+                                far_run_x2(my, base, -1, b_lo, base - bb * MOM_SEG - MOM_SEG, lane, xfi);
+                                far_run_x2(my, base, -1, base - ba * MOM_SEG + 1, bh, lane, xfi);
+                            } else {
+                                far_run_x2(my, base, -1, b_lo, bh, lane, xfi);
+                            }
+                        } else {
+                            far_run_x2(my, base, 1, r_lo, rh, lane, xfi);
+                            far_run_x2(my, base, -1, b_lo, bh, lane, xfi);
+                        }
                     }
                 } else {
                     wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
@@ -1001,8 +1074,24 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         kb_n = kb_nn;
         cnt_n = cnt_nn;
     }
+    if (mom_on) {
+        float* mw = mom_w + (warp * MOM_NSEG + mseg) * MOM_K;
+        mw[mpart] = mg0;
+        mw[mpart + 4] = mg1;
+        mw[mpart + 8] = mg2;
+    }
     __syncthreads();
-    // combine the warp copies in warp order, apply STIM and store
+    if (mom_on) {
+        // series coefficients of each segment, summed over the warps in order
+        for (int i = threadIdx.x; i < MOM_NSEG * MOM_K; i += blockDim.x) {
+            float t = 0.f;
+            for (int w = 0; w < nwarps; w++) t += mom_w[w * MOM_NSEG * MOM_K + i];
+            mom_sum[i] = t;
+        }
+        __syncthreads();
+    }
+    // combine the warp copies in warp order, add the far-wing series, apply
+    // STIM and store
     const DepthPar dp = a.depth[d];
     for (int b = threadIdx.x; b < span; b += blockDim.x) {
         R v;
@@ -1010,6 +1099,14 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
             float s = 0.f, cp = 0.f;
             for (int w = 0; w < nwarps; w++) {
                 kahan_add(s, cp, acc[w * W + b]);
+            }
+            if (mom_on) {
+                const float* ms = mom_sum + (b >> 7) * MOM_K;
+                const float u = ((float)(b & (MOM_SEG - 1)) - 63.5f) * (1.0f / 64.0f);
+                float f = ms[MOM_K - 1];
+#pragma unroll
+                for (int k = MOM_K - 2; k >= 0; k--) f = fmaf(f, u, ms[k]);
+                kahan_add(s, cp, f);
             }
             const float freq = a.freq_f[T0 + b];
             float stim = -expm1f(-freq * (float)dp.hkt_asynth);
@@ -1072,10 +1169,47 @@ __device__ __forceinline__ void parcoe_raw(const R* f, const R* x, int n, int j,
 }
 
 // INTEG (josh_solver.py:171-189) over PARCOE with its smoothing pass
-// (:154-166) folded in, streaming over the layers.  FP32 accumulates tau
-// with Kahan compensation.
+// (:154-166) folded in, streaming over the layers.
+//
+// FP64 evaluates each interval's integral from the polynomial's coefficients
+// in absolute column mass, a + b x + c x^2, as the reference does.  In FP32
+// that form cancels (the coefficients are large against the interval), so
+// the FP32 path uses the equivalent local form: every PARCOE polynomial of
+// interval i -- the line of the first and last intervals and of the
+// overridden second and third, the Newton parabolas through three
+// neighbouring points, and the smoothing blend of two parabolas that share
+// the interval's end points -- passes through (x_i, f_i) and
+// (x_{i+1}, f_{i+1}), so its integral is h (f_i + f_{i+1}) / 2 - c_i h^3 / 6
+// with h = x_{i+1} - x_i and c_i the smoothed curvature.  Only c is needed;
+// the integral is accumulated with Kahan compensation.
 template <typename R>
 __device__ void integ_tau(const R* x, const R* f, int n, R start, R* fint) {
+    if constexpr (sizeof(R) == 4) {
+        fint[0] = start;
+        if (n == 1) return;
+        float ci = 0.f, cn = 0.f, a_, b_;  // curvature at i and i+1 after the overrides
+        if (n > 2) parcoe_raw<R>(f, x, n, 1, a_, b_, cn);
+        float s = start, comp = 0.f;
+        for (int i = 0; i < n - 1; i++) {
+            float c_i = ci;
+            if (i >= 1 && i <= n - 2) {
+                if (i == n - 2) {
+                    c_i = 0.f;
+                } else if (ci != 0.f) {
+                    const float acn = fabsf(cn);
+                    const float den = acn + fabsf(ci);
+                    const float wt = den > 0.f ? tdiv(acn, den) : 0.f;
+                    c_i = cn + wt * (ci - cn);
+                }
+            }
+            const float dx = x[i + 1] - x[i];
+            kahan_add(s, comp, dx * (0.5f * (f[i] + f[i + 1]) - c_i * dx * dx * (1.0f / 6.0f)));
+            fint[i + 1] = s;
+            ci = cn;
+            if (i + 2 <= n - 1) parcoe_raw<R>(f, x, n, i + 2, a_, b_, cn);
+        }
+        return;
+    }
     fint[0] = start;
     if (n == 1) return;
     if (n == 2) {
@@ -1692,27 +1826,12 @@ struct TsMap {
     }
 };
 
-// PARCOE coefficients at layer j from f[j-1], f[j], f[j+1] (fm, f0, fp),
-// the cases of parcoe_raw for j >= 2.
-__device__ __forceinline__ void ts_parcoe(const float* x, int n, int j, float fm, float f0, float fp,
-                                          float& a, float& b, float& c) {
-    if (j == 2 && n > 3) {
-        const float den = x[j + 1] - x[j];
-        b = den != 0.f ? tdiv(fp - f0, den) : 0.f;
-        a = f0 - x[j] * b;
-        c = 0.f;
-        return;
-    }
-    if (j == n - 1) {
-        const float den = x[j] - x[j - 1];
-        b = den != 0.f ? tdiv(f0 - fm, den) : 0.f;
-        a = f0 - x[j] * b;
-        c = 0.f;
-        return;
-    }
+// PARCOE curvature at layer j from f[j-1], f[j], f[j+1] (fm, f0, fp), the
+// cases of parcoe_raw for j >= 2 (the local-form integral of integ_tau needs
+// no other coefficient).
+__device__ __forceinline__ float ts_parcoe_c(const float* x, int n, int j, float fm, float f0, float fp) {
+    if ((j == 2 && n > 3) || j == n - 1) return 0.f;
     const int j1 = j - 1;
-    const float den = x[j] - x[j1];
-    const float dd = den != 0.f ? tdiv(f0 - fm, den) : 0.f;
     const float den1 = (x[j + 1] - x[j]) * (x[j + 1] - x[j1]);
     const float term1 = den1 != 0.f ? tdiv(fp, den1) : 0.f;
     const float den2 = x[j + 1] - x[j1];
@@ -1724,9 +1843,7 @@ __device__ __forceinline__ void ts_parcoe(const float* x, int n, int j, float fm
         const float t2 = den3 != 0.f ? tdiv(f0, den3) : 0.f;
         part = tdiv(t1 - t2, den4);
     }
-    c = term1 + part;
-    b = dd - (x[j] + x[j1]) * c;
-    a = fm - x[j1] * dd + x[j] * x[j1] * c;
+    return term1 + part;
 }
 
 // One JOSH solve of one column, streamed; returns the sweep count, or 0 when
@@ -1760,45 +1877,29 @@ __device__ __forceinline__ int ts_solve(const TransferArgs& a, const CoefJ32& cj
     m.out = col;
     m.xtau = s_xtau;
     m.push(tau0, N0, G0);
-    // INTEG (josh_solver.py:171-189) with PARCOE's smoothing folded in
+    // INTEG (josh_solver.py:171-189) with PARCOE's smoothing folded in, in
+    // the local form of integ_tau (interval integral h (f_i + f_{i+1}) / 2 -
+    // c_i h^3 / 6; the curvature of layers 0 and 1 is 0 by PARCOE's overrides)
     const float* x = s_x;
-    float ai, bi, ci, an, bn, cn;
-    {
-        const float d0 = x[1] - x[0];
-        bi = d0 != 0.f ? tdiv(F1 - F0, d0) : 0.f;
-        ai = F0 - x[0] * bi;
-        ci = 0.f;
-        const float d1 = x[2] - x[1];
-        bn = d1 != 0.f ? tdiv(F2 - F1, d1) : 0.f;
-        an = F1 - x[1] * bn;
-        cn = 0.f;
-    }
+    float ci = 0.f, cn = 0.f;
     float s = tau0, comp = 0.f;
     for (int i = 0; i < n - 1; i++) {
-        float a_i = ai, b_i = bi, c_i = ci;
+        float c_i = ci;
         if (i >= 1) {
             if (i == n - 2) {
-                const float den = x[n - 1] - x[n - 2];
-                b_i = den != 0.f ? tdiv(F1 - F0, den) : 0.f;
-                a_i = F1 - x[n - 1] * b_i;
                 c_i = 0.f;
             } else if (ci != 0.f) {
                 const float acn = fabsf(cn);
                 const float den = acn + fabsf(ci);
                 const float wt = den > 0.f ? tdiv(acn, den) : 0.f;
-                a_i = an + wt * (ai - an);
-                b_i = bn + wt * (bi - bn);
                 c_i = cn + wt * (ci - cn);
             }
         }
-        const float xa = x[i], xb = x[i + 1];
-        const float dx = xb - xa;
-        float term = a_i + 0.5f * b_i * (xb + xa);
-        term += (c_i / 3.f) * ((xb + xa) * xb + xa * xa);
-        kahan_add(s, comp, term * dx);
+        const float dx = x[i + 1] - x[i];
+        kahan_add(s, comp, dx * (0.5f * (F0 + F1) - c_i * dx * dx * (1.0f / 6.0f)));
         m.push(s, N1, G1);
-        ai = an; bi = bn; ci = cn;
-        if (i + 2 <= n - 1) ts_parcoe(x, n, i + 2, F1, F2, F3, an, bn, cn);
+        ci = cn;
+        if (i + 2 <= n - 1) cn = ts_parcoe_c(x, n, i + 2, F1, F2, F3);
         F0 = F1; F1 = F2; F2 = F3;
         N0 = N1; N1 = N2; N2 = N3;
         G0 = G1; G1 = G2; G2 = G3;

@@ -47,9 +47,12 @@ def test_flag_surfaces_without_stats(precision):
         check_flags()
     assert e.value.code == 7 and "N10DOP" in str(e.value)
     check_flags()  # taken and cleared by the check above
-    # the same call with stats reports its own flags directly
+    # the same call with stats reports its own flags directly, and also
+    # leaves them in the sticky word (every flag since the last check)
     with pytest.raises(_native.KsError):
         syn.run(stats=True)
+    with pytest.raises(_native.KsError):
+        check_flags()
     check_flags()
 
 
