@@ -125,11 +125,6 @@ typedef struct {
     int32_t exact_sweeps;   /* FP64 precision only: 1 = solve the JOSH Gauss-Seidel system in FP64
                                to 1e-13 instead of the reference's FP32 sweep at 1e-5 (the
                                forward of the differentiable form, smooth in the inputs) */
-    int32_t far_series;     /* KS_PREC_MIXED with tile_bins a multiple of 128, <= 1024: far-wing
-                               contributions X/o^2 to 128-bin segments lying whole inside a far
-                               run at >= 256 bins from the line centre are accumulated as a
-                               12-term series per segment (truncation < 1e-7 relative); 0 =
-                               default (on), -1 = off (every contribution added bin by bin) */
 } ks_options;
 
 /* Counters of one synthesis (filled when a pointer is given). */

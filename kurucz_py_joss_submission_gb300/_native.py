@@ -70,7 +70,7 @@ class KsOptions(C.Structure):
         ("cutoff", C.c_double), ("microturb_kms", C.c_double), ("rhoxj", C.c_double),
         ("precision", C.c_int32), ("tile_bins", C.c_int32), ("warps_per_tile", C.c_int32),
         ("profile", C.c_int32), ("short_class", C.c_int32), ("transfer_path", C.c_int32),
-        ("long_class", C.c_int32), ("exact_sweeps", C.c_int32), ("far_series", C.c_int32),
+        ("long_class", C.c_int32), ("exact_sweeps", C.c_int32),
     ]
 
 

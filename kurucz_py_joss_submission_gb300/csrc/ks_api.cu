@@ -363,28 +363,33 @@ __global__ void grid_params_kernel(const double* g, int64_t n, double grid_origi
 
 // Centre bins (opacity.py:550-592) and wing bins (line_opacity.py:1030-1059)
 // per line, plus the single-precision line copies of the mixed path.  Flags
-// non-monotone wing bins (the accumulation searches them).
+// non-monotone wing bins (the accumulation searches them); the previous
+// line's wing bin comes from the neighbouring lane (lane 0 computes it).
+__device__ __forceinline__ int64_t wing_bin(double w, const GridPar& gp) {
+    return (int64_t)rint(log(w / gp.wbegin) / gp.ratiolg) - gp.grid_offset;
+}
+
 __global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __restrict__ wl,
                                  const GridPar* __restrict__ gpp, int32_t* center_out,
                                  int32_t* wing_out, const double* cgf, const double* elo,
                                  const double* gr, const double* gs, const double* gw,
                                  const double* gf, LineF* linef, int* flags) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_lines) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < n_lines;
     const GridPar gp = *gpp;
-    double w = wl[i];
+    const double w = act ? wl[i] : (n_lines > 0 ? wl[n_lines - 1] : 1.0);
     int64_t c = 0, wb = 0;
-    if (n_wl >= 2) {
+    if (n_wl >= 2) {  // uniform across the grid
         c = (int64_t)(log(w) / gp.ratiolg + 0.5) - gp.ix_start;
         if (w < gp.first) c = -1;
         if (w > gp.last) c = n_wl;
-        wb = (int64_t)rint(log(w / gp.wbegin) / gp.ratiolg) - gp.grid_offset;
-        if (i > 0) {
-            double wp = wl[i - 1];
-            int64_t wbp = (int64_t)rint(log(wp / gp.wbegin) / gp.ratiolg) - gp.grid_offset;
-            if (wbp > wb) atomicOr(flags, 8);
-        }
+        wb = wing_bin(w, gp);
+        int64_t wbp = __shfl_up_sync(0xffffffffu, wb, 1);
+        const int lane = threadIdx.x & 31;
+        if (lane == 0 && act && i > 0) wbp = wing_bin(wl[i - 1], gp);
+        if (act && i > 0 && wbp > wb) atomicOr(flags, 8);
     }
+    if (!act) return;
     if (center_out) center_out[i] = (int32_t)c;
     if (wing_out) wing_out[i] = (int32_t)wb;
     if (linef) {
@@ -824,8 +829,6 @@ static AccArgs acc_args(const ks_lines* l, const ks_atmos* atm, const ks_grid* g
     a.short_class = !opt || opt->short_class == 0 ? SHORT_CLASS
                     : opt->short_class < 0 ? 0 : min(opt->short_class, N_REACH_CLASSES);
     a.long_class = !opt || opt->long_class <= 0 ? LONG_CLASS : min(opt->long_class, N_REACH_CLASSES);
-    a.far_series = !fp64 && (opt && opt->far_series > 0) && a.tile_bins % MOM_SEG == 0 &&
-                   a.tile_bins <= MOM_SEG * MOM_NSEG;
     a.grid = g->wavelength;
     a.wing_idx = w.wing;
     a.class_pos = w.class_pos;

@@ -21,13 +21,6 @@ constexpr int NXTAU = 51;                   // JOSH optical-depth grid
 constexpr int MAX_LAYERS = 128;             // per-wavelength column bound
 constexpr int MAX_EDGES = 1024;             // continuum edges (the reference's tables have 341)
 constexpr int N_REACH_CLASSES = 22;         // reach classes 0..21 (2^20 > MAXPROF)
-// Far-wing series of the FP32 accumulation: 128-bin segments, 12 terms, used
-// for segments whose nearest bin is at least 256 bins from the line centre
-// (series ratio |t / D| <= 63.5 / 319.5 < 0.2: truncation <= 7e-8 relative).
-constexpr int MOM_SEG = 128;
-constexpr int MOM_NSEG = 8;                 // segments of a tile (tiles of up to 1024 bins)
-constexpr int MOM_K = 12;                   // series terms per segment
-constexpr int MOM_DMIN = 256;
 constexpr int LONG_CLASS = 8;               // default: classes 8+ (reach > 128 bins) in batches of 8 pairs
 constexpr int SHORT_CLASS = 7;              // default: classes 0-6 (reach <= 64 bins) one lane per pair
 constexpr double EPS38 = 1.0e-38;

@@ -107,7 +107,6 @@ struct AccArgs {
     int n_layers, tile_bins;
     int short_class;            // reach classes below it are accumulated one lane per pair
     int long_class;             // reach classes from it are dealt in batches of 8 pairs
-    int far_series;             // FP32: far wings of whole distant segments as a series (0: all exact)
     const double *grid;
     const int32_t *wing_idx;
     const int32_t *class_pos;   // per depth, per class: line positions, ascending

@@ -762,31 +762,6 @@ __device__ __forceinline__ void far_run_x2(float* my, int base, int sgn, int lo,
     }
 }
 
-// Far-wing series of one segment (FP32 accumulation).  A far run adds X / o^2
-// to every bin b it covers, o = |b - c| (line_opacity.py:577-579).  For a
-// 128-bin segment with centre m that lies whole inside the run, with
-// D = m - c and t = b - m (|t / D| < 0.2 from the segment's distance),
-//   X / (D + t)^2 = sum_k (k + 1) (X / D^2) (-64 / D)^k (t / 64)^k,
-// so the segment needs only M_k = sum over its runs of (k + 1) (X / D^2)
-// (-64 / D)^k, k < MOM_K (truncation below 1e-7 relative).  Lane 4 s + j of
-// a warp keeps M_j, M_{j+4}, M_{j+8} of segment s in registers; this adds
-// one run at distance `dist` = D.
-static_assert(MOM_SEG == 128 && MOM_K == 12 && MOM_NSEG * 4 == 32, "series layout: 8 segments x 4 lanes x 3 terms");
-__device__ __forceinline__ void far_series_add(float& m0, float& m1, float& m2, int part, float dist, float xf) {
-    const float inv = __frcp_rn(dist);
-    const float rho = -64.0f * inv;
-    const float amp = xf * inv * inv;
-    const float r2 = rho * rho, r4 = r2 * r2;
-    const float pj = part == 0 ? 1.0f : (part == 1 ? rho : (part == 2 ? r2 : r2 * rho));
-    const float t0 = amp * pj;
-    const float t1 = t0 * r4;
-    const float t2 = t1 * r4;
-    const float c = (float)(part + 1);
-    m0 = fmaf(c, t0, m0);
-    m1 = fmaf(c + 4.0f, t1, m1);
-    m2 = fmaf(c + 8.0f, t2, m2);
-}
-
 // Adds v to a bin of the warp's own copy with a shared-memory atomic (the
 // short pairs, where two lanes may hit one bin).  Only lanes of one warp
 // touch a copy, and a warp's atomics to one word are applied in a fixed
@@ -830,13 +805,6 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     R2* h01 = reinterpret_cast<R2*>(smem_raw);  // interleaved (H0, H1)
     size_t tab_bytes = (VOIGT_N * sizeof(R2) + 15) & ~size_t(15);
     CellT* acc = reinterpret_cast<CellT*>(smem_raw + tab_bytes);  // [nwarps][W]
-    // far-wing series (FP32): per warp [MOM_NSEG][MOM_K], then their sum
-    float* mom_w = reinterpret_cast<float*>(acc + (size_t)nwarps * W);
-    float* mom_sum = mom_w + nwarps * MOM_NSEG * MOM_K;
-    const bool mom_on = sizeof(R) == 4 && a.far_series != 0;
-    const int nseg = W / MOM_SEG;
-    const int mseg = lane >> 2, mpart = lane & 3;  // this lane's segment and series terms
-    float mg0 = 0.f, mg1 = 0.f, mg2 = 0.f;
     __shared__ int64_t cls_lo[N_REACH_CLASSES];        // absolute index of the class's first contributing pair
     __shared__ int64_t cls_n[N_REACH_CLASSES];         // contributing pairs of the class
     __shared__ int64_t bat_base[N_REACH_CLASSES + 1];  // first batch of each class
@@ -1022,40 +990,8 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
                     wing_run<R, R2, CellT, false>(my, base, 1, max(rl, m + 1), nr, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                     wing_run<R, R2, CellT, false>(my, base, -1, max(bl, m + 1), nb, lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
                     if (nzi != 0x7fffffff) {
-                        const int r_lo = max(rl, nzi + 1), b_lo = max(bl, nzi + 1);
-                        if (mom_on) {
-                            // segments whole inside the red / blue far run and at least
-                            // MOM_DMIN bins from the centre go to the series, the rest of
-                            // the run bin by bin
-                            int ra = 1, rb = 0, ba = 1, bb = 0;
-                            if (r_lo <= rh) {
-                                ra = max(max((base + r_lo + MOM_SEG - 1) >> 7, (base + MOM_DMIN + MOM_SEG - 1) >> 7), 0);
-                                rb = min(((base + rh + 1) >> 7) - 1, nseg - 1);
-                            }
-                            if (b_lo <= bh) {
-                                ba = max((base - bh + MOM_SEG - 1) >> 7, 0);
-                                bb = min(min(((base - b_lo + 1) >> 7) - 1, (base - MOM_DMIN - (MOM_SEG - 1)) >> 7),
-                                         nseg - 1);
-                            }
-                            if ((ra <= mseg && mseg <= rb) || (ba <= mseg && mseg <= bb))
-                                far_series_add(mg0, mg1, mg2, mpart, (float)(mseg * MOM_SEG - base) + 63.5f,
-                                               (float)xfi);
-                            if (ra <= rb) {
-                                far_run_x2(my, base, 1, r_lo, ra * MOM_SEG - base - 1, lane, xfi);
-                                far_run_x2(my, base, 1, rb * MOM_SEG + MOM_SEG - base, rh, lane, xfi);
-                            } else {
-                                far_run_x2(my, base, 1, r_lo, rh, lane, xfi);
-                            }
-                            if (ba <= bb) {
-                                far_run_x2(my, base, -1, b_lo, base - bb * MOM_SEG - MOM_SEG, lane, xfi);
-                                far_run_x2(my, base, -1, base - ba * MOM_SEG + 1, bh, lane, xfi);
-                            } else {
-                                far_run_x2(my, base, -1, b_lo, bh, lane, xfi);
-                            }
-                        } else {
-                            far_run_x2(my, base, 1, r_lo, rh, lane, xfi);
-                            far_run_x2(my, base, -1, b_lo, bh, lane, xfi);
-                        }
+                        far_run_x2(my, base, 1, max(rl, nzi + 1), rh, lane, xfi);
+                        far_run_x2(my, base, -1, max(bl, nzi + 1), bh, lane, xfi);
                     }
                 } else {
                     wing_run<R, R2, CellT, false>(my, base, 1, rl, min(rh, nzi), lane, k0i, adi, dvi, ts, xfi, h01, gh0, gh1, gh2);
@@ -1074,24 +1010,8 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         kb_n = kb_nn;
         cnt_n = cnt_nn;
     }
-    if (mom_on) {
-        float* mw = mom_w + (warp * MOM_NSEG + mseg) * MOM_K;
-        mw[mpart] = mg0;
-        mw[mpart + 4] = mg1;
-        mw[mpart + 8] = mg2;
-    }
     __syncthreads();
-    if (mom_on) {
-        // series coefficients of each segment, summed over the warps in order
-        for (int i = threadIdx.x; i < MOM_NSEG * MOM_K; i += blockDim.x) {
-            float t = 0.f;
-            for (int w = 0; w < nwarps; w++) t += mom_w[w * MOM_NSEG * MOM_K + i];
-            mom_sum[i] = t;
-        }
-        __syncthreads();
-    }
-    // combine the warp copies in warp order, add the far-wing series, apply
-    // STIM and store
+    // combine the warp copies in warp order, apply STIM and store
     const DepthPar dp = a.depth[d];
     for (int b = threadIdx.x; b < span; b += blockDim.x) {
         R v;
@@ -1099,14 +1019,6 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
             float s = 0.f, cp = 0.f;
             for (int w = 0; w < nwarps; w++) {
                 kahan_add(s, cp, acc[w * W + b]);
-            }
-            if (mom_on) {
-                const float* ms = mom_sum + (b >> 7) * MOM_K;
-                const float u = ((float)(b & (MOM_SEG - 1)) - 63.5f) * (1.0f / 64.0f);
-                float f = ms[MOM_K - 1];
-#pragma unroll
-                for (int k = MOM_K - 2; k >= 0; k--) f = fmaf(f, u, ms[k]);
-                kahan_add(s, cp, f);
             }
             const float freq = a.freq_f[T0 + b];
             float stim = -expm1f(-freq * (float)dp.hkt_asynth);

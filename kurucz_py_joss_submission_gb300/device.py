@@ -173,7 +173,7 @@ def check_flags(stream: Optional[torch.cuda.Stream] = None) -> None:
 
 def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", tile_bins=0,
                  warps_per_tile=0, profile=False, short_class=0,
-                 transfer_path=0, long_class=0, exact_sweeps=0, far_series=0) -> _native.KsOptions:
+                 transfer_path=0, long_class=0, exact_sweeps=0) -> _native.KsOptions:
     opt = _native.KsOptions()
     opt.cutoff = float(cutoff)
     opt.microturb_kms = float(microturb_kms)
@@ -186,7 +186,6 @@ def make_options(cutoff=1e-3, microturb_kms=0.0, rhoxj=0.0, precision="mixed", t
     opt.transfer_path = int(transfer_path)
     opt.long_class = int(long_class)
     opt.exact_sweeps = int(exact_sweeps)
-    opt.far_series = int(far_series)
     return opt
 
 
