@@ -311,6 +311,55 @@ ks_status ks_synthesize_noalloc(const ks_lines *lines, const ks_atmos *atm, cons
                                 const ks_options *opt, double *flux_total, double *flux_cont,
                                 void *asynth_out, void *stream);
 
+/* ---- batched synthesis -------------------------------------------------------- */
+
+/* One job of a batch: an atmosphere, its own wavelength grid (window), the
+ * rows of the batch's shared line list that lie in the window, and where its
+ * fluxes go.  atm and grid are host pointers to records whose arrays are on
+ * the device; they are read when the plan is made. */
+typedef struct {
+    const ks_atmos *atm;
+    const ks_grid *grid;
+    int64_t line_first;     /* first row of the shared (wavelength-sorted) list */
+    int64_t line_count;     /* rows in the job's window */
+    double *flux_total;     /* device, [grid->n], F_nu at the surface */
+    double *flux_cont;      /* device, [grid->n] */
+} ks_job;
+
+/* A plan for running many syntheses over one shared line list as one batch:
+ * every stage of ks_synthesize (bins, per-depth state, continuum, TRANSP and
+ * wing setup, reach-class partition, accumulation, transfer) is one
+ * persistent launch over all jobs -- blocks walk a device table of
+ * (job, block) work items with a precomputed per-job prefix, no atomics --
+ * 15 launches per batch whatever the number of jobs.  Each job gets the
+ * results a ks_synthesize call with the same options gives (bit for bit).
+ * The options (precision, tiling, cutoff, microturbulence, RHOXJ) are shared
+ * by all jobs.  No reference counterpart: the reference synthesises one
+ * atmosphere per run (synthe_py/engine/opacity.py:2084); this replaces a
+ * loop of run_synthesis calls.
+ *
+ * ks_batch_workspace_size: device bytes the plan needs (its job tables plus
+ * one ks_synthesize workspace per job).
+ * ks_batch_create: lays the jobs out in `workspace` (device, 256-byte
+ * aligned, owned by the caller and kept alive with the plan) and copies the
+ * job tables to it synchronously -- call it before any stream capture.
+ * ks_batch_run: enqueues the batch on `stream` (launches only, so it can be
+ * recorded in a CUDA graph and replayed); with stats it synchronises and
+ * returns the counters summed over the jobs (profile option: stage times).
+ * ks_batch_free: releases the host plan (not the workspace).
+ * ks_synthesize_batch: create, run and free in one call. */
+typedef struct ks_batch ks_batch;
+ks_status ks_batch_workspace_size(const ks_lines *lines, const ks_job *jobs, int32_t n_jobs,
+                                  const ks_options *opt, size_t *bytes);
+ks_status ks_batch_create(const ks_lines *lines, const ks_job *jobs, int32_t n_jobs,
+                          const ks_options *opt, void *workspace, size_t workspace_bytes,
+                          ks_batch **out);
+ks_status ks_batch_run(ks_batch *plan, ks_stats *stats, void *stream);
+void ks_batch_free(ks_batch *plan);
+ks_status ks_synthesize_batch(const ks_lines *lines, const ks_job *jobs, int32_t n_jobs,
+                              const ks_options *opt, void *workspace, size_t workspace_bytes,
+                              ks_stats *stats, void *stream);
+
 /* ---- gfall reader ---------------------------------------------------------- */
 
 /* Native reader of gfall line lists (synthe_py/io/lines/atomic.py:299

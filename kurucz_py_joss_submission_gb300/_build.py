@@ -1,10 +1,12 @@
 """Build of the native library ``_lib/libkurucz_gb300.so`` (sm_103a only).
 
-Four translation units compiled in parallel with nvcc and linked into one
+Six translation units compiled in parallel with nvcc and linked into one
 shared library exporting the C ABI of ``include/kurucz_gb300.h``:
 
 * ``ks_f32.cu``  kernels in single precision (mixed path)
+* ``ks_f32_batch.cu`` their batched launches (one per stage over a job table)
 * ``ks_f64.cu``  kernels in double precision, ``--fmad=false``
+* ``ks_f64_batch.cu`` their batched launches
 * ``ks_api.cu``  C ABI, tables, bins, reach-class partition, drivers
 * ``ks_gfall.cpp`` native gfall reader
 """
@@ -37,7 +39,9 @@ def _units():
                      "--expt-relaxed-constexpr"]
     return [
         (CSRC / "ks_f32.cu", common),
+        (CSRC / "ks_f32_batch.cu", common),
         (CSRC / "ks_f64.cu", common + ["--fmad=false"]),
+        (CSRC / "ks_f64_batch.cu", common + ["--fmad=false"]),
         (CSRC / "ks_api.cu", common),
         (CSRC / "ks_gfall.cpp", ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread"]),
     ]

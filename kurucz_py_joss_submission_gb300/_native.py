@@ -74,6 +74,17 @@ class KsOptions(C.Structure):
     ]
 
 
+class KsJob(C.Structure):
+    """One job of a batch (ks_job): host pointers to its atmosphere and grid
+    records, its rows of the shared line list, device outputs."""
+
+    _fields_ = [
+        ("atm", C.POINTER(KsAtmos)), ("grid", C.POINTER(KsGrid)),
+        ("line_first", C.c_int64), ("line_count", C.c_int64),
+        ("flux_total", P), ("flux_cont", P),
+    ]
+
+
 class KsStats(C.Structure):
     _fields_ = [
         ("valid_pairs", C.c_int64), ("evaluations", C.c_int64),
@@ -122,6 +133,14 @@ SIGNATURES = {
     "ks_synthesize_noalloc": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                           C.POINTER(KsOptions), P, P, P, P]),
     "ks_check_flags": (C.c_int32, [P, C.POINTER(C.c_int32)]),
+    "ks_batch_workspace_size": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsJob), C.c_int32,
+                                            C.POINTER(KsOptions), C.POINTER(C.c_size_t)]),
+    "ks_batch_create": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsJob), C.c_int32, C.POINTER(KsOptions),
+                                    P, C.c_size_t, C.POINTER(P)]),
+    "ks_batch_run": (C.c_int32, [P, C.POINTER(KsStats), P]),
+    "ks_batch_free": (None, [P]),
+    "ks_synthesize_batch": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsJob), C.c_int32,
+                                        C.POINTER(KsOptions), P, C.c_size_t, C.POINTER(KsStats), P]),
     "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,
                                   C.POINTER(P)]),
     "ks_gfall_sort": (C.c_int32, [P]),

@@ -1,40 +1,32 @@
-"""Autotuner of the accumulation's launch shape.
+"""Autotuner of the batched form's launch shape.
 
-The accumulation kernel's tile width (bins per CTA) and warps per tile trade
+The accumulation's tile width (bins per CTA), its warps per tile and the
+number of long-reach pairs dealt to a warp at once (``long_class``: classes
+from it go in batches of 8 pairs, the shorter ones in batches of 32) trade
 per-CTA fixed costs (staging the Voigt table, class ranges, the epilogue)
-against occupancy and the number of tiles a long wing is read by; the best
-choice depends on the grid size and the line density.  ``tune`` times each
-candidate on a representative job with the library's own stage timers
-(CUDA events on the launching stream) and keeps the fastest; results are
-cached per (device name, precision, size class) in a JSON file next to the
-built library.
+against occupancy, load balance and the number of tiles a long wing is read
+by; the best choice depends on the grid sizes and the line density of the
+batch.  :func:`tune` builds the batch plan for each candidate (sharing one
+workspace), times whole batch runs with CUDA events on the launching stream
+and keeps the fastest; results are cached per (device name, precision,
+batch signature) in a JSON file next to the built library.
 """
 
 from __future__ import annotations
 
-import ctypes as C
+import hashlib
 import json
 import os
 from pathlib import Path
-from typing import Dict, Optional
+from typing import Callable, Optional
 
 import torch
 
-from . import _build, _native
-from .device import _ptr, make_options
+from . import _build
 
-CANDIDATES = [dict(tile_bins=t, warps_per_tile=w) for t in (256, 512, 1024) for w in (4, 8)]
+CANDIDATES = ([dict(tile_bins=t, warps_per_tile=w, long_class=lc) for t in (512, 1024) for w in (4, 8)
+               for lc in (8, 10)] + [dict(tile_bins=2048, warps_per_tile=8, long_class=lc) for lc in (8, 10)])
 CACHE = Path(os.environ.get("KS_AUTOTUNE_CACHE", str(_build.OUT_DIR / "autotune.json")))
-
-
-def _time_total(lib, view, atm_rec, grid_rec, opt, ws: torch.Tensor, ft, fc, reps: int) -> float:
-    best = float("inf")
-    for _ in range(reps):
-        st = _native.KsStats()
-        _native.check(lib.ks_synthesize(C.byref(view), C.byref(atm_rec), C.byref(grid_rec), C.byref(opt),
-                                        _ptr(ws), ws.numel(), _ptr(ft), _ptr(fc), None, C.byref(st), None))
-        best = min(best, float(st.stage_ms[7]))
-    return best
 
 
 def _load_cache() -> dict:
@@ -44,44 +36,57 @@ def _load_cache() -> dict:
         return {}
 
 
-def tune(batch, reps: int = 3, use_cache: bool = True) -> Dict[int, dict]:
-    """Best candidate per size class of ``batch`` (a BatchSynthesizer built
-    without tuned options); returns {size class: options}."""
-    from .batch import bucket
+def signature(jobs, n_lines: int, layers) -> str:
+    """A key for a batch: its jobs' windows and atmospheres and the list size."""
+    h = hashlib.sha256()
+    h.update(repr((n_lines, [(j.atmosphere, round(j.wl_start, 6), round(j.wl_end, 6)) for j in jobs],
+                   list(layers))).encode())
+    return h.hexdigest()[:16]
 
-    lib = _native.load()
+
+def time_batch(bs, reps: int = 3) -> float:
+    """Best of ``reps`` runs of a batch plan, ms (CUDA events on the current stream)."""
+    bs.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = float("inf")
+    for _ in range(reps):
+        e0.record()
+        bs.run()
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def tune(make_batch: Callable[..., object], key: str, precision: str, reps: int = 3,
+         use_cache: bool = True, log: Optional[Callable[[str], None]] = None) -> dict:
+    """The fastest candidate for a batch.  ``make_batch(options, workspace)``
+    builds the BatchSynthesizer with the given options (a dict of
+    make_options keywords) over the given workspace (None: allocate); ``key``
+    identifies the batch (see :func:`signature`)."""
     dev = torch.cuda.get_device_name()
     cache = _load_cache() if use_cache else {}
-    reps_job: Dict[int, int] = {}
-    for i, g in enumerate(batch.grids):
-        b = bucket(g.n)
-        if b not in reps_job or batch.views[i].n_lines > batch.views[reps_job[b]].n_lines:
-            reps_job[b] = i
-    out: Dict[int, dict] = {}
-    for b, i in sorted(reps_job.items()):
-        key = f"{dev}|{batch.precision}|{b}"
-        if key in cache:
-            out[b] = cache[key]
-            continue
-        j = batch.jobs[i]
-        best, best_t = None, float("inf")
-        for cand in CANDIDATES:
-            opt = make_options(precision=batch.precision, profile=True, **cand)
-            ws_n = C.c_size_t()
-            _native.check(lib.ks_workspace_size(batch.views[i].n_lines, batch.atm[j.atmosphere].n_layers,
-                                                batch.grids[i].n, C.byref(opt), C.byref(ws_n)))
-            ws = torch.empty(int(ws_n.value), dtype=torch.uint8, device=batch.grids[i].wavelength.device)
-            t = _time_total(lib, batch.views[i], batch.atm[j.atmosphere].rec, batch.grids[i].rec, opt, ws,
-                            batch.flux_total[i], batch.flux_cont[i], reps)
-            if t < best_t:
-                best, best_t = cand, t
-            del ws
-        out[b] = dict(best)
-        cache[key] = dict(best)
+    ck = f"{dev}|{precision}|{key}"
+    if ck in cache:
+        return dict(cache[ck])
+    ws = None
+    best, best_t = None, float("inf")
+    for cand in CANDIDATES:
+        bs = make_batch(cand, ws)
+        if ws is None or bs.workspace.numel() > ws.numel():
+            ws = bs.workspace
+        t = time_batch(bs, reps)
+        if log:
+            log(f"autotune {cand}: {t:.3f} ms")
+        if t < best_t:
+            best, best_t = dict(cand), t
+        del bs
     if use_cache:
+        cache[ck] = best
         try:
             CACHE.parent.mkdir(parents=True, exist_ok=True)
             CACHE.write_text(json.dumps(cache, indent=1))
         except OSError:
             pass
-    return out
+    return best

@@ -1,15 +1,18 @@
-"""Many syntheses in one captured CUDA graph: the batched form.
+"""Many syntheses as one batch: the batched form.
 
 Each job is one atmosphere (its own layer count) and one wavelength window
 (its own grid); all jobs share one line list resident in HBM.  The list is
 sorted by wavelength, so the lines inside a job's DELLIM window
 (synthe_py/io/lines/atomic.py:762-816, one margin for every non-hydrogen
-line) are a contiguous slice of it, handed to the library as a pointer view
-(no copy).  Jobs are spread over several CUDA streams, each stream with one
-workspace sized for its largest job; :meth:`BatchSynthesizer.capture`
-records the whole batch -- every job's continuum, TRANSP, ASYNTH and
-transfer launches on every stream -- as one CUDA graph, and
-:meth:`BatchSynthesizer.replay` launches it.  Per-job tile options come from
+line) are a contiguous slice of it, handed to the library as a row range
+(no copy).  :class:`BatchSynthesizer` makes one batch plan
+(``ks_batch_create``): every stage of the synthesis -- bins, per-depth
+state, continuum, TRANSP and wing setup, reach-class partition, accumulation,
+transfer -- runs as one persistent launch over all jobs (15 launches per
+batch, whatever the number of jobs), the blocks walking a device table of
+(job, block) work items.  :meth:`BatchSynthesizer.capture` records the batch
+as a CUDA graph and :meth:`BatchSynthesizer.replay` launches it.  The tile
+width, warps per tile and the pairs dealt to a warp at once come from
 :mod:`kurucz_py_joss_submission_gb300.autotune`.
 """
 
@@ -23,7 +26,7 @@ import numpy as np
 import torch
 
 from . import _native
-from .device import DeviceAtmosphere, DeviceCatalog, DeviceGrid, _ptr, check_flags, make_options
+from .device import DeviceAtmosphere, DeviceCatalog, DeviceGrid, _ptr, check_flags, make_options, stream_handle
 from .io.atmosphere import AtmosphereModel
 from .io.lines.atomic import DELLIM
 
@@ -55,98 +58,75 @@ def window_slice(wavelength_sorted: np.ndarray, wl_min: float, wl_max: float) ->
     return slice(i0, i1)
 
 
-def lines_view(cat: DeviceCatalog, rows: slice) -> _native.KsLines:
-    """A ks_lines record for rows [start, stop) of a device catalog."""
-    i0, n = rows.start, rows.stop - rows.start
-    rec = _native.KsLines()
-    rec.n_lines = n
-
-    def at(name, size):
-        return cat.t[name].data_ptr() + i0 * size
-
-    rec.wavelength = at("wavelength", 8)
-    rec.gf = at("gf", 8)
-    rec.cgf = at("cgf", 8)
-    rec.gamma_rad = at("gamma_rad", 8)
-    rec.gamma_stark = at("gamma_stark", 8)
-    rec.gamma_vdw = at("gamma_vdw", 8)
-    rec.elo_cm = at("excitation_energy", 8)
-    rec.element_idx = at("element_idx", 4)
-    rec.ion_stage = at("ion_stages", 4)
-    rec.line_type = at("line_types", 4)
-    rec.process_mask = at("process_mask", 1)
-    rec.asynth_mask = at("asynth_mask", 1)
-    rec.sorted_by_wavelength = 1
-    return rec
-
-
 class BatchSynthesizer:
-    """Fused syntheses of ``jobs`` over shared lines, on ``n_streams`` streams."""
+    """Fused syntheses of ``jobs`` over the shared lines of ``catalog``, as
+    one batch plan.  ``options`` (keywords of :func:`device.make_options`,
+    e.g. from :func:`autotune.tune`) apply to every job."""
 
     def __init__(self, catalog: DeviceCatalog, atmospheres: Sequence[AtmosphereModel], jobs: Sequence[Job],
-                 precision: str = "mixed", resolution: float = 300000.0, n_streams: int = 32,
-                 tuned: Optional[Dict[int, dict]] = None, device="cuda"):
+                 precision: str = "mixed", resolution: float = 300000.0, options: Optional[dict] = None,
+                 workspace: Optional[torch.Tensor] = None, device="cuda"):
         host = catalog.host
         if np.any((np.abs(host.code - 1.0) < 1e-6) | np.isin(host.line_types, [-1, -2]) |
                   (host.element_idx == 0)):
             raise ValueError("BatchSynthesizer: line lists with hydrogen lines need per-job catalogs")
+        if catalog.order is not None:
+            raise ValueError("BatchSynthesizer: the shared catalog must be sorted by wavelength")
         self.lib = _native.load()
         self.catalog = catalog
         self.jobs = list(jobs)
         self.precision = precision
+        self.option_keys = dict(options or {})
+        self.options = make_options(precision=precision, **self.option_keys)
         self.atm = [DeviceAtmosphere(a, device=device) for a in atmospheres]
         self.grids: List[DeviceGrid] = []
-        self.views: List[_native.KsLines] = []
-        self.options: List[_native.KsOptions] = []
+        self.rows: List[slice] = []
         self.flux_total: List[torch.Tensor] = []
         self.flux_cont: List[torch.Tensor] = []
-        self.ws_bytes: List[int] = []
         wl_sorted = np.asarray(host.wavelength)
-        tuned = tuned or {}
         for j in self.jobs:
-            g = wavelength_grid(j.wl_start, j.wl_end, resolution)
-            dg = DeviceGrid(g, device=device)
-            rows = window_slice(wl_sorted, j.wl_start, j.wl_end)
-            view = lines_view(catalog, rows)
-            t = tuned.get(bucket(dg.n), {})
-            opt = make_options(precision=precision, **t)
-            ws = C.c_size_t()
-            _native.check(self.lib.ks_workspace_size(view.n_lines, self.atm[j.atmosphere].n_layers, dg.n,
-                                                     C.byref(opt), C.byref(ws)))
-            self.grids.append(dg)
-            self.views.append(view)
-            self.options.append(opt)
-            self.ws_bytes.append(int(ws.value))
-            self.flux_total.append(torch.empty(dg.n, dtype=torch.float64, device=dg.wavelength.device))
-            self.flux_cont.append(torch.empty(dg.n, dtype=torch.float64, device=dg.wavelength.device))
-        # largest jobs first, dealt round-robin to the streams
-        order = sorted(range(len(self.jobs)), key=lambda i: -self.ws_bytes[i])
-        self.n_streams = max(1, min(n_streams, len(self.jobs)))
-        self.assign: List[List[int]] = [order[s::self.n_streams] for s in range(self.n_streams)]
+            g = DeviceGrid(wavelength_grid(j.wl_start, j.wl_end, resolution), device=device)
+            self.grids.append(g)
+            self.rows.append(window_slice(wl_sorted, j.wl_start, j.wl_end))
+            self.flux_total.append(torch.empty(g.n, dtype=torch.float64, device=g.wavelength.device))
+            self.flux_cont.append(torch.empty(g.n, dtype=torch.float64, device=g.wavelength.device))
+        n = len(self.jobs)
+        self.job_recs = (_native.KsJob * n)()
+        for i, j in enumerate(self.jobs):
+            r = self.job_recs[i]
+            r.atm = C.pointer(self.atm[j.atmosphere].rec)
+            r.grid = C.pointer(self.grids[i].rec)
+            r.line_first = self.rows[i].start
+            r.line_count = self.rows[i].stop - self.rows[i].start
+            r.flux_total = self.flux_total[i].data_ptr()
+            r.flux_cont = self.flux_cont[i].data_ptr()
+        ws = C.c_size_t()
+        _native.check(self.lib.ks_batch_workspace_size(C.byref(catalog.rec), self.job_recs, n,
+                                                       C.byref(self.options), C.byref(ws)))
         dev = self.grids[0].wavelength.device if self.grids else torch.device(device)
-        self.streams = [torch.cuda.Stream(device=dev) for _ in range(self.n_streams)]
-        self.workspaces = [torch.empty(max([self.ws_bytes[i] for i in a] or [1]), dtype=torch.uint8, device=dev)
-                           for a in self.assign]
+        self.workspace_bytes = int(ws.value)
+        if workspace is not None and workspace.numel() >= self.workspace_bytes:
+            self.workspace = workspace  # the caller's (e.g. shared by the autotuner's candidates)
+        else:
+            self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=dev)
+        self.plan = C.c_void_p()
+        _native.check(self.lib.ks_batch_create(C.byref(catalog.rec), self.job_recs, n, C.byref(self.options),
+                                               _ptr(self.workspace), self.workspace.numel(),
+                                               C.byref(self.plan)))
         self.graph: Optional[torch.cuda.CUDAGraph] = None
 
-    def _enqueue(self):
-        cur = torch.cuda.current_stream()
-        for s, stream in enumerate(self.streams):
-            stream.wait_stream(cur)
-            ws = self.workspaces[s]
-            for i in self.assign[s]:
-                status = self.lib.ks_synthesize(
-                    C.byref(self.views[i]), C.byref(self.atm[self.jobs[i].atmosphere].rec),
-                    C.byref(self.grids[i].rec), C.byref(self.options[i]), _ptr(ws), ws.numel(),
-                    _ptr(self.flux_total[i]), _ptr(self.flux_cont[i]), None, None,
-                    C.c_void_p(stream.cuda_stream))
-                _native.check(status)
-        for stream in self.streams:
-            cur.wait_stream(stream)
+    def __del__(self):
+        plan = getattr(self, "plan", None)
+        if plan is not None and plan.value:
+            self.lib.ks_batch_free(plan)
+            self.plan = None
 
-    def run(self):
-        """Enqueue every job on the current stream's device (no graph)."""
-        self._enqueue()
+    def run(self, stats: bool = False, stream: Optional[torch.cuda.Stream] = None):
+        """Enqueue the batch on the current stream (no graph); with ``stats``
+        synchronise and return the counters summed over the jobs."""
+        st = _native.KsStats()
+        _native.check(self.lib.ks_batch_run(self.plan, C.byref(st) if stats else None, stream_handle(stream)))
+        return st.as_dict() if stats else None
 
     def capture(self):
         """Record the batch as one CUDA graph (after one eager run, which
@@ -155,7 +135,7 @@ class BatchSynthesizer:
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, capture_error_mode="thread_local"):
-            self._enqueue()
+            self.run()
         self.graph = g
         return g
 
@@ -170,21 +150,12 @@ class BatchSynthesizer:
             check_flags()
 
     def evaluations(self) -> int:
-        """Total line.depth.lambda evaluations of the batch (one synchronous pass)."""
-        tot = 0
-        for i, j in enumerate(self.jobs):
-            st = _native.KsStats()
-            ws = self.workspaces[next(s for s, a in enumerate(self.assign) if i in a)]
-            _native.check(self.lib.ks_synthesize(
-                C.byref(self.views[i]), C.byref(self.atm[j.atmosphere].rec), C.byref(self.grids[i].rec),
-                C.byref(self.options[i]), _ptr(ws), ws.numel(), _ptr(self.flux_total[i]),
-                _ptr(self.flux_cont[i]), None, C.byref(st), None))
-            tot += int(st.evaluations)
-        return tot
+        """Total line.depth.lambda evaluations of the batch (one synchronous run)."""
+        return int(self.run(stats=True)["evaluations"])
 
 
 def bucket(n: int) -> int:
-    """Size class of a job's grid for the tuned options (powers of 4 points)."""
+    """Size class of a grid (powers of 4 points)."""
     b = 0
     while n > 1024 and b < 8:
         n //= 4

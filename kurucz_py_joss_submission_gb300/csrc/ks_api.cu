@@ -335,7 +335,7 @@ extern "C" ks_status ks_check_flags(void* stream, int32_t* flags_out) {
 
 // Grid scalars (opacity.py:570-574; line_opacity.py:235-239 RESOLU and
 // :1035-1058 WBEGIN / grid offset of the wing bins).
-__global__ void grid_params_kernel(const double* g, int64_t n, double grid_origin, GridPar* gp) {
+__device__ __forceinline__ void grid_params_kernel_body(VB vb, const double* g, int64_t n, double grid_origin, GridPar* gp) {
     GridPar p;
     p.resolu = 300000.0;
     p.ratiolg = 0.0;
@@ -360,6 +360,10 @@ __global__ void grid_params_kernel(const double* g, int64_t n, double grid_origi
     }
     *gp = p;
 }
+__global__ void grid_params_kernel(const double* g, int64_t n, double grid_origin, GridPar* gp) {
+    grid_params_kernel_body(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, g, n, grid_origin, gp);
+}
+
 
 // Centre bins (opacity.py:550-592) and wing bins (line_opacity.py:1030-1059)
 // per line, plus the single-precision line copies of the mixed path.  Flags
@@ -369,12 +373,12 @@ __device__ __forceinline__ int64_t wing_bin(double w, const GridPar& gp) {
     return (int64_t)rint(log(w / gp.wbegin) / gp.ratiolg) - gp.grid_offset;
 }
 
-__global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __restrict__ wl,
+__device__ __forceinline__ void line_bins_kernel_body(VB vb, int64_t n_lines, int64_t n_wl, const double* __restrict__ wl,
                                  const GridPar* __restrict__ gpp, int32_t* center_out,
                                  int32_t* wing_out, const double* cgf, const double* elo,
                                  const double* gr, const double* gs, const double* gw,
                                  const double* gf, LineF* linef, int* flags) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = (int64_t)vb.x * blockDim.x + threadIdx.x;
     const bool act = i < n_lines;
     const GridPar gp = *gpp;
     const double w = act ? wl[i] : (n_lines > 0 ? wl[n_lines - 1] : 1.0);
@@ -405,6 +409,14 @@ __global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __
         linef[i] = f;
     }
 }
+__global__ void line_bins_kernel(int64_t n_lines, int64_t n_wl, const double* __restrict__ wl,
+                                 const GridPar* __restrict__ gpp, int32_t* center_out,
+                                 int32_t* wing_out, const double* cgf, const double* elo,
+                                 const double* gr, const double* gs, const double* gw,
+                                 const double* gf, LineF* linef, int* flags) {
+    line_bins_kernel_body(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, n_lines, n_wl, wl, gpp, center_out, wing_out, cgf, elo, gr, gs, gw, gf, linef, flags);
+}
+
 
 // ---- deterministic stable partition of the pairs by reach class ----
 // Each depth's lines are cut into chunks of kChunk; counts per (depth,
@@ -415,10 +427,10 @@ static const int kChunk = 4096;
 static const int kDefaultTile = 1024;  // accumulation tile (bins) unless ks_options.tile_bins says otherwise
 static const int kPartThreads = 256;
 
-__global__ void class_count_kernel(const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
+__device__ __forceinline__ void class_count_kernel_body(VB vb, const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
                                    int32_t* __restrict__ counts) {
     __shared__ int c[N_REACH_CLASSES];
-    int d = blockIdx.y, ch = blockIdx.x;
+    int d = vb.y, ch = vb.x;
     if (threadIdx.x < N_REACH_CLASSES) c[threadIdx.x] = 0;
     __syncthreads();
     const uint8_t* base = cls + (int64_t)d * stride + (int64_t)ch * kChunk;
@@ -430,15 +442,20 @@ __global__ void class_count_kernel(const uint8_t* __restrict__ cls, int64_t stri
     if (threadIdx.x < N_REACH_CLASSES)
         counts[((int64_t)d * nchunks + ch) * N_REACH_CLASSES + threadIdx.x] = c[threadIdx.x];
 }
+__global__ void class_count_kernel(const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
+                                   int32_t* __restrict__ counts) {
+    class_count_kernel_body(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, cls, stride, nchunks, counts);
+}
+
 
 // One block per depth.  chunk_base[d][ch][k] = absolute start of chunk ch's
 // class-k lines; class_off[d][k] = absolute start of class k.
-__global__ void class_scan_kernel(const int32_t* __restrict__ counts, int nchunks, int64_t stride,
+__device__ __forceinline__ void class_scan_kernel_body(VB vb, const int32_t* __restrict__ counts, int nchunks, int64_t stride,
                                   int64_t* __restrict__ chunk_base, int64_t* __restrict__ class_off,
                                   unsigned long long* valid_pairs) {
     __shared__ int64_t tot[N_REACH_CLASSES];
     __shared__ int64_t off[N_REACH_CLASSES + 1];
-    int d = blockIdx.x;
+    int d = vb.x;
     int k = threadIdx.x;
     const int32_t* cd = counts + (int64_t)d * nchunks * N_REACH_CLASSES;
     if (k < N_REACH_CLASSES) {
@@ -468,15 +485,21 @@ __global__ void class_scan_kernel(const int32_t* __restrict__ counts, int nchunk
         }
     }
 }
+__global__ void class_scan_kernel(const int32_t* __restrict__ counts, int nchunks, int64_t stride,
+                                  int64_t* __restrict__ chunk_base, int64_t* __restrict__ class_off,
+                                  unsigned long long* valid_pairs) {
+    class_scan_kernel_body(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, counts, nchunks, stride, chunk_base, class_off, valid_pairs);
+}
 
-__global__ void __launch_bounds__(kPartThreads) class_scatter_kernel(
+
+__device__ __forceinline__ void class_scatter_kernel_body(VB vb, 
     const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
     const int64_t* __restrict__ chunk_base, int32_t* __restrict__ class_pos) {
     constexpr int NW = kPartThreads / 32;
     constexpr int PER_WARP = kChunk / NW;
     __shared__ int wcount[NW][N_REACH_CLASSES];
     __shared__ int64_t wbase[NW][N_REACH_CLASSES];
-    int d = blockIdx.y, ch = blockIdx.x;
+    int d = vb.y, ch = vb.x;
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint8_t* base = cls + (int64_t)d * stride + (int64_t)ch * kChunk + warp * PER_WARP;
     if (lane < N_REACH_CLASSES) wcount[warp][lane] = 0;
@@ -509,6 +532,12 @@ __global__ void __launch_bounds__(kPartThreads) class_scatter_kernel(
         __syncwarp();
     }
 }
+__global__ void __launch_bounds__(kPartThreads) class_scatter_kernel(
+    const uint8_t* __restrict__ cls, int64_t stride, int nchunks,
+    const int64_t* __restrict__ chunk_base, int32_t* __restrict__ class_pos) {
+    class_scatter_kernel_body(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, cls, stride, nchunks, chunk_base, class_pos);
+}
+
 
 // For every (depth, tile, class): the range of the class's centre-sorted
 // list whose wing centres lie within the class's maximum reach (+1 bin) of
@@ -523,11 +552,11 @@ __device__ __forceinline__ int64_t lower_bound_wing(const int32_t* __restrict__ 
     return lo;
 }
 
-__global__ void tile_ranges_kernel(const int64_t* __restrict__ class_off, const int32_t* __restrict__ class_pos,
+__device__ __forceinline__ void tile_ranges_kernel_body(VB vb, const int64_t* __restrict__ class_off, const int32_t* __restrict__ class_pos,
                                    const int32_t* __restrict__ wing, int64_t n_wl, int tile_bins, int ntiles,
                                    int2* __restrict__ rng) {
-    const int d = blockIdx.y;
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = vb.y;
+    const int64_t idx = (int64_t)vb.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)ntiles * N_REACH_CLASSES) return;
     const int t = (int)(idx / N_REACH_CLASSES), k = (int)(idx % N_REACH_CLASSES);
     const int64_t* off = class_off + (int64_t)d * (N_REACH_CLASSES + 1);
@@ -539,6 +568,12 @@ __global__ void tile_ranges_kernel(const int64_t* __restrict__ class_off, const 
     const int64_t s1 = lower_bound_wing(class_pos, s0, hi, wing, T1 + h);
     rng[((int64_t)d * ntiles + t) * N_REACH_CLASSES + k] = make_int2((int)(s0 - lo), (int)(s1 - lo));
 }
+__global__ void tile_ranges_kernel(const int64_t* __restrict__ class_off, const int32_t* __restrict__ class_pos,
+                                   const int32_t* __restrict__ wing, int64_t n_wl, int tile_bins, int ntiles,
+                                   int2* __restrict__ rng) {
+    tile_ranges_kernel_body(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, class_off, class_pos, wing, n_wl, tile_bins, ntiles, rng);
+}
+
 
 // ---------------------------------------------------------------------------
 // workspace
@@ -1515,5 +1550,495 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     // scratch before use; everything else is written before it is read.
     if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s, tm);
     else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s, tm);
+    return st;
+}
+
+// ---------------------------------------------------------------------------
+// batched synthesis: every stage once over all jobs
+// ---------------------------------------------------------------------------
+
+#define KS_BATCH_LOOP(...)                                                       \
+    const int64_t total = g.first[g.n_jobs];                                    \
+    for (int64_t v = blockIdx.x; v < total; v += gridDim.x) {                   \
+        int x, y, gx, gy;                                                       \
+        const int j = batch_locate(g, v, x, y, gx, gy);                         \
+        const VB vb{x, y, gx, gy};                                              \
+        __VA_ARGS__;                                                            \
+        __syncthreads();                                                        \
+    }
+
+// Per job and depth (virtual block (0, d)): clear the job's flag word and
+// counters, set its class bytes of the padding slots to 0xff and, for a job
+// without lines, empty its class lists and tile ranges (the memsets that
+// synthesize_impl issues for one synthesis).
+__global__ void __launch_bounds__(256) reset_batch_kernel(const ResetJob* __restrict__ jobs, BatchGrid g) {
+    KS_BATCH_LOOP({
+        const ResetJob& J = jobs[j];
+        const int d = vb.y;
+        if (d == 0 && threadIdx.x == 0) {
+            *J.flags = 0;
+            for (int k = 0; k < 4; k++) J.counters[k] = 0ull;
+        }
+        uint8_t* row = J.cls + (int64_t)d * J.stride;
+        for (int64_t i = J.n_lines + threadIdx.x; i < J.stride; i += blockDim.x) row[i] = 0xff;
+        if (J.n_lines == 0) {
+            for (int k = threadIdx.x; k <= N_REACH_CLASSES; k += blockDim.x)
+                J.class_off[(int64_t)d * (N_REACH_CLASSES + 1) + k] = 0;
+            for (int64_t k = threadIdx.x; k < (int64_t)J.ntiles * N_REACH_CLASSES; k += blockDim.x)
+                J.tile_rng[(int64_t)d * J.ntiles * N_REACH_CLASSES + k] = make_int2(0, 0);
+        }
+    })
+}
+
+__global__ void __launch_bounds__(32) grid_params_batch_kernel(const BinsJob* __restrict__ jobs, BatchGrid g) {
+    KS_BATCH_LOOP(if (threadIdx.x == 0) grid_params_kernel_body(vb, jobs[j].grid, jobs[j].n_wl,
+                                                                 jobs[j].grid_origin, jobs[j].gp))
+}
+
+__global__ void __launch_bounds__(256) line_bins_batch_kernel(const BinsJob* __restrict__ jobs, BatchGrid g) {
+    KS_BATCH_LOOP({
+        const BinsJob& J = jobs[j];
+        line_bins_kernel_body(vb, J.n_lines, J.n_wl, J.wavelength, J.gp, J.center, J.wing, J.cgf, J.elo, J.gr,
+                              J.gs, J.gw, J.gf, J.linef, J.flags);
+    })
+}
+
+__global__ void __launch_bounds__(kPartThreads) class_count_batch_kernel(const PartJob* __restrict__ jobs,
+                                                                        BatchGrid g) {
+    KS_BATCH_LOOP(class_count_kernel_body(vb, jobs[j].cls, jobs[j].stride, jobs[j].nchunks, jobs[j].counts))
+}
+
+__global__ void __launch_bounds__(32) class_scan_batch_kernel(const PartJob* __restrict__ jobs, BatchGrid g) {
+    KS_BATCH_LOOP(class_scan_kernel_body(vb, jobs[j].counts, jobs[j].nchunks, jobs[j].stride, jobs[j].chunk_base,
+                                         jobs[j].class_off, jobs[j].counters))
+}
+
+__global__ void __launch_bounds__(kPartThreads) class_scatter_batch_kernel(const PartJob* __restrict__ jobs,
+                                                                          BatchGrid g) {
+    KS_BATCH_LOOP(class_scatter_kernel_body(vb, jobs[j].cls, jobs[j].stride, jobs[j].nchunks, jobs[j].chunk_base,
+                                            jobs[j].class_pos))
+}
+
+__global__ void __launch_bounds__(256) tile_ranges_batch_kernel(const PartJob* __restrict__ jobs, BatchGrid g) {
+    KS_BATCH_LOOP(tile_ranges_kernel_body(vb, jobs[j].class_off, jobs[j].class_pos, jobs[j].wing, jobs[j].n_wl,
+                                          jobs[j].tile_bins, jobs[j].ntiles, jobs[j].tile_rng))
+}
+
+__global__ void __launch_bounds__(32) flag_sink_batch_kernel(int* const* __restrict__ flags, BatchGrid g) {
+    KS_BATCH_LOOP(if (threadIdx.x == 0) {
+        const int f = *flags[j];
+        if (f) atomicOr(&g_sticky_flags, f);
+    })
+}
+
+#undef KS_BATCH_LOOP
+
+namespace {
+
+enum BatchStage {
+    BS_RESET, BS_GRID, BS_BINS, BS_PREP, BS_CONT, BS_PAIR, BS_COUNT, BS_SCAN, BS_SCATTER, BS_RANGES, BS_ACC,
+    BS_TRANS, BS_LIST, BS_SINK, BS_N
+};
+const int kBatchThreads[BS_N] = {256, 32, 256, 256, 256, 128, kPartThreads, 32, kPartThreads, 256, 0, 0, 0, 32};
+
+// Device tables of one stage: job records, block prefix and per-job grids.
+struct StageTable {
+    void* jobs = nullptr;
+    int64_t* first = nullptr;
+    int* dims = nullptr;
+    int64_t total = 0;
+    int grid = 1;
+};
+
+}  // namespace
+
+struct ks_batch {
+    int n_jobs = 0;
+    int dev = 0;
+    bool fp64 = false, stream_pass = true, profile = false;
+    int tile = 0, warps = 0;
+    StageTable st[BS_N];
+    std::vector<Workspace> ws;
+    std::vector<int64_t> n_wl;
+};
+
+namespace {
+
+struct BatchLayout {
+    size_t table_bytes = 0;
+    std::vector<size_t> job_off, job_bytes;
+    size_t total = 0;
+};
+
+size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+ks_status batch_check(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
+    ks_status st = check_lines(lines);
+    if (st) return st;
+    if (n_jobs <= 0 || !jobs) return fail(KS_ERR_INVALID, "ks_batch: no jobs");
+    if ((st = check_tiling(opt))) return st;
+    if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))
+        return fail(KS_ERR_INVALID, "transfer_path must be 0 (streaming) or 1 (per-column)");
+    for (int i = 0; i < n_jobs; i++) {
+        const ks_job& J = jobs[i];
+        if (!J.atm || !J.grid || !J.flux_total || !J.flux_cont)
+            return fail(KS_ERR_INVALID, "ks_batch: job " + std::to_string(i) + " has a NULL record or output");
+        if ((st = check_atmos(J.atm)) || (st = check_grid(J.grid)) || (st = check_cont(J.atm))) return st;
+        if (J.line_first < 0 || J.line_count < 0 || J.line_first + J.line_count > lines->n_lines)
+            return fail(KS_ERR_INVALID, "ks_batch: job " + std::to_string(i) + " line slice outside the list");
+    }
+    return KS_OK;
+}
+
+// Rows [line_first, line_first + line_count) of the shared list as a ks_lines view.
+ks_lines job_lines(const ks_lines* l, const ks_job& J) {
+    ks_lines v = *l;
+    const int64_t o = J.line_first;
+    v.n_lines = J.line_count;
+    v.wavelength = l->wavelength + o;
+    v.gf = l->gf + o;
+    v.cgf = l->cgf + o;
+    v.gamma_rad = l->gamma_rad + o;
+    v.gamma_stark = l->gamma_stark + o;
+    v.gamma_vdw = l->gamma_vdw + o;
+    v.elo_cm = l->elo_cm + o;
+    v.element_idx = l->element_idx + o;
+    v.ion_stage = l->ion_stage + o;
+    v.line_type = l->line_type + o;
+    v.process_mask = l->process_mask + o;
+    v.asynth_mask = l->asynth_mask + o;
+    return v;
+}
+
+// Bytes of one job's records over all stage tables.
+size_t batch_job_record_bytes(bool fp64) {
+    size_t r = sizeof(ResetJob) + sizeof(BinsJob) + sizeof(PrepArgs) + sizeof(PartJob) + sizeof(int*);
+    r += fp64 ? sizeof(ContJob<double>) + sizeof(PairJob<double>) + sizeof(AccJob<double>) + sizeof(TransferJob<double>)
+              : sizeof(ContJob<float>) + sizeof(PairJob<float>) + sizeof(AccJob<float>) + sizeof(TransferJob<float>);
+    return r;
+}
+
+BatchLayout batch_layout(const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
+    BatchLayout b;
+    const bool fp64 = opt && opt->precision == KS_PREC_FP64;
+    // job records (9 tables), then per stage the block prefix and the grids,
+    // each table 64-byte aligned
+    b.table_bytes = batch_job_record_bytes(fp64) * (size_t)n_jobs + 64 * (9 + 2 * BS_N) +
+                    BS_N * (sizeof(int64_t) * (n_jobs + 1) + sizeof(int) * 2 * (size_t)n_jobs);
+    size_t off = al256(b.table_bytes);
+    for (int i = 0; i < n_jobs; i++) {
+        Carve dry{nullptr, 0, 0, true};
+        Workspace w;
+        layout(dry, w, jobs[i].line_count, jobs[i].atm->n_layers, jobs[i].grid->n, jobs[i].atm->n_ion,
+               jobs[i].atm->n_elem, fp64, true, true, default_tile(opt, fp64));
+        b.job_off.push_back(off);
+        b.job_bytes.push_back(al256(dry.used));
+        off += al256(dry.used);
+    }
+    b.total = off;
+    return b;
+}
+
+template <typename R>
+ks_status batch_build(ks_batch* b, const ks_lines* lines, const ks_job* jobs, int32_t n, const ks_options* opt,
+                      char* base, const BatchLayout& lay, const DevTables& t) {
+    constexpr bool fp64 = sizeof(R) == 8;
+    std::vector<ResetJob> reset(n);
+    std::vector<BinsJob> bins(n);
+    std::vector<PrepArgs> prep(n);
+    std::vector<ContJob<R>> cont(n);
+    std::vector<PairJob<R>> pair(n);
+    std::vector<PartJob> part(n);
+    std::vector<AccJob<R>> acc(n);
+    std::vector<TransferJob<R>> tr(n);
+    std::vector<int*> sink(n);
+    std::vector<std::vector<int>> dims(BS_N, std::vector<int>(2 * (size_t)n, 1));
+    b->ws.resize(n);
+    b->n_wl.resize(n);
+    for (int i = 0; i < n; i++) {
+        const ks_job& J = jobs[i];
+        const ks_atmos* atm = J.atm;
+        const ks_grid* grid = J.grid;
+        const ks_lines lv = job_lines(lines, J);
+        const int L = atm->n_layers;
+        Carve c{base + lay.job_off[i], lay.job_bytes[i], 0, false};
+        Workspace& w = b->ws[i];
+        layout(c, w, lv.n_lines, L, grid->n, atm->n_ion, atm->n_elem, fp64, true, true, b->tile);
+        b->n_wl[i] = grid->n;
+        reset[i] = ResetJob{w.flags, w.counters, w.cls, lv.n_lines, w.stride, L, w.ntiles, w.class_off, w.tile_rng};
+        dims[BS_RESET][2 * i + 1] = L;
+        BinsJob& bj = bins[i];
+        bj.grid = grid->wavelength;
+        bj.n_wl = grid->n;
+        bj.grid_origin = grid->grid_origin;
+        bj.gp = w.gp;
+        bj.n_lines = lv.n_lines;
+        bj.wavelength = lv.wavelength;
+        bj.cgf = lv.cgf;
+        bj.elo = lv.elo_cm;
+        bj.gr = lv.gamma_rad;
+        bj.gs = lv.gamma_stark;
+        bj.gw = lv.gamma_vdw;
+        bj.gf = lv.gf;
+        bj.center = w.center;
+        bj.wing = w.wing;
+        bj.linef = fp64 ? nullptr : w.linef;
+        bj.flags = w.flags;
+        dims[BS_BINS][2 * i] = (int)((lv.n_lines + 255) / 256);
+        dims[BS_BINS][2 * i + 1] = lv.n_lines > 0 ? 1 : 0;
+        PrepArgs pa = prep_args(atm, opt, w);
+        ContArgs ca = cont_args(atm, grid);
+        if constexpr (!fp64) {
+            pa.n_coeff = (int64_t)L * (atm->n_edge - 1) * 3;
+            pa.abs_coeff = atm->cont_abs_coeff;
+            pa.scat_coeff = atm->cont_scat_coeff;
+            pa.abs_coeff_f = w.coef_f;
+            pa.scat_coeff_f = w.coef_f + (size_t)L * (MAX_EDGES - 1) * 3;
+            ca.abs_coeff_f = pa.abs_coeff_f;
+            ca.scat_coeff_f = pa.scat_coeff_f;
+            ca.freq_f = w.freq_f;
+        }
+        prep[i] = pa;
+        dims[BS_PREP][2 * i] = (int)(((int64_t)L * atm->n_ion * atm->n_elem + 255) / 256);
+        cont[i] = ContJob<R>{ca, (R*)w.cont_abs, (R*)w.cont_scat};
+        dims[BS_CONT][2 * i] = (int)((grid->n + 255) / 256);
+        pair[i] = PairJob<R>{pair_args(&lv, atm, grid, opt, w, t), (const R*)w.cont_abs, (const R*)w.cont_scat,
+                             (PairDesc<R>*)w.desc, w.cls};
+        const int Lp = lv.n_lines > 0 ? L : 0;
+        dims[BS_PAIR][2 * i] = (int)((lv.n_lines + 127) / 128);
+        dims[BS_PAIR][2 * i + 1] = Lp;
+        PartJob& pj = part[i];
+        pj.cls = w.cls;
+        pj.stride = w.stride;
+        pj.n_wl = grid->n;
+        pj.nchunks = w.nchunks;
+        pj.ntiles = w.ntiles;
+        pj.tile_bins = b->tile;
+        pj.counts = w.counts;
+        pj.chunk_base = w.chunk_base;
+        pj.class_off = w.class_off;
+        pj.class_pos = w.class_pos;
+        pj.wing = w.wing;
+        pj.tile_rng = w.tile_rng;
+        pj.counters = w.counters;
+        dims[BS_COUNT][2 * i] = w.nchunks;
+        dims[BS_COUNT][2 * i + 1] = Lp;
+        dims[BS_SCAN][2 * i] = Lp;
+        dims[BS_SCATTER][2 * i] = w.nchunks;
+        dims[BS_SCATTER][2 * i + 1] = Lp;
+        dims[BS_RANGES][2 * i] = (int)(((int64_t)w.ntiles * N_REACH_CLASSES + 255) / 256);
+        dims[BS_RANGES][2 * i + 1] = w.ntiles > 0 ? Lp : 0;
+        acc[i] = AccJob<R>{acc_args(&lv, atm, grid, opt, w, t, fp64), (const PairDesc<R>*)w.desc, (R*)w.asynth};
+        dims[BS_ACC][2 * i] = (int)((grid->n + b->tile - 1) / b->tile);
+        dims[BS_ACC][2 * i + 1] = L;
+        TransferArgs ta = transfer_args(atm, grid, w, t, J.flux_total, J.flux_cont, true, fp64);
+        ta.line_scat = (opt && opt->rhoxj > 0.0) ? 1 : 0;
+        if (fp64 && opt && opt->exact_sweeps) ta.coefj64 = t.coefj64;
+        tr[i] = TransferJob<R>{ta, (const R*)w.cont_abs, (const R*)w.cont_scat, (const R*)w.asynth, w.tlist,
+                               w.counters + 2};
+        dims[BS_TRANS][2 * i] = (int)((grid->n + 127) / 128);
+        dims[BS_LIST][2 * i] = b->stream_pass ? 2 : 0;
+        sink[i] = w.flags;
+    }
+    std::vector<char> host(lay.table_bytes, 0);
+    size_t off = 0;
+    bool overflow = false;
+    auto put = [&](const void* src, size_t bytes) -> void* {
+        off = (off + 63) & ~size_t(63);
+        if (off + bytes > host.size()) {
+            overflow = true;
+            return nullptr;
+        }
+        std::memcpy(host.data() + off, src, bytes);
+        void* dptr = base + off;
+        off += bytes;
+        return dptr;
+    };
+    void* d_reset = put(reset.data(), sizeof(ResetJob) * n);
+    void* d_bins = put(bins.data(), sizeof(BinsJob) * n);
+    void* d_prep = put(prep.data(), sizeof(PrepArgs) * n);
+    void* d_cont = put(cont.data(), sizeof(ContJob<R>) * n);
+    void* d_pair = put(pair.data(), sizeof(PairJob<R>) * n);
+    void* d_part = put(part.data(), sizeof(PartJob) * n);
+    void* d_acc = put(acc.data(), sizeof(AccJob<R>) * n);
+    void* d_tr = put(tr.data(), sizeof(TransferJob<R>) * n);
+    void* d_sink = put(sink.data(), sizeof(int*) * n);
+    void* stage_jobs[BS_N] = {d_reset, d_bins, d_bins, d_prep, d_cont, d_pair, d_part,
+                              d_part, d_part, d_part, d_acc, d_tr, d_tr, d_sink};
+    for (int s = 0; s < BS_N; s++) {
+        std::vector<int64_t> first(n + 1, 0);
+        for (int i = 0; i < n; i++) first[i + 1] = first[i] + (int64_t)dims[s][2 * i] * dims[s][2 * i + 1];
+        for (int i = 0; i < n; i++)
+            if (dims[s][2 * i] <= 0) dims[s][2 * i] = 1;  // a job without blocks: keep the divisor valid
+        StageTable& T = b->st[s];
+        T.jobs = stage_jobs[s];
+        T.first = (int64_t*)put(first.data(), sizeof(int64_t) * (n + 1));
+        T.dims = (int*)put(dims[s].data(), sizeof(int) * 2 * n);
+        T.total = first[n];
+    }
+    if (overflow) return fail(KS_ERR_NOMEM, "ks_batch: internal table overflow");
+    KS_CUDA(cudaMemcpy(base, host.data(), off, cudaMemcpyHostToDevice));
+    // persistent grids
+    int64_t totals[6] = {b->st[BS_PREP].total, b->st[BS_CONT].total, b->st[BS_PAIR].total, b->st[BS_ACC].total,
+                         b->st[BS_TRANS].total, b->st[BS_LIST].total};
+    int grids[6];
+    KS_CUDA(fp64 ? batch_grids_f64(b->warps, b->tile, b->stream_pass, totals, grids)
+                 : batch_grids_f32(b->warps, b->tile, b->stream_pass, totals, grids));
+    b->st[BS_PREP].grid = grids[0];
+    b->st[BS_CONT].grid = grids[1];
+    b->st[BS_PAIR].grid = grids[2];
+    b->st[BS_ACC].grid = grids[3];
+    b->st[BS_TRANS].grid = grids[4];
+    b->st[BS_LIST].grid = grids[5];
+    const void* fns[BS_N] = {(const void*)reset_batch_kernel, (const void*)grid_params_batch_kernel,
+                             (const void*)line_bins_batch_kernel, nullptr, nullptr, nullptr,
+                             (const void*)class_count_batch_kernel, (const void*)class_scan_batch_kernel,
+                             (const void*)class_scatter_batch_kernel, (const void*)tile_ranges_batch_kernel,
+                             nullptr, nullptr, nullptr, (const void*)flag_sink_batch_kernel};
+    int sms = 0;
+    KS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev));
+    for (int s = 0; s < BS_N; s++) {
+        if (!fns[s]) continue;
+        int per = 0;
+        KS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fns[s], kBatchThreads[s], 0));
+        const int64_t g = (int64_t)sms * (per > 0 ? per : 1);
+        const int64_t tot = b->st[s].total;
+        b->st[s].grid = (int)(tot < g ? (tot > 0 ? tot : 1) : g);
+    }
+    return KS_OK;
+}
+
+BatchGrid bgrid(const StageTable& T, int n) { return BatchGrid{T.first, T.dims, n}; }
+
+}  // namespace
+
+extern "C" ks_status ks_batch_workspace_size(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs,
+                                             const ks_options* opt, size_t* bytes) {
+    ks_status st = batch_check(lines, jobs, n_jobs, opt);
+    if (st) return st;
+    if (!bytes) return fail(KS_ERR_INVALID, "ks_batch_workspace_size: NULL output");
+    *bytes = batch_layout(jobs, n_jobs, opt).total;
+    return KS_OK;
+}
+
+extern "C" ks_status ks_batch_create(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs,
+                                     const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                     ks_batch** out) {
+    if (!out) return fail(KS_ERR_INVALID, "ks_batch_create: NULL output");
+    *out = nullptr;
+    ks_status st = batch_check(lines, jobs, n_jobs, opt);
+    if (st) return st;
+    DevTables t;
+    if ((st = device_tables(&t))) return st;
+    BatchLayout lay = batch_layout(jobs, n_jobs, opt);
+    if (!workspace || workspace_bytes < lay.total)
+        return fail(KS_ERR_NOMEM, "ks_batch_create: workspace too small (see ks_batch_workspace_size)");
+    if ((reinterpret_cast<uintptr_t>(workspace) & 255) != 0)
+        return fail(KS_ERR_INVALID, "ks_batch_create: workspace must be 256-byte aligned");
+    ks_batch* b = new ks_batch();
+    b->n_jobs = n_jobs;
+    b->fp64 = opt && opt->precision == KS_PREC_FP64;
+    b->stream_pass = !b->fp64 && !(opt && opt->transfer_path == 1);
+    b->profile = opt && opt->profile;
+    b->tile = default_tile(opt, b->fp64);
+    b->warps = default_warps(opt);
+    cudaError_t e = cudaGetDevice(&b->dev);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    st = b->fp64 ? batch_build<double>(b, lines, jobs, n_jobs, opt, (char*)workspace, lay, t)
+                 : batch_build<float>(b, lines, jobs, n_jobs, opt, (char*)workspace, lay, t);
+    if (st) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return KS_OK;
+}
+
+extern "C" ks_status ks_batch_run(ks_batch* b, ks_stats* stats, void* stream) {
+    if (!b) return fail(KS_ERR_INVALID, "ks_batch_run: NULL plan");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = b->n_jobs;
+    auto G = [&](int stage) { return bgrid(b->st[stage], n); };
+    StageTimer tm;
+    tm.start(s, stats != nullptr && b->profile);
+    reset_batch_kernel<<<b->st[BS_RESET].grid, 256, 0, s>>>((const ResetJob*)b->st[BS_RESET].jobs, G(BS_RESET));
+    KS_CUDA(cudaGetLastError());
+    grid_params_batch_kernel<<<b->st[BS_GRID].grid, 32, 0, s>>>((const BinsJob*)b->st[BS_GRID].jobs, G(BS_GRID));
+    KS_CUDA(cudaGetLastError());
+    line_bins_batch_kernel<<<b->st[BS_BINS].grid, 256, 0, s>>>((const BinsJob*)b->st[BS_BINS].jobs, G(BS_BINS));
+    KS_CUDA(cudaGetLastError());
+    KS_CUDA(b->fp64 ? launch_prep_batch_f64((const PrepArgs*)b->st[BS_PREP].jobs, G(BS_PREP), b->st[BS_PREP].grid, s)
+                    : launch_prep_batch_f32((const PrepArgs*)b->st[BS_PREP].jobs, G(BS_PREP), b->st[BS_PREP].grid, s));
+    tm.mark();
+    KS_CUDA(b->fp64 ? launch_continuum_batch_f64(b->st[BS_CONT].jobs, G(BS_CONT), b->st[BS_CONT].grid, s)
+                    : launch_continuum_batch_f32(b->st[BS_CONT].jobs, G(BS_CONT), b->st[BS_CONT].grid, s));
+    tm.mark();
+    KS_CUDA(b->fp64 ? launch_pair_setup_batch_f64(b->st[BS_PAIR].jobs, G(BS_PAIR), b->st[BS_PAIR].grid, s)
+                    : launch_pair_setup_batch_f32(b->st[BS_PAIR].jobs, G(BS_PAIR), b->st[BS_PAIR].grid, s));
+    tm.mark();
+    class_count_batch_kernel<<<b->st[BS_COUNT].grid, kPartThreads, 0, s>>>((const PartJob*)b->st[BS_COUNT].jobs,
+                                                                           G(BS_COUNT));
+    KS_CUDA(cudaGetLastError());
+    class_scan_batch_kernel<<<b->st[BS_SCAN].grid, 32, 0, s>>>((const PartJob*)b->st[BS_SCAN].jobs, G(BS_SCAN));
+    KS_CUDA(cudaGetLastError());
+    class_scatter_batch_kernel<<<b->st[BS_SCATTER].grid, kPartThreads, 0, s>>>(
+        (const PartJob*)b->st[BS_SCATTER].jobs, G(BS_SCATTER));
+    KS_CUDA(cudaGetLastError());
+    tile_ranges_batch_kernel<<<b->st[BS_RANGES].grid, 256, 0, s>>>((const PartJob*)b->st[BS_RANGES].jobs,
+                                                                  G(BS_RANGES));
+    KS_CUDA(cudaGetLastError());
+    tm.mark();
+    KS_CUDA(b->fp64 ? launch_accumulate_batch_f64(b->st[BS_ACC].jobs, G(BS_ACC), b->st[BS_ACC].grid, b->warps,
+                                                  b->tile, s)
+                    : launch_accumulate_batch_f32(b->st[BS_ACC].jobs, G(BS_ACC), b->st[BS_ACC].grid, b->warps,
+                                                  b->tile, s));
+    tm.mark();
+    KS_CUDA(b->fp64 ? launch_transfer_batch_f64(b->st[BS_TRANS].jobs, G(BS_TRANS), G(BS_LIST), &g_tables.cj,
+                                                b->st[BS_TRANS].grid, b->st[BS_LIST].grid, false, s)
+                    : launch_transfer_batch_f32(b->st[BS_TRANS].jobs, G(BS_TRANS), G(BS_LIST), &g_tables.cj,
+                                                b->st[BS_TRANS].grid, b->st[BS_LIST].grid, b->stream_pass, s));
+    tm.mark();
+    flag_sink_batch_kernel<<<b->st[BS_SINK].grid, 32, 0, s>>>((int* const*)b->st[BS_SINK].jobs, G(BS_SINK));
+    KS_CUDA(cudaGetLastError());
+    tm.finish(stats);
+    if (stats) {
+        int64_t vp = 0, ev = 0, maxj = 0, iters = 0;
+        int flags = 0;
+        ks_status first_err = KS_OK;
+        for (int i = 0; i < n; i++) {
+            ks_stats one;
+            std::memset(&one, 0, sizeof(one));
+            ks_status st = collect_stats(b->ws[i], b->n_wl[i], &one, s);
+            vp += one.valid_pairs;
+            ev += one.evaluations;
+            maxj += one.maxj_wavelengths;
+            iters += one.iterations;
+            flags |= one.device_flags;
+            if (st && !first_err) first_err = st;
+        }
+        stats->valid_pairs = vp;
+        stats->evaluations = ev;
+        stats->maxj_wavelengths = maxj;
+        stats->iterations = iters;
+        stats->device_flags = flags;
+        stats->kernel_launches = b->stream_pass ? 15 : 14;
+        return first_err;
+    }
+    return KS_OK;
+}
+
+extern "C" void ks_batch_free(ks_batch* b) { delete b; }
+
+extern "C" ks_status ks_synthesize_batch(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs,
+                                         const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                         ks_stats* stats, void* stream) {
+    ks_batch* b = nullptr;
+    ks_status st = ks_batch_create(lines, jobs, n_jobs, opt, workspace, workspace_bytes, &b);
+    if (st) return st;
+    st = ks_batch_run(b, stats, stream);
+    ks_batch_free(b);
     return st;
 }

@@ -9,6 +9,14 @@
 
 namespace ks {
 
+// Index of a block as its kernel body sees it: the hardware block of a
+// single-synthesis launch, or one job's block of a batched launch (the
+// batched kernels walk a job table and hand each job's blocks to the same
+// bodies).
+struct VB {
+    int x, y, gx, gy;
+};
+
 constexpr double C_LIGHT_NM = 2.99792458e17;
 constexpr double C_LIGHT_CM = 2.99792458e10;
 constexpr double C_LIGHT_KM = 299792.458;

@@ -173,4 +173,98 @@ struct LineGradArgs {
     double *d_loggf, *d_loggr, *d_loggs, *d_loggw;  // [n_lines] out
 };
 
+// ---- batched launches -------------------------------------------------------
+//
+// A batch runs every stage once over all its jobs: the launch walks a job
+// table, job j owning virtual blocks [first[j], first[j + 1]) laid out on its
+// own grid dims[j] (x, y) -- the grid a single synthesis of that job would
+// launch.  Blocks take virtual blocks v = blockIdx.x + k gridDim.x (a static,
+// atomic-free schedule, so a persistent grid of a few blocks per SM covers any
+// batch) and run the same kernel body as a single synthesis.
+struct BatchGrid {
+    const int64_t* first;  // [n_jobs + 1] prefix of the jobs' block counts
+    const int* dims;       // [2 n_jobs] grid x, y per job
+    int n_jobs;
+};
+
+template <typename R>
+struct ContJob {
+    ContArgs a;
+    R *cont_abs, *cont_scat;
+};
+
+template <typename R>
+struct PairJob {
+    PairArgs a;
+    const R *kap_a, *kap_b;
+    PairDesc<R>* desc;
+    uint8_t* cls;
+};
+
+template <typename R>
+struct AccJob {
+    AccArgs a;
+    const PairDesc<R>* desc;
+    R* out;
+};
+
+template <typename R>
+struct TransferJob {
+    TransferArgs a;
+    const R *cab, *csc, *lop;
+    int32_t* list;               // FP32 streaming pass: columns left to the per-column code
+    unsigned long long* count;   // its length
+};
+
+// The per-job arguments of the precision-independent stages.
+struct BinsJob {
+    const double* grid;
+    int64_t n_wl;
+    double grid_origin;
+    GridPar* gp;
+    int64_t n_lines;
+    const double *wavelength, *cgf, *elo, *gr, *gs, *gw, *gf;
+    int32_t *center, *wing;
+    LineF* linef;  // FP32 path
+    int* flags;
+};
+
+struct PartJob {
+    const uint8_t* cls;
+    int64_t stride, n_wl;
+    int nchunks, ntiles, tile_bins;
+    int32_t* counts;
+    int64_t *chunk_base, *class_off;
+    int32_t* class_pos;
+    const int32_t* wing;
+    int2* tile_rng;
+    unsigned long long* counters;
+};
+
+struct ResetJob {
+    int* flags;
+    unsigned long long* counters;  // [4]
+    uint8_t* cls;                  // padding slots [n_lines, stride) of every depth set to 0xff
+    int64_t n_lines, stride;
+    int n_layers, ntiles;
+    int64_t* class_off;            // jobs without lines: class lists and tile ranges empty
+    int2* tile_rng;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ int batch_locate(const BatchGrid& g, int64_t v, int& x, int& y, int& gx, int& gy) {
+    int lo = 0, hi = g.n_jobs - 1;  // the last job whose first block is <= v
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g.first[mid] <= v) lo = mid; else hi = mid - 1;
+    }
+    const int64_t local = v - g.first[lo];
+    gx = g.dims[2 * lo];
+    gy = g.dims[2 * lo + 1];
+    x = (int)(local % gx);
+    y = (int)(local / gx);
+    return lo;
+}
+#endif
+
 }  // namespace ks

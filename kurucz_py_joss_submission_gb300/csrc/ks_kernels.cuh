@@ -28,11 +28,11 @@ namespace ks {
 // DOPPLE for TRANSP only), :416-420 and :465 (N10DOP, DVOIGT from
 // DOPPLE = doppler width / wavelength).
 template <typename R>
-__global__ void prep_depth_kernel(PrepArgs a) {
+__device__ __forceinline__ void prep_depth_kernel_body(VB vb, const PrepArgs& a) {
     int64_t per_depth = (int64_t)a.n_ion * a.n_elem;
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i = (int64_t)vb.x * blockDim.x + threadIdx.x;
     if (a.abs_coeff_f) {
-        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        const int64_t stride = (int64_t)vb.gx * blockDim.x;
         for (int64_t k = i; k < a.n_coeff; k += stride) {
             a.abs_coeff_f[k] = (float)a.abs_coeff[k];
             a.scat_coeff_f[k] = (float)a.scat_coeff[k];
@@ -88,6 +88,11 @@ __global__ void prep_depth_kernel(PrepArgs a) {
     q.ok = ((pop > 0.0 && dop_t > 0.0 && rho > 0.0) ? 1 : 0) | ((pop > 0.0 && dop > 0.0) ? 2 : 0);
     a.ion[i] = q;
 }
+template <typename R>
+__global__ void prep_depth_kernel(PrepArgs a) {
+    prep_depth_kernel_body<R>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a);
+}
+
 
 // ---------------------------------------------------------------------------
 // continuum
@@ -96,8 +101,8 @@ __global__ void prep_depth_kernel(PrepArgs a) {
 // One thread per wavelength, looping over depths so the edge search and the
 // Lagrange weights are computed once per wavelength.  continuum.py:146-256.
 template <typename R>
-__global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __restrict__ cont_scat) {
-    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void continuum_kernel_body(VB vb, const ContArgs& a, R* __restrict__ cont_abs, R* __restrict__ cont_scat) {
+    int64_t j = (int64_t)vb.x * blockDim.x + threadIdx.x;
     if (j >= a.n) return;
     double w = a.grid[j];
     double aw = fabs(w);
@@ -157,6 +162,11 @@ __global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __rest
         cont_scat[(int64_t)d * a.n + j] = ls;
     }
 }
+template <typename R>
+__global__ void continuum_kernel(ContArgs a, R* __restrict__ cont_abs, R* __restrict__ cont_scat) {
+    continuum_kernel_body<R>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, cont_abs, cont_scat);
+}
+
 
 // ---------------------------------------------------------------------------
 // pair setup: TRANSP gates + wing descriptor
@@ -582,7 +592,7 @@ __device__ __forceinline__ void pair_wings(const PairArgs& a, const R* __restric
 // gates.  Each pair writes only its own descriptor slot and class byte, so
 // the queue order does not change the result.
 template <typename R, bool FUSED>
-__global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
+__device__ __forceinline__ void pair_setup_kernel_body(VB vb, const PairArgs& a, const R* __restrict__ kap_a,
                                                          const R* __restrict__ kap_b,
                                                          PairDesc<R>* __restrict__ desc,
                                                          uint8_t* __restrict__ cls) {
@@ -592,8 +602,8 @@ __global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __
     __shared__ R q_kc[128], q_k0[128];
     if (threadIdx.x == 0) q_n = 0;
     __syncthreads();
-    const int d = blockIdx.y;
-    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = vb.y;
+    const int64_t li = (int64_t)vb.x * blockDim.x + threadIdx.x;
     if (li < a.n_lines) {
         R kc, k0;
         int code, qi;
@@ -613,6 +623,14 @@ __global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __
     if (i < q_n)
         pair_wings<R>(a, kap_a, kap_b, desc, cls, q_li[i], d, q_kc[i], q_k0[i], q_code[i], q_num[i], q_qi[i]);
 }
+template <typename R, bool FUSED>
+__global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __restrict__ kap_a,
+                                                         const R* __restrict__ kap_b,
+                                                         PairDesc<R>* __restrict__ desc,
+                                                         uint8_t* __restrict__ cls) {
+    pair_setup_kernel_body<R, FUSED>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, kap_a, kap_b, desc, cls);
+}
+
 
 // ---------------------------------------------------------------------------
 // accumulation
@@ -788,7 +806,7 @@ __device__ __forceinline__ void cell_atomic(double* c, int b, double v) { atomic
 // (line_opacity.py:1338) and stored coalesced.  Every sum has a fixed order,
 // so results are bit-identical across runs.
 template <typename R>
-__global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
+__device__ __forceinline__ void accumulate_kernel_body(VB vb, const AccArgs& a, const PairDesc<R>* __restrict__ desc,
                                                          R* __restrict__ out) {
     using CellT = typename Cell<R>::T;
     using R2 = typename Vec2<R>::T;
@@ -797,8 +815,8 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const int nwarps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int d = blockIdx.y;
-    const int T0 = blockIdx.x * W;
+    const int d = vb.y;
+    const int T0 = vb.x * W;
     const int T1 = (int)min((int64_t)T0 + W, a.n_wl);
     const int span = T1 - T0;
 
@@ -814,7 +832,7 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
     const R* gh2 = sizeof(R) == 8 ? (const R*)a.h2d : (const R*)a.h2f;
     if (threadIdx.x < N_REACH_CLASSES) {
         const int k = threadIdx.x;
-        const int2 r = a.tile_rng[((int64_t)d * gridDim.x + blockIdx.x) * N_REACH_CLASSES + k];
+        const int2 r = a.tile_rng[((int64_t)d * vb.gx + vb.x) * N_REACH_CLASSES + k];
         cls_lo[k] = a.class_off[(int64_t)d * (N_REACH_CLASSES + 1) + k] + r.x;
         cls_n[k] = r.y - r.x;
     }
@@ -1038,6 +1056,12 @@ __global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDe
         if (lane == 0 && evals) atomicAdd(a.evals, evals);
     }
 }
+template <typename R>
+__global__ void __launch_bounds__(512) accumulate_kernel(AccArgs a, const PairDesc<R>* __restrict__ desc,
+                                                         R* __restrict__ out) {
+    accumulate_kernel_body<R>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, desc, out);
+}
+
 
 // ---------------------------------------------------------------------------
 // transfer (JOSH)
@@ -1869,8 +1893,8 @@ __device__ __forceinline__ int ts_solve(const TransferArgs& a, const CoefJ32& cj
 }
 
 template <typename R>
-__global__ void __launch_bounds__(TS_THREADS, 4) transfer_stream_kernel(
-    TransferArgs a, const __grid_constant__ CoefJ32 cj, const float* __restrict__ cab,
+__device__ __forceinline__ void transfer_stream_kernel_body(VB vb, 
+    const TransferArgs& a, const CoefJ32& cj, const float* __restrict__ cab,
     const float* __restrict__ csc, const float* __restrict__ lop, int32_t* __restrict__ list,
     unsigned long long* __restrict__ count) {
     extern __shared__ float2 ts_cols[];  // [NXTAU][TS_THREADS]
@@ -1893,7 +1917,7 @@ __global__ void __launch_bounds__(TS_THREADS, 4) transfer_stream_kernel(
         s_ok = ok ? 1 : 0;
     }
     __syncthreads();
-    const int64_t j = (int64_t)blockIdx.x * TS_THREADS + threadIdx.x;
+    const int64_t j = (int64_t)vb.x * TS_THREADS + threadIdx.x;
     if (j >= a.n) return;
     bool done = false;
     if (s_ok) {
@@ -1919,17 +1943,34 @@ __global__ void __launch_bounds__(TS_THREADS, 4) transfer_stream_kernel(
     }
     if (!done) list[atomicAdd(count, 1ull)] = (int32_t)j;
 }
+template <typename R>
+__global__ void __launch_bounds__(TS_THREADS, 4) transfer_stream_kernel(
+    TransferArgs a, const __grid_constant__ CoefJ32 cj, const float* __restrict__ cab,
+    const float* __restrict__ csc, const float* __restrict__ lop, int32_t* __restrict__ list,
+    unsigned long long* __restrict__ count) {
+    transfer_stream_kernel_body<R>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, cj, cab, csc, lop, list, count);
+}
+
 
 // transfer_column for the wavelengths the streaming pass listed.
+template <typename R>
+__device__ __forceinline__ void transfer_list_kernel_body(VB vb, const TransferArgs& a, const CoefJ32& cj,
+                                                            const R* __restrict__ cab, const R* __restrict__ csc,
+                                                            const R* __restrict__ lop,
+                                                            const int32_t* __restrict__ list,
+                                                            const unsigned long long* __restrict__ count) {
+    const int64_t nl = (int64_t)*count;
+    for (int64_t i = (int64_t)vb.x * blockDim.x + threadIdx.x; i < nl; i += (int64_t)vb.gx * blockDim.x)
+        transfer_column<R, false>(a, cj, cab, csc, lop, nullptr, nullptr, list[i]);
+}
 template <typename R>
 __global__ void __launch_bounds__(128) transfer_list_kernel(TransferArgs a, const __grid_constant__ CoefJ32 cj,
                                                             const R* __restrict__ cab, const R* __restrict__ csc,
                                                             const R* __restrict__ lop,
                                                             const int32_t* __restrict__ list,
                                                             const unsigned long long* __restrict__ count) {
-    const int64_t nl = (int64_t)*count;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x)
-        transfer_column<R, false>(a, cj, cab, csc, lop, nullptr, nullptr, list[i]);
+    transfer_list_kernel_body<R>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, cj, cab, csc, lop, list, count);
 }
+
 
 }  // namespace ks

@@ -31,7 +31,17 @@ struct CoefJ32 {
                                              const R* ca, const R* cs, const R* lo,               \
                                              int32_t* list, unsigned long long* count,            \
                                              cudaStream_t s);                                     \
-    size_t accumulate_smem_bytes_##SUF(int tile_bins, int warps);
+    size_t accumulate_smem_bytes_##SUF(int tile_bins, int warps);                                \
+    cudaError_t batch_grids_##SUF(int warps_per_tile, int tile_bins, bool stream_pass,            \
+                                  const int64_t* totals, int* grids);                             \
+    cudaError_t launch_prep_batch_##SUF(const PrepArgs* jobs, BatchGrid g, int grid, cudaStream_t s); \
+    cudaError_t launch_continuum_batch_##SUF(const void* jobs, BatchGrid g, int grid, cudaStream_t s); \
+    cudaError_t launch_pair_setup_batch_##SUF(const void* jobs, BatchGrid g, int grid, cudaStream_t s); \
+    cudaError_t launch_accumulate_batch_##SUF(const void* jobs, BatchGrid g, int grid, int warps,    \
+                                             int tile_bins, cudaStream_t s);                         \
+    cudaError_t launch_transfer_batch_##SUF(const void* jobs, BatchGrid g, BatchGrid g_list,         \
+                                           const CoefJ32* cj, int grid, int grid_list,               \
+                                           bool stream_pass, cudaStream_t s);
 
 KS_DECLARE_LAUNCHERS(float, f32)
 KS_DECLARE_LAUNCHERS(double, f64)
