@@ -646,13 +646,21 @@ def run_batch(args):
     dcat = DeviceCatalog(cat, dev)
 
     def make(options, workspace):
-        return BatchSynthesizer(dcat, atms, jobs, precision=args.precision, options=options,
+        o = dict(options)
+        groups = o.pop("groups", 1)
+        return BatchSynthesizer(dcat, atms, jobs, precision=args.precision, options=o, groups=groups,
                                 workspace=workspace, device=dev)
 
     tuned = autotune.tune(make, autotune.signature(jobs, len(cat), [a.layers for a in atms]), args.precision,
                           log=log)
     bs = make(tuned, None)
     evals = bs.evaluations()
+    # stage times of the plan (CUDA events between its launches), medians of 3
+    prof = make(dict(tuned, profile=True), bs.workspace)
+    stage_runs = [prof.run(stats=True)["stage_ms"] for _ in range(3)]
+    stage_ms = {k: statistics.median(r[k] for r in stage_runs) for k in stage_runs[0]}
+    del prof
+    bs = make(tuned, bs.workspace)
     bs.capture()
     for _ in range(args.warmup):
         bs.replay()
@@ -734,6 +742,7 @@ def run_batch(args):
                        "parallelism": "1 GPU" if world == 1 else f"{world} GPUs, jobs split across ranks"},
             "evaluations_per_s": evals * args.steps / (ms / 1e3),
             "evaluations_per_step": evals,
+            "stage_ms": stage_ms,
             "accuracy_vs_fp64": err,
             "e2e": {"value": len(jobs_all) / (e2e_ms / 1e3), "unit": "spectra/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

@@ -1,8 +1,9 @@
 """Autotuner of the batched form's launch shape.
 
-The accumulation's tile width (bins per CTA), its warps per tile and the
+The accumulation's tile width (bins per CTA), its warps per tile, the
 number of long-reach pairs dealt to a warp at once (``long_class``: classes
-from it go in batches of 8 pairs, the shorter ones in batches of 32) trade
+from it go in batches of 8 pairs, the shorter ones in batches of 32) and the
+number of job groups run side by side (``groups``) trade
 per-CTA fixed costs (staging the Voigt table, class ranges, the epilogue)
 against occupancy, load balance and the number of tiles a long wing is read
 by; the best choice depends on the grid sizes and the line density of the
@@ -26,6 +27,8 @@ from . import _build
 
 CANDIDATES = ([dict(tile_bins=t, warps_per_tile=w, long_class=lc) for t in (512, 1024) for w in (4, 8)
                for lc in (8, 10)] + [dict(tile_bins=2048, warps_per_tile=8, long_class=lc) for lc in (8, 10)])
+# job groups: plans run side by side on streams of their own
+GROUPS = (2, 4, 8)
 CACHE = Path(os.environ.get("KS_AUTOTUNE_CACHE", str(_build.OUT_DIR / "autotune.json")))
 
 
@@ -82,6 +85,19 @@ def tune(make_batch: Callable[..., object], key: str, precision: str, reps: int 
         if t < best_t:
             best, best_t = dict(cand), t
         del bs
+    # then the number of job groups (plans on streams of their own) for it
+    best_g, best_gt = 1, best_t
+    for groups in GROUPS:
+        bs = make_batch(dict(best, groups=groups), ws)
+        if bs.workspace.numel() > ws.numel():
+            ws = bs.workspace
+        t = time_batch(bs, reps)
+        if log:
+            log(f"autotune {best} x {groups} groups: {t:.3f} ms")
+        if t < best_gt:
+            best_g, best_gt = groups, t
+        del bs
+    best = dict(best, groups=best_g)
     if use_cache:
         cache[ck] = best
         try:

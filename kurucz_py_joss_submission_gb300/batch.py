@@ -60,12 +60,16 @@ def window_slice(wavelength_sorted: np.ndarray, wl_min: float, wl_max: float) ->
 
 class BatchSynthesizer:
     """Fused syntheses of ``jobs`` over the shared lines of ``catalog``, as
-    one batch plan.  ``options`` (keywords of :func:`device.make_options`,
-    e.g. from :func:`autotune.tune`) apply to every job."""
+    batch plans.  ``options`` (keywords of :func:`device.make_options`, e.g.
+    from :func:`autotune.tune`) apply to every job.  With ``groups`` > 1 the
+    jobs are dealt (largest first) to that many plans, each run on a stream of
+    its own, so that one group's compute-bound transfer overlaps another's
+    latency-bound pair setup; every group is still one persistent launch per
+    stage."""
 
     def __init__(self, catalog: DeviceCatalog, atmospheres: Sequence[AtmosphereModel], jobs: Sequence[Job],
                  precision: str = "mixed", resolution: float = 300000.0, options: Optional[dict] = None,
-                 workspace: Optional[torch.Tensor] = None, device="cuda"):
+                 workspace: Optional[torch.Tensor] = None, groups: int = 1, device="cuda"):
         host = catalog.host
         if np.any((np.abs(host.code - 1.0) < 1e-6) | np.isin(host.line_types, [-1, -2]) |
                   (host.element_idx == 0)):
@@ -100,33 +104,71 @@ class BatchSynthesizer:
             r.line_count = self.rows[i].stop - self.rows[i].start
             r.flux_total = self.flux_total[i].data_ptr()
             r.flux_cont = self.flux_cont[i].data_ptr()
-        ws = C.c_size_t()
-        _native.check(self.lib.ks_batch_workspace_size(C.byref(catalog.rec), self.job_recs, n,
-                                                       C.byref(self.options), C.byref(ws)))
+        # groups: jobs dealt round-robin in order of their work (lines x points)
+        self.n_groups = max(1, min(int(groups), n))
+        cost = [(self.rows[i].stop - self.rows[i].start) * self.grids[i].n for i in range(n)]
+        order = sorted(range(n), key=lambda i: -cost[i])
+        self.group_jobs = [sorted(order[g::self.n_groups]) for g in range(self.n_groups)]
+        self.group_recs, sizes = [], []
+        for members in self.group_jobs:
+            recs = (_native.KsJob * len(members))(*[self.job_recs[i] for i in members])
+            ws = C.c_size_t()
+            _native.check(self.lib.ks_batch_workspace_size(C.byref(catalog.rec), recs, len(members),
+                                                           C.byref(self.options), C.byref(ws)))
+            self.group_recs.append(recs)
+            sizes.append((int(ws.value) + 511) // 512 * 512)
         dev = self.grids[0].wavelength.device if self.grids else torch.device(device)
-        self.workspace_bytes = int(ws.value)
+        self.workspace_bytes = sum(sizes)
         if workspace is not None and workspace.numel() >= self.workspace_bytes:
             self.workspace = workspace  # the caller's (e.g. shared by the autotuner's candidates)
         else:
             self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=dev)
-        self.plan = C.c_void_p()
-        _native.check(self.lib.ks_batch_create(C.byref(catalog.rec), self.job_recs, n, C.byref(self.options),
-                                               _ptr(self.workspace), self.workspace.numel(),
-                                               C.byref(self.plan)))
+        self.plans: List[C.c_void_p] = []
+        off = 0
+        for recs, size in zip(self.group_recs, sizes):
+            plan = C.c_void_p()
+            _native.check(self.lib.ks_batch_create(C.byref(catalog.rec), recs, len(recs), C.byref(self.options),
+                                                   C.c_void_p(self.workspace.data_ptr() + off), size,
+                                                   C.byref(plan)))
+            self.plans.append(plan)
+            off += size
+        self.streams = [torch.cuda.Stream(device=dev) for _ in range(self.n_groups)] if self.n_groups > 1 else []
         self.graph: Optional[torch.cuda.CUDAGraph] = None
 
     def __del__(self):
-        plan = getattr(self, "plan", None)
-        if plan is not None and plan.value:
-            self.lib.ks_batch_free(plan)
-            self.plan = None
+        for plan in getattr(self, "plans", []):
+            if plan is not None and plan.value:
+                self.lib.ks_batch_free(plan)
+        self.plans = []
 
     def run(self, stats: bool = False, stream: Optional[torch.cuda.Stream] = None):
-        """Enqueue the batch on the current stream (no graph); with ``stats``
-        synchronise and return the counters summed over the jobs."""
-        st = _native.KsStats()
-        _native.check(self.lib.ks_batch_run(self.plan, C.byref(st) if stats else None, stream_handle(stream)))
-        return st.as_dict() if stats else None
+        """Enqueue the batch on the current stream (groups fork to their own
+        streams and join back); with ``stats`` synchronise and return the
+        counters summed over the jobs."""
+        if stats:
+            tot = None
+            for plan in self.plans:
+                st = _native.KsStats()
+                _native.check(self.lib.ks_batch_run(plan, C.byref(st), stream_handle(stream)))
+                d = st.as_dict()
+                if tot is None:
+                    tot = d
+                else:
+                    for k in ("valid_pairs", "evaluations", "maxj_wavelengths", "iterations", "kernel_launches"):
+                        tot[k] += d[k]
+                    tot["device_flags"] |= d["device_flags"]
+                    tot["stage_ms"] = {k: tot["stage_ms"][k] + d["stage_ms"][k] for k in tot["stage_ms"]}
+            return tot
+        if self.n_groups == 1:
+            _native.check(self.lib.ks_batch_run(self.plans[0], None, stream_handle(stream)))
+            return None
+        cur = stream if stream is not None else torch.cuda.current_stream()
+        for plan, s in zip(self.plans, self.streams):
+            s.wait_stream(cur)
+            _native.check(self.lib.ks_batch_run(plan, None, C.c_void_p(s.cuda_stream)))
+        for s in self.streams:
+            cur.wait_stream(s)
+        return None
 
     def capture(self):
         """Record the batch as one CUDA graph (after one eager run, which

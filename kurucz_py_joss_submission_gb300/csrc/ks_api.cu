@@ -1559,9 +1559,21 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
 
 #define KS_BATCH_LOOP(...)                                                       \
     const int64_t total = g.first[g.n_jobs];                                    \
+    int j = -1;                                                                 \
+    int64_t j_first = 0, j_end = -1;                                            \
     for (int64_t v = blockIdx.x; v < total; v += gridDim.x) {                   \
         int x, y, gx, gy;                                                       \
-        const int j = batch_locate(g, v, x, y, gx, gy);                         \
+        if (v >= j_end) { /* a new job: search the prefix */                    \
+            j = batch_locate(g, v, x, y, gx, gy);                               \
+            j_first = g.first[j];                                               \
+            j_end = g.first[j + 1];                                             \
+        } else {                                                                \
+            const int64_t local = v - j_first;                                  \
+            gx = g.dims[2 * j];                                                 \
+            gy = g.dims[2 * j + 1];                                             \
+            x = (int)(local % gx);                                              \
+            y = (int)(local / gx);                                              \
+        }                                                                       \
         const VB vb{x, y, gx, gy};                                              \
         __VA_ARGS__;                                                            \
         __syncthreads();                                                        \
@@ -1837,7 +1849,10 @@ ks_status batch_build(ks_batch* b, const ks_lines* lines, const ks_job* jobs, in
         tr[i] = TransferJob<R>{ta, (const R*)w.cont_abs, (const R*)w.cont_scat, (const R*)w.asynth, w.tlist,
                                w.counters + 2};
         dims[BS_TRANS][2 * i] = (int)((grid->n + 127) / 128);
-        dims[BS_LIST][2 * i] = b->stream_pass ? 2 : 0;
+        // the hand-over list may hold any of the job's columns (hot or
+        // saturated columns all go there): one virtual block per 128 of them;
+        // blocks past the list's length return at once
+        dims[BS_LIST][2 * i] = b->stream_pass ? (int)((grid->n + 127) / 128) : 0;
         sink[i] = w.flags;
     }
     std::vector<char> host(lay.table_bytes, 0);

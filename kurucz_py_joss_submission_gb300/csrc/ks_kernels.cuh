@@ -628,7 +628,8 @@ __global__ void __launch_bounds__(128) pair_setup_kernel(PairArgs a, const R* __
                                                          const R* __restrict__ kap_b,
                                                          PairDesc<R>* __restrict__ desc,
                                                          uint8_t* __restrict__ cls) {
-    pair_setup_kernel_body<R, FUSED>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, kap_a, kap_b, desc, cls);
+    pair_setup_kernel_body<R, FUSED>(VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y}, a, kap_a,
+                                     kap_b, desc, cls);
 }
 
 

@@ -65,6 +65,22 @@ def test_batch_jobs_equal_single_syntheses(precision, opt_i):
     assert st["device_flags"] == 0
 
 
+def test_job_groups_give_the_same_spectra():
+    """Jobs split over three plans on streams of their own: same bits."""
+    srt, atms = _inputs()
+    dcat = DeviceCatalog(srt)
+    one = batch.BatchSynthesizer(dcat, atms, JOBS)
+    one.run()
+    three = batch.BatchSynthesizer(dcat, atms, JOBS, groups=3)
+    three.capture()
+    three.replay(check=True)
+    torch.cuda.synchronize()
+    assert sorted(i for g in three.group_jobs for i in g) == list(range(len(JOBS)))
+    for a, b in zip(one.flux_total + one.flux_cont, three.flux_total + three.flux_cont):
+        assert torch.equal(a, b)
+    assert three.run(stats=True)["evaluations"] == one.run(stats=True)["evaluations"]
+
+
 def test_batch_through_the_c_entry_point():
     """ks_synthesize_batch (create, run, free in one call) gives the plan's result."""
     import ctypes as C
