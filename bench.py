@@ -599,9 +599,41 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+    if line is not None and world == 1 and not args.no_forms and args.window is None \
+            and WORKLOAD["name"] == "full_300_1800":
+        line["forms"] = run_forms()
     if line is not None:
         print(json.dumps(line), flush=True)
     return 0
+
+
+# The other forms of the path, each measured by a child run of this script
+# (its own process: memory freed in between, a failure recorded without
+# losing the headline): few steps, every timing rule as for the headline.
+FORMS = {
+    "batch_256": ["--workload", "batch_256", "--steps", "3", "--warmup", "3"],
+    "dense_10m": ["--workload", "dense_10m", "--steps", "3", "--warmup", "3", "--skip-cpu"],
+    "diff_400_700": ["--workload", "diff_400_700", "--steps", "3", "--warmup", "3", "--fd-params", "40"],
+}
+
+
+def run_forms() -> dict:
+    out = {}
+    for name, extra in FORMS.items():
+        t = time.time()
+        try:
+            r = subprocess.run([sys.executable, str(ROOT / "bench.py"), *extra, "--no-forms"], cwd=ROOT,
+                               capture_output=True, text=True, timeout=900)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": f"rc={r.returncode}: {r.stderr.strip().splitlines()[-1:]}"}
+            else:
+                out[name] = json.loads(lines[-1])
+        except Exception as e:  # noqa: BLE001 -- a form's failure must not lose the headline line
+            out[name] = {"error": repr(e)}
+        out[name]["wall_s"] = round(time.time() - t, 1)
+        log(f"form {name}: {out[name].get('value')} {out[name].get('unit')} ({out[name]['wall_s']} s)")
+    return out
 
 
 def batch_jobs(n_atm: int):
@@ -824,7 +856,7 @@ def run_diff(args):
         h = 1e-4
         names = ("log_gf", "log_gamma_rad", "log_gamma_stark", "log_gamma_vdw")
         errs = {k: [] for k in names}
-        picks = [(int(rng.integers(4)), int(rng.integers(n))) for _ in range(200)]
+        picks = [(int(rng.integers(4)), int(rng.integers(n))) for _ in range(args.fd_params)]
         for par, i in picks:
             vals = []
             for sgn in (+1, -1):
@@ -840,7 +872,7 @@ def run_diff(args):
             if scale * h > 1e-11 * max(abs(float(loss.item())), 1e-300):
                 errs[names[par]].append(abs(g_fd - g_ad) / scale)
         allerr = np.array([e for v in errs.values() for e in v])
-        fd = {"params_checked": 200, "params_resolved_by_fd": int(allerr.size), "h_dex": h,
+        fd = {"params_checked": args.fd_params, "params_resolved_by_fd": int(allerr.size), "h_dex": h,
               "rel_err_median": float(np.median(allerr)) if allerr.size else None,
               "rel_err_p90": float(np.percentile(allerr, 90)) if allerr.size else None,
               "frac_within_5pct": float(np.mean(allerr < 0.05)) if allerr.size else None,
@@ -877,6 +909,10 @@ def main():
     ap.add_argument("--warps-per-tile", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64-check", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="headline workload only: do not measure the batched, dense and differentiable forms")
+    ap.add_argument("--fd-params", type=int, default=200,
+                    help="diff_400_700: parameters checked by central finite differences")
     ap.add_argument("--window", type=float, nargs=2, default=None,
                     help="restrict the workload to a wavelength window (small profiling case)")
     ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS) + ["batch_256", "diff_400_700"],

@@ -762,6 +762,30 @@ typedef struct {
     float cdiag32[NXTAU];
 } josh_tables_t;
 
+/* Exact-sweep mode (not the reference's arithmetic): the JOSH system
+ * (I - diag(xalpha) COEFJ) xs = xsbar (1 - xalpha) solved in FP64 by
+ * Gauss-Seidel to 1e-13 instead of the reference's FP32 sweep with its 1e-5
+ * stop (josh_solver.py:24-92), so that the fluxes are smooth in the inputs
+ * and can be differenced to check gradients. */
+static int g_exact_sweeps = 0;
+void kso_set_exact_sweeps(int on) { g_exact_sweeps = on ? 1 : 0; }
+
+static int josh_iterate_exact(const double *coefj, double *xs, const double *xalpha, const double *xsbar_mod) {
+    for (int it = 0; it < 2000; it++) {
+        double dmax = 0.0;
+        for (int k = NXTAU - 1; k >= 0; k--) {
+            double sum = 0.0;
+            for (int m = 0; m < NXTAU; m++) sum += coefj[k * NXTAU + m] * xs[m];
+            double nv = sum * xalpha[k] + xsbar_mod[k];
+            double d = fabs(nv - xs[k]) / fmax(fabs(nv), 1e-300);
+            if (d > dmax) dmax = d;
+            xs[k] = nv;
+        }
+        if (dmax < 1e-13) return it + 1;
+    }
+    return 2000;
+}
+
 /* josh_solver.py:367-767 solve_josh_flux (IFSCAT=1 path, surface flux). */
 static double solve_josh(const josh_tables_t *T, int n, const double *acont,
                          const double *scont, const double *aline, const double *sline,
@@ -809,6 +833,18 @@ static double solve_josh(const josh_tables_t *T, int n, const double *acont,
                 xsbar[l] = snubar[0] > EPS ? snubar[0] : EPS;
                 xalpha[l] = alpha[0] < 0.0 ? 0.0 : (alpha[0] > 1.0 ? 1.0 : alpha[0]);
             }
+        }
+        if (g_exact_sweeps) {
+            double xm[NXTAU];
+            for (int l = 0; l < NXTAU; l++) {
+                xs[l] = xsbar[l];
+                xm[l] = xsbar[l] * (1.0 - xalpha[l]);
+            }
+            int it = josh_iterate_exact(T->coefj, xs, xalpha, xm);
+            if (iters_out) *iters_out = it;
+            double flux = 0.0;
+            for (int l = 0; l < NXTAU; l++) flux += T->ch[l] * xs[l];
+            return flux;
         }
         float xs32[NXTAU], xa32[NXTAU], xm32[NXTAU];
         for (int l = 0; l < NXTAU; l++) {

@@ -66,6 +66,12 @@ def set_threads(n: int) -> None:
     lib().kso_set_num_threads(int(n))
 
 
+def set_exact_sweeps(on: bool) -> None:
+    """Solve the JOSH system in FP64 to 1e-13 instead of the reference's FP32
+    sweep (smooth fluxes, for differencing gradients); off = the reference."""
+    lib().kso_set_exact_sweeps(1 if on else 0)
+
+
 def num_threads() -> int:
     return int(lib().kso_num_threads())
 

@@ -60,3 +60,67 @@ def test_adjoint_matches_finite_differences(name):
     # agree closely, a few may differ where a step is crossed within +-h
     assert np.median(errs) < 1e-2, errs
     assert np.mean(errs < 5e-2) >= 0.8, errs
+
+
+def test_adjoint_matches_differenced_oracle():
+    """The adjoint against central differences of the oracle -- the C
+    restatement of the reference path, run independently of this library --
+    with the JOSH system solved exactly (oracle.set_exact_sweeps; the
+    reference's FP32 sweep with its 1e-5 stop is not smooth enough to
+    difference).  h = 1e-4 dex on the most sensitive lines of each parameter
+    class (log gf and the three log damping constants) and on random ones.
+    Tolerance: 1e-4 relative where the difference resolves the gradient; a
+    parameter whose +-h step crosses a TRANSP gate or a wing-reach step (held
+    fixed by the adjoint) may differ, so 80 % of the checks must pass and the
+    median error must be below 1e-5."""
+    from oracle import gfall, oracle
+
+    name = "tiny_500_501"
+    ds, n = _setup(name)
+    dev = ds.flux_total.device
+    zeros = [torch.zeros(n, dtype=torch.float64, device=dev, requires_grad=True) for _ in range(4)]
+    ft0, fc0 = ds.forward()
+    target = ((ft0 / fc0).detach() * 0.98 + 0.01).cpu().numpy()
+    ft, fc = autodiff.synthesize(ds, *zeros)
+    loss = torch.sum((ft / fc - torch.as_tensor(target, device=dev)) ** 2)
+    loss.backward()
+    grads = [z.grad.cpu().numpy() for z in zeros]
+
+    # the oracle's catalog in the GPU's (stable, wavelength-sorted) order
+    w0, w1 = window(name)
+    tb = oracle.tables()
+    ocat = gfall.filter_window(gfall.parse_gfall(gfall_path(name), tb["potion"]), w0, w1)
+    order = np.argsort(ocat["wavelength"], kind="stable")
+    ocat = {k: v[order] for k, v in ocat.items()}
+    assert np.array_equal(ocat["wavelength"], ds.cat.host.wavelength)
+    atm = oracle.load_atmosphere(atm_path(name))
+    cols = ("log_gf", "gamma_rad", "gamma_stark", "gamma_vdw")
+
+    def oracle_loss(p, i, dex):
+        c = {k: v.copy() for k, v in ocat.items()}
+        if p == 0:
+            c["log_gf"][i] += dex
+        else:
+            c[cols[p]][i] *= 10.0 ** dex
+        r = oracle.synthesize(atm, c, w0, w1, tb=tb)
+        return float(np.sum((r["flux_total_hz"] / r["flux_cont_hz"] - target) ** 2))
+
+    h = 1e-4
+    rng = np.random.default_rng(11)
+    errs = []
+    oracle.set_exact_sweeps(True)
+    try:
+        for p in range(4):
+            g = grads[p]
+            for i in list(np.argsort(-np.abs(g))[:4]) + list(rng.integers(0, n, 2)):
+                fd = (oracle_loss(p, i, h) - oracle_loss(p, i, -h)) / (2 * h)
+                scale = max(abs(fd), abs(g[i]))
+                if scale * h <= 1e-11 * float(loss.item()):
+                    continue  # below what the difference resolves
+                errs.append(abs(fd - g[i]) / scale)
+    finally:
+        oracle.set_exact_sweeps(False)
+    errs = np.array(errs)
+    assert errs.size >= 12, errs
+    assert np.median(errs) < 1e-5, errs
+    assert np.mean(errs < 1e-4) >= 0.8, errs
