@@ -69,10 +69,11 @@ def test_adjoint_matches_differenced_oracle():
     reference's FP32 sweep with its 1e-5 stop is not smooth enough to
     difference).  h = 1e-4 dex on the most sensitive lines of each parameter
     class (log gf and the three log damping constants) and on random ones.
-    Tolerance: 1e-4 relative where the difference resolves the gradient; a
-    parameter whose +-h step crosses a TRANSP gate or a wing-reach step (held
-    fixed by the adjoint) may differ, so 80 % of the checks must pass and the
-    median error must be below 1e-5."""
+    The TRANSP gates and the integer wing reach are steps that the adjoint
+    holds fixed; the oracle reports every pair's validity and reach, so a
+    parameter whose +-h runs differ there has crossed a step and is left out
+    (the strongest lines, with the longest far wings, often do).  Every other
+    parameter must agree to 1e-4 relative (median below 1e-6)."""
     from oracle import gfall, oracle
 
     name = "tiny_500_501"
@@ -96,24 +97,30 @@ def test_adjoint_matches_differenced_oracle():
     atm = oracle.load_atmosphere(atm_path(name))
     cols = ("log_gf", "gamma_rad", "gamma_stark", "gamma_vdw")
 
-    def oracle_loss(p, i, dex):
+    def oracle_run(p, i, dex):
         c = {k: v.copy() for k, v in ocat.items()}
         if p == 0:
             c["log_gf"][i] += dex
         else:
             c[cols[p]][i] *= 10.0 ** dex
         r = oracle.synthesize(atm, c, w0, w1, tb=tb)
-        return float(np.sum((r["flux_total_hz"] / r["flux_cont_hz"] - target) ** 2))
+        return (float(np.sum((r["flux_total_hz"] / r["flux_cont_hz"] - target) ** 2)),
+                r["reach"][i].copy(), r["valid_mask"][i].copy())
 
     h = 1e-4
     rng = np.random.default_rng(11)
-    errs = []
+    errs, stepped = [], 0
     oracle.set_exact_sweeps(True)
     try:
         for p in range(4):
             g = grads[p]
-            for i in list(np.argsort(-np.abs(g))[:4]) + list(rng.integers(0, n, 2)):
-                fd = (oracle_loss(p, i, h) - oracle_loss(p, i, -h)) / (2 * h)
+            for i in list(np.argsort(-np.abs(g))[:5]) + list(rng.integers(0, n, 3)):
+                lp, reach_p, valid_p = oracle_run(p, i, h)
+                lm, reach_m, valid_m = oracle_run(p, i, -h)
+                if not (np.array_equal(reach_p, reach_m) and np.array_equal(valid_p, valid_m)):
+                    stepped += 1
+                    continue
+                fd = (lp - lm) / (2 * h)
                 scale = max(abs(fd), abs(g[i]))
                 if scale * h <= 1e-11 * float(loss.item()):
                     continue  # below what the difference resolves
@@ -121,6 +128,6 @@ def test_adjoint_matches_differenced_oracle():
     finally:
         oracle.set_exact_sweeps(False)
     errs = np.array(errs)
-    assert errs.size >= 12, errs
-    assert np.median(errs) < 1e-5, errs
-    assert np.mean(errs < 1e-4) >= 0.8, errs
+    assert errs.size >= 12, (errs, stepped)
+    assert np.median(errs) < 1e-6, errs
+    assert np.all(errs < 1e-4), errs
