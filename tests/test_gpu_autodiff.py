@@ -114,7 +114,7 @@ def test_adjoint_matches_differenced_oracle():
     try:
         for p in range(4):
             g = grads[p]
-            for i in list(np.argsort(-np.abs(g))[:5]) + list(rng.integers(0, n, 3)):
+            for i in list(np.argsort(-np.abs(g))[:6]) + list(rng.integers(0, n, 8)):
                 lp, reach_p, valid_p = oracle_run(p, i, h)
                 lm, reach_m, valid_m = oracle_run(p, i, -h)
                 if not (np.array_equal(reach_p, reach_m) and np.array_equal(valid_p, valid_m)):
