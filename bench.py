@@ -794,8 +794,9 @@ def run_diff(args):
     """Differentiable synthesis (400-700 nm, 500k lines, Teff 6000 K log g 4.3):
     loss = sum (F/Fc - target)^2 with the target synthesised from log gf offsets
     ~ N(0, 0.1); one step = forward + adjoint (gradients for 4 x 500k line
-    parameters); central finite differences on 200 random
-    parameters (h = 1e-4 dex) check the gradient."""
+    parameters); central finite differences (h = 1e-4 dex) on --fd-params
+    parameters, half the most sensitive lines of each class and half at
+    random, check the gradient."""
     import torch
 
     from kurucz_py_joss_submission_gb300 import autodiff, workloads
@@ -856,7 +857,10 @@ def run_diff(args):
         h = 1e-4
         names = ("log_gf", "log_gamma_rad", "log_gamma_stark", "log_gamma_vdw")
         errs = {k: [] for k in names}
-        picks = [(int(rng.integers(4)), int(rng.integers(n))) for _ in range(args.fd_params)]
+        # half among the most sensitive lines of each parameter class, half at random
+        k = max(1, args.fd_params // 8)
+        picks = [(p_, int(i)) for p_ in range(4) for i in np.argsort(-np.abs(grads[p_]))[:k]]
+        picks += [(int(rng.integers(4)), int(rng.integers(n))) for _ in range(args.fd_params - len(picks))]
         for par, i in picks:
             vals = []
             for sgn in (+1, -1):
