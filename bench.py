@@ -770,6 +770,7 @@ def run_batch(args):
                        "layers": sorted({a.layers for a in atms}), "grid_points_min": int(min(npts)),
                        "grid_points_max": int(max(npts)), "grid_points_total": int(sum(npts)),
                        "n_lines_shared": len(cat), "tuned": tuned, "precision": args.precision,
+                       "workspace_bytes": int(bs.workspace_bytes),
                        "l2": "inputs larger than L2 (shared lines 111 MB + per-job descriptors)",
                        "parallelism": "1 GPU" if world == 1 else f"{world} GPUs, jobs split across ranks"},
             "evaluations_per_s": evals * args.steps / (ms / 1e3),
