@@ -360,6 +360,97 @@ ks_status ks_synthesize_batch(const ks_lines *lines, const ks_job *jobs, int32_t
                               const ks_options *opt, void *workspace, size_t workspace_bytes,
                               ks_stats *stats, void *stream);
 
+/* ---- populations (FP64) ------------------------------------------------------ */
+
+/* Data tables of the population stage, host memory (the package's
+ * data/pops_tables.npz).  Once per process, before ks_populations.
+ *   potion [999], nnn [6 * 374] (row-major), atmass [99]:
+ *       synthe_py/data/fortran_data.npz as pops_exact.py:748 loads it;
+ *   pftab [7 * 56 * 10 * 9], pf_potlo / pf_potlolog [7]: the PFIRON table
+ *       (synthe_py/data/pfiron_data.npz, pops_exact.py:831);
+ *   level_e / level_g, level_n [14]: the explicit level sums of PFSAHA,
+ *       concatenated in the order H I, He I, He II, C I, C II, O I, Mg I,
+ *       Mg II, Al I, Si I, Si II, Na I, B I, K I (pops_exact.py:520-741);
+ *   pfg_first [n_pfg_first], pfg_second [n_pfg_second]: PFGROUND labels per
+ *       NELION; per label row r < n_pfg_label: pfg_label[r], the constant
+ *       pfg_g0[r] and the terms pfg_off[r] .. pfg_off[r+1]-1 of
+ *       (pfg_g, pfg_e) = weight * exp(-hc/kT * energy)
+ *       (synthe_py/tools/_pfground_table.py);
+ *   mol_code [n_mol], mol_equil [7 * n_mol] (row-major (7, n_mol)): the
+ *       molecular equilibrium table lines/molecules.dat as READMOL reads it
+ *       (synthe_py/tools/readmol_exact.py:20). */
+typedef struct {
+    const double *potion;
+    const int32_t *nnn;
+    const double *atmass;
+    const double *pftab;
+    const double *pf_potlo;
+    const double *pf_potlolog;
+    const double *level_e;
+    const double *level_g;
+    const int32_t *level_n;
+    const int32_t *pfg_first;
+    int32_t n_pfg_first;
+    const int32_t *pfg_second;
+    int32_t n_pfg_second;
+    const int32_t *pfg_label;
+    const double *pfg_g0;
+    const int32_t *pfg_off;
+    int32_t n_pfg_label;
+    const double *pfg_g;
+    const double *pfg_e;
+    const double *mol_code;
+    const double *mol_equil;
+    int32_t n_mol;
+} ks_pops_tables;
+
+ks_status ks_init_pops_tables(const ks_pops_tables *tables);
+
+/* The molecular system built from the table (READMOL): number of molecules,
+ * of equations, the element of each equation (0 = total particles, 100 =
+ * electrons) and, per element Z-1, 1 when POPS takes its populations from
+ * the molecular equilibrium.  Host; any pointer may be NULL (arrays of 32
+ * and 99 entries). */
+ks_status ks_pops_system(int32_t *n_molecules, int32_t *n_equations, int32_t *equation_element,
+                         int32_t *element_molecular);
+
+/* One model atmosphere for ks_populations: the columns of an ATLAS .atm model,
+ * layers in order of increasing column mass (device pointers). */
+typedef struct {
+    int32_t n_layers;               /* L, 1..4096 */
+    const double *temperature;      /* [L] K */
+    const double *gas_pressure;     /* [L] dyn cm^-2 */
+    const double *vturb;            /* [L] cm s^-1 */
+    const double *xabund;           /* [99] abundances as number fractions (the converter's
+                                       XABUND, convert_atm_to_npz.py:1775-1800) */
+    /* outputs (device) -- the fields of the converted atmosphere the synthesis reads */
+    double *electron_density;       /* [L] XNE after the molecular equilibrium */
+    double *mass_density;           /* [L] XNATOM * WTMOLE * 1.660e-24 */
+    double *hckt;                   /* [L] hc/kT */
+    double *xnf_h;                  /* [L] neutral H number density */
+    double *xnf_he1;                /* [L] neutral He number density */
+    double *xnf_h2;                 /* [L] H2 number density */
+    double *population;             /* [L, 6, 139] population_per_ion (number / partition
+                                       function, per element Z-1 and ion) */
+    double *doppler;                /* [L, 6, 139] doppler_per_ion (Doppler width / c) */
+    double *xnatom;                 /* [L] XNATOM (may be NULL) */
+    int32_t *nmolec_iterations;     /* [L] Newton iterations per layer (may be NULL) */
+} ks_pops_model;
+
+/* Replaces the population stage of synthe_py/tools/convert_atm_to_npz.py
+ * (:1860-2650): the molecular equilibrium NMOLEC (tools/nmolec_exact.py:1742,
+ * Newton iteration per layer, surface first), the ion populations POPS /
+ * PFSAHA (tools/pops_exact.py:1639, :941) of elements 1-99 and the Doppler
+ * widths (tools/pops_exact.py:2027), all in FP64, for n_models atmospheres
+ * in one launch per stage (one warp per model for the molecular
+ * equilibrium).  Workspace: ks_populations_workspace_size bytes of device
+ * memory, 256-byte aligned.  The call copies the model records to the
+ * workspace and returns when the results are ready (it synchronises the
+ * stream). */
+ks_status ks_populations_workspace_size(const ks_pops_model *models, int32_t n_models, size_t *bytes);
+ks_status ks_populations(const ks_pops_model *models, int32_t n_models, void *workspace,
+                         size_t workspace_bytes, void *stream);
+
 /* ---- gfall reader ---------------------------------------------------------- */
 
 /* Native reader of gfall line lists (synthe_py/io/lines/atomic.py:299

@@ -1,6 +1,6 @@
 """Build of the native library ``_lib/libkurucz_gb300.so`` (sm_103a only).
 
-Six translation units compiled in parallel with nvcc and linked into one
+Seven translation units compiled in parallel with nvcc and linked into one
 shared library exporting the C ABI of ``include/kurucz_gb300.h``:
 
 * ``ks_f32.cu``  kernels in single precision (mixed path), ``--fmad=false``
@@ -8,6 +8,7 @@ shared library exporting the C ABI of ``include/kurucz_gb300.h``:
 * ``ks_f64.cu``  kernels in double precision, ``--fmad=false``
 * ``ks_f64_batch.cu`` their batched launches
 * ``ks_api.cu``  C ABI, tables, bins, reach-class partition, drivers
+* ``ks_pops.cu`` FP64 populations (molecular equilibrium, Saha, Doppler), ``--fmad=false``
 * ``ks_gfall.cpp`` native gfall reader
 """
 
@@ -47,6 +48,8 @@ def _units():
         (CSRC / "ks_f64.cu", common + ["--fmad=false"]),
         (CSRC / "ks_f64_batch.cu", common + ["--fmad=false"]),
         (CSRC / "ks_api.cu", common),
+        # FP64 populations: products and sums rounded one by one, as the reference's
+        (CSRC / "ks_pops.cu", common + ["--fmad=false"]),
         (CSRC / "ks_gfall.cpp", ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread"]),
     ]
 

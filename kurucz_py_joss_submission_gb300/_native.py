@@ -19,6 +19,10 @@ from . import _build
 _lib: Optional[C.CDLL] = None
 _lock = threading.Lock()
 TABLES_NPZ = Path(__file__).resolve().parent / "data" / "synthe_tables.npz"
+POPS_TABLES_NPZ = Path(__file__).resolve().parent / "data" / "pops_tables.npz"
+# level tables of the explicit partition-function sums, in the library's order
+POPS_LEVEL_TABLES = ("hyd", "he1", "he2", "c1", "c2", "o1", "mg1", "mg2", "al1", "si1", "si2", "na1",
+                     "b1", "k1")
 
 KS_OK = 0
 KS_PREC_MIXED = 0
@@ -102,6 +106,30 @@ class KsStats(C.Structure):
         return d
 
 
+class KsPopsTables(C.Structure):
+    """ks_pops_tables: host pointers to the population-stage data tables."""
+
+    _fields_ = [
+        ("potion", P), ("nnn", P), ("atmass", P), ("pftab", P), ("pf_potlo", P), ("pf_potlolog", P),
+        ("level_e", P), ("level_g", P), ("level_n", P),
+        ("pfg_first", P), ("n_pfg_first", C.c_int32), ("pfg_second", P), ("n_pfg_second", C.c_int32),
+        ("pfg_label", P), ("pfg_g0", P), ("pfg_off", P), ("n_pfg_label", C.c_int32),
+        ("pfg_g", P), ("pfg_e", P),
+        ("mol_code", P), ("mol_equil", P), ("n_mol", C.c_int32),
+    ]
+
+
+class KsPopsModel(C.Structure):
+    """ks_pops_model: one atmosphere's .atm columns and the population outputs (device)."""
+
+    _fields_ = [
+        ("n_layers", C.c_int32),
+        ("temperature", P), ("gas_pressure", P), ("vturb", P), ("xabund", P),
+        ("electron_density", P), ("mass_density", P), ("hckt", P), ("xnf_h", P), ("xnf_he1", P),
+        ("xnf_h2", P), ("population", P), ("doppler", P), ("xnatom", P), ("nmolec_iterations", P),
+    ]
+
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "ks_version": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -141,6 +169,10 @@ SIGNATURES = {
     "ks_batch_free": (None, [P]),
     "ks_synthesize_batch": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsJob), C.c_int32,
                                         C.POINTER(KsOptions), P, C.c_size_t, C.POINTER(KsStats), P]),
+    "ks_init_pops_tables": (C.c_int32, [C.POINTER(KsPopsTables)]),
+    "ks_pops_system": (C.c_int32, [P, P, P, P]),
+    "ks_populations_workspace_size": (C.c_int32, [C.POINTER(KsPopsModel), C.c_int32, C.POINTER(C.c_size_t)]),
+    "ks_populations": (C.c_int32, [C.POINTER(KsPopsModel), C.c_int32, P, C.c_size_t, P]),
     "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,
                                   C.POINTER(P)]),
     "ks_gfall_sort": (C.c_int32, [P]),
@@ -183,8 +215,38 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         st = L.ks_init_tables(_pd(tabvi), _pd(tabh1), tabvi.size, _pd(xtau), _pd(ch), _pd(coefj))
         if st != KS_OK:
             raise KsError(st, L.ks_last_error().decode())
+        _init_pops_tables(L)
         _lib = L
         return _lib
+
+
+def _init_pops_tables(L: C.CDLL) -> None:
+    """Hand the population-stage tables (``data/pops_tables.npz``) to ``ks_init_pops_tables``."""
+    with np.load(POPS_TABLES_NPZ) as t:
+        a = {k: np.asarray(t[k]) for k in t.files}
+    f64 = lambda x: np.ascontiguousarray(x, dtype=np.float64)  # noqa: E731
+    i32 = lambda x: np.ascontiguousarray(x, dtype=np.int32)  # noqa: E731
+    keep = {
+        "potion": f64(a["potion"]), "nnn": i32(a["nnn"]), "atmass": f64(a["atmass"]),
+        "pftab": f64(a["pftab"]), "pf_potlo": f64(a["pf_potlo"]), "pf_potlolog": f64(a["pf_potlolog"]),
+        "level_e": f64(np.concatenate([a[f"lev_{n}_e"] for n in POPS_LEVEL_TABLES])),
+        "level_g": f64(np.concatenate([a[f"lev_{n}_g"] for n in POPS_LEVEL_TABLES])),
+        "level_n": i32([a[f"lev_{n}_e"].size for n in POPS_LEVEL_TABLES]),
+        "pfg_first": i32(a["pfg_first"]), "pfg_second": i32(a["pfg_second"]),
+        "pfg_label": i32(a["pfg_label"]), "pfg_g0": f64(a["pfg_g0"]), "pfg_off": i32(a["pfg_off"]),
+        "pfg_g": f64(a["pfg_g"]), "pfg_e": f64(a["pfg_e"]),
+        "mol_code": f64(a["mol_code"]), "mol_equil": f64(a["mol_equil"]),
+    }
+    t = KsPopsTables()
+    for k, v in keep.items():
+        setattr(t, k, v.ctypes.data)
+    t.n_pfg_first = keep["pfg_first"].size
+    t.n_pfg_second = keep["pfg_second"].size
+    t.n_pfg_label = keep["pfg_label"].size
+    t.n_mol = keep["mol_code"].size
+    st = L.ks_init_pops_tables(C.byref(t))
+    if st != KS_OK:
+        raise KsError(st, L.ks_last_error().decode())
 
 
 def _pd(a: np.ndarray):

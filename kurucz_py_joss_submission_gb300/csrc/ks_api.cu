@@ -38,6 +38,9 @@ static ks_status cuda_fail(cudaError_t e, const char* where) {
 
 extern "C" const char* ks_last_error(void) { return g_last_error.c_str(); }
 
+// Error setter for the other translation units of the library.
+ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(code, msg); }
+
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
     if (minor) *minor = 0;

@@ -3,6 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
+#include "kurucz_gb300.h"
 #include "ks_internal.h"
 
 namespace ks {
@@ -45,6 +48,9 @@ struct CoefJ32 {
 
 KS_DECLARE_LAUNCHERS(float, f32)
 KS_DECLARE_LAUNCHERS(double, f64)
+
+// records `msg` as the calling thread's last error (ks_last_error) and returns `code`
+ks_status set_error(ks_status code, const std::string& msg);
 
 // adjoint kernels (FP64 unit)
 cudaError_t launch_transfer_adjoint(const AdjArgs& a, cudaStream_t s);

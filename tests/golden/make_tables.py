@@ -21,7 +21,9 @@ Run once where the reference checkout exists (``--reference DIR`` or
 from __future__ import annotations
 
 import importlib.util
+import math
 import os
+import re
 import sys
 from pathlib import Path
 
@@ -69,7 +71,106 @@ def main(argv: list) -> int:
         extab=et.extab, extabf=et.extabf,
     )
     print(f"wrote {OUT}")
+    write_pops_tables()
     return 0
+
+
+# Level tables of the explicit partition-function sums of PFSAHA
+# (synthe_py/tools/pops_exact.py:520-741): energy (cm^-1) and weight per level.
+_LEVEL_TABLES = ("HYD", "HE1", "HE2", "C1", "C2", "O1", "MG1", "MG2", "AL1", "SI1", "SI2",
+                 "NA1", "B1", "K1")
+
+_TERM = re.compile(r"([+-]?)(?:([0-9.]+(?:[eE][+-]?[0-9]+)?)\*)?math\.exp\(-_HCK/T\*"
+                   r"([0-9.]+(?:[eE][+-]?[0-9]+)?)\)")
+
+
+def _parse_pfground(expr: str):
+    """Split one PFGROUND expression into its constant and (weight, energy) terms.
+
+    Every expression is ``g0 + g1*exp(-HCK/T*E1) + ...`` (a missing weight is 1);
+    the split is checked against the reference's own evaluation by the caller.
+    """
+    expr = expr.replace(" ", "")
+    m = re.match(r"^([0-9.]+(?:[eE][+-]?[0-9]+)?)", expr)
+    g0 = float(m.group(1))
+    rest = expr[m.end():]
+    terms = []
+    pos = 0
+    for t in _TERM.finditer(rest):
+        if t.start() != pos or t.group(1) != "+":
+            raise ValueError(f"unexpected PFGROUND form: {expr}")
+        terms.append((float(t.group(2)) if t.group(2) else 1.0, float(t.group(3))))
+        pos = t.end()
+    if pos != len(rest):
+        raise ValueError(f"unexpected PFGROUND form: {expr}")
+    return g0, terms
+
+
+def write_pops_tables() -> None:
+    """Write ``pops_tables.npz``: the data of the FP64 population stage.
+
+    * ``potion`` (999), ``nnn`` (6 x 374), ``atmass`` (99): ionisation
+      potentials, packed partition-function table and atomic masses
+      (``synthe_py/data/fortran_data.npz``);
+    * ``pftab`` (7 x 56 x 10 x 9), ``pf_potlo``/``pf_potlolog`` (7): the
+      iron-group partition-function table (``synthe_py/data/pfiron_data.npz``);
+    * ``lev_<name>_e``/``lev_<name>_g``: level energies and weights of the
+      explicit sums (``synthe_py/tools/pops_exact.py:520-741``);
+    * ``pfg_first`` (114), ``pfg_second`` (168): PFGROUND labels per NELION,
+      and per label its constant and (weight, energy) terms as a CSR table
+      ``pfg_label``, ``pfg_g0``, ``pfg_off``, ``pfg_g``, ``pfg_e``
+      (``synthe_py/tools/_pfground_table.py``);
+    * ``mol_code`` (nummol), ``mol_equil`` (7 x nummol): the molecular
+      equilibrium table ``lines/molecules.dat`` as READMOL reads it
+      (``synthe_py/tools/readmol_exact.py:20``).
+    """
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "numba_shim"))
+    sys.path.insert(0, str(REFERENCE))
+    import synthe_py.tools.pops_exact as pe
+    import synthe_py.tools._pfground_table as pg
+    from synthe_py.tools.readmol_exact import readmol_exact
+
+    out = {}
+    with np.load(REFERENCE / "synthe_py/data/fortran_data.npz") as d:
+        out["potion"] = np.asarray(d["potion"], dtype=np.float64)
+        out["nnn"] = np.asarray(d["nnn"], dtype=np.int32)
+        out["atmass"] = np.asarray(d["atmass"], dtype=np.float64)
+    with np.load(REFERENCE / "synthe_py/data/pfiron_data.npz") as d:
+        out["pftab"] = np.asarray(d["pftab"], dtype=np.float64)
+        out["pf_potlo"] = np.asarray(d["potlo"], dtype=np.float64)
+        out["pf_potlolog"] = np.asarray(d["potlolog"], dtype=np.float64)
+    for name in _LEVEL_TABLES:
+        out[f"lev_{name.lower()}_e"] = np.asarray(getattr(pe, "E" + name), dtype=np.float64)
+        out[f"lev_{name.lower()}_g"] = np.asarray(getattr(pe, "G" + name), dtype=np.float64)
+    labels = sorted(pg.PFGROUND_EXPRESSIONS)
+    g0s, offs, gs, es = [], [0], [], []
+    hck = 6.6256e-27 * 2.99792458e10 / 1.38054e-16
+    for lab in labels:
+        g0, terms = _parse_pfground(pg.PFGROUND_EXPRESSIONS[lab])
+        g0s.append(g0)
+        gs += [g for g, _ in terms]
+        es += [e for _, e in terms]
+        offs.append(len(gs))
+        ref = pe._PFGROUND_FUNCS[lab]
+        for t in (1500.0, 3000.0, 5000.0, 8000.0, 20000.0):
+            v = g0
+            for g, e in terms:
+                v = v + g * math.exp(-hck / t * e)
+            if v != float(ref(t)):
+                raise ValueError(f"PFGROUND label {lab}: split form differs at T={t}")
+    out["pfg_first"] = np.asarray(pg.FIRST_RANGE_LABELS, dtype=np.int32)
+    out["pfg_second"] = np.asarray(pg.SECOND_RANGE_LABELS, dtype=np.int32)
+    out["pfg_label"] = np.asarray(labels, dtype=np.int32)
+    out["pfg_g0"] = np.asarray(g0s, dtype=np.float64)
+    out["pfg_off"] = np.asarray(offs, dtype=np.int32)
+    out["pfg_g"] = np.asarray(gs, dtype=np.float64)
+    out["pfg_e"] = np.asarray(es, dtype=np.float64)
+    nummol, code_mol, equil, *_ = readmol_exact(REFERENCE / "lines" / "molecules.dat")
+    out["mol_code"] = np.asarray(code_mol[:nummol], dtype=np.float64)
+    out["mol_equil"] = np.asarray(equil[:, :nummol], dtype=np.float64)
+    path = OUT.parent / "pops_tables.npz"
+    np.savez_compressed(path, **out)
+    print(f"wrote {path}")
 
 
 if __name__ == "__main__":
