@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -614,6 +615,7 @@ FORMS = {
     "batch_256": ["--workload", "batch_256", "--steps", "3", "--warmup", "3"],
     "dense_10m": ["--workload", "dense_10m", "--steps", "3", "--warmup", "3", "--skip-cpu"],
     "diff_400_700": ["--workload", "diff_400_700", "--steps", "3", "--warmup", "3", "--fd-params", "40"],
+    "pops_256": ["--workload", "pops_256", "--steps", "5", "--warmup", "3"],
 }
 
 
@@ -791,6 +793,128 @@ def run_batch(args):
     return 0
 
 
+POPS_SEED = 404
+POPS_MODELS = 256
+
+
+def pops_models(work: Path) -> list:
+    """256 seeded grey ATLAS models with the batched workload's distributions:
+    layers uniform in 64..80, Teff log-uniform in 3500..40000 K, log g uniform
+    in 0..5, [M/H] uniform in -2..+0.5; written as .atm files."""
+    from kurucz_py_joss_submission_gb300 import workloads
+
+    rng = np.random.default_rng(POPS_SEED)
+    out = []
+    for k in range(POPS_MODELS):
+        n = int(rng.integers(64, 81))
+        teff = float(math.exp(rng.uniform(math.log(3500.0), math.log(40000.0))))
+        logg = float(rng.uniform(0.0, 5.0))
+        mh = float(rng.uniform(-2.0, 0.5))
+        p = work / f"model_{k}.atm"
+        workloads.grey_atmosphere_atm(p, teff, logg, mh, n_layers=n)
+        out.append((p, dict(n_layers=n, teff=teff, logg=logg, metallicity=mh)))
+    return out
+
+
+def run_pops(args):
+    """FP64 populations (molecular equilibrium, Saha ion populations, Doppler
+    widths) of 256 fresh model atmospheres in one ks_populations call per
+    step; atmospheres/s, accuracy against the oracle on a sample."""
+    import tempfile
+
+    import torch
+
+    from kurucz_py_joss_submission_gb300.physics import populations as P
+    from oracle import pops as opops
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if rank != 0:
+        return 0  # one call holds every model; replicas only
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    with tempfile.TemporaryDirectory(prefix="kgb300_pops_") as tmp:
+        models = pops_models(Path(tmp))
+        parsed = [P.parse_atm_file(p) for p, _ in models]
+        dp = P.DevicePopulations(parsed, device=dev)
+        for _ in range(args.warmup):
+            dp.run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record()
+            for _ in range(args.steps):
+                dp.run()
+            e1.record()
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        # end to end: the models' columns in from pinned host memory, every field out
+        ins = [(torch.empty(t.shape, dtype=t.dtype, pin_memory=True).copy_(t.cpu()), t)
+               for d in dp.inputs for t in d.values()]
+        outs = [(torch.empty(t.shape, dtype=t.dtype, pin_memory=True), t) for d in dp.outputs for t in d.values()]
+        h2d = sum(h.numel() * h.element_size() for h, _ in ins)
+        d2h = sum(h.numel() * h.element_size() for h, _ in outs)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            for h, t in ins:
+                t.copy_(h, non_blocking=True)
+            dp.run()
+            for h, t in outs:
+                h.copy_(t, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / args.steps
+        # accuracy and CPU baseline: the oracle (FP64 restatement, one core) on a sample
+        sample = [0, 1, 2, 3, 64, 128, 192, 255]
+        mol = {int(c) for c in opops.readmol()[0] if c < 100}
+        errs = {"scalars": 0.0, "populations_saha": 0.0, "populations_molecular": 0.0, "doppler": 0.0}
+        t0 = time.perf_counter()
+        for k in sample:
+            ref = opops.convert(models[k][0])
+            out = dp.host(k)
+
+            def rel(a, b):
+                m = (a != 0) | (b != 0)
+                return float(np.max(np.abs(a[m] - b[m]) / np.maximum(np.abs(b[m]), 1e-300))) if m.any() else 0.0
+
+            for f in ("electron_density", "mass_density", "hckt", "xnf_h", "xnf_he1", "xnf_h2"):
+                errs["scalars"] = max(errs["scalars"], rel(out[f], ref[f]))
+            errs["doppler"] = max(errs["doppler"], rel(out["doppler_per_ion"], ref["doppler_per_ion"]))
+            for z in range(1, 100):
+                key = "populations_molecular" if z in mol else "populations_saha"
+                errs[key] = max(errs[key], rel(out["population_per_ion"][:, :, z - 1],
+                                               ref["population_per_ion"][:, :, z - 1]))
+        cpu_s = (time.perf_counter() - t0) / len(sample)
+        layers = [m[1]["n_layers"] for m in models]
+        teffs = [m[1]["teff"] for m in models]
+        iters = np.concatenate([dp.host(k)["nmolec_iterations"] for k in range(len(models))])
+    line = {
+        "metric": "atmospheres/s (FP64 populations: molecular equilibrium, Saha ion populations, Doppler "
+                  "widths; 256 models per ks_populations call)",
+        "value": POPS_MODELS / (ms / 1e3), "unit": "atmospheres/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "pops_256", "models": POPS_MODELS, "layers": [min(layers), max(layers)],
+                   "layers_total": int(sum(layers)), "teff_K": [round(min(teffs)), round(max(teffs))],
+                   "seed": POPS_SEED, "l2": "small inputs (~0.2 MB); outputs 245 MB per step, larger than L2",
+                   "parallelism": "1 GPU"},
+        "newton_iterations": {"total": int(iters.sum()), "max_per_layer": int(iters.max()),
+                              "mean_per_layer": float(iters.mean())},
+        "accuracy_vs_oracle": dict(errs, models_checked=len(sample)),
+        "e2e": {"value": POPS_MODELS / (e2e_ms / 1e3), "unit": "atmospheres/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+        "roofline": None,
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "atmospheres/s", "cores": 1, "kind": "port",
+                         "sample": f"oracle (FP64 numpy restatement) on {len(sample)} of the models, "
+                                   f"{cpu_s:.2f} s per model"},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_diff(args):
     """Differentiable synthesis (400-700 nm, 500k lines, Teff 6000 K log g 4.3):
     loss = sum (F/Fc - target)^2 with the target synthesised from log gf offsets
@@ -920,7 +1044,7 @@ def main():
                     help="diff_400_700: parameters checked by central finite differences")
     ap.add_argument("--window", type=float, nargs=2, default=None,
                     help="restrict the workload to a wavelength window (small profiling case)")
-    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS) + ["batch_256", "diff_400_700"],
+    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS) + ["batch_256", "diff_400_700", "pops_256"],
                     default="full_300_1800",
                     help="full_300_1800 (headline: 1.5M lines, Teff 5800 K), window_500_510 (20k lines, "
                          "the CPU-runnable reference case), dense_10m (10M lines, Teff 2500 K, log g -1)")
@@ -931,6 +1055,11 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no gradients"}))
             return 0
         return run_diff(args)
+    if args.workload == "pops_256":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "population workload: timed on the GPU path only"}))
+            return 0
+        return run_pops(args)
     if args.workload == "batch_256":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "batched workload: timed on the GPU path only"}))

@@ -48,6 +48,9 @@ def build_parser() -> argparse.ArgumentParser:
     p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     p.add_argument("--tile-bins", type=int, default=0)
     p.add_argument("--warps-per-tile", type=int, default=0)
+    p.add_argument("--populations", choices=["npz", "gpu"], default="npz",
+                   help="npz: populations from the converted model; gpu: recomputed from MODEL.atm on the GPU "
+                        "in FP64 (molecular equilibrium, Saha, Doppler), continuum tables from the .npz")
     return p
 
 
@@ -71,6 +74,7 @@ def main(argv: Optional[list] = None) -> int:
         rhoxj_scale=args.rhoxj, npz_path=args.npz, n_workers=args.n_workers,
         allow_tfort_runtime=args.allow_tfort_runtime, precision=args.precision,
         tile_bins=args.tile_bins, warps_per_tile=args.warps_per_tile,
+        populations=args.populations,
     )
     cfg.log_level = args.log_level
     logging.basicConfig(level=getattr(logging, args.log_level),

@@ -61,6 +61,10 @@ class SynthesisConfig:
     precision: str = "mixed"
     tile_bins: int = 0
     warps_per_tile: int = 0
+    # "npz": every atmosphere field from the converted model; "gpu": the
+    # populations, Doppler widths, electron and mass densities recomputed from
+    # the .atm model on the GPU (FP64), the continuum tables from the .npz
+    populations: str = "npz"
 
     @classmethod
     def from_cli(
@@ -90,6 +94,7 @@ class SynthesisConfig:
         precision: str = "mixed",
         tile_bins: int = 0,
         warps_per_tile: int = 0,
+        populations: str = "npz",
     ) -> "SynthesisConfig":
         return cls(
             wavelength_grid=WavelengthGrid(start=wl_start, end=wl_end, resolution=resolution,
@@ -104,7 +109,7 @@ class SynthesisConfig:
             enable_helium_wings=enable_helium_wings, skip_hydrogen_wings=skip_hydrogen_wings,
             line_filter=line_filter, wavelength_subsample=wavelength_subsample,
             n_workers=n_workers, precision=precision, tile_bins=tile_bins,
-            warps_per_tile=warps_per_tile,
+            warps_per_tile=warps_per_tile, populations=populations,
         )
 
 

@@ -78,7 +78,15 @@ def _load_atmosphere(cfg: SynthesisConfig) -> atm_io.AtmosphereModel:
                 f"Could not find cached .npz atmosphere file for {path}; convert it first "
                 "(synthe_py/tools/convert_atm_to_npz.py) or pass --npz")
         path = cand
-    return atm_io.load_cached(path)
+    atm = atm_io.load_cached(path)
+    if cfg.populations == "gpu":
+        from ..physics.populations import DevicePopulations
+
+        model = Path(cfg.atmosphere.model_path)
+        if model.suffix == ".npz":
+            raise ValueError("--populations gpu needs the ATLAS .atm model as MODEL")
+        atm = DevicePopulations([model]).run().atmosphere(0, continuum=atm)
+    return atm
 
 
 def run_synthesis(cfg: SynthesisConfig) -> SynthResult:

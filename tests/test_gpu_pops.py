@@ -103,3 +103,26 @@ def test_rejects_bad_models():
         P.layer_columns({"glog": 4.0, "layers": [
             {"RHOX": 2.0, "T": 5000.0, "P": 1e4, "XNE": 1e12, "ABROSS": 0, "ACCRAD": 0, "VTURB": 0},
             {"RHOX": 1.0, "T": 5000.0, "P": 1e4, "XNE": 1e12, "ABROSS": 0, "ACCRAD": 0, "VTURB": 0}]})
+
+
+def test_cli_gpu_populations_spec(tmp_path):
+    """``cli.main MODEL.atm LINES.gf --populations gpu``: populations from the
+    .atm on the GPU, continuum tables from the converted model beside it; the
+    .spec columns equal the reference's to its printed precision."""
+    from kurucz_py_joss_submission_gb300 import cli
+
+    name = "tiny_500_501"
+    g = golden(name)
+    w0, w1 = window(name)
+    atm = tmp_path / "model.atm"
+    atm.write_text((GOLDEN / "atm_t5800g444.atm").read_text())
+    (tmp_path / "model.npz").write_bytes((GOLDEN / "atm_t5800g444.npz").read_bytes())
+    spec = tmp_path / "out.spec"
+    rc = cli.main([str(atm), str(gfall_path(name)), "--spec", str(spec), "--wl-start", str(w0),
+                   "--wl-end", str(w1), "--precision", "fp64", "--populations", "gpu"])
+    assert rc == 0
+    ours = np.loadtxt(spec)
+    ref = g["spec"]
+    assert ours.shape == ref.shape
+    assert np.array_equal(ours[:, 0], ref[:, 0])
+    assert np.allclose(ours[:, 1:], ref[:, 1:], rtol=1e-6, atol=0.0)
