@@ -288,6 +288,37 @@ ks_status ks_synthesize_adjoint(const ks_lines *lines, const ks_atmos *atm, cons
                                 double *d_log_gf, double *d_log_gamma_rad, double *d_log_gamma_stark,
                                 double *d_log_gamma_vdw, ks_stats *stats, void *stream);
 
+/* The adjoint of ks_synthesize_adjoint, plus the atmosphere terms that carry
+ * the gradient on to the populations (and through ks_populations_tangent to
+ * the abundances).  Lines are grouped by species by the caller: line_order
+ * holds the rows of `lines` grouped by (element_idx, ion_stage), each group
+ * in ascending row order, group g = line_order[group_first[g] ..
+ * group_first[g+1]) with species (ion_stage - 1) * n_elem + element_idx in
+ * group_species[g] (device arrays), so every sum has a fixed order.  Out
+ * (device, double): dLoss/d ln population_per_ion [L, n_ion, n_elem] (zero
+ * for species without lines), dLoss/d ln mass_density [L] (through
+ * XNFDOP = POP / (RHO DOPPLE)), dLoss/dXNE and dLoss/dTXNXN [L] (through the
+ * Stark and van der Waals damping).  The continuum opacity tables, the TRANSP
+ * gates and the wing reach are held fixed.  No counterpart in the
+ * reference. */
+typedef struct {
+    const int32_t *line_order;
+    const int32_t *group_first;
+    const int32_t *group_species;
+    int32_t n_groups;
+    double *d_ln_population;
+    double *d_ln_mass_density;
+    double *d_electron_density;
+    double *d_txnxn;
+} ks_atm_grad;
+
+ks_status ks_synthesize_adjoint_atmos(const ks_lines *lines, const ks_atmos *atm, const ks_grid *grid,
+                                      const ks_options *opt, void *workspace, size_t workspace_bytes,
+                                      const double *g_flux_total, double *flux_total, double *flux_cont,
+                                      double *d_log_gf, double *d_log_gamma_rad, double *d_log_gamma_stark,
+                                      double *d_log_gamma_vdw, const ks_atm_grad *atm_grad, ks_stats *stats,
+                                      void *stream);
+
 /* The fused synthesis of ks_synthesize for callers that cannot allocate
  * device memory: a plug-in running inside a host application that owns all
  * device memory, or a runtime reached through an FFI with no CUDA allocator,
@@ -450,6 +481,32 @@ typedef struct {
 ks_status ks_populations_workspace_size(const ks_pops_model *models, int32_t n_models, size_t *bytes);
 ks_status ks_populations(const ks_pops_model *models, int32_t n_models, void *workspace,
                          size_t workspace_bytes, void *stream);
+
+/* Forward-mode derivatives of the population stage with respect to the log10
+ * abundance (dex) of one element: `model` as for ks_populations (its value
+ * outputs may be NULL, except none are needed), `element` = Z-1, and device
+ * arrays receiving d(field)/d(log10 XABUND[element]) for the fields the
+ * synthesis reads (the Doppler widths and hc/kT do not depend on the
+ * abundances).  Every step of ks_populations is differentiated as computed
+ * (dual numbers through the Newton iterations, the same pivots and iteration
+ * counts), one warp per (model, element) pair, so any number of pairs cost
+ * about one model's time.  No counterpart in the reference (it has no
+ * gradients). */
+typedef struct {
+    ks_pops_model model;
+    int32_t element;
+    double *d_electron_density;     /* [L] */
+    double *d_mass_density;         /* [L] */
+    double *d_xnf_h;                /* [L] */
+    double *d_xnf_he1;              /* [L] */
+    double *d_xnf_h2;               /* [L] */
+    double *d_population;           /* [L, 6, 139] */
+} ks_pops_tangent;
+
+ks_status ks_populations_tangent_workspace_size(const ks_pops_tangent *tangents, int32_t n,
+                                                size_t *bytes);
+ks_status ks_populations_tangent(const ks_pops_tangent *tangents, int32_t n, void *workspace,
+                                 size_t workspace_bytes, void *stream);
 
 /* ---- gfall reader ---------------------------------------------------------- */
 

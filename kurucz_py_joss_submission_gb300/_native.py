@@ -130,6 +130,25 @@ class KsPopsModel(C.Structure):
     ]
 
 
+class KsPopsTangent(C.Structure):
+    """ks_pops_tangent: a model and the derivative outputs for one element's log10 abundance."""
+
+    _fields_ = [
+        ("model", KsPopsModel), ("element", C.c_int32),
+        ("d_electron_density", P), ("d_mass_density", P), ("d_xnf_h", P), ("d_xnf_he1", P),
+        ("d_xnf_h2", P), ("d_population", P),
+    ]
+
+
+class KsAtmGrad(C.Structure):
+    """ks_atm_grad: line groups by species and the atmosphere-term outputs of the adjoint."""
+
+    _fields_ = [
+        ("line_order", P), ("group_first", P), ("group_species", P), ("n_groups", C.c_int32),
+        ("d_ln_population", P), ("d_ln_mass_density", P), ("d_electron_density", P), ("d_txnxn", P),
+    ]
+
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "ks_version": (C.c_int32, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
@@ -158,6 +177,9 @@ SIGNATURES = {
     "ks_synthesize_adjoint": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                           C.POINTER(KsOptions), P, C.c_size_t, P, P, P, P, P, P, P,
                                           C.POINTER(KsStats), P]),
+    "ks_synthesize_adjoint_atmos": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
+                                                C.POINTER(KsOptions), P, C.c_size_t, P, P, P, P, P, P, P,
+                                                C.POINTER(KsAtmGrad), C.POINTER(KsStats), P]),
     "ks_synthesize_noalloc": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsAtmos), C.POINTER(KsGrid),
                                           C.POINTER(KsOptions), P, P, P, P]),
     "ks_check_flags": (C.c_int32, [P, C.POINTER(C.c_int32)]),
@@ -173,6 +195,9 @@ SIGNATURES = {
     "ks_pops_system": (C.c_int32, [P, P, P, P]),
     "ks_populations_workspace_size": (C.c_int32, [C.POINTER(KsPopsModel), C.c_int32, C.POINTER(C.c_size_t)]),
     "ks_populations": (C.c_int32, [C.POINTER(KsPopsModel), C.c_int32, P, C.c_size_t, P]),
+    "ks_populations_tangent_workspace_size": (C.c_int32, [C.POINTER(KsPopsTangent), C.c_int32,
+                                                          C.POINTER(C.c_size_t)]),
+    "ks_populations_tangent": (C.c_int32, [C.POINTER(KsPopsTangent), C.c_int32, P, C.c_size_t, P]),
     "ks_gfall_read": (C.c_int32, [C.c_char_p, C.c_double, C.c_double, PD, C.c_int32,
                                   C.POINTER(P)]),
     "ks_gfall_sort": (C.c_int32, [P]),

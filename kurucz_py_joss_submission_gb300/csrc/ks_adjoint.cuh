@@ -561,4 +561,69 @@ __global__ void line_grad_kernel(LineGradArgs a) {
     a.d_loggw[li] = ln10 * a.gamma_vdw[li] * sw;
 }
 
+// Atmosphere terms, stage 1: one block per (species group, depth).  With the
+// line's contributions c proportional to kappa0 = CGF * POP / (RHO * DOPPLE)
+// * BOLT (line_opacity.py:101-184, :1141-1294), sum G c over a pair is
+// dLoss/d ln POP of its species at that depth (and minus dLoss/d ln RHO); with
+// a = (GAMRF + GAMSF * XNE + GAMWF * TXNXN) / DOPPLE, sum G dc/da * GAMSF /
+// DOPPLE is its dLoss/dXNE and * GAMWF / DOPPLE its dLoss/dTXNXN.  The gates
+// and the wing reach are held fixed, as for the line gradients.  Lanes take
+// the group's lines in a fixed stride and the block sums in a fixed tree.
+__global__ void __launch_bounds__(128) atm_grad_group_kernel(AtmGradArgs a) {
+    const int g = blockIdx.x, d = blockIdx.y;
+    const int f0 = a.group_first[g], f1 = a.group_first[g + 1];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int k = f0 + (int)threadIdx.x; k < f1; k += blockDim.x) {
+        const int64_t li = a.order[k];
+        const int64_t slot = (int64_t)d * a.stride + li;
+        if (a.cls[slot] == 0xff) continue;
+        s0 += a.g_gf[slot];
+        const double ga = a.g_a[slot];
+        if (ga == 0.0) continue;
+        const int e = a.element_idx[li], ion = a.ion_stage[li];
+        if (e < 0 || e >= a.n_elem || ion <= 0 || ion > a.n_ion) continue;
+        const IonPar& q = a.ion[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
+        if (!(q.dop > 0.0) || !(a.desc[slot].adamp > 1e-12)) continue;
+        const double f = ga / q.dop;
+        s1 += f * a.gamma_stark[li];
+        s2 += f * a.gamma_vdw[li];
+    }
+    __shared__ double r0[128], r1[128], r2[128];
+    r0[threadIdx.x] = s0;
+    r1[threadIdx.x] = s1;
+    r2[threadIdx.x] = s2;
+    __syncthreads();
+    for (int w = 64; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            r0[threadIdx.x] += r0[threadIdx.x + w];
+            r1[threadIdx.x] += r1[threadIdx.x + w];
+            r2[threadIdx.x] += r2[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double* p = a.part + ((int64_t)d * a.n_groups + g) * 3;
+        p[0] = r0[0];
+        p[1] = r1[0];
+        p[2] = r2[0];
+        a.d_ln_pop[(int64_t)d * a.n_ion * a.n_elem + a.group_species[g]] = r0[0];
+    }
+}
+
+// Stage 2: per depth, the groups' sums in group order.
+__global__ void atm_grad_depth_kernel(AtmGradArgs a) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= a.n_layers) return;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int g = 0; g < a.n_groups; g++) {
+        const double* p = a.part + ((int64_t)d * a.n_groups + g) * 3;
+        s0 += p[0];
+        s1 += p[1];
+        s2 += p[2];
+    }
+    a.d_ln_rho[d] = -s0;
+    a.d_xne[d] = s1;
+    a.d_txnxn[d] = s2;
+}
+
 }  // namespace ks

@@ -1377,11 +1377,11 @@ extern "C" ks_status ks_transfer_opacity(const ks_atmos* atm, const ks_grid* gri
 // adjoints of the transfer and of the accumulation for a loss whose
 // derivative with respect to F_total is g_flux_total: gradients with respect
 // to log10 gf and the three log10 damping constants of every line.
-extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
-                                           const ks_options* opt, void* workspace, size_t workspace_bytes,
-                                           const double* g_flux_total, double* flux_total, double* flux_cont,
-                                           double* d_log_gf, double* d_log_gamma_rad, double* d_log_gamma_stark,
-                                           double* d_log_gamma_vdw, ks_stats* stats, void* stream) {
+static ks_status adjoint_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                              const ks_options* opt, void* workspace, size_t workspace_bytes,
+                              const double* g_flux_total, double* flux_total, double* flux_cont,
+                              double* d_log_gf, double* d_log_gamma_rad, double* d_log_gamma_stark,
+                              double* d_log_gamma_vdw, const ks_atm_grad* ag, ks_stats* stats, void* stream) {
     ks_status st = check_atmos(atm);
     if (!st) st = check_grid(grid);
     if (!st) st = check_lines(lines);
@@ -1395,6 +1395,9 @@ extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos
         !d_log_gamma_vdw)
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: NULL input/output");
     if ((st = check_tiling(opt))) return st;
+    if (ag && (!ag->d_ln_population || !ag->d_ln_mass_density || !ag->d_electron_density || !ag->d_txnxn ||
+               ag->n_groups < 0 || (ag->n_groups > 0 && (!ag->line_order || !ag->group_first || !ag->group_species))))
+        return fail(KS_ERR_INVALID, "ks_synthesize_adjoint_atmos: incomplete ks_atm_grad record");
     DevTables t;
     if ((st = device_tables(&t))) return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1415,11 +1418,13 @@ extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos
     // adjoint scratch
     const size_t n_asy = (size_t)L * grid->n, n_slot = (size_t)L * w.stride;
     char* buf = nullptr;
-    const size_t bytes = sizeof(double) * (n_asy + 2 * n_slot) + 256;
+    const size_t n_part = ag ? (size_t)L * (size_t)ag->n_groups * 3 : 0;
+    const size_t bytes = sizeof(double) * (n_asy + 2 * n_slot + n_part) + 256;
     KS_CUDA(cudaMallocAsync((void**)&buf, bytes, s));
     double* g_asy = (double*)buf;
     double* g_gf = g_asy + n_asy;
     double* g_a = g_gf + n_slot;
+    double* part = g_a + n_slot;
     unsigned long long* skipped = w.counters + 3;
     AdjArgs aa;
     aa.n = grid->n;
@@ -1472,6 +1477,33 @@ extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos
     cudaError_t e = launch_transfer_adjoint(aa, s);
     if (e == cudaSuccess) e = launch_line_adjoint(la, s);
     if (e == cudaSuccess) e = launch_line_grad(lg, s);
+    if (e == cudaSuccess && ag) {
+        AtmGradArgs g;
+        g.stride = w.stride;
+        g.n_layers = L;
+        g.n_ion = atm->n_ion;
+        g.n_elem = atm->n_elem;
+        g.n_groups = ag->n_groups;
+        g.cls = w.cls;
+        g.g_gf = g_gf;
+        g.g_a = g_a;
+        g.ion = w.ion;
+        g.desc = (const PairDesc<double>*)w.desc;
+        g.element_idx = lines->element_idx;
+        g.ion_stage = lines->ion_stage;
+        g.gamma_stark = lines->gamma_stark;
+        g.gamma_vdw = lines->gamma_vdw;
+        g.order = ag->line_order;
+        g.group_first = ag->group_first;
+        g.group_species = ag->group_species;
+        g.part = part;
+        g.d_ln_pop = ag->d_ln_population;
+        g.d_ln_rho = ag->d_ln_mass_density;
+        g.d_xne = ag->d_electron_density;
+        g.d_txnxn = ag->d_txnxn;
+        e = cudaMemsetAsync(ag->d_ln_population, 0, sizeof(double) * (size_t)L * atm->n_ion * atm->n_elem, s);
+        if (e == cudaSuccess) e = launch_atm_grad(g, s);
+    }
     cudaFreeAsync(buf, s);
     if (e != cudaSuccess) return fail(KS_ERR_CUDA, cudaGetErrorString(e));
     if (stats) {
@@ -1480,10 +1512,31 @@ extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos
         KS_CUDA(cudaMemcpyAsync(&sk, skipped, sizeof(sk), cudaMemcpyDeviceToHost, s));
         KS_CUDA(cudaStreamSynchronize(s));
         stats->maxj_wavelengths = (int64_t)sk;  // columns given zero gradient (MAXJ = 1 or masked layers)
-        stats->kernel_launches = fused_launches(lines->n_lines > 0, true, &o, true) + 3;
+        stats->kernel_launches = fused_launches(lines->n_lines > 0, true, &o, true) + 3 +
+                                 (ag ? (ag->n_groups > 0 ? 2 : 1) : 0);
         return st;
     }
     return KS_OK;
+}
+
+extern "C" ks_status ks_synthesize_adjoint(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                                           const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                           const double* g_flux_total, double* flux_total, double* flux_cont,
+                                           double* d_log_gf, double* d_log_gamma_rad, double* d_log_gamma_stark,
+                                           double* d_log_gamma_vdw, ks_stats* stats, void* stream) {
+    return adjoint_impl(lines, atm, grid, opt, workspace, workspace_bytes, g_flux_total, flux_total, flux_cont,
+                        d_log_gf, d_log_gamma_rad, d_log_gamma_stark, d_log_gamma_vdw, nullptr, stats, stream);
+}
+
+extern "C" ks_status ks_synthesize_adjoint_atmos(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                                                 const ks_options* opt, void* workspace, size_t workspace_bytes,
+                                                 const double* g_flux_total, double* flux_total, double* flux_cont,
+                                                 double* d_log_gf, double* d_log_gamma_rad,
+                                                 double* d_log_gamma_stark, double* d_log_gamma_vdw,
+                                                 const ks_atm_grad* atm_grad, ks_stats* stats, void* stream) {
+    if (!atm_grad) return fail(KS_ERR_INVALID, "ks_synthesize_adjoint_atmos: NULL ks_atm_grad");
+    return adjoint_impl(lines, atm, grid, opt, workspace, workspace_bytes, g_flux_total, flux_total, flux_cont,
+                        d_log_gf, d_log_gamma_rad, d_log_gamma_stark, d_log_gamma_vdw, atm_grad, stats, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -28,4 +28,15 @@ cudaError_t launch_line_grad(const LineGradArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_atm_grad(const AtmGradArgs& a, cudaStream_t s) {
+    if (a.n_layers == 0) return cudaSuccess;
+    if (a.n_groups > 0) {
+        atm_grad_group_kernel<<<dim3((unsigned)a.n_groups, (unsigned)a.n_layers), 128, 0, s>>>(a);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    atm_grad_depth_kernel<<<(unsigned)((a.n_layers + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 }  // namespace ks

@@ -173,6 +173,24 @@ struct LineGradArgs {
     double *d_loggf, *d_loggr, *d_loggs, *d_loggw;  // [n_lines] out
 };
 
+// Atmosphere terms of the adjoint: per depth, the per-pair sums of the line
+// adjoint gathered by species (lines grouped by the caller, each group in
+// row order, so every sum has a fixed order).
+struct AtmGradArgs {
+    int64_t stride;
+    int n_layers, n_ion, n_elem, n_groups;
+    const uint8_t* cls;
+    const double *g_gf, *g_a;
+    const IonPar* ion;
+    const PairDesc<double>* desc;
+    const int32_t *element_idx, *ion_stage;
+    const double *gamma_stark, *gamma_vdw;
+    const int32_t *order, *group_first, *group_species;
+    double* part;             // scratch [L, n_groups, 3]: sum G c, sum G dc/da * gs/dop, * gw/dop
+    double* d_ln_pop;         // [L, n_ion, n_elem] out (entries of the groups' species)
+    double *d_ln_rho, *d_xne, *d_txnxn;  // [L] out
+};
+
 // ---- batched launches -------------------------------------------------------
 //
 // A batch runs every stage once over all its jobs: the launch walks a job

@@ -56,5 +56,6 @@ ks_status set_error(ks_status code, const std::string& msg);
 cudaError_t launch_transfer_adjoint(const AdjArgs& a, cudaStream_t s);
 cudaError_t launch_line_adjoint(const LineAdjArgs& a, cudaStream_t s);
 cudaError_t launch_line_grad(const LineGradArgs& a, cudaStream_t s);
+cudaError_t launch_atm_grad(const AtmGradArgs& a, cudaStream_t s);
 
 }  // namespace ks

@@ -154,6 +154,74 @@ constexpr int kMaxDev = 64;
 bool g_dev_ready[kMaxDev];
 
 // ---------------------------------------------------------------------------
+// scalar types: double, and a forward-mode dual number (value, derivative)
+// carrying d/d(log10 XABUND of one element) through the same code
+// ---------------------------------------------------------------------------
+
+struct D1 {
+    double v, d;
+    __host__ __device__ constexpr D1() : v(0.0), d(0.0) {}
+    __host__ __device__ constexpr D1(double x) : v(x), d(0.0) {}
+    __host__ __device__ constexpr D1(double x, double dx) : v(x), d(dx) {}
+};
+__device__ __forceinline__ D1 mk(double v, double d = 0.0) { return D1{v, d}; }
+__device__ __forceinline__ D1 operator+(D1 a, D1 b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ D1 operator-(D1 a, D1 b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ D1 operator-(D1 a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ D1 operator*(D1 a, D1 b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ D1 operator/(D1 a, D1 b) {
+    const double q = a.v / b.v;
+    return {q, (a.d - q * b.d) / b.v};
+}
+__device__ __forceinline__ D1 operator+(D1 a, double b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ D1 operator+(double a, D1 b) { return {a + b.v, b.d}; }
+__device__ __forceinline__ D1 operator-(D1 a, double b) { return {a.v - b, a.d}; }
+__device__ __forceinline__ D1 operator-(double a, D1 b) { return {a - b.v, -b.d}; }
+__device__ __forceinline__ D1 operator*(D1 a, double b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ D1 operator*(double a, D1 b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ D1 operator/(D1 a, double b) { return {a.v / b, a.d / b}; }
+__device__ __forceinline__ D1 operator/(double a, D1 b) {
+    const double q = a / b.v;
+    return {q, -q * b.d / b.v};
+}
+__device__ __forceinline__ D1& operator+=(D1& a, D1 b) { return a = a + b; }
+__device__ __forceinline__ D1& operator*=(D1& a, D1 b) { return a = a * b; }
+// elementary functions of a scalar that may be a dual number
+__device__ __forceinline__ double sexp(double x) { return exp(x); }
+__device__ __forceinline__ D1 sexp(D1 a) {
+    const double e = exp(a.v);
+    return {e, e * a.d};
+}
+__device__ __forceinline__ double ssqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ D1 ssqrt(D1 a) {
+    const double r = sqrt(a.v);
+    return {r, a.d / (2.0 * r)};
+}
+__device__ __forceinline__ double slog10(double x) { return log10(x); }
+__device__ __forceinline__ D1 slog10(D1 a) { return {log10(a.v), a.d / (a.v * 2.302585092994046)}; }
+__device__ __forceinline__ double spow(double x, double p) { return pow(x, p); }
+__device__ __forceinline__ D1 spow(D1 a, double p) {
+    const double r = pow(a.v, p);
+    return {r, p * pow(a.v, p - 1.0) * a.d};
+}
+
+__device__ __forceinline__ double val(double x) { return x; }
+__device__ __forceinline__ double val(D1 x) { return x.v; }
+__device__ __forceinline__ double der(double) { return 0.0; }
+__device__ __forceinline__ double der(D1 x) { return x.d; }
+template <typename S>
+__device__ __forceinline__ S lift(double v);
+template <>
+__device__ __forceinline__ double lift<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ D1 lift<D1>(double v) { return D1{v, 0.0}; }
+// min / max by value (the choice the reference's arithmetic makes)
+template <typename S>
+__device__ __forceinline__ S smin(S a, S b) { return val(b) < val(a) ? b : a; }
+template <typename S>
+__device__ __forceinline__ S smax(S a, S b) { return val(b) > val(a) ? b : a; }
+
+// ---------------------------------------------------------------------------
 // PFSAHA (pops_exact.py:987-1636) for one layer
 // ---------------------------------------------------------------------------
 
@@ -178,7 +246,8 @@ __device__ double pfground_dev(int nelion, double t) {
     return v;
 }
 
-__device__ double pfiron_dev(int iz, int ion, double tlog10, double potlow) {
+template <typename S>
+__device__ S pfiron_dev(int iz, int ion, double tlog10, S potlow) {
     const PopsTables& P = g_pops;
     const int e = iz - 20, i = ion - 1;
     int it;
@@ -198,14 +267,14 @@ __device__ double pfiron_dev(int iz, int ion, double tlog10, double potlow) {
     it = it < 1 ? 1 : (it > 56 ? 56 : it);
     const int a = it - 1, b = (it - 2) > 0 ? it - 2 : 0;
     auto tab = [&](int low, int k) { return P.pftab[((low * 56 + k) * 10 + i) * 9 + e]; };
-    if (potlow < P.pf_potlo[0]) return f * tab(0, a) + (1.0 - f) * tab(0, b);
+    if (val(potlow) < P.pf_potlo[0]) return lift<S>(f * tab(0, a) + (1.0 - f) * tab(0, b));
     int low = 6;
     for (int k = 1; k < 7; k++)
-        if (potlow < P.pf_potlo[k]) {
+        if (val(potlow) < P.pf_potlo[k]) {
             low = k;
             break;
         }
-    const double p = (log10(potlow) - P.pf_potlolog[low - 1]) / 0.30103;
+    const S p = (slog10(potlow) - P.pf_potlolog[low - 1]) / 0.30103;
     return p * (f * tab(low, a) + (1.0 - f) * tab(low, b)) +
            (1.0 - p) * (f * tab(low - 1, a) + (1.0 - f) * tab(low - 1, b));
 }
@@ -216,14 +285,17 @@ __device__ __forceinline__ int potion_index(int iz, int ion) {
 
 // Saha fractions F[0..nion2) (normalised) and partition functions PART of
 // element iz for a layer; returns NION2 = min(nion + 2, number of ions).
-__device__ int pfsaha_dev(int iz, int nion, const LayerState& s, double xne, double* F, double* PART) {
+// Only the electron density carries a derivative (S = D1); the partition
+// functions depend on it through the lowered ionisation potential.
+template <typename S>
+__device__ int pfsaha_dev(int iz, int nion, const LayerState& s, S xne, S* F, S* PART) {
     const PopsTables& P = g_pops;
-    double charge = xne * 2.0;
-    const double excess = 2.0 * xne - s.p / s.tk;
-    if (excess > 0.0) charge = charge + 2.0 * excess;
-    if (charge == 0.0) charge = 1.0;
-    const double debye = sqrt(s.tk / 2.8965e-18 / charge);
-    const double potlow = fmin(1.0, 1.44e-7 / debye);
+    S charge = xne * 2.0;
+    const S excess = 2.0 * xne - s.p / s.tk;
+    if (val(excess) > 0.0) charge = charge + 2.0 * excess;
+    if (val(charge) == 0.0) charge = lift<S>(1.0);
+    const S debye = ssqrt(s.tk / 2.8965e-18 / charge);
+    const S potlow = smin<S>(lift<S>(1.0), 1.44e-7 / debye);
     int n, nions;
     if (iz <= 28) {
         n = c_locz[iz - 1];
@@ -237,32 +309,33 @@ __device__ int pfsaha_dev(int iz, int nion, const LayerState& s, double xne, dou
     else if (iz == 8) { n = 367; nions = 8; }
     if (iz >= 20 && iz < 29) nions = 10;
     const int nion2 = (nion + 2) < nions ? nion + 2 : nions;
-    double IP[10], POTLO[10];
+    double IP[10];
+    S POTLO[10];
     const double T = s.t, hckt = s.hckt;
     for (int ion = 1; ion <= nion2; ion++) {
         const double z = (double)ion;
         POTLO[ion - 1] = potlow * z;
         IP[ion - 1] = 0.0;
-        PART[ion - 1] = 1.0;
+        PART[ion - 1] = lift<S>(1.0);
         const int pi = potion_index(iz, ion) - 1;
         if (pi >= 0 && pi < 999) {
             IP[ion - 1] = P.potion[pi] / kEvToCm;
             if (IP[ion - 1] == 0.0 && pi > 0) IP[ion - 1] = P.potion[pi - 1] / kEvToCm;
         }
         if (iz >= 20 && iz < 29) {
-            PART[ion - 1] = pfiron_dev(iz, ion, s.tlog / 2.30258509299405, POTLO[ion - 1] * kEvToCm);
+            PART[ion - 1] = pfiron_dev<S>(iz, ion, s.tlog / 2.30258509299405, POTLO[ion - 1] * kEvToCm);
             continue;
         }
         const int col = n - 1 + ion;  // 1-based NNN column
         const int c0 = col - 1;
-        double G = 0.0, D1 = 0.0;
+        double G = 0.0, D1v = 0.0;
         if (c0 < 374) {
             const int v = P.nnn[5 * 374 + c0];
             G = (double)(v - (v / 100) * 100);
         }
         bool handled = false;
         if (col == 2) {
-            PART[ion - 1] = 1.0;
+            PART[ion - 1] = lift<S>(1.0);
             handled = true;
         }
         for (int q = 0; q < kNSpecial; q++) {
@@ -285,8 +358,8 @@ __device__ int pfsaha_dev(int iz, int nion, const LayerState& s, double xne, dou
                 }
                 part += x;
             }
-            PART[ion - 1] = part;
-            if (sp.d1_num > 0.0) D1 = sp.d1_num / sp.d1_n / sp.d1_n * hckt;
+            PART[ion - 1] = lift<S>(part);
+            if (sp.d1_num > 0.0) D1v = sp.d1_num / sp.d1_n / sp.d1_n * hckt;
             if (sp.g_over > 0.0) G = sp.g_over;
             handled = true;
             break;
@@ -315,28 +388,28 @@ __device__ int pfsaha_dev(int iz, int nion, const LayerState& s, double xne, dou
                 ks1 = ks1 < 0 ? 0 : (ks1 > 3 ? 3 : ks1);
                 p2 = (double)(v1 / 100000) * c_scale[ks1];
             }
-            PART[ion - 1] = fmax(pmin, p1 + (p2 - p1) * dt);
+            PART[ion - 1] = lift<S>(fmax(pmin, p1 + (p2 - p1) * dt));
         } else if (!handled) {
-            PART[ion - 1] = 1.0;
+            PART[ion - 1] = lift<S>(1.0);
         }
         bool skip_high_t = false;
         if (IP[ion - 1] > 0.0) {
             const double t2000 = IP[ion - 1] * 2000.0 / 11.0;
             if (T < t2000 * 2.0) {
                 const double pg = pfground_dev((iz - 1) * 6 + ion, T);
-                if (pg > 0.0) PART[ion - 1] = fmax(PART[ion - 1], pg);
+                if (pg > 0.0) PART[ion - 1] = smax<S>(PART[ion - 1], lift<S>(pg));
                 skip_high_t = true;
             }
         }
-        const bool bypass = D1 > 0.0;
-        if (!skip_high_t && (G > 0.0 || D1 > 0.0) && (bypass || POTLO[ion - 1] >= 0.1) && IP[ion - 1] > 0.0) {
+        const bool bypass = D1v > 0.0;
+        if (!skip_high_t && (G > 0.0 || D1v > 0.0) && (bypass || val(POTLO[ion - 1]) >= 0.1) && IP[ion - 1] > 0.0) {
             const double t2000 = IP[ion - 1] * 2000.0 / 11.0;
             if (bypass || T >= t2000 * 4.0) {
                 double tvu = s.tkev;
                 if (T > t2000 * 11.0) tvu = (t2000 * 11.0) * 8.6171e-5;
-                const double d1v = D1 <= 0.0 ? 0.1 / tvu : D1;
-                const double d2 = POTLO[ion - 1] / tvu;
-                double term1 = pow(sqrt(13.595 * z * z / tvu / d2), 3.0);
+                const double d1v = D1v <= 0.0 ? 0.1 / tvu : D1v;
+                const S d2 = POTLO[ion - 1] / tvu;
+                S term1 = spow(ssqrt(13.595 * z * z / tvu / d2), 3.0);
                 term1 *= 1.0 / 3.0 + (1.0 - (0.5 + (1.0 / 18.0 + d2 / 120.0) * d2) * d2) * d2;
                 double term2 = pow(sqrt(13.595 * z * z / tvu / d1v), 3.0);
                 term2 *= 1.0 / 3.0 + (1.0 - (0.5 + (1.0 / 18.0 + d1v / 120.0) * d1v) * d1v) * d1v;
@@ -344,12 +417,12 @@ __device__ int pfsaha_dev(int iz, int nion, const LayerState& s, double xne, dou
             }
         }
     }
-    const double cf = 2.0 * 2.4148e15 * T * sqrt(T) / xne;
-    F[0] = 1.0;
+    const S cf = 2.0 * 2.4148e15 * T * sqrt(T) / xne;
+    F[0] = lift<S>(1.0);
     for (int ion = 2; ion <= nion2; ion++)
-        F[ion - 1] = PART[ion - 2] > 0.0
-                         ? cf * PART[ion - 1] / PART[ion - 2] * exp(-(IP[ion - 2] - POTLO[ion - 2]) / s.tkev)
-                         : 0.0;
+        F[ion - 1] = val(PART[ion - 2]) > 0.0
+                         ? cf * PART[ion - 1] / PART[ion - 2] * sexp(-(IP[ion - 2] - POTLO[ion - 2]) / s.tkev)
+                         : lift<S>(0.0);
     int l = nion2 + 1;
     for (int ion = 2; ion <= nion2; ion++) {
         l -= 1;
@@ -375,19 +448,20 @@ __device__ LayerState layer_state(double t, double p, double vturb) {
 
 // Equilibrium constant of molecule m in a layer (nmolec_exact.py:2268-2531);
 // the NLTE partition-function corrections are 1 in LTE.
-__device__ double equilj_dev(int m, const LayerState& s, double xne) {
+template <typename S>
+__device__ S equilj_dev(int m, const LayerState& s, S xne) {
     const PopsTables& P = g_pops;
     const int ncomp = P.locj[m + 1] - P.locj[m];
     const double code = P.mol_code[m];
     if (P.mol_equil[m] == 0.0) {
-        if (ncomp <= 1) return 1.0;
-        double F[10], PART[10];
-        pfsaha_dev((int)code, ncomp, s, xne, F, PART);
-        const double f0 = F[0];
-        if (f0 == 0.0 || fabs(f0) < 1e-300 || !isfinite(f0)) return 0.0;
-        return F[ncomp - 1] / f0 * pow(xne, (double)(ncomp - 1));
+        if (ncomp <= 1) return lift<S>(1.0);
+        S F[10], PART[10];
+        pfsaha_dev<S>((int)code, ncomp, s, xne, F, PART);
+        const S f0 = F[0];
+        if (val(f0) == 0.0 || fabs(val(f0)) < 1e-300 || !isfinite(val(f0))) return lift<S>(0.0);
+        return F[ncomp - 1] / f0 * spow(xne, (double)(ncomp - 1));
     }
-    if (s.t > 10000.0) return 0.0;
+    if (s.t > 10000.0) return lift<S>(0.0);
     const int ion = (int)((code - (double)(int)code) * 100.0 + 0.5);
     const double T = s.t;
     double arg;
@@ -403,29 +477,36 @@ __device__ double equilj_dev(int m, const LayerState& s, double xne) {
         arg = E(0) / s.tkev - E(1) + (E(2) + (-E(3) + (E(4) + (-E(5) + E(6) * T) * T) * T) * T) * T -
               1.5 * (double)(ncomp - ion - ion - 1) * s.tlog;
     }
-    return exp(arg);
+    return lift<S>(exp(arg));
 }
 
 // ---------------------------------------------------------------------------
 // nmolec_kernel: NMOLEC (nmolec_exact.py:1742-3575), one warp per model
 // ---------------------------------------------------------------------------
 
-struct PopsJob {
+template <typename S>
+struct PopsJobT {
     int n_layers;
+    int dparam;          // D1: Z-1 of the element whose log10 abundance is differentiated
     const double *t, *p, *vturb, *xabund;
     double *xne, *rho, *xnatom, *hckt, *xnf_h, *xnf_he1, *xnf_h2, *population, *doppler;
     int32_t* iterations;
-    double* xnmol;       // workspace [L, kMaxMol]
-    double* xnat;        // workspace [L] XNATOM
+    // D1: derivatives of the outputs (device) w.r.t. log10 XABUND[dparam]
+    double *d_xne, *d_rho, *d_xnf_h, *d_xnf_he1, *d_xnf_h2, *d_population;
+    S* xnmol;            // workspace [L, kMaxMol]
+    S* xnat;             // workspace [L] XNATOM
+    S* xnes;             // workspace [L] XNE
     LayerState* state;   // workspace [L]
 };
+using PopsJob = PopsJobT<double>;
 
+template <typename S>
 struct WarpShared {
-    double a[kMaxEq * kMaxEq];  // DEQ, row-major [row][col]
-    double b[kMaxEq];           // EQ, then the Newton step
-    double xn[kMaxEq], xab[kMaxEq], eqold[kMaxEq];
-    double equilj[kMaxMol], term[kMaxMol];
-    double pivot;
+    S a[kMaxEq * kMaxEq];  // DEQ, row-major [row][col]
+    S b[kMaxEq];           // EQ, then the Newton step
+    S xn[kMaxEq], xab[kMaxEq], eqold[kMaxEq];
+    S equilj[kMaxMol], term[kMaxMol];
+    unsigned char skip[kMaxMol];  // molecules the sums skip this iteration
     int iferr;
 };
 
@@ -434,67 +515,71 @@ __device__ __forceinline__ int comp_eq(int kr, int ne) { return kr >= ne ? ne - 
 // Column k of DEQ and EQ[k] for the current XN (nmolec_exact.py:760-926):
 // the element and charge equations, then every molecule holding equation k
 // in table order, each adding in the reference's component order.
-__device__ void assemble_column(WarpShared& S, int k, double xntot) {
+template <typename S>
+__device__ void assemble_column(WarpShared<S>& W, int k, double xntot) {
     const PopsTables& P = g_pops;
     const int ne = P.nequa, e = ne - 1;
-    for (int r = 0; r < ne; r++) S.a[r * kMaxEq + k] = 0.0;
-    double eqk;
+    for (int r = 0; r < ne; r++) W.a[r * kMaxEq + k] = lift<S>(0.0);
+    S eqk;
     if (k == 0) {
-        eqk = -xntot;
+        eqk = lift<S>(-xntot);
         for (int q = 1; q < ne; q++) {
-            eqk = eqk + S.xn[q];
-            S.a[q * kMaxEq + 0] = -S.xab[q];
+            eqk = eqk + W.xn[q];
+            W.a[q * kMaxEq + 0] = -W.xab[q];
         }
         for (int m = 0; m < P.nmol; m++) {
-            if (P.locj[m + 1] - P.locj[m] <= 1) continue;
-            const double t = S.term[m];
-            if (t != t) continue;  // NaN marks a molecule the sums skip
-            eqk = eqk + t;
+            if (P.locj[m + 1] - P.locj[m] <= 1 || W.skip[m]) continue;
+            eqk = eqk + W.term[m];
         }
-        S.b[0] = eqk;
+        W.b[0] = eqk;
         return;
     }
-    S.a[0 * kMaxEq + k] = 1.0;
-    S.a[k * kMaxEq + k] = 1.0;
-    eqk = S.xn[k] - S.xab[k] * S.xn[0];
+    W.a[0 * kMaxEq + k] = lift<S>(1.0);
+    W.a[k * kMaxEq + k] = lift<S>(1.0);
+    eqk = W.xn[k] - W.xab[k] * W.xn[0];
     if (P.has_e && k == e) {
-        eqk = -S.xn[e];
-        S.a[e * kMaxEq + e] = -1.0;
+        eqk = -W.xn[e];
+        W.a[e * kMaxEq + e] = lift<S>(-1.0);
     }
     for (int q = P.col_off[k]; q < P.col_off[k + 1]; q++) {
         const int m = P.col_mol[q];
-        const double t = S.term[m];
-        if (t != t) continue;
+        if (W.skip[m]) continue;
+        const S t = W.term[m];
         const int l1 = P.locj[m], l2 = P.locj[m + 1];
         for (int lk = l1; lk < l2; lk++) {
             const int kr = P.kcomps[lk];
             if (comp_eq(kr, ne) != k) continue;
-            const double d = kr >= ne ? -t / S.xn[e] : t / S.xn[kr];
+            const S d = kr >= ne ? -t / W.xn[e] : t / W.xn[kr];
             eqk = eqk + t;
-            S.a[0 * kMaxEq + k] = S.a[0 * kMaxEq + k] + d;
+            W.a[0 * kMaxEq + k] = W.a[0 * kMaxEq + k] + d;
             for (int lm = l1; lm < l2; lm++) {
                 const int mm = comp_eq(P.kcomps[lm], ne);
-                S.a[mm * kMaxEq + k] = S.a[mm * kMaxEq + k] + d;
+                W.a[mm * kMaxEq + k] = W.a[mm * kMaxEq + k] + d;
             }
         }
         if (P.has_e && P.kcomps[l2 - 1] == e) {
             for (int lk = l1; lk < l2; lk++) {
                 const int kk = comp_eq(P.kcomps[lk], ne);
                 if (kk != k) continue;
-                const double d = t / S.xn[kk];
+                const S d = t / W.xn[kk];
                 if (kk == e) eqk = eqk - t - t;
-                S.a[e * kMaxEq + k] = S.a[e * kMaxEq + k] - d - d;
+                W.a[e * kMaxEq + k] = W.a[e * kMaxEq + k] - d - d;
             }
         }
     }
-    S.b[k] = eqk;
+    W.b[k] = eqk;
 }
+
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 
 // SOLVIT (nmolec_exact.py:3671-3765): Gauss-Jordan elimination with the
 // full pivot search (largest |a| over unpivoted rows and columns, first in
 // row-major order on ties), rows swapped to put the pivot on the diagonal.
-// Lane r owns row r.  The solution is left in S.b.
-__device__ void solvit_warp(WarpShared& S, int n, int lane) {
+// Lane r owns row r.  The solution is left in W.b.  With S = D1 the pivots
+// are chosen on the values, so the derivative is that of the same
+// elimination.
+template <typename S>
+__device__ void solvit_warp(WarpShared<S>& W, int n, int lane) {
     int pcount = 0;  // ipivot of the column this lane stands for
     for (int step = 0; step < n; step++) {
         const unsigned done = __ballot_sync(0xffffffffu, lane < n && pcount == 1);
@@ -503,7 +588,7 @@ __device__ void solvit_warp(WarpShared& S, int n, int lane) {
         if (lane < n && !((done >> lane) & 1u)) {
             for (int c = 0; c < n; c++) {
                 if ((done >> c) & 1u) continue;
-                const double v = fabs(S.a[lane * kMaxEq + c]);
+                const double v = fabs(val(W.a[lane * kMaxEq + c]));
                 if (v > best) {
                     best = v;
                     bidx = lane * n + c;
@@ -511,7 +596,7 @@ __device__ void solvit_warp(WarpShared& S, int n, int lane) {
             }
         }
         for (int o = 16; o > 0; o >>= 1) {
-            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const double ob = shfl_xor(best, o);
             const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
             if (ob > best || (ob == best && oi < bidx)) {
                 best = ob;
@@ -526,30 +611,30 @@ __device__ void solvit_warp(WarpShared& S, int n, int lane) {
         if (lane == icol) pcount += 1;
         if (irow != icol) {
             if (lane < n) {
-                const double x = S.a[irow * kMaxEq + lane];
-                S.a[irow * kMaxEq + lane] = S.a[icol * kMaxEq + lane];
-                S.a[icol * kMaxEq + lane] = x;
+                const S x = W.a[irow * kMaxEq + lane];
+                W.a[irow * kMaxEq + lane] = W.a[icol * kMaxEq + lane];
+                W.a[icol * kMaxEq + lane] = x;
             }
             if (lane == 0) {
-                const double x = S.b[irow];
-                S.b[irow] = S.b[icol];
-                S.b[icol] = x;
+                const S x = W.b[irow];
+                W.b[irow] = W.b[icol];
+                W.b[icol] = x;
             }
         }
         __syncwarp();
-        const double pivot = S.a[icol * kMaxEq + icol];
+        const S pivot = W.a[icol * kMaxEq + icol];
         __syncwarp();
-        if (lane < n) S.a[icol * kMaxEq + lane] = (lane == icol ? 1.0 : S.a[icol * kMaxEq + lane]) / pivot;
-        if (lane == 0) S.b[icol] = S.b[icol] / pivot;
+        if (lane < n) W.a[icol * kMaxEq + lane] = (lane == icol ? lift<S>(1.0) : W.a[icol * kMaxEq + lane]) / pivot;
+        if (lane == 0) W.b[icol] = W.b[icol] / pivot;
         __syncwarp();
         if (lane < n && lane != icol) {
-            double* row = &S.a[lane * kMaxEq];
-            const double t = row[icol];
-            if (t != 0.0) {
-                row[icol] = 0.0;
-                const double* prow = &S.a[icol * kMaxEq];
+            S* row = &W.a[lane * kMaxEq];
+            const S t = row[icol];
+            if (val(t) != 0.0) {
+                row[icol] = lift<S>(0.0);
+                const S* prow = &W.a[icol * kMaxEq];
                 for (int c = 0; c < n; c++) row[c] = row[c] - prow[c] * t;
-                S.b[lane] = S.b[lane] - S.b[icol] * t;
+                W.b[lane] = W.b[lane] - W.b[icol] * t;
             }
         }
         __syncwarp();
@@ -558,122 +643,151 @@ __device__ void solvit_warp(WarpShared& S, int n, int lane) {
 
 // numpy's pairwise sum of 99 values (8 accumulators, then the rest), the
 // order np.sum gives WTMOLE in the reference.
-__device__ double wtmole_dev(const double* xabund) {
+template <typename S>
+__device__ S wtmole_dev(const S* xabund) {
     const PopsTables& P = g_pops;
-    double r[8];
+    S r[8];
     for (int j = 0; j < 8; j++) r[j] = xabund[j] * P.atmass[j];
     int i = 8;
     for (; i < kNEl - (kNEl % 8); i += 8)
         for (int j = 0; j < 8; j++) r[j] += xabund[i + j] * P.atmass[i + j];
-    double res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+    S res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
     for (; i < kNEl; i++) res += xabund[i] * P.atmass[i];
     return res;
 }
 
-__global__ void __launch_bounds__(32 * kWarps) nmolec_kernel(const PopsJob* __restrict__ jobs, int n_jobs) {
-    __shared__ WarpShared sh[kWarps];
+template <typename S>
+__device__ __forceinline__ S abundance(const PopsJobT<S>& J, int z0) {
+    const double x = J.xabund[z0];
+    if constexpr (sizeof(S) == sizeof(double)) {
+        return x;
+    } else {
+        return D1{x, z0 == J.dparam ? 2.302585092994046 * x : 0.0};
+    }
+}
+
+template <typename S>
+__device__ __forceinline__ void store(double* v, double* d, size_t i, S x) {
+    if (v) v[i] = val(x);
+    if constexpr (sizeof(S) != sizeof(double)) {
+        if (d) d[i] = der(x);
+    }
+}
+
+template <typename S, int NW>
+__global__ void __launch_bounds__(32 * NW) nmolec_kernel(const PopsJobT<S>* __restrict__ jobs, int n_jobs) {
+    __shared__ WarpShared<S> sh[NW];
+    __shared__ S xab_all[NW][kNEl];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int job = blockIdx.x * kWarps + w;
+    const int job = blockIdx.x * NW + w;
     if (job >= n_jobs) return;  // whole warps only
-    WarpShared& S = sh[w];
-    const PopsJob J = jobs[job];
+    WarpShared<S>& W = sh[w];
+    const PopsJobT<S> J = jobs[job];
     const PopsTables& P = g_pops;
     const int ne = P.nequa, e = ne - 1, nmol = P.nmol;
     const bool has_e = P.has_e != 0;
+    for (int z = lane; z < kNEl; z += 32) xab_all[w][z] = abundance<S>(J, z);
+    __syncwarp();
     if (lane < ne) {
-        double x = 0.0;
-        if (lane >= 1 && P.idequa[lane] < 100) x = fmax(J.xabund[P.idequa[lane] - 1], 1e-20);
-        S.xab[lane] = x;
+        S x = lift<S>(0.0);
+        if (lane >= 1 && P.idequa[lane] < 100) x = smax<S>(xab_all[w][P.idequa[lane] - 1], lift<S>(1e-20));
+        W.xab[lane] = x;
     }
-    double wtmole = 0.0;
-    if (lane == 0) wtmole = wtmole_dev(J.xabund);
-    double xne_prev = 0.0, p_prev = 0.0;
+    S wtmole = lift<S>(0.0);
+    if (lane == 0) wtmole = wtmole_dev<S>(xab_all[w]);
+    S xne_prev = lift<S>(0.0);
+    double p_prev = 0.0;
     __syncwarp();
     for (int j = 0; j < J.n_layers; j++) {
         const LayerState s = layer_state(J.t[j], J.p[j], J.vturb[j]);
-        double xne_j;
+        S xne_j;
         if (j == 0) {
             const double x0 = s.xntot / 2.0;
             const double x = x0 / 10.0;
-            if (lane < ne) S.xn[lane] = lane == 0 ? x0 : (has_e && lane == e ? x : x * S.xab[lane]);
-            xne_j = x;
+            if (lane < ne) W.xn[lane] = lane == 0 ? lift<S>(x0) : (has_e && lane == e ? lift<S>(x) : x * W.xab[lane]);
+            xne_j = lift<S>(x);
         } else {
             const double ratio = s.p / p_prev;
-            if (lane < ne) S.xn[lane] = S.xn[lane] * ratio;
+            if (lane < ne) W.xn[lane] = W.xn[lane] * ratio;
             xne_j = xne_prev * ratio;
         }
-        if (lane < ne) S.eqold[lane] = 0.0;
-        for (int m = lane; m < nmol; m += 32) S.equilj[m] = equilj_dev(m, s, xne_j);
+        if (lane < ne) W.eqold[lane] = lift<S>(0.0);
+        for (int m = lane; m < nmol; m += 32) W.equilj[m] = equilj_dev<S>(m, s, xne_j);
         __syncwarp();
         int it = 0;
         for (it = 1; it <= kMaxIter; it++) {
             for (int m = lane; m < nmol; m += 32) {
-                double t = S.equilj[m];
-                if (!(isfinite(t) && t > 0.0)) {
-                    S.term[m] = __longlong_as_double(0x7ff8000000000000ll);
+                S t = W.equilj[m];
+                if (!(isfinite(val(t)) && val(t) > 0.0)) {
+                    W.skip[m] = 1;
                     continue;
                 }
                 for (int lk = P.locj[m]; lk < P.locj[m + 1]; lk++) {
                     const int kr = P.kcomps[lk];
-                    t = kr >= ne ? t / S.xn[e] : t * S.xn[kr];
+                    t = kr >= ne ? t / W.xn[e] : t * W.xn[kr];
                 }
-                S.term[m] = isfinite(t) ? t : __longlong_as_double(0x7ff8000000000000ll);
+                W.term[m] = t;
+                W.skip[m] = isfinite(val(t)) ? 0 : 1;
             }
             __syncwarp();
-            if (lane < ne) assemble_column(S, lane, s.xntot);
+            if (lane < ne) assemble_column<S>(W, lane, s.xntot);
             __syncwarp();
-            solvit_warp(S, ne, lane);
+            solvit_warp<S>(W, ne, lane);
             if (lane == 0) {
                 int iferr = 0;
                 double scale = 100.0;
                 for (int k = 0; k < ne; k++) {
-                    double d = S.b[k];
-                    const double x = S.xn[k];
-                    const double ratio = x == 0.0 ? (d == 0.0 ? 0.0 : INFINITY) : fabs(d / x);
+                    S d = W.b[k];
+                    const S x = W.xn[k];
+                    const double dv = val(d), xv = val(x);
+                    const double ratio = xv == 0.0 ? (dv == 0.0 ? 0.0 : INFINITY) : fabs(dv / xv);
                     if (ratio > 0.001) iferr = 1;
-                    const bool flip = (S.eqold[k] > 0.0 && d < 0.0) || (S.eqold[k] < 0.0 && d > 0.0);
-                    if (flip && isfinite(d)) d = d * 0.69;
-                    const double xneq = (isfinite(x) && isfinite(d) && fabs(x) > 2.2250738585072014e-308)
-                                            ? x * (1.0 - d / x)
-                                            : x - d;
-                    if (xneq < x / 100.0) {
-                        S.xn[k] = x / scale;
+                    const double eo = val(W.eqold[k]);
+                    const bool flip = (eo > 0.0 && dv < 0.0) || (eo < 0.0 && dv > 0.0);
+                    if (flip && isfinite(dv)) d = d * 0.69;
+                    const S xneq = (isfinite(xv) && isfinite(val(d)) && fabs(xv) > 2.2250738585072014e-308)
+                                       ? x * (1.0 - d / x)
+                                       : x - d;
+                    if (val(xneq) < xv / 100.0) {
+                        W.xn[k] = x / scale;
                         if (flip) scale = sqrt(scale);
                     } else {
-                        S.xn[k] = xneq;
+                        W.xn[k] = xneq;
                     }
-                    S.eqold[k] = d;
+                    W.eqold[k] = d;
                 }
-                S.iferr = iferr;
+                W.iferr = iferr;
             }
             __syncwarp();
-            if (S.iferr == 0) break;
+            if (W.iferr == 0) break;
         }
         if (it > kMaxIter) it = kMaxIter;
-        if (has_e) xne_j = S.xn[e];
+        if (has_e) xne_j = W.xn[e];
         // molecule densities XNMOL (nmolec_exact.py:3556-3575)
-        double* xnmol = J.xnmol + (size_t)j * kMaxMol;
+        S* xnmol = J.xnmol + (size_t)j * kMaxMol;
         for (int m = lane; m < nmol; m += 32) {
-            double v = S.equilj[m];
+            S v = W.equilj[m];
             for (int lk = P.locj[m]; lk < P.locj[m + 1]; lk++) {
                 const int kr = P.kcomps[lk];
-                v = kr >= ne ? v / S.xn[e] : v * S.xn[kr];
+                v = kr >= ne ? v / W.xn[e] : v * W.xn[kr];
             }
             xnmol[m] = v;
         }
         __syncwarp();
         if (lane == 0) {
             J.state[j] = s;
-            J.xne[j] = xne_j;
-            J.rho[j] = S.xn[0] * wtmole * 1.660e-24;
-            J.xnat[j] = S.xn[0];
-            if (J.xnatom) J.xnatom[j] = S.xn[0];
-            J.hckt[j] = s.hckt;
+            J.xnes[j] = xne_j;
+            J.xnat[j] = W.xn[0];
+            store<S>(J.xne, J.d_xne, j, xne_j);
+            store<S>(J.rho, J.d_rho, j, W.xn[0] * wtmole * 1.660e-24);
+            if (J.xnatom) J.xnatom[j] = val(W.xn[0]);
+            if (J.hckt) J.hckt[j] = s.hckt;
             if (J.iterations) J.iterations[j] = it;
-            const double h1 = fmax(P.row_h1 >= 0 ? xnmol[P.row_h1] : 0.0, 1e-40);
-            J.xnf_h[j] = h1;
-            J.xnf_he1[j] = fmax(P.row_he1 >= 0 ? xnmol[P.row_he1] : 0.0, 1e-40);
-            double h2 = 0.0;
+            const S h1 = smax<S>(P.row_h1 >= 0 ? xnmol[P.row_h1] : lift<S>(0.0), lift<S>(1e-40));
+            store<S>(J.xnf_h, J.d_xnf_h, j, h1);
+            store<S>(J.xnf_he1, J.d_xnf_he1, j,
+                     smax<S>(P.row_he1 >= 0 ? xnmol[P.row_he1] : lift<S>(0.0), lift<S>(1e-40)));
+            S h2 = lift<S>(0.0);
             if (!(s.t > 9000.0)) {
                 const double T = s.t;
                 const double eqk = exp(4.478 / s.tkev - 4.64584e1 +
@@ -686,7 +800,7 @@ __global__ void __launch_bounds__(32 * kWarps) nmolec_kernel(const PopsJob* __re
                                        1.5 * s.tlog);
                 h2 = h1 * h1 * eqk;
             }
-            J.xnf_h2[j] = h2;
+            store<S>(J.xnf_h2, J.d_xnf_h2, j, h2);
         }
         xne_prev = xne_j;
         p_prev = s.p;
@@ -702,8 +816,9 @@ __device__ __forceinline__ double doppler_width(double tk, double mass, double v
     return sqrt(2.0 * tk / mass / 1.660e-24 + vt * vt) / kCcms;
 }
 
-__global__ void __launch_bounds__(128) pops_kernel(const PopsJob* __restrict__ jobs, const int* __restrict__ first,
-                                                   int n_jobs) {
+template <typename S>
+__global__ void __launch_bounds__(128) pops_kernel(const PopsJobT<S>* __restrict__ jobs,
+                                                   const int* __restrict__ first, int n_jobs) {
     // block -> (job, layer) through the prefix of layer counts
     int lo = 0, hi = n_jobs - 1;
     const int b = blockIdx.x;
@@ -712,22 +827,22 @@ __global__ void __launch_bounds__(128) pops_kernel(const PopsJob* __restrict__ j
         if (first[mid] <= b) lo = mid;
         else hi = mid - 1;
     }
-    const PopsJob& J = jobs[lo];
+    const PopsJobT<S>& J = jobs[lo];
     const int j = b - first[lo];
     if (j < 0 || j >= J.n_layers) return;
     const PopsTables& P = g_pops;
     const LayerState s = J.state[j];
-    const double xne = J.xne[j];
-    const double xnat = J.xnat[j];
-    const double* xnmol = J.xnmol + (size_t)j * kMaxMol;
-    double* pop = J.population + (size_t)j * kNIon * kNSpec;
-    double* dop = J.doppler + (size_t)j * kNIon * kNSpec;
+    const S xne = J.xnes[j];
+    const S xnat = J.xnat[j];
+    const S* xnmol = J.xnmol + (size_t)j * kMaxMol;
+    const size_t row0 = (size_t)j * kNIon * kNSpec;
     const int tid = threadIdx.x;
     for (int sp = tid; sp < kNSpec; sp += blockDim.x) {
-        double v[kNIon] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        S v[kNIon];
+        for (int i = 0; i < kNIon; i++) v[i] = lift<S>(0.0);
         if (sp < kNEl) {
             const int z = sp + 1;
-            double F[10], PART[10];
+            S F[10], PART[10];
             if (P.elem_mol_branch[sp]) {
                 // number density over partition function of each ion from
                 // the molecular equilibrium (XNFPMOL, pops_exact.py:130-150)
@@ -735,18 +850,20 @@ __global__ void __launch_bounds__(128) pops_kernel(const PopsJob* __restrict__ j
                     const int row = P.elem_mol_row[sp][ion];
                     if (row < 0) continue;
                     const int ncomp = P.locj[row + 1] - P.locj[row];
-                    pfsaha_dev(z, ncomp, s, xne, F, PART);
+                    pfsaha_dev<S>(z, ncomp, s, xne, F, PART);
                     v[ion] = xnmol[row] / PART[ncomp - 1];
                 }
             } else {
                 const int nion = P.elem_nion[sp];
-                const int nion2 = pfsaha_dev(z, nion, s, xne, F, PART);
+                const int nion2 = pfsaha_dev<S>(z, nion, s, xne, F, PART);
                 const int n = nion < nion2 ? nion : nion2;
-                for (int i = 0; i < n && i < kNIon; i++) v[i] = F[i] / PART[i] * xnat * J.xabund[sp];
+                const S ab = abundance<S>(J, sp);
+                for (int i = 0; i < n && i < kNIon; i++) v[i] = F[i] / PART[i] * xnat * ab;
             }
         }
-        for (int ion = 0; ion < kNIon; ion++) pop[ion * kNSpec + sp] = v[ion];
+        for (int ion = 0; ion < kNIon; ion++) store<S>(J.population, J.d_population, row0 + ion * kNSpec + sp, v[ion]);
     }
+    if (!J.doppler) return;
     for (int q = tid; q < kNIon * kNSpec; q += blockDim.x) {
         const int ion = q / kNSpec, sp = q - ion * kNSpec;
         double v = 0.0;
@@ -765,7 +882,7 @@ __global__ void __launch_bounds__(128) pops_kernel(const PopsJob* __restrict__ j
             const double mm = P.momass[sp - 39];
             if (mm > 0.0) v = doppler_width(s.tk, mm, s.vturb);
         }
-        dop[q] = v;
+        J.doppler[row0 + q] = v;
     }
 }
 
@@ -958,17 +1075,47 @@ ks_status check_models(const ks_pops_model* models, int32_t n) {
     return KS_OK;
 }
 
+template <typename S>
+size_t job_ws_bytes(Carve& c, size_t L) {
+    c.take(sizeof(S) * L * kMaxMol);
+    c.take(sizeof(S) * L);
+    c.take(sizeof(S) * L);
+    c.take(sizeof(LayerState) * L);
+    return c.off;
+}
+
 size_t pops_ws_bytes(const ks_pops_model* models, int32_t n) {
     Carve c;
     c.take(sizeof(PopsJob) * (size_t)n);
     c.take(sizeof(int) * ((size_t)n + 1));
-    for (int i = 0; i < n; i++) {
-        const size_t L = (size_t)models[i].n_layers;
-        c.take(sizeof(double) * L * kMaxMol);
-        c.take(sizeof(double) * L);
-        c.take(sizeof(LayerState) * L);
-    }
+    for (int i = 0; i < n; i++) job_ws_bytes<double>(c, (size_t)models[i].n_layers);
     return c.off + 256;
+}
+
+template <typename S>
+void fill_job(PopsJobT<S>& J, const ks_pops_model& m, char* base, Carve& c) {
+    std::memset(&J, 0, sizeof(J));
+    const size_t L = (size_t)m.n_layers;
+    J.n_layers = m.n_layers;
+    J.dparam = -1;
+    J.t = m.temperature;
+    J.p = m.gas_pressure;
+    J.vturb = m.vturb;
+    J.xabund = m.xabund;
+    J.xne = m.electron_density;
+    J.rho = m.mass_density;
+    J.xnatom = m.xnatom;
+    J.hckt = m.hckt;
+    J.xnf_h = m.xnf_h;
+    J.xnf_he1 = m.xnf_he1;
+    J.xnf_h2 = m.xnf_h2;
+    J.population = m.population;
+    J.doppler = m.doppler;
+    J.iterations = m.nmolec_iterations;
+    J.xnmol = (S*)(base + c.take(sizeof(S) * L * kMaxMol));
+    J.xnat = (S*)(base + c.take(sizeof(S) * L));
+    J.xnes = (S*)(base + c.take(sizeof(S) * L));
+    J.state = (LayerState*)(base + c.take(sizeof(LayerState) * L));
 }
 
 }  // namespace
@@ -1086,39 +1233,106 @@ extern "C" ks_status ks_populations(const ks_pops_model* models, int32_t n_model
     std::vector<int> first(n_models + 1);
     int total = 0;
     for (int i = 0; i < n_models; i++) {
-        const ks_pops_model& m = models[i];
-        PopsJob& J = jobs[i];
-        const size_t L = (size_t)m.n_layers;
-        J.n_layers = m.n_layers;
-        J.t = m.temperature;
-        J.p = m.gas_pressure;
-        J.vturb = m.vturb;
-        J.xabund = m.xabund;
-        J.xne = m.electron_density;
-        J.rho = m.mass_density;
-        J.xnatom = m.xnatom;
-        J.hckt = m.hckt;
-        J.xnf_h = m.xnf_h;
-        J.xnf_he1 = m.xnf_he1;
-        J.xnf_h2 = m.xnf_h2;
-        J.population = m.population;
-        J.doppler = m.doppler;
-        J.iterations = m.nmolec_iterations;
-        J.xnmol = (double*)(base + c.take(sizeof(double) * L * kMaxMol));
-        J.xnat = (double*)(base + c.take(sizeof(double) * L));
-        J.state = (LayerState*)(base + c.take(sizeof(LayerState) * L));
+        fill_job<double>(jobs[i], models[i], base, c);
         first[i] = total;
-        total += m.n_layers;
+        total += models[i].n_layers;
     }
     first[n_models] = total;
     KP_CUDA(cudaMemcpyAsync(base + o_jobs, jobs.data(), sizeof(PopsJob) * n_models, cudaMemcpyHostToDevice, s));
     KP_CUDA(cudaMemcpyAsync(base + o_first, first.data(), sizeof(int) * (n_models + 1), cudaMemcpyHostToDevice, s));
     const PopsJob* dj = (const PopsJob*)(base + o_jobs);
-    nmolec_kernel<<<(n_models + kWarps - 1) / kWarps, 32 * kWarps, 0, s>>>(dj, n_models);
+    nmolec_kernel<double, kWarps><<<(n_models + kWarps - 1) / kWarps, 32 * kWarps, 0, s>>>(dj, n_models);
     KP_CUDA(cudaGetLastError());
-    pops_kernel<<<total, 128, 0, s>>>(dj, (const int*)(base + o_first), n_models);
+    pops_kernel<double><<<total, 128, 0, s>>>(dj, (const int*)(base + o_first), n_models);
     KP_CUDA(cudaGetLastError());
     // the host copies of the job records must outlive the copies: wait for them
+    KP_CUDA(cudaStreamSynchronize(s));
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// forward-mode derivatives w.r.t. the log10 abundance of one element
+// ---------------------------------------------------------------------------
+
+namespace {
+
+ks_status check_tangents(const ks_pops_tangent* t, int32_t n) {
+    if (!t || n <= 0) return perr(KS_ERR_INVALID, "ks_populations_tangent: no models");
+    for (int i = 0; i < n; i++) {
+        const ks_pops_model& m = t[i].model;
+        if (m.n_layers < 1 || m.n_layers > 4096)
+            return perr(KS_ERR_INVALID, "ks_populations_tangent: n_layers must be 1..4096");
+        if (!m.temperature || !m.gas_pressure || !m.vturb || !m.xabund)
+            return perr(KS_ERR_INVALID, "ks_populations_tangent: null input pointer");
+        if (t[i].element < 0 || t[i].element >= kNEl)
+            return perr(KS_ERR_INVALID, "ks_populations_tangent: element must be 0..98 (Z-1)");
+        if (!t[i].d_electron_density || !t[i].d_mass_density || !t[i].d_xnf_h || !t[i].d_xnf_he1 ||
+            !t[i].d_xnf_h2 || !t[i].d_population)
+            return perr(KS_ERR_INVALID, "ks_populations_tangent: null derivative output");
+    }
+    return KS_OK;
+}
+
+size_t tangent_ws_bytes(const ks_pops_tangent* t, int32_t n) {
+    Carve c;
+    c.take(sizeof(PopsJobT<D1>) * (size_t)n);
+    c.take(sizeof(int) * ((size_t)n + 1));
+    for (int i = 0; i < n; i++) job_ws_bytes<D1>(c, (size_t)t[i].model.n_layers);
+    return c.off + 256;
+}
+
+}  // namespace
+
+extern "C" ks_status ks_populations_tangent_workspace_size(const ks_pops_tangent* tangents, int32_t n,
+                                                           size_t* bytes) {
+    ks_status st = check_tangents(tangents, n);
+    if (st != KS_OK) return st;
+    if (!bytes) return perr(KS_ERR_INVALID, "ks_populations_tangent_workspace_size: null output");
+    *bytes = tangent_ws_bytes(tangents, n);
+    return KS_OK;
+}
+
+extern "C" ks_status ks_populations_tangent(const ks_pops_tangent* tangents, int32_t n, void* workspace,
+                                            size_t workspace_bytes, void* stream) {
+    ks_status st = check_tangents(tangents, n);
+    if (st != KS_OK) return st;
+    if (!workspace || (reinterpret_cast<uintptr_t>(workspace) & 255) != 0)
+        return perr(KS_ERR_INVALID, "ks_populations_tangent: workspace must be non-null and 256-byte aligned");
+    if (workspace_bytes < tangent_ws_bytes(tangents, n))
+        return perr(KS_ERR_NOMEM, "ks_populations_tangent: workspace smaller than its workspace size");
+    st = device_pops();
+    if (st != KS_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    char* base = (char*)workspace;
+    Carve c;
+    const size_t o_jobs = c.take(sizeof(PopsJobT<D1>) * (size_t)n);
+    const size_t o_first = c.take(sizeof(int) * ((size_t)n + 1));
+    std::vector<PopsJobT<D1>> jobs(n);
+    std::vector<int> first(n + 1);
+    int total = 0;
+    for (int i = 0; i < n; i++) {
+        const ks_pops_tangent& t = tangents[i];
+        fill_job<D1>(jobs[i], t.model, base, c);
+        PopsJobT<D1>& J = jobs[i];
+        J.dparam = t.element;
+        J.d_xne = t.d_electron_density;
+        J.d_rho = t.d_mass_density;
+        J.d_xnf_h = t.d_xnf_h;
+        J.d_xnf_he1 = t.d_xnf_he1;
+        J.d_xnf_h2 = t.d_xnf_h2;
+        J.d_population = t.d_population;
+        J.doppler = nullptr;  // the Doppler widths do not depend on the abundances
+        first[i] = total;
+        total += t.model.n_layers;
+    }
+    first[n] = total;
+    KP_CUDA(cudaMemcpyAsync(base + o_jobs, jobs.data(), sizeof(PopsJobT<D1>) * n, cudaMemcpyHostToDevice, s));
+    KP_CUDA(cudaMemcpyAsync(base + o_first, first.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+    const PopsJobT<D1>* dj = (const PopsJobT<D1>*)(base + o_jobs);
+    nmolec_kernel<D1, 1><<<n, 32, 0, s>>>(dj, n);
+    KP_CUDA(cudaGetLastError());
+    pops_kernel<D1><<<total, 128, 0, s>>>(dj, (const int*)(base + o_first), n);
+    KP_CUDA(cudaGetLastError());
     KP_CUDA(cudaStreamSynchronize(s));
     return KS_OK;
 }

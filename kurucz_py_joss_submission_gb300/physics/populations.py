@@ -229,3 +229,54 @@ def molecular_system() -> dict:
     _native.check(L.ks_pops_system(C.byref(nm), C.byref(ne), eqe.ctypes.data, em.ctypes.data))
     return {"n_molecules": int(nm.value), "n_equations": int(ne.value),
             "equation_element": eqe[:ne.value].copy(), "element_molecular": em.astype(bool)}
+
+
+class PopulationTangents:
+    """``ks_populations_tangent``: derivatives of model ``k`` of a
+    :class:`DevicePopulations` with respect to the log10 abundances (dex) of
+    ``elements`` (atomic numbers), one warp per element, all in one launch.
+    ``run()`` fills ``d[field]`` ([n_elements, ...] device tensors) for the
+    fields electron_density, mass_density, xnf_h, xnf_he1, xnf_h2 and
+    population_per_ion at the model's current inputs."""
+
+    FIELDS = ("electron_density", "mass_density", "xnf_h", "xnf_he1", "xnf_h2", "population_per_ion")
+
+    def __init__(self, pops: DevicePopulations, k: int, elements: Sequence[int]):
+        L = _native.load()
+        self.pops, self.k = pops, k
+        self.elements = [int(z) for z in elements]
+        if any(z < 1 or z > 99 for z in self.elements):
+            raise ValueError("elements are atomic numbers 1..99")
+        n = pops.recs[k].n_layers
+        dev = pops.device
+        ne = len(self.elements)
+        self.d = {f: torch.empty((ne, n), dtype=torch.float64, device=dev) for f in self.FIELDS[:-1]}
+        self.d["population_per_ion"] = torch.empty((ne, n, N_ION, N_SPECIES), dtype=torch.float64, device=dev)
+        recs = (_native.KsPopsTangent * ne)()
+        base = pops.recs[k]
+        for i, z in enumerate(self.elements):
+            r = recs[i]
+            r.model.n_layers = base.n_layers
+            r.model.temperature = base.temperature
+            r.model.gas_pressure = base.gas_pressure
+            r.model.vturb = base.vturb
+            r.model.xabund = base.xabund
+            r.element = z - 1
+            r.d_electron_density = self.d["electron_density"][i].data_ptr()
+            r.d_mass_density = self.d["mass_density"][i].data_ptr()
+            r.d_xnf_h = self.d["xnf_h"][i].data_ptr()
+            r.d_xnf_he1 = self.d["xnf_he1"][i].data_ptr()
+            r.d_xnf_h2 = self.d["xnf_h2"][i].data_ptr()
+            r.d_population = self.d["population_per_ion"][i].data_ptr()
+        self.recs = recs
+        size = C.c_size_t(0)
+        _native.check(L.ks_populations_tangent_workspace_size(recs, ne, C.byref(size)))
+        self.workspace = torch.empty(int(size.value) + 256, dtype=torch.uint8, device=dev)
+        self._ws_ptr = (self.workspace.data_ptr() + 255) & ~255
+        self._ws_bytes = int(size.value)
+
+    def run(self, stream: Optional[torch.cuda.Stream] = None) -> "PopulationTangents":
+        L = _native.load()
+        _native.check(L.ks_populations_tangent(self.recs, len(self.elements), C.c_void_p(self._ws_ptr),
+                                               self._ws_bytes, stream_handle(stream)))
+        return self

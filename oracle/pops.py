@@ -118,8 +118,9 @@ def abundances(atm: dict) -> np.ndarray:
     return out
 
 
-def derived(atm: dict) -> dict:
-    """Per-layer state (convert_atm_to_npz.py:374-655, 1700-1730)."""
+def derived(atm: dict, abundance_offsets: dict = None) -> dict:
+    """Per-layer state (convert_atm_to_npz.py:374-655, 1700-1730).
+    ``abundance_offsets`` {Z: dex} scales XABUND (used to difference the stage)."""
     L = atm["layers"]
     rhox, T, P, xne, vturb = L[:, 0], L[:, 1].copy(), L[:, 2].copy(), L[:, 3].copy(), L[:, 6].copy()
     if rhox[0] < 0:
@@ -131,6 +132,8 @@ def derived(atm: dict) -> dict:
     if p_ratio > 1e5 and not (0.9 < p_ratio < 1.1):
         P = P * 1e6
     xabund = abundances(atm)
+    for z, dx in (abundance_offsets or {}).items():
+        xabund[int(z) - 1] *= 10.0 ** dx
     wtmole = float(np.sum(xabund * tables()["atmass"][:99]))
     xnatm = np.maximum(P / tk - xne, 1e-30)
     return dict(
@@ -766,10 +769,11 @@ def molecule_masses() -> np.ndarray:
     return out
 
 
-def convert(atm_path: Path) -> dict:
-    """The fields the synthesis path reads, as the converter computes them from ``atm_path``."""
+def convert(atm_path: Path, abundance_offsets: dict = None) -> dict:
+    """The fields the synthesis path reads, as the converter computes them from
+    ``atm_path`` (``abundance_offsets`` {Z: dex}: abundances scaled first)."""
     atm = parse_atm(atm_path)
-    st = derived(atm)
+    st = derived(atm, abundance_offsets)
     xabund = st["xabund"]
     nm = nmolec(st, xabund)
     xne = nm["xne"]
