@@ -179,6 +179,12 @@ class AtmosphereDiffSynthesizer(DiffSynthesizer):
         """Scale the selected elements' abundances by 10**d_ab (dex, device tensor
         [n_elements] or None) and recompute the populations into the synthesis
         atmosphere."""
+        key = None if d_ab is None else d_ab.detach().to(torch.float64).clone()
+        last = getattr(self, "_last_ab", ())
+        if last != () and ((key is None and last is None) or
+                           (key is not None and last is not None and torch.equal(key, last))):
+            return  # the populations of these abundances are already in the atmosphere
+        self._last_ab = key
         xab = self.xabund0.clone()
         if d_ab is not None:
             idx = torch.tensor([z - 1 for z in self.elements], dtype=torch.long, device=xab.device)
