@@ -8,18 +8,13 @@
 // (:2027), every step in double precision.  Compiled with --fmad=false, so
 // every product and sum is rounded separately as in the reference.
 //
-// Two kernels:
-//   nmolec_kernel  one warp per model atmosphere.  The layers are solved in
-//                  order (each layer's Newton iteration starts from the
-//                  previous layer's solution scaled by the pressure ratio), so
-//                  a model is one sequential chain; the warp's lanes share the
-//                  work inside a layer: equilibrium constants per molecule,
-//                  one column of the Jacobian per lane (each column summed in
-//                  the reference's molecule order), and Gauss-Jordan
-//                  elimination with full pivot search, one row per lane.
-//   pops_kernel    one block per (model, layer): the ion populations of the
-//                  99 elements (one thread per element) and the Doppler
-//                  widths of the 6 x 139 species.
+// Two kernels, each templated on the scalar (double, or a dual number that
+// carries d/d log10 XABUND of one element for the forward-mode derivatives):
+//   nmolec_block_kernel  one block per model atmosphere: the molecular
+//                        equilibrium, layer after layer (see below).
+//   pops_kernel          one block per (model, layer): the ion populations of
+//                        the 99 elements (one thread per element) and the
+//                        Doppler widths of the 6 x 139 species.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -37,7 +32,6 @@ constexpr int kMaxEq = 32;     // one lane per equation (the reference allows 30
 constexpr int kMaxMol = 200;   // MAXMOL (nmolec_exact.py:26)
 constexpr int kMaxLoc = 600;   // MAXLOC
 constexpr int kNIon = 6, kNSpec = 139, kNEl = 99;
-constexpr int kWarps = 2;      // models per nmolec block (one warp each)
 constexpr int kMaxIter = 200;  // Newton iterations per layer (nmolec_exact.py:2544)
 constexpr int kNLevTab = 14;
 constexpr int kLevCap = 192;
@@ -132,6 +126,7 @@ struct PopsTables {
     int idequa[kMaxEq];
     int col_off[kMaxEq + 1];        // molecules holding equation k (ascending), CSR
     int col_mol[kMaxLoc];
+    int slot_mol[kMaxLoc];          // molecule of each component slot
     // POPS molecular branch (pops_exact.py:1855-1900) per element: 1 when the
     // element's populations come from the molecule table; the table row of
     // each ion (-1: none, the population is zero)
@@ -481,7 +476,7 @@ __device__ S equilj_dev(int m, const LayerState& s, S xne) {
 }
 
 // ---------------------------------------------------------------------------
-// nmolec_kernel: NMOLEC (nmolec_exact.py:1742-3575), one warp per model
+// job records and shared helpers of the molecular equilibrium
 // ---------------------------------------------------------------------------
 
 template <typename S>
@@ -500,146 +495,9 @@ struct PopsJobT {
 };
 using PopsJob = PopsJobT<double>;
 
-template <typename S>
-struct WarpShared {
-    S a[kMaxEq * kMaxEq];  // DEQ, row-major [row][col]
-    S b[kMaxEq];           // EQ, then the Newton step
-    S xn[kMaxEq], xab[kMaxEq], eqold[kMaxEq];
-    S equilj[kMaxMol], term[kMaxMol];
-    unsigned char skip[kMaxMol];  // molecules the sums skip this iteration
-    int iferr;
-};
-
 __device__ __forceinline__ int comp_eq(int kr, int ne) { return kr >= ne ? ne - 1 : kr; }
 
-// Column k of DEQ and EQ[k] for the current XN (nmolec_exact.py:760-926):
-// the element and charge equations, then every molecule holding equation k
-// in table order, each adding in the reference's component order.
-template <typename S>
-__device__ void assemble_column(WarpShared<S>& W, int k, double xntot) {
-    const PopsTables& P = g_pops;
-    const int ne = P.nequa, e = ne - 1;
-    for (int r = 0; r < ne; r++) W.a[r * kMaxEq + k] = lift<S>(0.0);
-    S eqk;
-    if (k == 0) {
-        eqk = lift<S>(-xntot);
-        for (int q = 1; q < ne; q++) {
-            eqk = eqk + W.xn[q];
-            W.a[q * kMaxEq + 0] = -W.xab[q];
-        }
-        for (int m = 0; m < P.nmol; m++) {
-            if (P.locj[m + 1] - P.locj[m] <= 1 || W.skip[m]) continue;
-            eqk = eqk + W.term[m];
-        }
-        W.b[0] = eqk;
-        return;
-    }
-    W.a[0 * kMaxEq + k] = lift<S>(1.0);
-    W.a[k * kMaxEq + k] = lift<S>(1.0);
-    eqk = W.xn[k] - W.xab[k] * W.xn[0];
-    if (P.has_e && k == e) {
-        eqk = -W.xn[e];
-        W.a[e * kMaxEq + e] = lift<S>(-1.0);
-    }
-    for (int q = P.col_off[k]; q < P.col_off[k + 1]; q++) {
-        const int m = P.col_mol[q];
-        if (W.skip[m]) continue;
-        const S t = W.term[m];
-        const int l1 = P.locj[m], l2 = P.locj[m + 1];
-        for (int lk = l1; lk < l2; lk++) {
-            const int kr = P.kcomps[lk];
-            if (comp_eq(kr, ne) != k) continue;
-            const S d = kr >= ne ? -t / W.xn[e] : t / W.xn[kr];
-            eqk = eqk + t;
-            W.a[0 * kMaxEq + k] = W.a[0 * kMaxEq + k] + d;
-            for (int lm = l1; lm < l2; lm++) {
-                const int mm = comp_eq(P.kcomps[lm], ne);
-                W.a[mm * kMaxEq + k] = W.a[mm * kMaxEq + k] + d;
-            }
-        }
-        if (P.has_e && P.kcomps[l2 - 1] == e) {
-            for (int lk = l1; lk < l2; lk++) {
-                const int kk = comp_eq(P.kcomps[lk], ne);
-                if (kk != k) continue;
-                const S d = t / W.xn[kk];
-                if (kk == e) eqk = eqk - t - t;
-                W.a[e * kMaxEq + k] = W.a[e * kMaxEq + k] - d - d;
-            }
-        }
-    }
-    W.b[k] = eqk;
-}
-
 __device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
-
-// SOLVIT (nmolec_exact.py:3671-3765): Gauss-Jordan elimination with the
-// full pivot search (largest |a| over unpivoted rows and columns, first in
-// row-major order on ties), rows swapped to put the pivot on the diagonal.
-// Lane r owns row r.  The solution is left in W.b.  With S = D1 the pivots
-// are chosen on the values, so the derivative is that of the same
-// elimination.
-template <typename S>
-__device__ void solvit_warp(WarpShared<S>& W, int n, int lane) {
-    int pcount = 0;  // ipivot of the column this lane stands for
-    for (int step = 0; step < n; step++) {
-        const unsigned done = __ballot_sync(0xffffffffu, lane < n && pcount == 1);
-        double best = 0.0;
-        int bidx = 0x7fffffff;
-        if (lane < n && !((done >> lane) & 1u)) {
-            for (int c = 0; c < n; c++) {
-                if ((done >> c) & 1u) continue;
-                const double v = fabs(val(W.a[lane * kMaxEq + c]));
-                if (v > best) {
-                    best = v;
-                    bidx = lane * n + c;
-                }
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ob = shfl_xor(best, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-            if (ob > best || (ob == best && oi < bidx)) {
-                best = ob;
-                bidx = oi;
-            }
-        }
-        int irow = 0, icol = 0;
-        if (best > 0.0) {
-            irow = bidx / n;
-            icol = bidx - irow * n;
-        }
-        if (lane == icol) pcount += 1;
-        if (irow != icol) {
-            if (lane < n) {
-                const S x = W.a[irow * kMaxEq + lane];
-                W.a[irow * kMaxEq + lane] = W.a[icol * kMaxEq + lane];
-                W.a[icol * kMaxEq + lane] = x;
-            }
-            if (lane == 0) {
-                const S x = W.b[irow];
-                W.b[irow] = W.b[icol];
-                W.b[icol] = x;
-            }
-        }
-        __syncwarp();
-        const S pivot = W.a[icol * kMaxEq + icol];
-        __syncwarp();
-        if (lane < n) W.a[icol * kMaxEq + lane] = (lane == icol ? lift<S>(1.0) : W.a[icol * kMaxEq + lane]) / pivot;
-        if (lane == 0) W.b[icol] = W.b[icol] / pivot;
-        __syncwarp();
-        if (lane < n && lane != icol) {
-            S* row = &W.a[lane * kMaxEq];
-            const S t = row[icol];
-            if (val(t) != 0.0) {
-                row[icol] = lift<S>(0.0);
-                const S* prow = &W.a[icol * kMaxEq];
-                for (int c = 0; c < n; c++) row[c] = row[c] - prow[c] * t;
-                W.b[lane] = W.b[lane] - W.b[icol] * t;
-            }
-        }
-        __syncwarp();
-    }
-}
 
 // numpy's pairwise sum of 99 values (8 accumulators, then the rest), the
 // order np.sum gives WTMOLE in the reference.
@@ -674,113 +532,307 @@ __device__ __forceinline__ void store(double* v, double* d, size_t i, S x) {
     }
 }
 
-template <typename S, int NW>
-__global__ void __launch_bounds__(32 * NW) nmolec_kernel(const PopsJobT<S>* __restrict__ jobs, int n_jobs) {
-    __shared__ WarpShared<S> sh[NW];
-    __shared__ S xab_all[NW][kNEl];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int job = blockIdx.x * NW + w;
-    if (job >= n_jobs) return;  // whole warps only
-    WarpShared<S>& W = sh[w];
+// ---------------------------------------------------------------------------
+// nmolec_block_kernel: NMOLEC (nmolec_exact.py:1742-3575), one block of
+// kPopThreads per model.  The layers are solved surface first, each Newton
+// iteration seeded from the previous layer's solution times the pressure
+// ratio, so a model is one sequential chain.  FP64 arithmetic is scarce on
+// this part (1/64 of the FP32 rate), so the work of an iteration is spread
+// over the block: the molecular terms and every division of the Jacobian
+// (term / XN of each component slot) in parallel, then each column of DEQ
+// summed by one thread in the reference's molecule and component order
+// (:760-926; every DEQ and EQ entry gets the reference's additions in the
+// reference's order), SOLVIT (:3671-3765) with one matrix entry per thread
+// in the elimination, and the divisions of the update in parallel ahead of
+// its sequential SCALE logic.
+// ---------------------------------------------------------------------------
+
+constexpr int kPopThreads = 128;
+
+template <typename S>
+struct BlockShared {
+    S a[kMaxEq * kMaxEq];
+    S b[kMaxEq];
+    S xn[kMaxEq], xab[kMaxEq], eqold[kMaxEq], dcol[kMaxEq];
+    S equilj[kMaxMol], term[kMaxMol];
+    S dmain[kMaxLoc];               // term / XN (minus for an inverse electron) per component slot
+    S dcorr[kMaxLoc];               // term / XN of the slot's equation (negative-ion correction)
+    S xab_all[kNEl];
+    S xneq[kMaxEq];
+    unsigned char skip[kMaxMol];
+    unsigned char ratio_err[kMaxEq], flip[kMaxEq];
+    double best[kPopThreads / 32];
+    int bidx[kPopThreads / 32];
+    int piv_row, piv_col;
+    int pcount[kMaxEq];
+    int iferr;
+};
+
+template <typename S>
+__device__ void assemble_column_pre(BlockShared<S>& B, int k, double xntot) {
+    const PopsTables& P = g_pops;
+    const int ne = P.nequa, e = ne - 1;
+    for (int r = 0; r < ne; r++) B.a[r * kMaxEq + k] = lift<S>(0.0);
+    S eqk;
+    if (k == 0) {
+        eqk = lift<S>(-xntot);
+        for (int q = 1; q < ne; q++) {
+            eqk = eqk + B.xn[q];
+            B.a[q * kMaxEq + 0] = -B.xab[q];
+        }
+        for (int m = 0; m < P.nmol; m++) {
+            if (P.locj[m + 1] - P.locj[m] <= 1 || B.skip[m]) continue;
+            eqk = eqk + B.term[m];
+        }
+        B.b[0] = eqk;
+        return;
+    }
+    B.a[0 * kMaxEq + k] = lift<S>(1.0);
+    B.a[k * kMaxEq + k] = lift<S>(1.0);
+    eqk = B.xn[k] - B.xab[k] * B.xn[0];
+    if (P.has_e && k == e) {
+        eqk = -B.xn[e];
+        B.a[e * kMaxEq + e] = lift<S>(-1.0);
+    }
+    for (int q = P.col_off[k]; q < P.col_off[k + 1]; q++) {
+        const int m = P.col_mol[q];
+        if (B.skip[m]) continue;
+        const S t = B.term[m];
+        const int l1 = P.locj[m], l2 = P.locj[m + 1];
+        for (int lk = l1; lk < l2; lk++) {
+            if (comp_eq(P.kcomps[lk], ne) != k) continue;
+            const S d = B.dmain[lk];
+            eqk = eqk + t;
+            B.a[0 * kMaxEq + k] = B.a[0 * kMaxEq + k] + d;
+            for (int lm = l1; lm < l2; lm++) {
+                const int mm = comp_eq(P.kcomps[lm], ne);
+                B.a[mm * kMaxEq + k] = B.a[mm * kMaxEq + k] + d;
+            }
+        }
+        if (P.has_e && P.kcomps[l2 - 1] == e) {
+            for (int lk = l1; lk < l2; lk++) {
+                const int kk = comp_eq(P.kcomps[lk], ne);
+                if (kk != k) continue;
+                const S d = B.dcorr[lk];
+                if (kk == e) eqk = eqk - t - t;
+                B.a[e * kMaxEq + k] = B.a[e * kMaxEq + k] - d - d;
+            }
+        }
+    }
+    B.b[k] = eqk;
+}
+
+// SOLVIT (nmolec_exact.py:3671-3765): Gauss-Jordan elimination with the
+// full pivot search (largest |a| over unpivoted rows and columns, first in
+// row-major order on ties; pivots chosen on the values, so with dual numbers
+// the derivative is that of the same elimination), rows swapped to put the
+// pivot on the diagonal, one matrix entry per thread in the elimination.
+// The solution is left in B.b.
+template <typename S>
+__device__ void solvit_block(BlockShared<S>& B, int n) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid < kMaxEq) B.pcount[tid] = 0;
+    __syncthreads();
+    for (int step = 0; step < n; step++) {
+        double best = 0.0;
+        int bi = 0x7fffffff;
+        for (int idx = tid; idx < n * n; idx += kPopThreads) {
+            const int r = idx / n, c = idx - r * n;
+            if (B.pcount[r] == 1 || B.pcount[c] == 1) continue;
+            const double v = fabs(val(B.a[r * kMaxEq + c]));
+            if (v > best) {  // ascending idx per thread: the first maximum
+                best = v;
+                bi = idx;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = shfl_xor(best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            B.best[w] = best;
+            B.bidx[w] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double bb = B.best[0];
+            int ii = B.bidx[0];
+            for (int q = 1; q < kPopThreads / 32; q++)
+                if (B.best[q] > bb || (B.best[q] == bb && B.bidx[q] < ii)) {
+                    bb = B.best[q];
+                    ii = B.bidx[q];
+                }
+            int irow = 0, icol = 0;
+            if (bb > 0.0) {
+                irow = ii / n;
+                icol = ii - irow * n;
+            }
+            B.piv_row = irow;
+            B.piv_col = icol;
+            B.pcount[icol] += 1;
+        }
+        __syncthreads();
+        const int irow = B.piv_row, icol = B.piv_col;
+        if (irow != icol) {
+            if (tid < n) {
+                const S x = B.a[irow * kMaxEq + tid];
+                B.a[irow * kMaxEq + tid] = B.a[icol * kMaxEq + tid];
+                B.a[icol * kMaxEq + tid] = x;
+            }
+            if (tid == 0) {
+                const S x = B.b[irow];
+                B.b[irow] = B.b[icol];
+                B.b[icol] = x;
+            }
+            __syncthreads();
+        }
+        const S pivot = B.a[icol * kMaxEq + icol];
+        __syncthreads();
+        if (tid < n) B.a[icol * kMaxEq + tid] = (tid == icol ? lift<S>(1.0) : B.a[icol * kMaxEq + tid]) / pivot;
+        if (tid == kPopThreads - 1) B.b[icol] = B.b[icol] / pivot;
+        __syncthreads();
+        if (tid < n) B.dcol[tid] = B.a[tid * kMaxEq + icol];
+        __syncthreads();
+        for (int idx = tid; idx < n * n; idx += kPopThreads) {
+            const int l = idx / n, c = idx - l * n;
+            if (l == icol) continue;
+            const S t = B.dcol[l];
+            if (val(t) == 0.0) continue;
+            const S cur = c == icol ? lift<S>(0.0) : B.a[l * kMaxEq + c];
+            B.a[l * kMaxEq + c] = cur - B.a[icol * kMaxEq + c] * t;
+        }
+        if (tid < n && tid != icol) {
+            const S t = B.dcol[tid];
+            if (val(t) != 0.0) B.b[tid] = B.b[tid] - B.b[icol] * t;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kPopThreads) nmolec_block_kernel(const PopsJobT<S>* __restrict__ jobs, int n_jobs) {
+    __shared__ BlockShared<S> B;
+    const int job = blockIdx.x;
+    if (job >= n_jobs) return;
+    const int tid = threadIdx.x;
     const PopsJobT<S> J = jobs[job];
     const PopsTables& P = g_pops;
-    const int ne = P.nequa, e = ne - 1, nmol = P.nmol;
+    const int ne = P.nequa, e = ne - 1, nmol = P.nmol, nloc = P.locj[P.nmol];
     const bool has_e = P.has_e != 0;
-    for (int z = lane; z < kNEl; z += 32) xab_all[w][z] = abundance<S>(J, z);
-    __syncwarp();
-    if (lane < ne) {
+    for (int z = tid; z < kNEl; z += kPopThreads) B.xab_all[z] = abundance<S>(J, z);
+    __syncthreads();
+    if (tid < ne) {
         S x = lift<S>(0.0);
-        if (lane >= 1 && P.idequa[lane] < 100) x = smax<S>(xab_all[w][P.idequa[lane] - 1], lift<S>(1e-20));
-        W.xab[lane] = x;
+        if (tid >= 1 && P.idequa[tid] < 100) x = smax<S>(B.xab_all[P.idequa[tid] - 1], lift<S>(1e-20));
+        B.xab[tid] = x;
     }
     S wtmole = lift<S>(0.0);
-    if (lane == 0) wtmole = wtmole_dev<S>(xab_all[w]);
+    if (tid == 0) wtmole = wtmole_dev<S>(B.xab_all);
     S xne_prev = lift<S>(0.0);
     double p_prev = 0.0;
-    __syncwarp();
+    __syncthreads();
     for (int j = 0; j < J.n_layers; j++) {
         const LayerState s = layer_state(J.t[j], J.p[j], J.vturb[j]);
         S xne_j;
         if (j == 0) {
             const double x0 = s.xntot / 2.0;
             const double x = x0 / 10.0;
-            if (lane < ne) W.xn[lane] = lane == 0 ? lift<S>(x0) : (has_e && lane == e ? lift<S>(x) : x * W.xab[lane]);
+            if (tid < ne) B.xn[tid] = tid == 0 ? lift<S>(x0) : (has_e && tid == e ? lift<S>(x) : x * B.xab[tid]);
             xne_j = lift<S>(x);
         } else {
             const double ratio = s.p / p_prev;
-            if (lane < ne) W.xn[lane] = W.xn[lane] * ratio;
+            if (tid < ne) B.xn[tid] = B.xn[tid] * ratio;
             xne_j = xne_prev * ratio;
         }
-        if (lane < ne) W.eqold[lane] = lift<S>(0.0);
-        for (int m = lane; m < nmol; m += 32) W.equilj[m] = equilj_dev<S>(m, s, xne_j);
-        __syncwarp();
+        if (tid < ne) B.eqold[tid] = lift<S>(0.0);
+        for (int m = tid; m < nmol; m += kPopThreads) B.equilj[m] = equilj_dev<S>(m, s, xne_j);
+        __syncthreads();
         int it = 0;
         for (it = 1; it <= kMaxIter; it++) {
-            for (int m = lane; m < nmol; m += 32) {
-                S t = W.equilj[m];
+            for (int m = tid; m < nmol; m += kPopThreads) {
+                S t = B.equilj[m];
                 if (!(isfinite(val(t)) && val(t) > 0.0)) {
-                    W.skip[m] = 1;
+                    B.skip[m] = 1;
                     continue;
                 }
                 for (int lk = P.locj[m]; lk < P.locj[m + 1]; lk++) {
                     const int kr = P.kcomps[lk];
-                    t = kr >= ne ? t / W.xn[e] : t * W.xn[kr];
+                    t = kr >= ne ? t / B.xn[e] : t * B.xn[kr];
                 }
-                W.term[m] = t;
-                W.skip[m] = isfinite(val(t)) ? 0 : 1;
+                B.term[m] = t;
+                B.skip[m] = isfinite(val(t)) ? 0 : 1;
             }
-            __syncwarp();
-            if (lane < ne) assemble_column<S>(W, lane, s.xntot);
-            __syncwarp();
-            solvit_warp<S>(W, ne, lane);
-            if (lane == 0) {
+            __syncthreads();
+            for (int q = tid; q < nloc; q += kPopThreads) {
+                const int m = P.slot_mol[q];
+                if (B.skip[m]) continue;
+                const S t = B.term[m];
+                const int kr = P.kcomps[q];
+                B.dmain[q] = kr >= ne ? -t / B.xn[e] : t / B.xn[kr];
+                B.dcorr[q] = t / B.xn[comp_eq(kr, ne)];
+            }
+            __syncthreads();
+            if (tid < ne) assemble_column_pre<S>(B, tid, s.xntot);
+            __syncthreads();
+            solvit_block<S>(B, ne);
+            if (tid < ne) {
+                S d = B.b[tid];
+                const S x = B.xn[tid];
+                const double dv = val(d), xv = val(x);
+                const double ratio = xv == 0.0 ? (dv == 0.0 ? 0.0 : INFINITY) : fabs(dv / xv);
+                B.ratio_err[tid] = ratio > 0.001;
+                const double eo = val(B.eqold[tid]);
+                const bool flip = (eo > 0.0 && dv < 0.0) || (eo < 0.0 && dv > 0.0);
+                B.flip[tid] = flip;
+                if (flip && isfinite(dv)) d = d * 0.69;
+                B.b[tid] = d;
+                B.xneq[tid] = (isfinite(xv) && isfinite(val(d)) && fabs(xv) > 2.2250738585072014e-308)
+                                  ? x * (1.0 - d / x)
+                                  : x - d;
+            }
+            __syncthreads();
+            if (tid == 0) {
                 int iferr = 0;
                 double scale = 100.0;
                 for (int k = 0; k < ne; k++) {
-                    S d = W.b[k];
-                    const S x = W.xn[k];
-                    const double dv = val(d), xv = val(x);
-                    const double ratio = xv == 0.0 ? (dv == 0.0 ? 0.0 : INFINITY) : fabs(dv / xv);
-                    if (ratio > 0.001) iferr = 1;
-                    const double eo = val(W.eqold[k]);
-                    const bool flip = (eo > 0.0 && dv < 0.0) || (eo < 0.0 && dv > 0.0);
-                    if (flip && isfinite(dv)) d = d * 0.69;
-                    const S xneq = (isfinite(xv) && isfinite(val(d)) && fabs(xv) > 2.2250738585072014e-308)
-                                       ? x * (1.0 - d / x)
-                                       : x - d;
-                    if (val(xneq) < xv / 100.0) {
-                        W.xn[k] = x / scale;
-                        if (flip) scale = sqrt(scale);
+                    if (B.ratio_err[k]) iferr = 1;
+                    const S x = B.xn[k];
+                    if (val(B.xneq[k]) < val(x) / 100.0) {
+                        B.xn[k] = x / scale;
+                        if (B.flip[k]) scale = sqrt(scale);
                     } else {
-                        W.xn[k] = xneq;
+                        B.xn[k] = B.xneq[k];
                     }
-                    W.eqold[k] = d;
+                    B.eqold[k] = B.b[k];
                 }
-                W.iferr = iferr;
+                B.iferr = iferr;
             }
-            __syncwarp();
-            if (W.iferr == 0) break;
+            __syncthreads();
+            if (B.iferr == 0) break;
         }
         if (it > kMaxIter) it = kMaxIter;
-        if (has_e) xne_j = W.xn[e];
-        // molecule densities XNMOL (nmolec_exact.py:3556-3575)
+        if (has_e) xne_j = B.xn[e];
         S* xnmol = J.xnmol + (size_t)j * kMaxMol;
-        for (int m = lane; m < nmol; m += 32) {
-            S v = W.equilj[m];
+        for (int m = tid; m < nmol; m += kPopThreads) {
+            S v = B.equilj[m];
             for (int lk = P.locj[m]; lk < P.locj[m + 1]; lk++) {
                 const int kr = P.kcomps[lk];
-                v = kr >= ne ? v / W.xn[e] : v * W.xn[kr];
+                v = kr >= ne ? v / B.xn[e] : v * B.xn[kr];
             }
             xnmol[m] = v;
         }
-        __syncwarp();
-        if (lane == 0) {
+        __syncthreads();
+        if (tid == 0) {
             J.state[j] = s;
             J.xnes[j] = xne_j;
-            J.xnat[j] = W.xn[0];
+            J.xnat[j] = B.xn[0];
             store<S>(J.xne, J.d_xne, j, xne_j);
-            store<S>(J.rho, J.d_rho, j, W.xn[0] * wtmole * 1.660e-24);
-            if (J.xnatom) J.xnatom[j] = val(W.xn[0]);
+            store<S>(J.rho, J.d_rho, j, B.xn[0] * wtmole * 1.660e-24);
+            if (J.xnatom) J.xnatom[j] = val(B.xn[0]);
             if (J.hckt) J.hckt[j] = s.hckt;
             if (J.iterations) J.iterations[j] = it;
             const S h1 = smax<S>(P.row_h1 >= 0 ? xnmol[P.row_h1] : lift<S>(0.0), lift<S>(1e-40));
@@ -804,7 +856,7 @@ __global__ void __launch_bounds__(32 * NW) nmolec_kernel(const PopsJobT<S>* __re
         }
         xne_prev = xne_j;
         p_prev = s.p;
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -958,6 +1010,8 @@ ks_status build_molecules(PopsTables& T, const double* code, const double* equil
     for (size_t q = 0; q < comps.size(); q++) T.kcomps[q] = ifequa[comps[q]] - 1;
     T.nmol = nmol;
     T.has_e = T.idequa[T.nequa - 1] == 100;
+    for (int m = 0; m < nmol; m++)
+        for (int l = T.locj[m]; l < T.locj[m + 1]; l++) T.slot_mol[l] = m;
     // per equation, the molecules (more than one component) that hold it
     const int ne = T.nequa;
     int n = 0;
@@ -1241,7 +1295,7 @@ extern "C" ks_status ks_populations(const ks_pops_model* models, int32_t n_model
     KP_CUDA(cudaMemcpyAsync(base + o_jobs, jobs.data(), sizeof(PopsJob) * n_models, cudaMemcpyHostToDevice, s));
     KP_CUDA(cudaMemcpyAsync(base + o_first, first.data(), sizeof(int) * (n_models + 1), cudaMemcpyHostToDevice, s));
     const PopsJob* dj = (const PopsJob*)(base + o_jobs);
-    nmolec_kernel<double, kWarps><<<(n_models + kWarps - 1) / kWarps, 32 * kWarps, 0, s>>>(dj, n_models);
+    nmolec_block_kernel<double><<<n_models, kPopThreads, 0, s>>>(dj, n_models);
     KP_CUDA(cudaGetLastError());
     pops_kernel<double><<<total, 128, 0, s>>>(dj, (const int*)(base + o_first), n_models);
     KP_CUDA(cudaGetLastError());
@@ -1329,7 +1383,7 @@ extern "C" ks_status ks_populations_tangent(const ks_pops_tangent* tangents, int
     KP_CUDA(cudaMemcpyAsync(base + o_jobs, jobs.data(), sizeof(PopsJobT<D1>) * n, cudaMemcpyHostToDevice, s));
     KP_CUDA(cudaMemcpyAsync(base + o_first, first.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
     const PopsJobT<D1>* dj = (const PopsJobT<D1>*)(base + o_jobs);
-    nmolec_kernel<D1, 1><<<n, 32, 0, s>>>(dj, n);
+    nmolec_block_kernel<D1><<<n, kPopThreads, 0, s>>>(dj, n);
     KP_CUDA(cudaGetLastError());
     pops_kernel<D1><<<total, 128, 0, s>>>(dj, (const int*)(base + o_first), n);
     KP_CUDA(cudaGetLastError());
