@@ -532,6 +532,10 @@ ks_status ks_gfall_fetch(const ks_gfall *g, double *wavelength, double *log_gf, 
                          double *gamma_vdw, int32_t *element_idx, int32_t *ion_stage,
                          int32_t *line_type, uint8_t *process_mask, uint8_t *asynth_mask,
                          double *code, int64_t *catalog_index);
+/* NBLO / NBUP of every record (columns 103-106 of the fixed-width form,
+ * synthe_py/io/lines/atomic.py:520-532): the principal quantum numbers of
+ * hydrogen lines, 0 when blank.  Same order as ks_gfall_fetch. */
+ks_status ks_gfall_fetch_levels(const ks_gfall *g, int32_t *n_lower, int32_t *n_upper);
 void ks_gfall_free(ks_gfall *g);
 
 #ifdef __cplusplus

@@ -203,6 +203,7 @@ SIGNATURES = {
     "ks_gfall_sort": (C.c_int32, [P]),
     "ks_gfall_count": (C.c_int64, [P]),
     "ks_gfall_fetch": (C.c_int32, [P] + [P] * 15),
+    "ks_gfall_fetch_levels": (C.c_int32, [P, P, P]),
     "ks_gfall_free": (None, [P]),
 }
 

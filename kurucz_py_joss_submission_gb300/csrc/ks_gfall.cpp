@@ -452,4 +452,13 @@ extern "C" ks_status ks_gfall_fetch(const ks_gfall* g, double* wavelength, doubl
     return KS_OK;
 }
 
+extern "C" ks_status ks_gfall_fetch_levels(const ks_gfall* g, int32_t* n_lower, int32_t* n_upper) {
+    if (!g) return KS_ERR_INVALID;
+    for (size_t k = 0; k < g->recs.size(); k++) {
+        if (n_lower) n_lower[k] = g->recs[k].nblo;
+        if (n_upper) n_upper[k] = g->recs[k].nbup;
+    }
+    return KS_OK;
+}
+
 extern "C" void ks_gfall_free(ks_gfall* g) { delete g; }

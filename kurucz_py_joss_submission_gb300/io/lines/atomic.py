@@ -39,6 +39,8 @@ class LineCatalog:
     asynth_mask: np.ndarray
     code: np.ndarray
     catalog_index: np.ndarray
+    n_lower: np.ndarray   # NBLO: lower principal quantum number (hydrogen lines), 0 if blank
+    n_upper: np.ndarray   # NBUP
 
     def __len__(self) -> int:
         return int(self.wavelength.size)
@@ -86,11 +88,14 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
             gamma_vdw=np.zeros(n), element_idx=np.zeros(n, np.int32), ion_stages=np.zeros(n, np.int32),
             line_types=np.zeros(n, np.int32), process_mask=np.zeros(n, np.uint8),
             asynth_mask=np.zeros(n, np.uint8), code=np.zeros(n), catalog_index=np.zeros(n, np.int64),
+            n_lower=np.zeros(n, np.int32), n_upper=np.zeros(n, np.int32),
         )
         order = ["wavelength", "log_gf", "gf", "cgf", "excitation_energy", "gamma_rad", "gamma_stark",
                  "gamma_vdw", "element_idx", "ion_stages", "line_types", "process_mask",
                  "asynth_mask", "code", "catalog_index"]
         _native.check(L.ks_gfall_fetch(h, *[cols[k].ctypes.data_as(C.c_void_p) for k in order]))
+        _native.check(L.ks_gfall_fetch_levels(h, cols["n_lower"].ctypes.data_as(C.c_void_p),
+                                              cols["n_upper"].ctypes.data_as(C.c_void_p)))
     finally:
         L.ks_gfall_free(h)
     return LineCatalog(**cols)

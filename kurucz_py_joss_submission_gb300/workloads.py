@@ -218,9 +218,37 @@ class LineDraw:
     log_gamma_rad: np.ndarray
     log_gamma_stark: np.ndarray
     log_gamma_vdw: np.ndarray
+    n_lower: Optional[np.ndarray] = None   # NBLO / NBUP of hydrogen lines (None: blank)
+    n_upper: Optional[np.ndarray] = None
 
     def __len__(self) -> int:
         return int(self.wavelength_nm.size)
+
+    def levels(self):
+        n = len(self)
+        lo = self.n_lower if self.n_lower is not None else np.zeros(n, np.int32)
+        up = self.n_upper if self.n_upper is not None else np.zeros(n, np.int32)
+        return np.asarray(lo, np.int32), np.asarray(up, np.int32)
+
+
+# Hydrogen level energies (cm^-1) of SYNTHE's table (n = 1..8) and log gf of
+# the Balmer lines (Kurucz's gfall values for H I 2 -> m).
+_EHYD = (0.0, 82259.105, 97492.302, 102823.893, 105291.651, 106632.160, 107440.444, 107965.051)
+_BALMER_LOG_GF = {3: 0.710, 4: -0.020, 5: -0.447, 6: -0.753, 7: -0.993, 8: -1.190}
+
+
+def balmer_lines(upper) -> LineDraw:
+    """Hydrogen Balmer lines 2 -> m (m in ``upper``, 3..8) as gfall records with
+    NBLO = 2, NBUP = m; the wavelength is the one the level energies give."""
+    m = np.asarray(sorted(upper), dtype=np.int32)
+    e_lo = np.full(m.size, _EHYD[1])
+    e_up = np.array([_EHYD[k - 1] for k in m])
+    wl = 1.0e7 / (e_up - e_lo)
+    z = np.zeros(m.size)
+    return LineDraw(wavelength_nm=wl, log_gf=np.array([_BALMER_LOG_GF[k] for k in m]),
+                    code=np.full(m.size, 1.00), e_lower_cm=e_lo, log_gamma_rad=z + 8.76,
+                    log_gamma_stark=z - 4.5, log_gamma_vdw=z - 7.5,
+                    n_lower=np.full(m.size, 2, np.int32), n_upper=m)
 
 
 def random_atomic_lines(
@@ -323,6 +351,9 @@ def merge_lines(*draws: LineDraw) -> LineDraw:
     cat = {f: np.concatenate([getattr(d, f) for d in draws]) for f in
            ("wavelength_nm", "log_gf", "code", "e_lower_cm", "log_gamma_rad", "log_gamma_stark",
             "log_gamma_vdw")}
+    if any(d.n_lower is not None for d in draws):
+        cat["n_lower"] = np.concatenate([d.levels()[0] for d in draws])
+        cat["n_upper"] = np.concatenate([d.levels()[1] for d in draws])
     order = np.argsort(cat["wavelength_nm"], kind="stable")
     return LineDraw(**{k: v[order] for k, v in cat.items()})
 
@@ -343,11 +374,16 @@ def format_gfall(lines: LineDraw) -> str:
     gw = _nonzero_f62(lines.log_gamma_vdw)
     rows = []
     blank_tail = " " * (160 - 98)
+    nlo, nup = lines.levels()
     for i in range(len(lines)):
+        tail = blank_tail
+        if nlo[i] > 0 or nup[i] > 0:
+            # REF (4 columns) blank, then NBLO and NBUP (I2 each, columns 103-106)
+            tail = f"{'':4s}{nlo[i]:2d}{nup[i]:2d}" + " " * (160 - 106)
         rows.append(
             f"{wl[i]:11.4f}{lines.log_gf[i]:7.3f}{lines.code[i]:6.2f}{e[i]:12.3f}"
             f"{1.0:5.1f} {'SYNTH   '}{'  '}{ep[i]:12.3f}{2.0:5.1f} {'SYNTH   '}{'  '}"
-            f"{gr[i]:6.2f}{gs[i]:6.2f}{gw[i]:6.2f}{blank_tail}\n"
+            f"{gr[i]:6.2f}{gs[i]:6.2f}{gw[i]:6.2f}{tail}\n"
         )
     return "".join(rows)
 

@@ -95,6 +95,16 @@ CASES = {
     # near-wing Voigt table index at rounding ties of TABI (see t5800g444_tabi)
     "tabi_500_501": dict(atm="t5800g444_tabi", wl_start=500.0, wl_end=501.0,
                          n_lines=200, draw=(499.85, 501.15), log_uniform=False, seed=18),
+    # hydrogen Balmer lines (HPROF4 profiles, engine/opacity.py:1706): H beta
+    # centred in the window (wings of the 2 -> 4 line: the simple-wing branch)
+    # and H gamma (2 -> 5: the tapered wings with the m -+ 1, 2 cuts), with
+    # H delta beside each, on top of metal lines
+    "hbeta_486": dict(atm="t5800g444", wl_start=485.6, wl_end=486.9,
+                      n_lines=150, draw=(485.45, 487.05), log_uniform=False, seed=19,
+                      hydrogen=[4, 5, 6]),
+    "hgamma_434": dict(atm="t5800g444", wl_start=433.5, wl_end=434.8,
+                       n_lines=150, draw=(433.35, 434.95), log_uniform=False, seed=20,
+                       hydrogen=[4, 5, 6]),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -117,6 +127,8 @@ def case_lines(case: dict) -> workloads.LineDraw:
         bands = workloads.random_band_lines(case["band_lines"], case["draw"][0], case["draw"][1],
                                             case["band_seed"])
         lines = workloads.merge_lines(lines, bands)
+    if case.get("hydrogen"):
+        lines = workloads.merge_lines(lines, workloads.balmer_lines(case["hydrogen"]))
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth
         # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)
@@ -206,6 +218,9 @@ def run_case(name: str, full_npz: Path, work: Path) -> None:
     )
     transp = np.asarray(s3["transp"])
     asynth = np.asarray(s4["asynth"])
+    if case.get("hydrogen"):
+        # the line opacity the transfer sees: ASYNTH plus the hydrogen profiles
+        out["line_opacity"] = np.asarray(s5["line_opacity"])
     if name in LARGE_CASES:
         rng = np.random.default_rng(7)
         vi = np.argwhere(np.asarray(s3["valid_mask"]))

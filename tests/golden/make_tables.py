@@ -72,7 +72,33 @@ def main(argv: list) -> int:
     )
     print(f"wrote {OUT}")
     write_pops_tables()
+    write_hydrogen_tables()
     return 0
+
+
+def write_hydrogen_tables() -> None:
+    """Write ``hydrogen_tables.npz``: the data of the hydrogen line profiles
+    (HPROF4, ``synthe_py/physics/profiles/hydrogen.py:23-1405``: Stark
+    correction tables PROPBM/C/D/PP/BETA, fine-structure components
+    STALPH/STWTAL/ISTAL/LNGHAL/STCOMP/STCPWT/LNCOMP, the Lyman cutoff tables,
+    ASUM/ASUMLYMAN, Y1WTM, XKNMTB), the hydrogen level energies EHYD
+    (``synthe_py/engine/opacity.py:49``) and the continuum edges CONTH of the
+    wing tables (``synthe_py/physics/tables.py:152``)."""
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "numba_shim"))
+    sys.path.insert(0, str(REFERENCE))
+    from synthe_py.physics.profiles.hydrogen import hydrogen_tables
+    from synthe_py.physics.tables import metal_wing_tables
+    import synthe_py.engine.opacity as eo
+
+    t = hydrogen_tables()
+    out = {k: np.asarray(v) for k, v in t.__dict__.items() if k not in ("tabvi", "tabh1")}
+    for k in ("istal", "lnghal", "lncomp"):
+        out[k] = out[k].astype(np.int32)
+    out["ehyd"] = np.asarray(eo._EHYD_CM, dtype=np.float64)
+    out["conth"] = np.asarray(metal_wing_tables().conth, dtype=np.float64)
+    path = OUT.parent / "hydrogen_tables.npz"
+    np.savez_compressed(path, **out)
+    print(f"wrote {path}")
 
 
 # Level tables of the explicit partition-function sums of PFSAHA
