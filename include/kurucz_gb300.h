@@ -78,6 +78,8 @@ typedef struct {
     const double *cont_abs_coeff;   /* [L, n_edge-1, 3] log10 coefficients */
     const double *cont_scat_coeff;  /* [L, n_edge-1, 3] */
     int32_t coeff_log10;            /* 1: coefficients are log10 (always in practice) */
+    const double *turbulent_velocity; /* [L] cm/s (the H Doppler width of hydrogen lines; may be
+                                         NULL when the lines hold no hydrogen line) */
 } ks_atmos;
 
 /* The log-lambda grid, device pointer. */
@@ -104,6 +106,14 @@ typedef struct {
     const uint8_t *process_mask;    /* 1 = TRANSP processes it (line_opacity.py:740-765) */
     const uint8_t *asynth_mask;     /* 1 = centre added to ASYNTH (line_opacity.py:1094) */
     int32_t sorted_by_wavelength;   /* 1 if wavelength is non-decreasing */
+    /* hydrogen lines (line types -1/-2 of neutral H), added with the HPROF4
+     * profile (synthe_py/engine/opacity.py:1706): their rows, in catalog
+     * order, and their principal quantum numbers (device; n_hydrogen = 0 for
+     * none; at most 256) */
+    int32_t n_hydrogen;
+    const int32_t *hydrogen_rows;
+    const int32_t *hydrogen_n_lower;
+    const int32_t *hydrogen_n_upper;
 } ks_lines;
 
 typedef struct {
@@ -163,6 +173,22 @@ ks_status ks_check_flags(void *stream, int32_t *flags_out);
  * (synthe_py/physics/josh_tables.py:6,120,177).  Once per process. */
 ks_status ks_init_tables(const double *tabvi, const double *tabh1, int32_t n_tab,
                          const double *xtau, const double *ch, const double *coefj);
+
+/* The hydrogen line profile tables (host memory, the package's
+ * data/hydrogen_tables.npz): the Stark-profile corrections PROPBM [7*5*15],
+ * C and D [5*7], PP [5], BETA [15], the fine-structure components STALPH and
+ * STWTAL [34], STCOMP and STCPWT [5*4], ISTAL, LNGHAL and LNCOMP [4], the
+ * Lyman cutoff tables [111] and [91], ASUMLYMAN [100], ASUM [96], Y1WTM
+ * [2*2] and XKNMTB [4*3] (synthe_py/physics/profiles/hydrogen.py:23-1405),
+ * the level energies EHYD [8] (synthe_py/engine/opacity.py:49) and the
+ * continuum edges CONTH [15] (synthe_py/physics/tables.py:152), all
+ * row-major.  Once per process, before a synthesis with hydrogen lines. */
+typedef struct {
+    const double *propbm, *c, *d, *pp, *beta, *stalph, *stwtal, *stcomp, *stcpwt;
+    const int32_t *istal, *lnghal, *lncomp;
+    const double *cutoff_h2_plus, *cutoff_h2, *asum_lyman, *asum, *y1wtm, *xknmtb, *ehyd, *conth;
+} ks_hydrogen_tables;
+ks_status ks_init_hydrogen_tables(const ks_hydrogen_tables *tables);
 
 /* Host copies of the derived tables (2001-point H0/H1/H2, 1001-point
  * EXTAB/EXTABF of tables.py:14-42), for verification.  Any pointer may be

@@ -1,6 +1,6 @@
 """Build of the native library ``_lib/libkurucz_gb300.so`` (sm_103a only).
 
-Seven translation units compiled in parallel with nvcc and linked into one
+Eight translation units compiled in parallel with nvcc and linked into one
 shared library exporting the C ABI of ``include/kurucz_gb300.h``:
 
 * ``ks_f32.cu``  kernels in single precision (mixed path), ``--fmad=false``
@@ -9,6 +9,7 @@ shared library exporting the C ABI of ``include/kurucz_gb300.h``:
 * ``ks_f64_batch.cu`` their batched launches
 * ``ks_api.cu``  C ABI, tables, bins, reach-class partition, drivers
 * ``ks_pops.cu`` FP64 populations (molecular equilibrium, Saha, Doppler), ``--fmad=false``
+* ``ks_hydrogen.cu`` hydrogen line opacity (HPROF4 profiles, FP64), ``--fmad=false``
 * ``ks_gfall.cpp`` native gfall reader
 """
 
@@ -50,6 +51,7 @@ def _units():
         (CSRC / "ks_api.cu", common),
         # FP64 populations: products and sums rounded one by one, as the reference's
         (CSRC / "ks_pops.cu", common + ["--fmad=false"]),
+        (CSRC / "ks_hydrogen.cu", common + ["--fmad=false"]),
         (CSRC / "ks_gfall.cpp", ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread"]),
     ]
 

@@ -20,11 +20,14 @@ _lib: Optional[C.CDLL] = None
 _lock = threading.Lock()
 TABLES_NPZ = Path(__file__).resolve().parent / "data" / "synthe_tables.npz"
 POPS_TABLES_NPZ = Path(__file__).resolve().parent / "data" / "pops_tables.npz"
+HYDROGEN_TABLES_NPZ = Path(__file__).resolve().parent / "data" / "hydrogen_tables.npz"
 # level tables of the explicit partition-function sums, in the library's order
 POPS_LEVEL_TABLES = ("hyd", "he1", "he2", "c1", "c2", "o1", "mg1", "mg2", "al1", "si1", "si2", "na1",
                      "b1", "k1")
 
 KS_OK = 0
+KS_ERR_INVALID = 1
+KS_ERR_UNSUPPORTED = 6
 KS_PREC_MIXED = 0
 KS_PREC_FP64 = 1
 
@@ -51,6 +54,7 @@ class KsAtmos(C.Structure):
         ("n_edge", C.c_int32),
         ("cont_abs_coeff", P), ("cont_scat_coeff", P),
         ("coeff_log10", C.c_int32),
+        ("turbulent_velocity", P),
     ]
 
 
@@ -66,6 +70,8 @@ class KsLines(C.Structure):
         ("element_idx", P), ("ion_stage", P), ("line_type", P),
         ("process_mask", P), ("asynth_mask", P),
         ("sorted_by_wavelength", C.c_int32),
+        ("n_hydrogen", C.c_int32),
+        ("hydrogen_rows", P), ("hydrogen_n_lower", P), ("hydrogen_n_upper", P),
     ]
 
 
@@ -104,6 +110,18 @@ class KsStats(C.Structure):
         d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "stage_ms"}
         d["stage_ms"] = {n: float(v) for n, v in zip(self.STAGES, self.stage_ms) if n != "unused"}
         return d
+
+
+class KsHydrogenTables(C.Structure):
+    """ks_hydrogen_tables: host pointers to the hydrogen line profile tables."""
+
+    _fields_ = [(k, P) for k in (
+        "propbm", "c", "d", "pp", "beta", "stalph", "stwtal", "stcomp", "stcpwt",
+        "istal", "lnghal", "lncomp",
+        "cutoff_h2_plus", "cutoff_h2", "asum_lyman", "asum", "y1wtm", "xknmtb", "ehyd", "conth")]
+
+
+HYDROGEN_INT_TABLES = ("istal", "lnghal", "lncomp")
 
 
 class KsPopsTables(C.Structure):
@@ -192,6 +210,7 @@ SIGNATURES = {
     "ks_synthesize_batch": (C.c_int32, [C.POINTER(KsLines), C.POINTER(KsJob), C.c_int32,
                                         C.POINTER(KsOptions), P, C.c_size_t, C.POINTER(KsStats), P]),
     "ks_init_pops_tables": (C.c_int32, [C.POINTER(KsPopsTables)]),
+    "ks_init_hydrogen_tables": (C.c_int32, [C.POINTER(KsHydrogenTables)]),
     "ks_pops_system": (C.c_int32, [P, P, P, P]),
     "ks_populations_workspace_size": (C.c_int32, [C.POINTER(KsPopsModel), C.c_int32, C.POINTER(C.c_size_t)]),
     "ks_populations": (C.c_int32, [C.POINTER(KsPopsModel), C.c_int32, P, C.c_size_t, P]),
@@ -242,6 +261,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         if st != KS_OK:
             raise KsError(st, L.ks_last_error().decode())
         _init_pops_tables(L)
+        _init_hydrogen_tables(L)
         _lib = L
         return _lib
 
@@ -271,6 +291,19 @@ def _init_pops_tables(L: C.CDLL) -> None:
     t.n_pfg_label = keep["pfg_label"].size
     t.n_mol = keep["mol_code"].size
     st = L.ks_init_pops_tables(C.byref(t))
+    if st != KS_OK:
+        raise KsError(st, L.ks_last_error().decode())
+
+
+def _init_hydrogen_tables(L: C.CDLL) -> None:
+    """Hand the hydrogen profile tables (``data/hydrogen_tables.npz``) to ``ks_init_hydrogen_tables``."""
+    with np.load(HYDROGEN_TABLES_NPZ) as t:
+        keep = {k: np.ascontiguousarray(t[k], dtype=np.int32 if k in HYDROGEN_INT_TABLES else np.float64)
+                for k, _ in KsHydrogenTables._fields_}
+    t = KsHydrogenTables()
+    for k, v in keep.items():
+        setattr(t, k, v.ctypes.data)
+    st = L.ks_init_hydrogen_tables(C.byref(t))
     if st != KS_OK:
         raise KsError(st, L.ks_last_error().decode())
 

@@ -43,7 +43,7 @@ ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(co
 
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
-    if (minor) *minor = 0;
+    if (minor) *minor = 1;
     return KS_OK;
 }
 
@@ -614,9 +614,15 @@ struct Workspace {
     float* coef_f;   // continuum coefficient tables in FP32: absorption, then scattering
     float* freq_f;   // c / lambda per grid point in FP32
     int* flags;
+    HydPar* hyd_par;  // hydrogen lines: per (line, depth) state and walk limits
+    int2* hyd_walk;
+    int hyd_cap;
     int64_t stride;
     int nchunks;
 };
+
+// Hydrogen lines a synthesis takes (their scratch is part of every workspace).
+static const int kMaxHydrogenLines = 256;
 
 static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl, int n_ion,
                    int n_elem, bool fp64, bool need_cont, bool need_asynth, int tile_bins = 0) {
@@ -648,6 +654,9 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.coef_f = c.take<float>(2 * (size_t)L * (MAX_EDGES - 1) * 3);
     w.freq_f = c.take<float>(n_wl > 0 ? n_wl : 1);
     w.flags = c.take<int>(1);
+    w.hyd_cap = (int)std::max<int64_t>(1, std::min<int64_t>(n_lines, kMaxHydrogenLines));
+    w.hyd_par = c.take<HydPar>((size_t)w.hyd_cap * L);
+    w.hyd_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
 }
 
 extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_t n_wavelengths,
@@ -705,6 +714,12 @@ static ks_status check_lines(const ks_lines* l) {
     if (!l->sorted_by_wavelength)
         return fail(KS_ERR_INVALID, "lines must be sorted by wavelength (sorted_by_wavelength = 1)");
     if (l->n_lines > 0x7fffffffLL) return fail(KS_ERR_UNSUPPORTED, "more than 2^31 lines");
+    if (l->n_hydrogen < 0 || l->n_hydrogen > l->n_lines)
+        return fail(KS_ERR_INVALID, "n_hydrogen must lie in [0, n_lines]");
+    if (l->n_hydrogen > kMaxHydrogenLines)
+        return fail(KS_ERR_UNSUPPORTED, "more than 256 hydrogen lines");
+    if (l->n_hydrogen > 0 && (!l->hydrogen_rows || !l->hydrogen_n_lower || !l->hydrogen_n_upper))
+        return fail(KS_ERR_INVALID, "lines: a hydrogen column is NULL");
     return KS_OK;
 }
 
@@ -1153,6 +1168,58 @@ static int fused_launches(bool has_lines, bool fp64, const ks_options* opt, bool
     return 5 + (has_lines ? 6 : 0) + (with_transfer ? (stream_pass ? 2 : 1) : 0);
 }
 
+// Hydrogen lines (HPROF4 profiles) onto the line opacity cube, after the
+// accumulation of the catalog's other lines (synthe_py/engine/opacity.py:2465-2503:
+// with RHOXJ = 0 the transfer's line opacity is ASYNTH + AHLINE).
+template <typename R>
+static ks_status run_hydrogen(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                              const ks_options* opt, const Workspace& w, const DevTables& t, const R* cabs,
+                              const R* cscat, R* cube, cudaStream_t s) {
+    if (!atm->turbulent_velocity)
+        return fail(KS_ERR_INVALID, "hydrogen lines need ks_atmos.turbulent_velocity");
+    if (lines->n_hydrogen > w.hyd_cap) return fail(KS_ERR_INVALID, "hydrogen lines exceed the workspace");
+    const HydTables* tab = nullptr;
+    ks_status st = hydrogen_device_tables(&tab);
+    if (st) return st;
+    HydArgs h;
+    h.n_h = lines->n_hydrogen;
+    h.n_layers = atm->n_layers;
+    h.n_ion = atm->n_ion;
+    h.n_elem = atm->n_elem;
+    h.n_wl = grid->n;
+    h.rows = lines->hydrogen_rows;
+    h.n_lower = lines->hydrogen_n_lower;
+    h.n_upper = lines->hydrogen_n_upper;
+    h.wavelength = lines->wavelength;
+    h.gf = lines->gf;
+    h.elo = lines->elo_cm;
+    h.center = w.center;
+    h.grid = grid->wavelength;
+    h.temperature = atm->temperature;
+    h.xne = atm->electron_density;
+    h.rho = atm->mass_density;
+    h.hckt = atm->hckt;
+    h.vturb = atm->turbulent_velocity;
+    h.xnf_he1 = atm->xnf_he1;
+    h.xnf_h2 = atm->xnf_h2;
+    h.population = atm->population;
+    h.doppler = atm->doppler;
+    h.cutoff = opt ? opt->cutoff : 1e-3;
+    h.microturb_kms = opt ? opt->microturb_kms : 0.0;
+    h.cabs = cabs;
+    h.cscat = cscat;
+    h.extab = t.extab;
+    h.extabf = t.extabf;
+    h.tab = tab;
+    h.par = w.hyd_par;
+    h.walk = w.hyd_walk;
+    cudaError_t e;
+    if constexpr (sizeof(R) == 8) e = launch_hydrogen_f64(h, cube, s);
+    else e = launch_hydrogen_f32(h, cube, s);
+    if (e != cudaSuccess) return fail(KS_ERR_CUDA, std::string("hydrogen lines: ") + cudaGetErrorString(e));
+    return KS_OK;
+}
+
 template <typename R>
 static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
                                  const ks_options* opt, Workspace& w, const DevTables& t,
@@ -1215,6 +1282,9 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f64(a, warps, (const PairDesc<double>*)w.desc, asynth, s));
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
+    if (lines->n_hydrogen > 0 &&
+        (st = run_hydrogen<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
+        return st;
     tm.mark();
     if (do_transfer) {
         if ((st = run_transfer<R>(atm, grid, opt, w, t, cabs, cscat, asynth, flux_total, flux_cont, s)))
@@ -1391,6 +1461,8 @@ static ks_status adjoint_impl(const ks_lines* lines, const ks_atmos* atm, const 
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: options with precision KS_PREC_FP64 are required");
     if (opt->rhoxj > 0.0 || opt->microturb_kms > 0.0)
         return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: line scattering and microturbulence are not covered");
+    if (lines->n_hydrogen > 0)
+        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: hydrogen lines are not covered");
     if (!g_flux_total || !flux_total || !flux_cont || !d_log_gf || !d_log_gamma_rad || !d_log_gamma_stark ||
         !d_log_gamma_vdw)
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: NULL input/output");
@@ -1743,6 +1815,8 @@ size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 ks_status batch_check(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
     ks_status st = check_lines(lines);
     if (st) return st;
+    if (lines->n_hydrogen > 0)
+        return fail(KS_ERR_UNSUPPORTED, "ks_batch: hydrogen lines are taken by ks_synthesize only");
     if (n_jobs <= 0 || !jobs) return fail(KS_ERR_INVALID, "ks_batch: no jobs");
     if ((st = check_tiling(opt))) return st;
     if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))

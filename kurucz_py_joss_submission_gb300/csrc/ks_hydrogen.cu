@@ -1,0 +1,681 @@
+// ks_hydrogen.cu -- hydrogen line opacity (FP64), added to the line opacity
+// after the accumulation of the plain lines.
+//
+// The reference computes the opacity of the catalog's hydrogen lines (line
+// types -1/-2, neutral H) apart from ASYNTH, with Kurucz's HPROF4 profile
+// (synthe_py/physics/profiles/hydrogen.py:1541), and adds it to the line
+// opacity before the transfer (synthe_py/engine/opacity.py:1706-1884,
+// :2465-2503).  Per (line, depth) it walks the grid outward from the line
+// centre, red and blue, until the profile falls below the continuum cutoff or
+// a cut of the neighbouring series members ends the wing (:1547-1703).
+//
+// Three kernels, all FP64 with every product and sum rounded separately:
+//   hyd_setup_kernel   one thread per (line, depth): the TRANSP-style gates,
+//                      kappa0, the merge and tail wavelengths, the line's
+//                      series-neighbour wavelengths and the hydrogen depth
+//                      state (synthe_py/physics/populations.py:93-125);
+//   hyd_march_kernel   one warp per (line, depth, side): the walk, 32 offsets
+//                      at a time, each lane evaluating one offset; a ballot
+//                      finds where the walk ends;
+//   hyd_gather_kernel  one thread per (depth, grid point): the contributions
+//                      of the lines whose walks cover the point, recomputed
+//                      and summed in catalog order (the order of the
+//                      reference's buffer), then added to the line opacity.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "ks_common.cuh"
+#include "ks_launch.h"
+
+namespace ks {
+namespace {
+
+constexpr double kRydH = 3.2880515e15;
+constexpr double kClightA = 2.99792458e18;   // Angstrom/s
+constexpr double kClightCm = 2.99792458e10;
+constexpr double kClightNm = 2.99792458e17;
+constexpr double kClightKms = 299792.458;
+constexpr double kLyAlphaWn = 82259.10;
+constexpr double kHydRyd = 109677.576;
+constexpr double kHydEinf = 109678.764;
+constexpr double kCgf = 0.026538 / 1.77245;
+constexpr double kKboltz = 1.380649e-16;
+constexpr double kAmu = 1.66054e-24;
+constexpr double kHPlanck = 6.62607015e-27;
+constexpr double kPi = 3.141592653589793;
+
+__device__ __forceinline__ double fastex(double x, const double* extab, const double* extabf) {
+    if (x <= 0.0) return x == 0.0 ? 1.0 : exp(-x);
+    const double fl = floor(x);
+    if (fl >= (double)EXP_N) return exp(-x);
+    const int i = (int)fl;
+    int j = (int)((x - (double)i) * 1000.0 + 0.5);
+    j = j < 0 ? 0 : (j > EXP_N - 1 ? EXP_N - 1 : j);
+    return extab[i] * extabf[j];
+}
+
+__device__ double vcse1f(double x, const double* extab, const double* extabf) {
+    if (x <= 0) return 0.0;
+    if (x <= 0.01) return -log(x) - 0.577215 + x;
+    if (x <= 1.0)
+        return -log(x) - 0.57721566 +
+               x * (0.99999193 + x * (-0.24991055 + x * (0.05519968 + x * (-0.00976004 + x * 0.00107857))));
+    if (x > 30.0) return 0.0;
+    return (x * (x + 2.334733) + 0.25062) / ((x * (x + 3.330657) + 1.681534) * x) * fastex(x, extab, extabf);
+}
+
+__device__ double sofbeta(double beta, double p, int n, int m, const HydTables& T) {
+    double corr = 1.0;
+    const double b2 = beta * beta;
+    const double sb = sqrt(beta);
+    if (beta <= 500.0) {
+        int indx = 7;
+        const int mmn = m - n;
+        if (n <= 3 && mmn <= 2) indx = 2 * (n - 1) + mmn;
+        indx = indx < 1 ? 1 : (indx > 7 ? 7 : indx);
+        int im = (int)(5.0 * p) + 1;
+        im = im > 4 ? 4 : im;
+        im = im < 1 ? 1 : im;
+        const int ip = im + 1;
+        double wtp = 5.0 * (p - T.pp[im - 1]);
+        wtp = wtp < 0.0 ? 0.0 : (wtp > 1.0 ? 1.0 : wtp);
+        const double wtm = 1.0 - wtp;
+        if (beta <= 25.12) {
+            // searchsorted(beta grid, beta, side="right")
+            int j = 0;
+            while (j < 15 && T.beta[j] <= beta) j++;
+            j = j < 1 ? 1 : (j > 14 ? 14 : j);
+            const int jm = j - 1, jp = j;
+            const double denom = T.beta[jp] - T.beta[jm];
+            const double wtb = denom <= 0 ? 0.0 : (beta - T.beta[jm]) / denom;
+            const double wtbm = 1.0 - wtb;
+            const double* prop = T.propbm + (indx - 1) * 5 * 15;
+            const double cbp = prop[(ip - 1) * 15 + jp] * wtp + prop[(im - 1) * 15 + jp] * wtm;
+            const double cbm = prop[(ip - 1) * 15 + jm] * wtp + prop[(im - 1) * 15 + jm] * wtm;
+            corr = 1.0 + cbp * wtb + cbm * wtbm;
+            double pr1 = 0.0, pr2 = 0.0;
+            double wt = 0.5 * (10.0 - beta);
+            wt = wt > 1.0 ? 1.0 : wt;
+            wt = wt < 0.0 ? 0.0 : wt;
+            if (beta <= 10.0) pr1 = 8.0 / (83.0 + (2.0 + 0.95 * b2) * beta);
+            if (beta >= 8.0) pr2 = (1.5 / sb + 27.0 / b2) / b2;
+            return (pr1 * wt + pr2 * (1.0 - wt)) * corr;
+        }
+        const double cc = T.c[(im - 1) * 7 + indx - 1] * wtp + T.c[(ip - 1) * 7 + indx - 1] * wtm;
+        const double dd = T.d[(im - 1) * 7 + indx - 1] * wtp + T.d[(ip - 1) * 7 + indx - 1] * wtm;
+        corr = 1.0 + dd / (cc + beta * sb);
+    }
+    return (1.5 / sb + 27.0 / b2) / b2 * corr;
+}
+
+__device__ double hf_nm(int n, int m) {
+    if (m <= n) return 0.0;
+    const double xn = (double)n;
+    const double ginf = 0.2027 / pow(xn, 0.71);
+    const double gca = 0.124 / xn;
+    const double fkn = xn * 1.9603;
+    const double wtc = 0.45 - 2.4 / pow(xn, 3.0) * (xn - 1.0);
+    const double xm = (double)m;
+    const double xmn = xm - xn;
+    const double fk = fkn * pow(xm / (xmn * (xm + xn)), 3.0);
+    const double xmn12 = pow(xmn, 1.2);
+    const double wt = (xmn12 - 1.0) / (xmn12 + wtc);
+    return fk * (1.0 - wt * ginf - (0.222 + gca / xm) * (1.0 - wt));
+}
+
+__device__ double interp_cutoff(double dwn, const double* tab, int n, double start, double step, bool* ok) {
+    *ok = true;
+    if (dwn > start + step * (double)(n - 1)) {
+        *ok = false;
+        return 0.0;
+    }
+    if (dwn <= start) return tab[0] + (tab[1] - tab[0]) * ((dwn - start) / step);
+    const double pos = (dwn - start) / step;
+    const int i = (int)floor(pos);
+    const double frac = pos - (double)i;
+    if (i >= n - 1) return tab[n - 1];
+    return tab[i] + (tab[i + 1] - tab[i]) * frac;
+}
+
+// HPROF4 (profiles/hydrogen.py:1541-1710) for the transition n -> m at
+// wavelength offset dlam_nm from the line centre, in the depth state q.
+__device__ double hprof4(int n, int m, const HydPar& q, double dlam_nm, const HydTables& T, const double* extab,
+                         const double* extabf) {
+    const int mmn = m - n;
+    const double xn = (double)n, xm = (double)m;
+    const double xn2 = xn * xn, xm2 = xm * xm;
+    const double xm2mn2 = xm2 - xn2;
+    const double xmn2 = xm2 * xn2;
+    const double gnm = xm2mn2 / xmn2;
+    if (mmn <= 0) return 0.0;
+    double xknm;
+    if (mmn <= 3 && n <= 4) xknm = T.xknmtb[(n - 1) * 3 + mmn - 1];
+    else xknm = 5.5e-5 / gnm * xmn2 / (1.0 + 0.13 / (double)mmn);
+    const double freqnm = kRydH * gnm;
+    const double wavenm = kClightA / freqnm;
+    const double dbeta = kClightA / (freqnm * freqnm * xknm);
+    const double c1con = xknm / wavenm * gnm * xm2mn2;
+    const double c2con = pow(xknm / wavenm, 2.0);
+    double radamp = T.asum[n - 1] + T.asum[m - 1];
+    if (n == 1) radamp = T.asum_lyman[m - 1];
+    radamp /= 12.5664;
+    radamp /= freqnm;
+    double resont = hf_nm(1, m) / xm / (1.0 - 1.0 / xm2);
+    if (n != 1) resont += hf_nm(1, n) / xn / (1.0 - 1.0 / xn2);
+    resont *= 3.579e-24 / gnm;
+    const double vdw = 4.45e-26 / gnm * pow(xm2 * (7.0 * xm2 + 5.0), 0.4);
+    const double hwvdw = vdw * q.t3nhe + 2.0 * vdw * q.t3nh2;
+    const double hwrad = radamp;
+    const double stark = 1.6678e-18 * freqnm * xknm;
+    const double hwres = resont * q.xnfph0 * 2.0;
+    const double hwstk = stark * q.fo;
+    const double hwlor = hwres + hwvdw + hwrad;
+    const double wl = wavenm + dlam_nm * 10.0;
+    const double freq = kClightA / wl;
+    const double del_freq = fabs(freq - freqnm);
+    const double dph = fmax(q.dopph, 1e-40);
+    const double dop = freqnm * dph;
+    const double hfwidth = freqnm * fmax(fmax(dph, hwlor), hwstk);
+    const bool ifcore = del_freq <= hfwidth;
+    int nwid = 1;
+    if (!(dph >= hwstk && dph >= hwlor)) {
+        nwid = 2;
+        if (hwlor < hwstk) nwid = 3;
+    }
+    // Doppler core over the fine-structure components (profiles/hydrogen.py:1516)
+    double core = 0.0;
+    {
+        const double dopc = fmax(dop, 1e-30);
+        if (n > 4 || m > 10) {
+            const double d = fabs(freq - (freqnm + 0.0)) / dopc;
+            if (d <= 7.0) core += fastex(d * d, extab, extabf) * 1.0;
+        } else if (mmn != 1) {
+            const int k = T.lncomp[n - 1];
+            for (int i = 0; i < k; i++) {
+                const double off = T.stcomp[i * 4 + n - 1] * 1.0e7;
+                const double w = T.stcpwt[i * 4 + n - 1] / xn2;
+                const double d = fabs(freq - (freqnm + off)) / dopc;
+                if (d <= 7.0) core += fastex(d * d, extab, extabf) * w;
+            }
+        } else {
+            const int k = T.lnghal[n - 1], i0 = T.istal[n - 1];
+            for (int i = 0; i < k; i++) {
+                const double off = T.stalph[i0 + i] * 1.0e7;
+                const double w = T.stwtal[i0 + i] / xn2 / 3.0;
+                const double d = fabs(freq - (freqnm + off)) / dopc;
+                if (d <= 7.0) core += fastex(d * d, extab, extabf) * w;
+            }
+        }
+    }
+    double lorentz = 0.0;
+    const double hhw = freqnm * hwlor;
+    if (n == 1 && m == 2) {
+        // Lyman alpha (profiles/hydrogen.py:1731-1797)
+        if (dop > 0.0) {
+            const double hwres_near = hwres * 4.0;
+            const double hwlor_near = hwres_near + hwvdw + hwrad;
+            const double hhw_near = freqnm * fmax(hwlor_near, 0.0);
+            const double dwn = freq / kClightCm - kLyAlphaWn;
+            double hres, hhw_use;
+            if (freq > (kLyAlphaWn - 4000.0) * kClightCm && hhw_near > 0.0) {
+                hres = hwres_near * freqnm / kPi / (del_freq * del_freq + hhw_near * hhw_near) * 1.77245 * dop;
+                hhw_use = hhw_near;
+            } else {
+                double cut = 0.0;
+                bool ok;
+                const double lg = interp_cutoff(dwn, T.cutoff_h2, 91, -22000.0, 200.0, &ok);
+                if (ok) cut = pow(10.0, lg - 14.0) * q.xnfph0 * 2.0 / kClightCm;
+                hres = cut * 1.77245 * dop;
+                hhw_use = freqnm * fmax(hwres + hwvdw + hwrad, 0.0);
+            }
+            double hrad = 0.0, hvdw = 0.0;
+            if (hwrad > 0.0 && hhw_use > 0.0 && freq > 2.4190611e15 && freq < 0.77 * kRydH)
+                hrad = hwrad * freqnm / kPi / (del_freq * del_freq + hhw_use * hhw_use) * 1.77245 * dop;
+            if (hwvdw > 0.0 && hhw_use > 0.0 && freq >= 1.8e15)
+                hvdw = hwvdw * freqnm / kPi / (del_freq * del_freq + hhw_use * hhw_use) * 1.77245 * dop;
+            lorentz = hres + hrad + hvdw;
+        }
+    } else {
+        double top = hhw;
+        if (n == 1 && (m == 3 || m == 4 || m == 5)) {
+            const double fr = freq / kRydH;
+            if ((m == 3 && 0.885 <= fr && fr <= 0.890) || (m == 4 && 0.936 <= fr && fr <= 0.938) ||
+                (m == 5 && 0.959 <= fr && fr <= 0.961))
+                top = fmax(hhw - freqnm * hwrad, 0.0);
+        }
+        if (hhw > 0.0) lorentz = top / kPi / (del_freq * del_freq + hhw * hhw) * 1.77245 * dop;
+    }
+    const double y1num = m == 2 ? 550.0 : (m == 3 ? 380.0 : 320.0);
+    double y1wht = mmn <= 3 ? 1.0e14 : 1.0e13;
+    if (mmn <= 2 && n <= 2) y1wht = T.y1wtm[(n - 1) * 2 + mmn - 1];
+    const double wty1 = 1.0 / (1.0 + fmax(q.xne, 0.0) / fmax(y1wht, 1e-30));
+    const double y1_scal = y1num * q.y1s * wty1 + q.y1b * (1.0 - wty1);
+    const double c1 = q.c1d * c1con * y1_scal;
+    const double c2 = q.c2d * c2con;
+    const double beta = del_freq / fmax(q.fo, 1e-30) * dbeta;
+    const double y1 = c1 * beta;
+    const double y2 = c2 * beta * beta;
+    const double g1 = 6.77 * sqrt(fmax(c1, 1e-30));
+    const double ratio = (c1 > 0.0 && c2 > 0.0) ? sqrt(c2) / fmax(c1, 1e-30) : 0.0;
+    const double log_term = ratio > 0.0 ? log(fmax(ratio, 1e-30)) : 0.0;
+    double gamma = g1 * fmax(0.0, 0.2114 + log_term) * (1.0 - q.gcon1 - q.gcon2);
+    if (y2 > 1e-4 && y1 > 1e-5)
+        gamma = g1 *
+                (0.5 * fastex(fmin(80.0, y1), extab, extabf) + vcse1f(y1, extab, extabf) -
+                 0.5 * vcse1f(y2, extab, extabf)) *
+                (1.0 - q.gcon1 / (1.0 + pow(90.0 * y1, 3.0)) - q.gcon2 / (1.0 + 2000.0 * y1));
+    const double f = gamma > 0 ? gamma / kPi / (gamma * gamma + beta * beta) : 0.0;
+    double prqs = sofbeta(beta, q.pp, n, m, T);
+    double extra = 0.0;
+    if (m <= 2) {
+        prqs *= 0.5;
+        // quasi-static cutoff (profiles/hydrogen.py:1800-1841)
+        if (q.fo > 0.0) {
+            const double dwn = freq / kClightCm - kLyAlphaWn;
+            if (!(dwn < -20000.0)) {
+                if (dwn <= -4000.0) {
+                    bool ok;
+                    const double lg = interp_cutoff(dwn, T.cutoff_h2_plus, 111, -15000.0, 100.0, &ok);
+                    if (ok) extra += pow(10.0, lg - 14.0) * q.xnfph1 / kClightCm * 1.77245 * dop;
+                } else {
+                    const double beta4000 = 4000.0 * kClightCm / fmax(q.fo, 1e-30) * dbeta;
+                    const double prqs4000 = sofbeta(beta4000, q.pp, n, m, T) * 0.5;
+                    const double norm = prqs4000 / fmax(q.fo, 1e-30) * dbeta;
+                    const double cut4000 = pow(10.0, -11.07 - 14.0) * q.xnfph1 / kClightCm;
+                    if (norm > 0.0) extra += cut4000 / norm * (prqs / fmax(q.fo, 1e-30) * dbeta) * 1.77245 * dop;
+                }
+            }
+        }
+    }
+    const double p1 = pow(0.9 * y1, 2.0);
+    const double fns = (p1 + 0.03 * sqrt(fmax(y1, 0.0))) / (p1 + 1.0);
+    const double stark_core = (prqs * (1.0 + fns) + f) / fmax(q.fo, 1e-30) * dbeta * 1.77245 * dop;
+    if (ifcore) {
+        if (nwid == 1) return fmax(core, 0.0);
+        if (nwid == 2) return fmax(lorentz, 0.0);
+        return fmax(stark_core + extra, 0.0);
+    }
+    return fmax(core + lorentz + stark_core + extra, 0.0);
+}
+
+__device__ __forceinline__ double ehyd(int n, const HydTables& T) {
+    return (n >= 1 && n <= 8) ? T.ehyd[n - 1] : kHydEinf - kHydRyd / (double)(n * n);
+}
+
+template <typename R>
+__device__ __forceinline__ double abtot(const HydArgs& a, int d, int64_t b) {
+    const int64_t i = (int64_t)d * a.n_wl + b;
+    return (double)((const R*)a.cabs)[i] + (double)((const R*)a.cscat)[i];
+}
+
+__device__ __forceinline__ double stim_at(const HydArgs& a, const HydPar& q, int64_t b) {
+    const double freq = kClightCm / (a.grid[b] * 1e-7);
+    return 1.0 - exp(-freq * q.hkt);
+}
+
+// Value the walk adds at grid point b on `side` (+1 red, -1 blue) or at the
+// centre (side 0); *stop = true where the reference's walk ends there,
+// *add = false where it passes the point without adding (red, below WCON).
+template <typename R>
+__device__ double walk_value(const HydArgs& a, const HydPar& q, int64_t b, int side, bool* stop, bool* add) {
+    const HydTables& T = *a.tab;
+    const double w = a.grid[b];
+    const bool simple = q.nu <= q.nl + 2;
+    const bool taper = !simple && (q.wtail > q.wcon);
+    const double stim = stim_at(a, q, b);
+    const double cut = abtot<R>(a, q.d, b) * a.cutoff;
+    *stop = false;
+    *add = true;
+    if (side == 0) {
+        if (!simple && w < q.wcon) {
+            *add = false;
+            return 0.0;
+        }
+        double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+        if (taper && w < q.wtail) v *= (w - q.wcon) / (q.wtail - q.wcon);
+        if (!(v >= cut)) *add = false;
+        return v;
+    }
+    if (side > 0) {
+        if (!simple) {
+            if (w > q.wlm1) {
+                *stop = true;
+                return 0.0;
+            }
+            if (w < q.wcon) {
+                *add = false;
+                return 0.0;
+            }
+            double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+            if (taper && w < q.wtail) v *= (w - q.wcon) / (q.wtail - q.wcon);
+            if (w > q.redcut) {
+                const int um2 = q.nu - 2 > q.nl + 1 ? q.nu - 2 : q.nl + 1;
+                double v2 = q.kappa0 * hprof4(q.nl, um2, q, w - q.wlm2, T, a.extab, a.extabf) * stim;
+                if (taper && w < q.wtail) v2 *= (w - q.wcon) / (q.wtail - q.wcon);
+                if (v2 >= v) {
+                    *stop = true;
+                    return 0.0;
+                }
+            }
+            if (v <= 0.0 || v < cut) *stop = true;
+            return v;
+        }
+        const double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+        if (v <= 0.0 || v < cut) *stop = true;
+        return v;
+    }
+    if (!simple && (w < q.wcon || w < q.wlp1)) {
+        *stop = true;
+        return 0.0;
+    }
+    double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+    if (!simple) {
+        if (taper && w < q.wtail) v *= (w - q.wcon) / (q.wtail - q.wcon);
+        if (w < q.bluecut) {
+            double v2 = q.kappa0 * hprof4(q.nl, q.nu + 2, q, w - q.wlp2, T, a.extab, a.extabf) * stim;
+            if (taper && w < q.wtail) v2 *= (w - q.wcon) / (q.wtail - q.wcon);
+            if (v2 >= v) {
+                *stop = true;
+                return 0.0;
+            }
+        }
+    }
+    if (v <= 0.0 || v < cut) *stop = true;
+    return v;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) hyd_setup_kernel(HydArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_h * a.n_layers) return;
+    const int h = (int)(i / a.n_layers), d = (int)(i - (int64_t)h * a.n_layers);
+    const HydTables& T = *a.tab;
+    HydPar q;
+    q.active = 0;
+    q.d = d;
+    const int row = a.rows[h];
+    q.wl0 = a.wavelength[row];
+    q.ci = a.center[row];
+    const int nl = a.n_lower[h], nu = a.n_upper[h];
+    q.nl = nl > 1 ? nl : 1;
+    q.nu = nu > nl + 1 ? nu : nl + 1;
+    // depth state (populations.py:93-125, :183-216)
+    const double temp = fmax(a.temperature[d], 1.0);
+    const double xne_raw = a.xne[d];
+    const double xne = fmax(xne_raw, 1e-40);
+    const double xne16 = pow(xne, 1.0 / 6.0);
+    q.pp = xne16 * 0.08989 / sqrt(fmax(temp, 1.0));
+    q.fo = pow(xne16, 4.0) * 1.25e-9;
+    q.y1b = 2.0 / (1.0 + 0.012 / fmax(temp, 1.0) * sqrt(xne / fmax(temp, 1.0)));
+    const double t4 = temp / 10000.0;
+    const double t43 = pow(t4, 0.3);
+    q.y1s = t43 / xne16;
+    const double he1 = a.xnf_he1 ? a.xnf_he1[d] : 0.0;
+    const double h2 = a.xnf_h2 ? a.xnf_h2[d] : 0.0;
+    q.t3nhe = t43 * he1;
+    q.t3nh2 = t43 * h2;
+    q.c1d = q.fo * 78940.0 / fmax(temp, 1.0);
+    q.c2d = pow(q.fo, 2.0) / 5.96e-23 / xne;
+    q.gcon1 = 0.2 + 0.09 * sqrt(fmax(t4, 1e-12)) / (1.0 + xne / 1.0e13);
+    q.gcon2 = 0.2 / (1.0 + xne / 1.0e15);
+    const int64_t per = (int64_t)a.n_ion * a.n_elem;
+    q.xnfph0 = a.population[(int64_t)d * per + 0 * a.n_elem + 0];
+    q.xnfph1 = a.population[(int64_t)d * per + 1 * a.n_elem + 0];
+    {
+        const double vt = (a.vturb[d] / 1e5) / kClightKms;
+        const double micro = a.microturb_kms > 0 ? a.microturb_kms / kClightKms : 0.0;
+        const double total = sqrt(vt * vt + micro * micro);
+        const double thermal = sqrt(2.0 * kKboltz * temp / (1.008 * kAmu)) / kClightCm;
+        q.dopph = sqrt(thermal * thermal + total * total);
+    }
+    q.xne = xne_raw;
+    q.hkt = kHPlanck / (kKboltz * a.temperature[d]);
+    // the line's series neighbours and cuts (engine/opacity.py:1780-1815)
+    const int ncon = nl < 1 ? 1 : (nl > 15 ? 15 : nl);
+    const double conth = T.conth[ncon - 1];
+    const double elo = ehyd(nl, T);
+    q.wlm1 = nu - 1 > nl ? 1.0e7 / (ehyd(nu - 1, T) - elo) : q.wl0;
+    q.wlm2 = nu - 2 > nl ? 1.0e7 / (ehyd(nu - 2, T) - elo) : q.wl0;
+    q.wlp1 = 1.0e7 / (ehyd(nu + 1, T) - elo);
+    q.wlp2 = 1.0e7 / (ehyd(nu + 2, T) - elo);
+    q.redcut = 1.0e7 / (T.conth[0] - kHydRyd / pow((double)nu - 0.8, 2.0) - elo);
+    q.bluecut = 1.0e7 / (T.conth[0] - kHydRyd / pow((double)nu + 0.8, 2.0) - elo);
+    // gates (engine/opacity.py:1817-1845)
+    const double pv = q.xnfph0;
+    double dv = a.doppler[(int64_t)d * per + 0 * a.n_elem + 0];
+    const double micro = a.microturb_kms > 0.0 ? a.microturb_kms / kClightKms : 0.0;
+    if (micro > 0.0) dv = sqrt(dv * dv + micro * micro);
+    const double rho = a.rho[d];
+    q.kappa0 = 0.0;
+    if (pv > 0.0 && dv > 0.0 && rho > 0.0) {
+        const double cgf = kCgf * a.gf[row] / (kClightNm / q.wl0);
+        const double k0pre = cgf * (pv / (rho * dv));
+        const int64_t cc = q.ci < 0 ? 0 : (q.ci > a.n_wl - 1 ? a.n_wl - 1 : q.ci);
+        const double kapmin = abtot<R>(a, d, cc) * a.cutoff;
+        if (k0pre >= kapmin) {
+            const double k0 = k0pre * fastex(a.elo[row] * a.hckt[d], a.extab, a.extabf);
+            if (k0 >= kapmin) {
+                q.kappa0 = k0;
+                q.active = 1;
+            }
+        }
+    }
+    // merge and tail wavelengths (engine/opacity.py:1755-1757, :1846-1858)
+    double inglis = 1600.0 / pow(xne, 2.0 / 15.0);
+    double nmerge = fmax(inglis - 1.5, 1.0);
+    const double emerge = kHydRyd / fmax(nmerge * nmerge, 1e-12);
+    const double wshift = 1.0e7 / (conth - kHydRyd / (81.0 * 81.0));
+    double wmerge = 1.0e7 / (conth - emerge);
+    if (wmerge < 0.0) wmerge = wshift + wshift;
+    double wcon = fmax(wshift, wmerge);
+    double wtail = wcon > 0.0 ? 1.0e7 / (1.0e7 / wcon - 500.0) : wcon + wcon;
+    wcon = fmin(wshift + wshift, wcon);
+    if (wtail < 0.0) wtail = wcon + wcon;
+    wtail = fmin(wcon + wcon, wtail);
+    q.wcon = wcon;
+    q.wtail = wtail;
+    a.par[i] = q;
+}
+
+// One warp per (line, depth, side): the walk's first and end offsets.
+template <typename R>
+__global__ void __launch_bounds__(128) hyd_march_kernel(HydArgs a) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= (int64_t)a.n_h * a.n_layers * 2) return;
+    const int64_t pd = gw >> 1;
+    const int side = (gw & 1) ? -1 : 1;
+    const HydPar q = a.par[pd];
+    int2 out = make_int2(1, 1);  // walk offsets [x, y)
+    if (q.active) {
+        const int64_t n = a.n_wl;
+        const int64_t ci = q.ci;
+        int64_t first = 1;
+        bool alive = true;
+        if (ci >= n) {
+            if (side > 0) alive = false;
+            first = ci - (n - 1) > 1 ? ci - (n - 1) : 1;
+        } else if (ci < 0) {
+            if (side < 0) alive = false;
+            first = -ci > 1 ? -ci : 1;
+        }
+        const int64_t max_steps = ci > n - ci - 1 ? ci : n - ci - 1;
+        int64_t end = first;
+        if (alive) {
+            for (int64_t o0 = first; o0 <= max_steps; o0 += 32) {
+                const int64_t o = o0 + lane;
+                bool stop = false;
+                if (o <= max_steps) {
+                    const int64_t b = ci + side * o;
+                    if (b < 0 || b >= n) {
+                        stop = true;
+                    } else {
+                        bool add;
+                        walk_value<R>(a, q, b, side, &stop, &add);
+                    }
+                } else {
+                    stop = true;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, stop);
+                if (m) {
+                    end = o0 + (__ffs(m) - 1);
+                    break;
+                }
+                end = o0 + 32;
+            }
+        }
+        out = make_int2((int)first, (int)end);
+    }
+    if (lane == 0) a.walk[gw] = out;
+}
+
+// One thread per (depth, grid point): every line whose walk covers the point
+// adds its value, in catalog order; the sum goes onto the line opacity.
+template <typename R>
+__global__ void __launch_bounds__(256) hyd_gather_kernel(HydArgs a, R* __restrict__ cube) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_layers * a.n_wl) return;
+    const int d = (int)(i / a.n_wl);
+    const int64_t b = i - (int64_t)d * a.n_wl;
+    double acc = 0.0;
+    bool any = false;
+    for (int h = 0; h < a.n_h; h++) {
+        const int64_t pd = (int64_t)h * a.n_layers + d;
+        if (!a.par[pd].active) continue;
+        const int64_t ci = a.par[pd].ci;
+        int side;
+        int64_t o;
+        if (b == ci) {
+            side = 0;
+            o = 0;
+        } else if (b > ci) {
+            side = 1;
+            o = b - ci;
+        } else {
+            side = -1;
+            o = ci - b;
+        }
+        if (side != 0) {
+            const int2 wk = a.walk[pd * 2 + (side > 0 ? 0 : 1)];
+            if (o < wk.x || o >= wk.y) continue;
+        }
+        const HydPar q = a.par[pd];
+        bool stop, add;
+        const double v = walk_value<R>(a, q, b, side, &stop, &add);
+        if (!add) continue;
+        acc += v;
+        any = true;
+    }
+    if (any) cube[i] = (R)((double)cube[i] + acc);
+}
+
+}  // namespace
+
+template <typename R>
+static cudaError_t launch_hydrogen_t(const HydArgs& a, R* cube, cudaStream_t s) {
+    if (a.n_h <= 0) return cudaSuccess;
+    const int64_t nhd = (int64_t)a.n_h * a.n_layers;
+    hyd_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    hyd_march_kernel<R><<<(unsigned)((nhd * 2 * 32 + 127) / 128), 128, 0, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t cells = (int64_t)a.n_layers * a.n_wl;
+    if (cells > 0) hyd_gather_kernel<R><<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(a, cube);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hydrogen_f32(const HydArgs& a, float* cube, cudaStream_t s) {
+    return launch_hydrogen_t<float>(a, cube, s);
+}
+cudaError_t launch_hydrogen_f64(const HydArgs& a, double* cube, cudaStream_t s) {
+    return launch_hydrogen_t<double>(a, cube, s);
+}
+
+}  // namespace ks
+
+// ---------------------------------------------------------------------------
+// tables: host copy (ks_init_hydrogen_tables), device copy per device
+// ---------------------------------------------------------------------------
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+namespace {
+__device__ ks::HydTables g_hyd;
+ks::HydTables g_hyd_host;
+bool g_hyd_ready = false;
+bool g_hyd_dev[64];
+std::mutex g_hyd_mu;
+
+template <typename T>
+void copy_n(T* dst, const T* src, size_t n) {
+    std::memcpy(dst, src, sizeof(T) * n);
+}
+}  // namespace
+
+extern "C" ks_status ks_init_hydrogen_tables(const ks_hydrogen_tables* t) {
+    if (!t || !t->propbm || !t->c || !t->d || !t->pp || !t->beta || !t->stalph || !t->stwtal || !t->stcomp ||
+        !t->stcpwt || !t->istal || !t->lnghal || !t->lncomp || !t->cutoff_h2_plus || !t->cutoff_h2 ||
+        !t->asum_lyman || !t->asum || !t->y1wtm || !t->xknmtb || !t->ehyd || !t->conth)
+        return ks::set_error(KS_ERR_INVALID, "ks_init_hydrogen_tables: null table pointer");
+    ks::HydTables h;
+    copy_n(h.propbm, t->propbm, 7 * 5 * 15);
+    copy_n(h.c, t->c, 5 * 7);
+    copy_n(h.d, t->d, 5 * 7);
+    copy_n(h.pp, t->pp, 5);
+    copy_n(h.beta, t->beta, 15);
+    copy_n(h.stalph, t->stalph, 34);
+    copy_n(h.stwtal, t->stwtal, 34);
+    copy_n(h.stcomp, t->stcomp, 5 * 4);
+    copy_n(h.stcpwt, t->stcpwt, 5 * 4);
+    for (int i = 0; i < 4; i++) {
+        h.istal[i] = t->istal[i];
+        h.lnghal[i] = t->lnghal[i];
+        h.lncomp[i] = t->lncomp[i];
+        if (h.lncomp[i] < 0 || h.lncomp[i] > 5 || h.lnghal[i] < 0 || h.istal[i] < 0 || h.istal[i] > 34)
+            return ks::set_error(KS_ERR_INVALID, "ks_init_hydrogen_tables: fine-structure table out of range");
+        // the reference slices STALPH[ISTAL : ISTAL + LNGHAL] with its 1-based
+        // ISTAL as a 0-based start (profiles/hydrogen.py:1529-1532); a slice
+        // past the 34 entries ends at the last one
+        if (h.istal[i] + h.lnghal[i] > 34) h.lnghal[i] = 34 - h.istal[i];
+    }
+    copy_n(h.cutoff_h2_plus, t->cutoff_h2_plus, 111);
+    copy_n(h.cutoff_h2, t->cutoff_h2, 91);
+    copy_n(h.asum_lyman, t->asum_lyman, 100);
+    copy_n(h.asum, t->asum, 96);
+    copy_n(h.y1wtm, t->y1wtm, 4);
+    copy_n(h.xknmtb, t->xknmtb, 12);
+    copy_n(h.ehyd, t->ehyd, 8);
+    copy_n(h.conth, t->conth, 15);
+    std::lock_guard<std::mutex> lk(g_hyd_mu);
+    g_hyd_host = h;
+    g_hyd_ready = true;
+    for (bool& r : g_hyd_dev) r = false;
+    return KS_OK;
+}
+
+ks_status ks::hydrogen_device_tables(const ks::HydTables** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return ks::set_error(KS_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) return ks::set_error(KS_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_hyd_mu);
+    if (!g_hyd_ready)
+        return ks::set_error(KS_ERR_INVALID, "hydrogen lines given but the hydrogen tables are not initialised "
+                                             "(ks_init_hydrogen_tables)");
+    if (!g_hyd_dev[dev]) {
+        e = cudaMemcpyToSymbol(g_hyd, &g_hyd_host, sizeof(ks::HydTables));
+        if (e != cudaSuccess)
+            return ks::set_error(KS_ERR_CUDA, std::string("hydrogen tables: ") + cudaGetErrorString(e));
+        g_hyd_dev[dev] = true;
+    }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_hyd);
+    if (e != cudaSuccess) return ks::set_error(KS_ERR_CUDA, std::string("hydrogen tables: ") + cudaGetErrorString(e));
+    *out = (const ks::HydTables*)p;
+    return KS_OK;
+}

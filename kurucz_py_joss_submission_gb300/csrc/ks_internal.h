@@ -191,6 +191,39 @@ struct AtmGradArgs {
     double *d_ln_rho, *d_xne, *d_txnxn;  // [L] out
 };
 
+// Hydrogen line profile tables (HPROF4, synthe_py/physics/profiles/hydrogen.py),
+// resident on the device.
+struct HydTables {
+    double propbm[7 * 5 * 15], c[5 * 7], d[5 * 7], pp[5], beta[15];
+    double stalph[34], stwtal[34], stcomp[5 * 4], stcpwt[5 * 4];
+    int istal[4], lnghal[4], lncomp[4];
+    double cutoff_h2_plus[111], cutoff_h2[91], asum_lyman[100], asum[96], y1wtm[2 * 2], xknmtb[4 * 3];
+    double ehyd[8], conth[15];
+};
+
+// One (hydrogen line, depth): gates, walk limits and the hydrogen depth state.
+struct HydPar {
+    double wl0, kappa0, wcon, wtail, wlm1, wlm2, wlp1, wlp2, redcut, bluecut;
+    double pp, fo, y1b, y1s, t3nhe, t3nh2, c1d, c2d, gcon1, gcon2, xnfph0, xnfph1, dopph, xne, hkt;
+    int ci, nl, nu, d, active;
+};
+
+struct HydArgs {
+    int n_h, n_layers, n_ion, n_elem;
+    int64_t n_wl;
+    const int32_t *rows, *n_lower, *n_upper;  // per hydrogen line: catalog row, NBLO, NBUP
+    const double *wavelength, *gf, *elo;      // catalog columns
+    const int32_t* center;                    // centre bins of every catalog row
+    const double* grid;
+    const double *temperature, *xne, *rho, *hckt, *vturb, *xnf_he1, *xnf_h2, *population, *doppler;
+    double cutoff, microturb_kms;
+    const void *cabs, *cscat;                 // continuum cubes (the precision's type)
+    const double *extab, *extabf;             // FASTEX tables
+    const HydTables* tab;
+    HydPar* par;                              // [n_h, L]
+    int2* walk;                               // [n_h, L, 2] walk offsets [x, y), red then blue
+};
+
 // ---- batched launches -------------------------------------------------------
 //
 // A batch runs every stage once over all its jobs: the launch walks a job

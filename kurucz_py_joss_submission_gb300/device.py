@@ -78,11 +78,12 @@ class DeviceAtmosphere:
         put("delta_edge", atm.continuum_delta_edge)
         put("cont_abs_coeff", atm.continuum_abs_coeff)
         put("cont_scat_coeff", atm.continuum_scat_coeff)
+        put("turbulent_velocity", atm.turbulent_velocity)
         rec = _native.KsAtmos()
         rec.n_layers = L
         for name in ("rhox", "temperature", "electron_density", "mass_density", "hckt", "xnf_h",
                      "xnf_he1", "xnf_h2", "population", "doppler", "wledge", "half_edge",
-                     "delta_edge", "cont_abs_coeff", "cont_scat_coeff"):
+                     "delta_edge", "cont_abs_coeff", "cont_scat_coeff", "turbulent_velocity"):
             t = self.t.get(name)
             setattr(rec, name, t.data_ptr() if t is not None else None)
         rec.n_ion = int(pop.shape[1])
@@ -151,6 +152,28 @@ class DeviceCatalog:
         rec.process_mask = self.t["process_mask"].data_ptr()
         rec.asynth_mask = self.t["asynth_mask"].data_ptr()
         rec.sorted_by_wavelength = 1
+        # hydrogen lines (line types -1/-2, neutral H; engine/opacity.py:1773-1778):
+        # their device rows listed in catalog order, the order the reference
+        # adds their profiles in
+        lt = np.asarray(cat.line_types)
+        hyd = np.flatnonzero(((lt == -1) | (lt == -2)) & (np.asarray(cat.ion_stages) == 1))
+        self.n_hydrogen = int(hyd.size)
+        if self.n_hydrogen > 256:
+            raise ValueError(f"{self.n_hydrogen} hydrogen lines: the synthesis takes at most 256")
+        if self.n_hydrogen:
+            if self.order is None:
+                rows = hyd
+            else:
+                inv = np.empty_like(self.order)
+                inv[self.order] = np.arange(self.order.size)
+                rows = inv[hyd]
+            self.t["hydrogen_rows"] = _dev(rows, np.int32, dev)
+            self.t["hydrogen_n_lower"] = _dev(np.asarray(cat.n_lower)[hyd], np.int32, dev)
+            self.t["hydrogen_n_upper"] = _dev(np.asarray(cat.n_upper)[hyd], np.int32, dev)
+            rec.n_hydrogen = self.n_hydrogen
+            rec.hydrogen_rows = self.t["hydrogen_rows"].data_ptr()
+            rec.hydrogen_n_lower = self.t["hydrogen_n_lower"].data_ptr()
+            rec.hydrogen_n_upper = self.t["hydrogen_n_upper"].data_ptr()
         self.rec = rec
 
     def to_catalog_order(self, per_line: np.ndarray) -> np.ndarray:

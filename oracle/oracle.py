@@ -211,7 +211,8 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
                wl_end: float, resolution: float = 300000.0, cutoff: float = 1e-3,
                microturb: float = 0.0, rhoxj: float = 0.0, tb=None,
                timings: Optional[Dict[str, float]] = None) -> Dict[str, np.ndarray]:
-    """Whole plain-line LTE synthesis on the CPU.  ``cat`` must already be
+    """Whole LTE synthesis on the CPU: plain lines, and the hydrogen lines'
+    HPROF4 profiles when the catalog holds any.  ``cat`` must already be
     window-filtered (``gfall.filter_window``)."""
     from . import gfall
 
@@ -232,6 +233,19 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
     fscat = np.exp(-rhox / rhoxj) if rhoxj > 0.0 else np.zeros_like(rhox)
     line_op = asy * (1.0 - fscat[:, None])
     line_sc = asy * fscat[:, None]
+    extra = {}
+    lt = np.asarray(cat["line_type"])
+    if np.any(((lt == -1) | (lt == -2)) & (np.asarray(cat["ion_stage"]) == 1)):
+        # hydrogen lines: AHLINE added to the line opacity
+        # (synthe_py/engine/opacity.py:2465-2503)
+        from . import hydrogen
+        hc = dict(wavelength=cat["wavelength"], gf=10.0 ** cat["log_gf"], elo=cat["excitation_energy"],
+                  n_lower=cat["n_lower"], n_upper=cat["n_upper"], line_type=lt,
+                  ion_stage=cat["ion_stage"], center=cidx)
+        ah = hydrogen.line_opacity(hc, atm, grid, kapmin, cutoff=cutoff, microturb_kms=microturb)
+        line_op = line_op + ah * (1.0 - fscat[:, None])
+        line_sc = (asy + ah) * fscat[:, None]
+        extra = dict(ahline=ah, line_opacity=line_op)
     src = line_source(atm, grid)
     ft, fc, iters = transfer(atm, grid, ca, cs, line_op, line_sc, src, tb)
     t4 = time.perf_counter()
@@ -242,7 +256,7 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
         wavelength=grid, center_indices=cidx, wing_indices=widx, cont_abs=ca, cont_scat=cs,
         transp=tr, valid_mask=valid, asynth=asy, evals_per_depth=evals, reach=reach,
         flux_total_hz=ft, flux_cont_hz=fc, flux_total=ft * conv, flux_cont=fc * conv,
-        iterations=iters,
+        iterations=iters, **extra,
     )
 
 

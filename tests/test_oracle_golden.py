@@ -47,6 +47,10 @@ def test_oracle_against_reference(name, tb):
         rows = g["asynth_rows"]
         assert rel(r["asynth"][rows], g["asynth"]) < 1e-12
         assert rel(r["cont_abs"][rows], g["cont_abs_rows"]) < 1e-13
+    if "line_opacity" in g:
+        # hydrogen lines: ASYNTH + AHLINE (bit for bit on the golden ASYNTH
+        # and continuum, test_hydrogen_oracle.py; here on the oracle's own)
+        assert rel(r["line_opacity"], g["line_opacity"]) < 1e-12
     assert rel(r["flux_total_hz"], g["flux_total_hz"]) < 1e-12
     assert rel(r["flux_cont_hz"], g["flux_cont_hz"]) < 1e-12
 
