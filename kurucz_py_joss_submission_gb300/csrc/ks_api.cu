@@ -319,6 +319,8 @@ static ks_status sink_flags(const int* flags, cudaStream_t s) {
 
 static ks_status flags_status(int flags) {
     if (flags & 8) return fail(KS_ERR_DEVICE, "wing bins are not monotone in the line order");
+    if (flags & FLAG_HYDROGEN_LINE)
+        return fail(KS_ERR_DEVICE, "a hydrogen line's row lies outside the catalog or its upper level above 94");
     if (flags & FLAG_N10DOP_RANGE)
         return fail(KS_ERR_DEVICE, "a pair exceeded a packed descriptor field (N10DOP or centre offset)");
     if (flags) return fail(KS_ERR_DEVICE, "a kernel raised device flag " + std::to_string(flags));
@@ -1177,6 +1179,8 @@ static ks_status run_hydrogen(const ks_lines* lines, const ks_atmos* atm, const 
                               const R* cscat, R* cube, cudaStream_t s) {
     if (!atm->turbulent_velocity)
         return fail(KS_ERR_INVALID, "hydrogen lines need ks_atmos.turbulent_velocity");
+    if (atm->n_ion < 2 || atm->n_elem < 1)
+        return fail(KS_ERR_INVALID, "hydrogen lines need the H I and H II populations (n_ion >= 2)");
     if (lines->n_hydrogen > w.hyd_cap) return fail(KS_ERR_INVALID, "hydrogen lines exceed the workspace");
     const HydTables* tab = nullptr;
     ks_status st = hydrogen_device_tables(&tab);
@@ -1187,6 +1191,8 @@ static ks_status run_hydrogen(const ks_lines* lines, const ks_atmos* atm, const 
     h.n_ion = atm->n_ion;
     h.n_elem = atm->n_elem;
     h.n_wl = grid->n;
+    h.n_lines = lines->n_lines;
+    h.flags = w.flags;
     h.rows = lines->hydrogen_rows;
     h.n_lower = lines->hydrogen_n_lower;
     h.n_upper = lines->hydrogen_n_upper;

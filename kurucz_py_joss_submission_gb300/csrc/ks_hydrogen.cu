@@ -395,11 +395,22 @@ __global__ void __launch_bounds__(128) hyd_setup_kernel(HydArgs a) {
     q.active = 0;
     q.d = d;
     const int row = a.rows[h];
-    q.wl0 = a.wavelength[row];
-    q.ci = a.center[row];
     const int nl = a.n_lower[h], nu = a.n_upper[h];
     q.nl = nl > 1 ? nl : 1;
     q.nu = nu > nl + 1 ? nu : nl + 1;
+    // the profile reads ASUM at the upper level and at two levels above it
+    // (96 entries): a line outside those, or a row outside the catalog, is
+    // flagged and left out
+    if (row < 0 || (int64_t)row >= a.n_lines || q.nu + 2 > 96) {
+        if (d == 0) atomicOr(a.flags, FLAG_HYDROGEN_LINE);
+        q.nl = 1;
+        q.nu = 2;
+        q.ci = 0;
+        a.par[i] = q;
+        return;
+    }
+    q.wl0 = a.wavelength[row];
+    q.ci = a.center[row];
     // depth state (populations.py:93-125, :183-216)
     const double temp = fmax(a.temperature[d], 1.0);
     const double xne_raw = a.xne[d];

@@ -210,7 +210,8 @@ struct HydPar {
 
 struct HydArgs {
     int n_h, n_layers, n_ion, n_elem;
-    int64_t n_wl;
+    int64_t n_wl, n_lines;
+    int* flags;                               // FLAG_HYDROGEN_LINE
     const int32_t *rows, *n_lower, *n_upper;  // per hydrogen line: catalog row, NBLO, NBUP
     const double *wavelength, *gf, *elo;      // catalog columns
     const int32_t* center;                    // centre bins of every catalog row

@@ -161,6 +161,11 @@ class DeviceCatalog:
         if self.n_hydrogen > 256:
             raise ValueError(f"{self.n_hydrogen} hydrogen lines: the synthesis takes at most 256")
         if self.n_hydrogen:
+            lo = np.asarray(cat.n_lower)[hyd]
+            up = np.maximum(np.asarray(cat.n_upper)[hyd], lo + 1)
+            if np.any(up + 2 > 96):
+                raise ValueError("hydrogen line with an upper level above 94: the profile tables "
+                                 "(ASUM) end at level 96")
             if self.order is None:
                 rows = hyd
             else:
