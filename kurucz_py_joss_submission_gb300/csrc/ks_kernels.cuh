@@ -851,8 +851,7 @@ __device__ __forceinline__ void accumulate_kernel_body(VB vb, const AccArgs& a, 
         int64_t nb = 0;
         for (int k = 0; k < N_REACH_CLASSES; k++) {
             bat_base[k] = nb;
-            const int bs = k < a.long_class ? 32 : 8;
-            nb += (cls_n[k] + bs - 1) / bs;
+            nb += k < a.long_class ? (cls_n[k] + 31) >> 5 : (cls_n[k] + 7) >> 3;
         }
         bat_base[N_REACH_CLASSES] = nb;
     }
