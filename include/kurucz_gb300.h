@@ -114,6 +114,13 @@ typedef struct {
     const int32_t *hydrogen_rows;
     const int32_t *hydrogen_n_lower;
     const int32_t *hydrogen_n_upper;
+    /* helium lines (line types -3/-4/-6: He I, 3He I, He II) without fort.19
+     * continuum limits: the helium wing pass (synthe_py/engine/opacity.py:
+     * 2515-3590, Voigt wings of _apply_fort19_profile :996-1061), added to the
+     * line opacity as AHE x STIM (:3650-3660); their rows in catalog order
+     * (device; n_helium = 0 for none; at most 256) */
+    int32_t n_helium;
+    const int32_t *helium_rows;
 } ks_lines;
 
 typedef struct {

@@ -72,6 +72,7 @@ class KsLines(C.Structure):
         ("sorted_by_wavelength", C.c_int32),
         ("n_hydrogen", C.c_int32),
         ("hydrogen_rows", P), ("hydrogen_n_lower", P), ("hydrogen_n_upper", P),
+        ("n_helium", C.c_int32), ("helium_rows", P),
     ]
 
 

@@ -43,7 +43,7 @@ ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(co
 
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
-    if (minor) *minor = 1;
+    if (minor) *minor = 2;
     return KS_OK;
 }
 
@@ -319,6 +319,7 @@ static ks_status sink_flags(const int* flags, cudaStream_t s) {
 
 static ks_status flags_status(int flags) {
     if (flags & 8) return fail(KS_ERR_DEVICE, "wing bins are not monotone in the line order");
+    if (flags & FLAG_HELIUM_LINE) return fail(KS_ERR_DEVICE, "a helium line's row lies outside the catalog");
     if (flags & FLAG_HYDROGEN_LINE)
         return fail(KS_ERR_DEVICE, "a hydrogen line's row lies outside the catalog or its upper level above 94");
     if (flags & FLAG_N10DOP_RANGE)
@@ -619,11 +620,14 @@ struct Workspace {
     HydPar* hyd_par;  // hydrogen lines: per (line, depth) state and walk limits
     int2* hyd_walk;
     int hyd_cap;
+    HePar* he_par;    // helium lines: per (line, depth) wing parameters and walk limits
+    int2* he_walk;
     int64_t stride;
     int nchunks;
 };
 
-// Hydrogen lines a synthesis takes (their scratch is part of every workspace).
+// Hydrogen lines, and helium lines, a synthesis takes (their scratch is part
+// of every workspace).
 static const int kMaxHydrogenLines = 256;
 
 static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl, int n_ion,
@@ -659,6 +663,8 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.hyd_cap = (int)std::max<int64_t>(1, std::min<int64_t>(n_lines, kMaxHydrogenLines));
     w.hyd_par = c.take<HydPar>((size_t)w.hyd_cap * L);
     w.hyd_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
+    w.he_par = c.take<HePar>((size_t)w.hyd_cap * L);
+    w.he_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
 }
 
 extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_t n_wavelengths,
@@ -722,6 +728,10 @@ static ks_status check_lines(const ks_lines* l) {
         return fail(KS_ERR_UNSUPPORTED, "more than 256 hydrogen lines");
     if (l->n_hydrogen > 0 && (!l->hydrogen_rows || !l->hydrogen_n_lower || !l->hydrogen_n_upper))
         return fail(KS_ERR_INVALID, "lines: a hydrogen column is NULL");
+    if (l->n_helium < 0 || l->n_helium > l->n_lines)
+        return fail(KS_ERR_INVALID, "n_helium must lie in [0, n_lines]");
+    if (l->n_helium > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 helium lines");
+    if (l->n_helium > 0 && !l->helium_rows) return fail(KS_ERR_INVALID, "lines: helium_rows is NULL");
     return KS_OK;
 }
 
@@ -1226,6 +1236,55 @@ static ks_status run_hydrogen(const ks_lines* lines, const ks_atmos* atm, const 
     return KS_OK;
 }
 
+// Helium lines: the reference's helium wing pass, AHE x STIM onto the line
+// opacity cube after the hydrogen lines (synthe_py/engine/opacity.py:3650-3660).
+template <typename R>
+static ks_status run_helium(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
+                            const ks_options* opt, const Workspace& w, const DevTables& t, const R* cabs,
+                            const R* cscat, R* cube, cudaStream_t s) {
+    if (atm->n_ion < 2 || atm->n_elem < 2)
+        return fail(KS_ERR_INVALID, "helium lines need the He populations (n_ion >= 2, n_elem >= 2)");
+    if (lines->n_helium > w.hyd_cap) return fail(KS_ERR_INVALID, "helium lines exceed the workspace");
+    HeArgs h;
+    h.n_he = lines->n_helium;
+    h.n_layers = atm->n_layers;
+    h.n_ion = atm->n_ion;
+    h.n_elem = atm->n_elem;
+    h.n_wl = grid->n;
+    h.n_lines = lines->n_lines;
+    h.flags = w.flags;
+    h.rows = lines->helium_rows;
+    h.wavelength = lines->wavelength;
+    h.gf = lines->gf;
+    h.elo = lines->elo_cm;
+    h.gamma_rad = lines->gamma_rad;
+    h.gamma_stark = lines->gamma_stark;
+    h.gamma_vdw = lines->gamma_vdw;
+    h.ion_stage = lines->ion_stage;
+    h.line_type = lines->line_type;
+    h.center = w.center;
+    h.grid = grid->wavelength;
+    h.temperature = atm->temperature;
+    h.population = atm->population;
+    h.doppler = atm->doppler;
+    h.depth = w.depth;
+    h.cutoff = opt ? opt->cutoff : 1e-3;
+    h.cabs = cabs;
+    h.cscat = cscat;
+    h.extab = t.extab;
+    h.extabf = t.extabf;
+    h.h0 = t.h0d;
+    h.h1 = t.h1d;
+    h.h2 = t.h2d;
+    h.par = w.he_par;
+    h.walk = w.he_walk;
+    cudaError_t e;
+    if constexpr (sizeof(R) == 8) e = launch_helium_f64(h, cube, s);
+    else e = launch_helium_f32(h, cube, s);
+    if (e != cudaSuccess) return fail(KS_ERR_CUDA, std::string("helium lines: ") + cudaGetErrorString(e));
+    return KS_OK;
+}
+
 template <typename R>
 static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
                                  const ks_options* opt, Workspace& w, const DevTables& t,
@@ -1290,6 +1349,8 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
     if (lines->n_hydrogen > 0 &&
         (st = run_hydrogen<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
+        return st;
+    if (lines->n_helium > 0 && (st = run_helium<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
         return st;
     tm.mark();
     if (do_transfer) {
@@ -1467,8 +1528,8 @@ static ks_status adjoint_impl(const ks_lines* lines, const ks_atmos* atm, const 
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: options with precision KS_PREC_FP64 are required");
     if (opt->rhoxj > 0.0 || opt->microturb_kms > 0.0)
         return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: line scattering and microturbulence are not covered");
-    if (lines->n_hydrogen > 0)
-        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: hydrogen lines are not covered");
+    if (lines->n_hydrogen > 0 || lines->n_helium > 0)
+        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: hydrogen and helium lines are not covered");
     if (!g_flux_total || !flux_total || !flux_cont || !d_log_gf || !d_log_gamma_rad || !d_log_gamma_stark ||
         !d_log_gamma_vdw)
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: NULL input/output");
@@ -1821,8 +1882,8 @@ size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 ks_status batch_check(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
     ks_status st = check_lines(lines);
     if (st) return st;
-    if (lines->n_hydrogen > 0)
-        return fail(KS_ERR_UNSUPPORTED, "ks_batch: hydrogen lines are taken by ks_synthesize only");
+    if (lines->n_hydrogen > 0 || lines->n_helium > 0)
+        return fail(KS_ERR_UNSUPPORTED, "ks_batch: hydrogen and helium lines are taken by ks_synthesize only");
     if (n_jobs <= 0 || !jobs) return fail(KS_ERR_INVALID, "ks_batch: no jobs");
     if ((st = check_tiling(opt))) return st;
     if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))

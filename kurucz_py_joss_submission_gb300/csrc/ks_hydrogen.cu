@@ -1,5 +1,5 @@
-// ks_hydrogen.cu -- hydrogen line opacity (FP64), added to the line opacity
-// after the accumulation of the plain lines.
+// ks_hydrogen.cu -- hydrogen and helium line opacity (FP64), added to the line
+// opacity after the accumulation of the plain lines.
 //
 // The reference computes the opacity of the catalog's hydrogen lines (line
 // types -1/-2, neutral H) apart from ASYNTH, with Kurucz's HPROF4 profile
@@ -21,6 +21,12 @@
 //                      of the lines whose walks cover the point, recomputed
 //                      and summed in catalog order (the order of the
 //                      reference's buffer), then added to the line opacity.
+//
+// The helium lines (line types -3/-4/-6) get the reference's helium wing pass
+// (synthe_py/engine/opacity.py:2515-3590: per layer and line the TRANSP-style
+// gates, then ``_apply_fort19_profile``'s Voigt walk for TYPE < -2, :966-1061)
+// and enter the line opacity as AHE x STIM (:3650-3660), with the same three
+// kernel shapes (he_setup_kernel, he_march_kernel, he_gather_kernel).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -309,6 +315,12 @@ __device__ __forceinline__ double abtot(const HydArgs& a, int d, int64_t b) {
     return (double)((const R*)a.cabs)[i] + (double)((const R*)a.cscat)[i];
 }
 
+template <typename R>
+__device__ __forceinline__ double abtot_he(const HeArgs& a, int d, int64_t b) {
+    const int64_t i = (int64_t)d * a.n_wl + b;
+    return (double)((const R*)a.cabs)[i] + (double)((const R*)a.cscat)[i];
+}
+
 __device__ __forceinline__ double stim_at(const HydArgs& a, const HydPar& q, int64_t b) {
     const double freq = kClightCm / (a.grid[b] * 1e-7);
     return 1.0 - exp(-freq * q.hkt);
@@ -581,7 +593,176 @@ __global__ void __launch_bounds__(256) hyd_gather_kernel(HydArgs a, R* __restric
     if (any) cube[i] = (R)((double)cube[i] + acc);
 }
 
+// ---------------------------------------------------------------------------
+// helium lines
+// ---------------------------------------------------------------------------
+
+// One thread per (helium line, depth): the gates and wing parameters of
+// process_depth (engine/opacity.py:2686-2910) and _apply_fort19_profile
+// (:996-1016) for a line without fort.19 continuum limits (NCON = 0).
+template <typename R>
+__global__ void __launch_bounds__(128) he_setup_kernel(HeArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_he * a.n_layers) return;
+    const int h = (int)(i / a.n_layers), d = (int)(i - (int64_t)h * a.n_layers);
+    HePar q;
+    q.active = 0;
+    q.d = d;
+    q.ci = 0;
+    q.pad = 0;
+    q.wl0 = q.keff = q.dop = q.adamp = 0.0;
+    const int row = a.rows[h];
+    if (row < 0 || (int64_t)row >= a.n_lines) {
+        if (d == 0) atomicOr(a.flags, FLAG_HELIUM_LINE);
+        a.par[i] = q;
+        return;
+    }
+    const int ci = a.center[row];
+    const int nelion = a.ion_stage[row];
+    // centre outside the grid (:2690-2696); ion stage beyond the table (:2838)
+    if (ci < 0 || (int64_t)ci >= a.n_wl || nelion < 1 || nelion > a.n_ion) {
+        a.par[i] = q;
+        return;
+    }
+    q.ci = ci;
+    const DepthPar& dp = a.depth[d];
+    const int64_t k = ((int64_t)d * a.n_ion + (nelion - 1)) * a.n_elem + 1;  // element He
+    const double pv = a.population[k], dv = a.doppler[k];
+    if (pv <= 0.0 || dv <= 0.0 || !(dp.rho > 0.0)) {
+        a.par[i] = q;
+        return;
+    }
+    const double xnfdop = pv / (dp.rho * dv);
+    const double wl = a.wavelength[row];
+    const double dw = dv * wl;
+    const double boltz = fastex(a.elo[row] * dp.hckt, a.extab, a.extabf);
+    const double cgf = kCgf * a.gf[row] / (kClightNm / wl);
+    const double kmin = abtot_he<R>(a, d, ci) * a.cutoff;
+    const double k0pre = cgf * xnfdop;
+    if (k0pre < kmin || dw <= 0.0) {
+        a.par[i] = q;
+        return;
+    }
+    const double k0 = k0pre * boltz;
+    if (k0 < kmin) {
+        a.par[i] = q;
+        return;
+    }
+    double dop = fmax(dw, 1e-12), keff = k0;
+    if (a.line_type[row] == -4) {  // 3He
+        keff /= 1.155;
+        dop *= 1.155;
+    }
+    const double dn = (a.gamma_rad[row] + a.gamma_stark[row] * dp.xne + a.gamma_vdw[row] * dp.txnxn) /
+                      fmax(dop / wl, 1e-40);
+    q.wl0 = wl;
+    q.keff = keff;
+    q.dop = dop;
+    q.adamp = fmax(dn, 1e-12);
+    q.active = 1;
+    a.par[i] = q;
+}
+
+template <typename R>
+__device__ __forceinline__ double he_value(const HeArgs& a, const HePar& q, int64_t b) {
+    return q.keff * voigt_hv<double>(fabs(a.grid[b] - q.wl0) / q.dop, q.adamp, a.h0, a.h1, a.h2);
+}
+
+// One warp per (helium line, depth, side): the red walk takes offsets
+// 0, 1, ... from the centre bin and ends before the first value below the
+// cutoff; the blue walk takes 1, 2, ... and ends after it (the reference adds
+// that value, then stops).  Stored as offsets [x, y).
+template <typename R>
+__global__ void __launch_bounds__(128) he_march_kernel(HeArgs a) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= (int64_t)a.n_he * a.n_layers * 2) return;
+    const int64_t pd = gw >> 1;
+    const bool red = (gw & 1) == 0;
+    const HePar q = a.par[pd];
+    const int64_t n = a.n_wl;
+    int2 out = make_int2(1, 1);
+    bool alive = q.active != 0;
+    if (alive) {
+        if (red) alive = q.wl0 <= a.grid[n - 1];
+        else alive = q.ci > 0 && q.wl0 >= a.grid[0];
+    }
+    if (alive) {
+        const int64_t first = red ? 0 : 1;
+        const int64_t last = red ? n - 1 - q.ci : q.ci;  // largest offset inside the grid
+        int64_t end = last + 1;
+        for (int64_t o0 = first; o0 <= last; o0 += 32) {
+            const int64_t o = o0 + lane;
+            bool stop = false;
+            if (o <= last) {
+                const int64_t b = red ? q.ci + o : q.ci - o;
+                stop = he_value<R>(a, q, b) < abtot_he<R>(a, q.d, b) * a.cutoff;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, stop);
+            if (m) {
+                const int64_t hit = o0 + (__ffs(m) - 1);
+                end = red ? hit : hit + 1;
+                break;
+            }
+        }
+        out = make_int2((int)first, (int)end);
+    }
+    if (lane == 0) a.walk[gw] = out;
+}
+
+// One thread per (depth, grid point): the wing values of the helium lines
+// whose walks cover the point, summed in catalog order (AHE), times STIM,
+// added to the cube.
+template <typename R>
+__global__ void __launch_bounds__(256) he_gather_kernel(HeArgs a, R* __restrict__ cube) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_layers * a.n_wl) return;
+    const int d = (int)(i / a.n_wl);
+    const int64_t b = i - (int64_t)d * a.n_wl;
+    double acc = 0.0;
+    bool any = false;
+    for (int h = 0; h < a.n_he; h++) {
+        const int64_t pd = (int64_t)h * a.n_layers + d;
+        if (!a.par[pd].active) continue;
+        const int64_t ci = a.par[pd].ci;
+        const bool red = b >= ci;
+        const int64_t o = red ? b - ci : ci - b;
+        const int2 wk = a.walk[pd * 2 + (red ? 0 : 1)];
+        if (o < wk.x || o >= wk.y) continue;
+        const HePar q = a.par[pd];
+        acc += he_value<R>(a, q, b);
+        any = true;
+    }
+    if (any) {
+        const double freq = kClightCm / (a.grid[b] * 1e-7);
+        const double stim = 1.0 - exp(-freq * (kHPlanck / (kKboltz * a.temperature[d])));
+        cube[i] = (R)((double)cube[i] + acc * stim);
+    }
+}
+
 }  // namespace
+
+template <typename R>
+static cudaError_t launch_helium_t(const HeArgs& a, R* cube, cudaStream_t s) {
+    if (a.n_he <= 0) return cudaSuccess;
+    const int64_t nhd = (int64_t)a.n_he * a.n_layers;
+    he_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    he_march_kernel<R><<<(unsigned)((nhd * 2 * 32 + 127) / 128), 128, 0, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t cells = (int64_t)a.n_layers * a.n_wl;
+    if (cells > 0) he_gather_kernel<R><<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(a, cube);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_helium_f32(const HeArgs& a, float* cube, cudaStream_t s) {
+    return launch_helium_t<float>(a, cube, s);
+}
+cudaError_t launch_helium_f64(const HeArgs& a, double* cube, cudaStream_t s) {
+    return launch_helium_t<double>(a, cube, s);
+}
 
 template <typename R>
 static cudaError_t launch_hydrogen_t(const HydArgs& a, R* cube, cudaStream_t s) {

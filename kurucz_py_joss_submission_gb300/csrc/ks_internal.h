@@ -225,6 +225,31 @@ struct HydArgs {
     int2* walk;                               // [n_h, L, 2] walk offsets [x, y), red then blue
 };
 
+// One (helium line, depth) of the helium wing pass: the gated kappa (3He:
+// / 1.155), the Doppler width in nm (3He: x 1.155) and the damping.
+struct HePar {
+    double wl0, keff, dop, adamp;
+    int ci, d, active, pad;
+};
+
+struct HeArgs {
+    int n_he, n_layers, n_ion, n_elem;
+    int64_t n_wl, n_lines;
+    int* flags;                               // FLAG_HELIUM_LINE
+    const int32_t* rows;                      // per helium line: catalog row, in catalog order
+    const double *wavelength, *gf, *elo, *gamma_rad, *gamma_stark, *gamma_vdw;  // catalog columns
+    const int32_t *ion_stage, *line_type, *center;
+    const double* grid;
+    const double *temperature, *population, *doppler;
+    const DepthPar* depth;                    // XNE, TXNXN, HCKT, RHO per layer
+    double cutoff;
+    const void *cabs, *cscat;                 // continuum cubes (the precision's type)
+    const double *extab, *extabf;             // FASTEX tables
+    const double *h0, *h1, *h2;               // Voigt tables (FP64)
+    HePar* par;                               // [n_he, L]
+    int2* walk;                               // [n_he, L, 2] walk offsets [x, y), red then blue
+};
+
 // ---- batched launches -------------------------------------------------------
 //
 // A batch runs every stage once over all its jobs: the launch walks a job

@@ -109,6 +109,13 @@ class DeviceGrid:
         self.rec = rec
 
 
+def inv_order(order: np.ndarray) -> np.ndarray:
+    """Catalog row -> device row, for a device order given as catalog rows."""
+    inv = np.empty_like(order)
+    inv[order] = np.arange(order.size)
+    return inv
+
+
 class DeviceCatalog:
     """A line catalog in HBM, sorted by wavelength (the kernels require it).
 
@@ -166,12 +173,7 @@ class DeviceCatalog:
             if np.any(up + 2 > 96):
                 raise ValueError("hydrogen line with an upper level above 94: the profile tables "
                                  "(ASUM) end at level 96")
-            if self.order is None:
-                rows = hyd
-            else:
-                inv = np.empty_like(self.order)
-                inv[self.order] = np.arange(self.order.size)
-                rows = inv[hyd]
+            rows = hyd if self.order is None else inv_order(self.order)[hyd]
             self.t["hydrogen_rows"] = _dev(rows, np.int32, dev)
             self.t["hydrogen_n_lower"] = _dev(np.asarray(cat.n_lower)[hyd], np.int32, dev)
             self.t["hydrogen_n_upper"] = _dev(np.asarray(cat.n_upper)[hyd], np.int32, dev)
@@ -179,6 +181,16 @@ class DeviceCatalog:
             rec.hydrogen_rows = self.t["hydrogen_rows"].data_ptr()
             rec.hydrogen_n_lower = self.t["hydrogen_n_lower"].data_ptr()
             rec.hydrogen_n_upper = self.t["hydrogen_n_upper"].data_ptr()
+        # helium lines (line types -3/-4/-6; engine/opacity.py:2531-2544): the
+        # helium wing pass, device rows in catalog order
+        he = np.flatnonzero(np.isin(lt, (-3, -4, -6)))
+        self.n_helium = int(he.size)
+        if self.n_helium > 256:
+            raise ValueError(f"{self.n_helium} helium lines: the synthesis takes at most 256")
+        if self.n_helium:
+            self.t["helium_rows"] = _dev(he if self.order is None else inv_order(self.order)[he], np.int32, dev)
+            rec.n_helium = self.n_helium
+            rec.helium_rows = self.t["helium_rows"].data_ptr()
         self.rec = rec
 
     def to_catalog_order(self, per_line: np.ndarray) -> np.ndarray:

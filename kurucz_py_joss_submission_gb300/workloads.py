@@ -251,6 +251,32 @@ def balmer_lines(upper) -> LineDraw:
                     n_lower=np.full(m.size, 2, np.int32), n_upper=m)
 
 
+# Helium lines (vacuum wavelength nm, log gf, lower level cm^-1, gfall CODE):
+# He I 2p 3P - 4d 3D (447.1 nm air), 2p 1P - 5d 1D (438.8), 2p 3P - 5d 3D
+# (402.6), 2p 1P - 4d 1D (492.2), 2s 1S - 3p 1P (501.6) and He II n = 3 - 4
+# (468.6 nm air).
+_HELIUM_LINES = (
+    (447.2735, 0.052, 169086.8, 2.00),
+    (438.9166, -0.883, 171134.9, 2.00),
+    (402.7328, -0.370, 169086.8, 2.00),
+    (492.3304, -0.435, 171134.9, 2.00),
+    (501.7077, -0.820, 166277.4, 2.00),
+    (468.7087, 1.180, 390140.0, 2.01),
+)
+
+
+def helium_lines(w0: float, w1: float) -> LineDraw:
+    """The He I / He II lines of a small table that lie in [w0, w1] nm, as gfall
+    records (CODE 2.00 / 2.01, NBLO = NBUP = 0: line types -3 and -6)."""
+    rows = [r for r in _HELIUM_LINES if w0 <= r[0] <= w1]
+    wl = np.array([r[0] for r in rows], dtype=np.float64)
+    z = np.zeros(wl.size)
+    return LineDraw(wavelength_nm=wl, log_gf=np.array([r[1] for r in rows], dtype=np.float64),
+                    code=np.array([r[3] for r in rows], dtype=np.float64),
+                    e_lower_cm=np.array([r[2] for r in rows], dtype=np.float64),
+                    log_gamma_rad=z + 8.5, log_gamma_stark=z - 4.2, log_gamma_vdw=z - 7.6)
+
+
 def random_atomic_lines(
     n_lines: int,
     wl_min: float,

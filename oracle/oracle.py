@@ -246,6 +246,17 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
         line_op = line_op + ah * (1.0 - fscat[:, None])
         line_sc = (asy + ah) * fscat[:, None]
         extra = dict(ahline=ah, line_opacity=line_op)
+    if np.any(np.isin(lt, (-3, -4, -6))):
+        # helium lines: AHE x STIM added to the line opacity
+        # (synthe_py/engine/opacity.py:3650-3660)
+        from . import helium
+        ec = dict(wavelength=cat["wavelength"], gf=10.0 ** cat["log_gf"], elo=cat["excitation_energy"],
+                  gamma_rad=cat["gamma_rad"], gamma_stark=cat["gamma_stark"], gamma_vdw=cat["gamma_vdw"],
+                  ion_stage=cat["ion_stage"], line_type=lt, center=cidx)
+        he = helium.line_opacity(ec, atm, grid, kapmin, cutoff=cutoff)
+        line_op = line_op + he * (1.0 - fscat[:, None])
+        line_sc = line_sc + he * fscat[:, None]
+        extra = dict(extra, ahe_stim=he, line_opacity=line_op)
     src = line_source(atm, grid)
     ft, fc, iters = transfer(atm, grid, ca, cs, line_op, line_sc, src, tb)
     t4 = time.perf_counter()

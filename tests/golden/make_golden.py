@@ -54,6 +54,7 @@ ATMOSPHERES = {
     "t5800g444": dict(teff=5800.0, logg=4.44, metallicity=0.0),
     "t6000g430": dict(teff=6000.0, logg=4.30, metallicity=0.0),
     "t2500gm10": dict(teff=2500.0, logg=-1.0, metallicity=0.0),
+    "t20000g400": dict(teff=20000.0, logg=4.0, metallicity=0.0),
     # t5800g444 with the Doppler widths of Fe and Ti set so that the Voigt
     # table step TABSTEP = 200 / (DOPPLE * RESOLU) is 0.7 (Fe) and 1.1 (Ti):
     # for such steps the reference's incremental TABI (line_opacity.py:540-548)
@@ -105,6 +106,15 @@ CASES = {
     "hgamma_434": dict(atm="t5800g444", wl_start=433.5, wl_end=434.8,
                        n_lines=150, draw=(433.35, 434.95), log_uniform=False, seed=20,
                        hydrogen=[4, 5, 6]),
+    # helium lines (line types -3 / -6, the helium wing pass of
+    # engine/opacity.py:2515-3590 added as AHE x STIM, :3650-3660) in a
+    # 20,000 K atmosphere: He I 447.1 nm and He II 468.6 nm on metal lines
+    "hei_447": dict(atm="t20000g400", wl_start=446.9, wl_end=447.7,
+                    n_lines=120, draw=(446.75, 447.85), log_uniform=False, seed=21,
+                    helium=True),
+    "heii_468": dict(atm="t20000g400", wl_start=468.3, wl_end=469.1,
+                     n_lines=120, draw=(468.15, 469.25), log_uniform=False, seed=22,
+                     helium=True),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -129,6 +139,8 @@ def case_lines(case: dict) -> workloads.LineDraw:
         lines = workloads.merge_lines(lines, bands)
     if case.get("hydrogen"):
         lines = workloads.merge_lines(lines, workloads.balmer_lines(case["hydrogen"]))
+    if case.get("helium"):
+        lines = workloads.merge_lines(lines, workloads.helium_lines(*case["draw"]))
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth
         # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)
@@ -218,8 +230,9 @@ def run_case(name: str, full_npz: Path, work: Path) -> None:
     )
     transp = np.asarray(s3["transp"])
     asynth = np.asarray(s4["asynth"])
-    if case.get("hydrogen"):
-        # the line opacity the transfer sees: ASYNTH plus the hydrogen profiles
+    if case.get("hydrogen") or case.get("helium"):
+        # the line opacity the transfer sees: ASYNTH plus the hydrogen
+        # profiles and the helium wings
         out["line_opacity"] = np.asarray(s5["line_opacity"])
     if name in LARGE_CASES:
         rng = np.random.default_rng(7)
