@@ -10,6 +10,7 @@ synthesis is one call with no allocation once the plan exists.
 from __future__ import annotations
 
 import ctypes as C
+import warnings
 from dataclasses import dataclass
 from typing import Dict, Optional
 
@@ -127,7 +128,11 @@ class DeviceCatalog:
     COLUMNS_I32 = ("element_idx", "ion_stages", "line_types")
     COLUMNS_U8 = ("process_mask", "asynth_mask")
 
-    def __init__(self, cat: LineCatalog, device="cuda"):
+    def __init__(self, cat: LineCatalog, device="cuda", hydrogen: bool = True, helium: bool = True):
+        """``hydrogen`` / ``helium``: add the hydrogen profiles and the helium
+        wing pass (SynthesisConfig.skip_hydrogen_wings / enable_helium_wings,
+        engine/opacity.py:2465, :2515); without them those lines keep only
+        what TRANSP/ASYNTH give them."""
         dev = _require_cuda(device)
         if cat.is_sorted():
             self.order = None
@@ -163,7 +168,7 @@ class DeviceCatalog:
         # their device rows listed in catalog order, the order the reference
         # adds their profiles in
         lt = np.asarray(cat.line_types)
-        hyd = np.flatnonzero(((lt == -1) | (lt == -2)) & (np.asarray(cat.ion_stages) == 1))
+        hyd = np.flatnonzero(((lt == -1) | (lt == -2)) & (np.asarray(cat.ion_stages) == 1) & hydrogen)
         self.n_hydrogen = int(hyd.size)
         if self.n_hydrogen > 256:
             raise ValueError(f"{self.n_hydrogen} hydrogen lines: the synthesis takes at most 256")
@@ -181,9 +186,20 @@ class DeviceCatalog:
             rec.hydrogen_rows = self.t["hydrogen_rows"].data_ptr()
             rec.hydrogen_n_lower = self.t["hydrogen_n_lower"].data_ptr()
             rec.hydrogen_n_upper = self.t["hydrogen_n_upper"].data_ptr()
+        # lines the reference routes to fort.19 besides hydrogen and helium
+        # (io/lines/fort19.py:343-347: autoionizing TYPE 1, merged-continuum
+        # TYPE > 3, others with NBLO/NBUP) get their special profiles there
+        # (engine/opacity.py:1335 _add_fort19_asynth), which are not computed here
+        nb = np.abs(np.asarray(cat.n_lower)) + np.abs(np.asarray(cat.n_upper))
+        f19 = ((lt == 1) | (lt > 3) | ((nb != 0) & ~np.isin(lt, (-1, -2, -3, -4, -6))))
+        self.n_fort19_skipped = int(np.count_nonzero(f19))
+        if self.n_fort19_skipped:
+            warnings.warn(f"{self.n_fort19_skipped} lines of the fort.19 classes (autoionizing, merged "
+                          "continuum, NBLO/NBUP-tagged metal lines) contribute no opacity here",
+                          RuntimeWarning, stacklevel=2)
         # helium lines (line types -3/-4/-6; engine/opacity.py:2531-2544): the
         # helium wing pass, device rows in catalog order
-        he = np.flatnonzero(np.isin(lt, (-3, -4, -6)))
+        he = np.flatnonzero(np.isin(lt, (-3, -4, -6)) & helium)
         self.n_helium = int(he.size)
         if self.n_helium > 256:
             raise ValueError(f"{self.n_helium} helium lines: the synthesis takes at most 256")

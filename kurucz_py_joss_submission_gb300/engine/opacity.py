@@ -111,7 +111,7 @@ def run_synthesis(cfg: SynthesisConfig) -> SynthResult:
     logger.info("Catalog: %d lines, grid: %d points", len(catalog), wavelength.size)
 
     t = time.perf_counter()
-    dcat = DeviceCatalog(catalog)
+    dcat = DeviceCatalog(catalog, hydrogen=not cfg.skip_hydrogen_wings, helium=cfg.enable_helium_wings)
     datm = DeviceAtmosphere(atm)
     dgrid = DeviceGrid(wavelength, grid_origin=grid_origin)
     opt = make_options(cutoff=cfg.cutoff, microturb_kms=g.velocity_microturb, rhoxj=cfg.rhoxj_scale,
