@@ -121,6 +121,15 @@ typedef struct {
      * (device; n_helium = 0 for none; at most 256) */
     int32_t n_helium;
     const int32_t *helium_rows;
+    /* fort.19 NORMAL lines (NBLO/NBUP set, line type 0, no continuum-merge
+     * limits): the profiles of _add_fort19_asynth (synthe_py/engine/
+     * opacity.py:1335-1488) added to ASYNTH; their rows in catalog order and
+     * the fort.19 record's CGF and damping constants, rounded to single
+     * precision as the record stores them (io/lines/fort19.py:368-402);
+     * device; n_f19 = 0 for none; at most 256 */
+    int32_t n_f19;
+    const int32_t *f19_rows;
+    const double *f19_cgf, *f19_gamma_rad, *f19_gamma_stark, *f19_gamma_vdw;
 } ks_lines;
 
 typedef struct {
@@ -569,6 +578,11 @@ ks_status ks_gfall_fetch(const ks_gfall *g, double *wavelength, double *log_gf, 
  * synthe_py/io/lines/atomic.py:520-532): the principal quantum numbers of
  * hydrogen lines, 0 when blank.  Same order as ks_gfall_fetch. */
 ks_status ks_gfall_fetch_levels(const ks_gfall *g, int32_t *n_lower, int32_t *n_upper);
+/* ISO1 / ISO2 of every record (columns 107-109 and 117-119,
+ * synthe_py/io/lines/atomic.py:344-346, :535-546), 0 when blank; fort.19
+ * takes ISO2 as the continuum index NCON when ISO1 is 0
+ * (io/lines/fort19.py:338).  Same order as ks_gfall_fetch. */
+ks_status ks_gfall_fetch_iso(const ks_gfall *g, int32_t *iso1, int32_t *iso2);
 void ks_gfall_free(ks_gfall *g);
 
 #ifdef __cplusplus

@@ -43,7 +43,7 @@ ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(co
 
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
-    if (minor) *minor = 2;
+    if (minor) *minor = 3;
     return KS_OK;
 }
 
@@ -320,6 +320,8 @@ static ks_status sink_flags(const int* flags, cudaStream_t s) {
 static ks_status flags_status(int flags) {
     if (flags & 8) return fail(KS_ERR_DEVICE, "wing bins are not monotone in the line order");
     if (flags & FLAG_HELIUM_LINE) return fail(KS_ERR_DEVICE, "a helium line's row lies outside the catalog");
+    if (flags & FLAG_F19_LINE)
+        return fail(KS_ERR_DEVICE, "a fort.19 line's row, element or ion lies outside the tables");
     if (flags & FLAG_HYDROGEN_LINE)
         return fail(KS_ERR_DEVICE, "a hydrogen line's row lies outside the catalog or its upper level above 94");
     if (flags & FLAG_N10DOP_RANGE)
@@ -622,6 +624,7 @@ struct Workspace {
     int hyd_cap;
     HePar* he_par;    // helium lines: per (line, depth) wing parameters and walk limits
     int2* he_walk;
+    F19Par* f19_par;  // fort.19 NORMAL lines: per (line, depth) gates and wing
     int64_t stride;
     int nchunks;
 };
@@ -665,6 +668,7 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.hyd_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
     w.he_par = c.take<HePar>((size_t)w.hyd_cap * L);
     w.he_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
+    w.f19_par = c.take<F19Par>((size_t)w.hyd_cap * L);
 }
 
 extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_t n_wavelengths,
@@ -732,6 +736,11 @@ static ks_status check_lines(const ks_lines* l) {
         return fail(KS_ERR_INVALID, "n_helium must lie in [0, n_lines]");
     if (l->n_helium > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 helium lines");
     if (l->n_helium > 0 && !l->helium_rows) return fail(KS_ERR_INVALID, "lines: helium_rows is NULL");
+    if (l->n_f19 < 0 || l->n_f19 > l->n_lines) return fail(KS_ERR_INVALID, "n_f19 must lie in [0, n_lines]");
+    if (l->n_f19 > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 fort.19 lines");
+    if (l->n_f19 > 0 && (!l->f19_rows || !l->f19_cgf || !l->f19_gamma_rad || !l->f19_gamma_stark ||
+                         !l->f19_gamma_vdw))
+        return fail(KS_ERR_INVALID, "lines: a fort.19 column is NULL");
     return KS_OK;
 }
 
@@ -1236,6 +1245,56 @@ static ks_status run_hydrogen(const ks_lines* lines, const ks_atmos* atm, const 
     return KS_OK;
 }
 
+// fort.19 NORMAL lines (NBLO/NBUP set): _add_fort19_asynth's profiles, TMP x
+// STIM onto ASYNTH before the hydrogen lines (synthe_py/engine/opacity.py:
+// 1335-1488, called at :2366).
+template <typename R>
+static ks_status run_f19(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid, const ks_options* opt,
+                         const Workspace& w, const DevTables& t, const R* cabs, const R* cscat, R* cube,
+                         cudaStream_t s) {
+    if (!atm->turbulent_velocity)
+        return fail(KS_ERR_INVALID, "fort.19 lines need ks_atmos.turbulent_velocity");
+    if (lines->n_f19 > w.hyd_cap) return fail(KS_ERR_INVALID, "fort.19 lines exceed the workspace");
+    F19Args f;
+    f.n_f19 = lines->n_f19;
+    f.n_layers = atm->n_layers;
+    f.n_ion = atm->n_ion;
+    f.n_elem = atm->n_elem;
+    f.n_wl = grid->n;
+    f.n_lines = lines->n_lines;
+    f.flags = w.flags;
+    f.rows = lines->f19_rows;
+    f.cgf = lines->f19_cgf;
+    f.gamma_rad = lines->f19_gamma_rad;
+    f.gamma_stark = lines->f19_gamma_stark;
+    f.gamma_vdw = lines->f19_gamma_vdw;
+    f.wavelength = lines->wavelength;
+    f.elo = lines->elo_cm;
+    f.element_idx = lines->element_idx;
+    f.ion_stage = lines->ion_stage;
+    f.center = w.center;
+    f.grid = grid->wavelength;
+    f.temperature = atm->temperature;
+    f.vturb = atm->turbulent_velocity;
+    f.population = atm->population;
+    f.depth = w.depth;
+    f.cutoff = opt ? opt->cutoff : 1e-3;
+    f.microturb_kms = opt ? opt->microturb_kms : 0.0;
+    f.cabs = cabs;
+    f.cscat = cscat;
+    f.extab = t.extab;
+    f.extabf = t.extabf;
+    f.h0 = t.h0d;
+    f.h1 = t.h1d;
+    f.h2 = t.h2d;
+    f.par = w.f19_par;
+    cudaError_t e;
+    if constexpr (sizeof(R) == 8) e = launch_f19_f64(f, cube, s);
+    else e = launch_f19_f32(f, cube, s);
+    if (e != cudaSuccess) return fail(KS_ERR_CUDA, std::string("fort.19 lines: ") + cudaGetErrorString(e));
+    return KS_OK;
+}
+
 // Helium lines: the reference's helium wing pass, AHE x STIM onto the line
 // opacity cube after the hydrogen lines (synthe_py/engine/opacity.py:3650-3660).
 template <typename R>
@@ -1347,6 +1406,8 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f64(a, warps, (const PairDesc<double>*)w.desc, asynth, s));
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
+    if (lines->n_f19 > 0 && (st = run_f19<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
+        return st;
     if (lines->n_hydrogen > 0 &&
         (st = run_hydrogen<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
         return st;
@@ -1528,8 +1589,8 @@ static ks_status adjoint_impl(const ks_lines* lines, const ks_atmos* atm, const 
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: options with precision KS_PREC_FP64 are required");
     if (opt->rhoxj > 0.0 || opt->microturb_kms > 0.0)
         return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: line scattering and microturbulence are not covered");
-    if (lines->n_hydrogen > 0 || lines->n_helium > 0)
-        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: hydrogen and helium lines are not covered");
+    if (lines->n_hydrogen > 0 || lines->n_helium > 0 || lines->n_f19 > 0)
+        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_adjoint: hydrogen, helium and fort.19 lines are not covered");
     if (!g_flux_total || !flux_total || !flux_cont || !d_log_gf || !d_log_gamma_rad || !d_log_gamma_stark ||
         !d_log_gamma_vdw)
         return fail(KS_ERR_INVALID, "ks_synthesize_adjoint: NULL input/output");
@@ -1882,8 +1943,9 @@ size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 ks_status batch_check(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
     ks_status st = check_lines(lines);
     if (st) return st;
-    if (lines->n_hydrogen > 0 || lines->n_helium > 0)
-        return fail(KS_ERR_UNSUPPORTED, "ks_batch: hydrogen and helium lines are taken by ks_synthesize only");
+    if (lines->n_hydrogen > 0 || lines->n_helium > 0 || lines->n_f19 > 0)
+        return fail(KS_ERR_UNSUPPORTED,
+                    "ks_batch: hydrogen, helium and fort.19 lines are taken by ks_synthesize only");
     if (n_jobs <= 0 || !jobs) return fail(KS_ERR_INVALID, "ks_batch: no jobs");
     if ((st = check_tiling(opt))) return st;
     if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))

@@ -40,6 +40,7 @@ constexpr int FLAG_LAYERS = 2;         // more layers than MAX_LAYERS
 constexpr int FLAG_MAXJ_NONCONV = 4;   // informational
 constexpr int FLAG_HYDROGEN_LINE = 16; // a hydrogen line's row or levels outside the tables
 constexpr int FLAG_HELIUM_LINE = 32;   // a helium line's row outside the catalog
+constexpr int FLAG_F19_LINE = 64;      // a fort.19 line's row or ion outside the tables
 
 // Kurucz VOIGT H(a, v) approximation (synthe_py/physics/voigt_jit.py:17-69).
 // Tables are passed as one pointer to interleaved (h0, h1) pairs plus h2.

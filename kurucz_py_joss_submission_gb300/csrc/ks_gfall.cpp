@@ -39,7 +39,7 @@ const double kDellim[7] = {100.0, 30.0, 10.0, 3.0, 1.0, 0.3, 0.1};
 
 struct Rec {
     double wl, loggf, code, elo, gr, gs, gw;
-    int nelem, ion, lt, nblo, nbup, line_size, anum;
+    int nelem, ion, lt, nblo, nbup, line_size, anum, iso1, iso2;
     bool is_h_elem;  // element symbol is H / D (DELLIM special case)
 };
 
@@ -225,6 +225,12 @@ bool parse_fixed(const char* line, int len, const double* potion, int np, Rec* r
         bool e1;
         if (field_int(line, len, 106, 109, &a, &e1) && !e1) iso1 = a;
     }
+    int iso2 = 0;
+    if (len >= 119) {
+        int a;
+        bool e1;
+        if (field_int(line, len, 116, 119, &a, &e1) && !e1) iso2 = a;
+    }
     int line_size = 0;
     std::string tag;
     if (len >= 144) {
@@ -260,6 +266,8 @@ bool parse_fixed(const char* line, int len, const double* potion, int np, Rec* r
     r->nblo = nblo;
     r->nbup = nbup;
     r->line_size = line_size;
+    r->iso1 = iso1;
+    r->iso2 = iso2;
     // element symbol: tfort symbols up to U, else "Z<n>" (unknown to TRANSP)
     r->anum = (nelem > 0 && nelem < kNSym) ? nelem : 0;
     r->is_h_elem = nelem == 1;
@@ -317,6 +325,8 @@ bool parse_ws(const char* line, int len, Rec* r) {
     r->nblo = nlo;
     r->nbup = nup;
     r->line_size = 0;
+    r->iso1 = 0;
+    r->iso2 = 0;
     r->anum = z;
     std::string u;
     for (char ch : el) u += (char)std::toupper((unsigned char)ch);
@@ -457,6 +467,15 @@ extern "C" ks_status ks_gfall_fetch_levels(const ks_gfall* g, int32_t* n_lower, 
     for (size_t k = 0; k < g->recs.size(); k++) {
         if (n_lower) n_lower[k] = g->recs[k].nblo;
         if (n_upper) n_upper[k] = g->recs[k].nbup;
+    }
+    return KS_OK;
+}
+
+extern "C" ks_status ks_gfall_fetch_iso(const ks_gfall* g, int32_t* iso1, int32_t* iso2) {
+    if (!g) return KS_ERR_INVALID;
+    for (size_t k = 0; k < g->recs.size(); k++) {
+        if (iso1) iso1[k] = g->recs[k].iso1;
+        if (iso2) iso2[k] = g->recs[k].iso2;
     }
     return KS_OK;
 }

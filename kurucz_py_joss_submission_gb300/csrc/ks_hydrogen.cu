@@ -740,7 +740,218 @@ __global__ void __launch_bounds__(256) he_gather_kernel(HeArgs a, R* __restrict_
     }
 }
 
+// ---------------------------------------------------------------------------
+// fort.19 NORMAL lines (NBLO/NBUP set, not H/He/autoionizing/coronal/PRD)
+// ---------------------------------------------------------------------------
+
+template <typename R>
+__device__ __forceinline__ double abtot_f19(const F19Args& a, int d, int64_t b) {
+    const int64_t i = (int64_t)d * a.n_wl + b;
+    return (double)((const R*)a.cabs)[i] + (double)((const R*)a.cscat)[i];
+}
+
+// Near-wing profile value at step k (k <= N10DOP): the incremental TABI of
+// opacity.py:151-162 (k additions of TABSTEP to 0.5) or the Voigt function.
+__device__ __forceinline__ double f19_near(const F19Args& a, const F19Par& q, int k) {
+    if (q.adamp < 0.2) {
+        double tabi = 0.5;
+        for (int j = 0; j < k; j++) tabi = tabi + q.tabstep;
+        int it = (int)tabi;
+        it = it < 0 ? 0 : (it > VOIGT_N - 1 ? VOIGT_N - 1 : it);
+        return q.kappa0 * (a.h0[it] + q.adamp * a.h1[it]);
+    }
+    return q.kappa0 * voigt_hv<double>((double)k * q.dvoigt, q.adamp, a.h0, a.h1, a.h2);
+}
+
+// One thread per (line, depth): _add_fort19_asynth's gates and KAPCEN
+// (opacity.py:1388-1447) and the near-wing scan of
+// _accumulate_metal_profile_kernel (:117-196), sequential like the reference.
+template <typename R>
+__global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_f19 * a.n_layers) return;
+    const int h = (int)(i / a.n_layers), d = (int)(i - (int64_t)h * a.n_layers);
+    F19Par q;
+    q.kappa0 = q.adamp = q.tabstep = q.dvoigt = q.x_far = q.kapcen = 0.0;
+    q.ci = q.cc = q.n10 = q.nstep = q.early = q.active = q.kc_ok = 0;
+    q.d = d;
+    const int row = a.rows[h];
+    const int e = (row >= 0 && (int64_t)row < a.n_lines) ? a.element_idx[row] : -1;
+    const int ion = (row >= 0 && (int64_t)row < a.n_lines) ? a.ion_stage[row] : 0;
+    if (e < 0 || e >= a.n_elem || ion < 1 || ion > a.n_ion) {
+        if (d == 0) atomicOr(a.flags, FLAG_F19_LINE);
+        a.par[i] = q;
+        return;
+    }
+    const DepthPar& dp = a.depth[d];
+    const double pv = a.population[((int64_t)d * a.n_ion + (ion - 1)) * a.n_elem + e];
+    const int64_t n = a.n_wl;
+    const int ci = a.center[row];
+    const double wl = a.wavelength[row];
+    if (!(pv > 0.0) || (int64_t)ci >= n || !(dp.rho > 0.0)) {
+        a.par[i] = q;
+        return;
+    }
+    const double boltz = fastex(a.elo[row] * dp.hckt, a.extab, a.extabf);
+    // the line's Doppler width in the depth state (populations.py:158-195):
+    // thermal velocity of mass 56, model and synthesis microturbulence
+    const double temp = fmax(a.temperature[d], 1.0);
+    const double thermal = sqrt(2.0 * kKboltz * temp / (56.0 * kAmu)) / kClightCm;
+    const double vt = (a.vturb[d] / 1e5) / kClightKms;
+    const double micro = a.microturb_kms > 0 ? a.microturb_kms / kClightKms : 0.0;
+    const double total = sqrt(vt * vt + micro * micro);
+    const double dw = wl * sqrt(total * total + thermal * thermal);
+    if (wl <= 0.0 || dw <= 0.0) {
+        a.par[i] = q;
+        return;
+    }
+    const double dopple = dw / wl;
+    if (dopple <= 0.0) {
+        a.par[i] = q;
+        return;
+    }
+    const double xnfdop = pv / (dp.rho * dopple);
+    const double k0pre = a.cgf[h] * xnfdop;
+    const int cc = ci < 0 ? 0 : (ci > (int)n - 1 ? (int)n - 1 : ci);
+    const double kapmin = abtot_f19<R>(a, d, cc) * a.cutoff;
+    if (k0pre < kapmin) {
+        a.par[i] = q;
+        return;
+    }
+    const double k0 = k0pre * boltz;
+    if (k0 < kapmin) {
+        a.par[i] = q;
+        return;
+    }
+    const double gt = a.gamma_rad[h] + a.gamma_stark[h] * dp.xne + a.gamma_vdw[h] * dp.txnxn;
+    const double adamp = dopple > 0.0 ? gt / dopple : 0.0;
+    q.kapcen = adamp < 0.2 ? k0 * (1.0 - 1.128 * adamp) : k0 * voigt_hv<double>(0.0, adamp, a.h0, a.h1, a.h2);
+    q.kc_ok = q.kapcen >= kapmin;
+    q.ci = ci;
+    q.cc = cc;
+    q.active = 1;
+    // wing (_accumulate_metal_profile_kernel, no WCON/WTAIL)
+    if (k0 <= 0.0) {
+        q.nstep = 0;
+        q.early = 1;
+        a.par[i] = q;
+        return;
+    }
+    q.kappa0 = k0;
+    q.adamp = fmax(adamp, 1e-12);
+    const double kmin = a.cutoff * abtot_f19<R>(a, d, cc);
+    double resolu;
+    if (cc < (int)n - 1) resolu = 1.0 / (a.grid[cc + 1] / a.grid[cc] - 1.0);
+    else if (cc > 0) resolu = 1.0 / (a.grid[cc] / a.grid[cc - 1] - 1.0);
+    else resolu = 300000.0;
+    int n10 = (int)(10.0 * dopple * resolu);
+    n10 = n10 > MAX_PROFILE_STEPS ? MAX_PROFILE_STEPS : n10;
+    q.n10 = n10;
+    q.tabstep = (dopple * resolu) > 0 ? 200.0 / (dopple * resolu) : 200.0;
+    q.dvoigt = (dopple * resolu) > 0 ? 1.0 / dopple / resolu : 1e-6;
+    double p_n10 = 0.0;
+    if (q.adamp < 0.2) {
+        double tabi = 0.5;
+        for (int k = 1; k <= n10; k++) {
+            tabi = tabi + q.tabstep;
+            int it = (int)tabi;
+            it = it < 0 ? 0 : (it > VOIGT_N - 1 ? VOIGT_N - 1 : it);
+            const double p = k0 * (a.h0[it] + q.adamp * a.h1[it]);
+            if (k == n10) p_n10 = p;
+            if (p < kmin) {
+                q.nstep = k;
+                q.early = 1;
+                break;
+            }
+        }
+    } else {
+        for (int k = 1; k <= n10; k++) {
+            const double p = k0 * voigt_hv<double>((double)k * q.dvoigt, q.adamp, a.h0, a.h1, a.h2);
+            if (k == n10) p_n10 = p;
+            if (p < kmin) {
+                q.nstep = k;
+                q.early = 1;
+                break;
+            }
+        }
+    }
+    if (!q.early) {
+        q.x_far = (n10 > 0 && p_n10 > 0) ? p_n10 * ((double)n10 * (double)n10) : 0.0;
+        int maxstep = n10;
+        if (q.x_far > 0 && kmin > 0) {
+            const double ms = sqrt(q.x_far / kmin) + 1.0;
+            maxstep = ms >= (double)MAX_PROFILE_STEPS ? MAX_PROFILE_STEPS : (int)ms;
+        }
+        q.nstep = maxstep;
+    }
+    a.par[i] = q;
+}
+
+__device__ __forceinline__ double f19_value(const F19Args& a, const F19Par& q, int k) {
+    const int near_end = q.early ? q.nstep : q.n10;
+    if (k <= near_end) return f19_near(a, q, k);
+    return q.x_far / ((double)k * (double)k);
+}
+
+// One thread per (depth, grid point): the fort.19 lines' KAPCEN and wing
+// steps at the point, in catalog (fort.19) order, times STIM, onto the cube
+// (opacity.py:1485-1486).
+template <typename R>
+__global__ void __launch_bounds__(256) f19_gather_kernel(F19Args a, R* __restrict__ cube) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)a.n_layers * a.n_wl) return;
+    const int d = (int)(i / a.n_wl);
+    const int b = (int)(i - (int64_t)d * a.n_wl);
+    const int n = (int)a.n_wl;
+    double acc = 0.0;
+    bool any = false;
+    for (int h = 0; h < a.n_f19; h++) {
+        const F19Par& q = a.par[(int64_t)h * a.n_layers + d];
+        if (!q.active) continue;
+        if (q.kc_ok && b == q.cc) {
+            acc += q.kapcen;
+            any = true;
+        }
+        const int ci = q.ci, ns = q.nstep;
+        if (ns <= 0 || ci + ns < 0 || ci - ns >= n) continue;
+        if (b > ci && ci < n - 1) {
+            const int k = b - ci;
+            const int maxred = ci >= 0 ? min(n - 1 - ci, ns) : min(n - 1, ns);
+            if (k >= max(1, -ci) && k <= maxred) {
+                acc += f19_value(a, q, k);
+                any = true;
+            }
+        } else if (b < ci && ci > 0) {
+            const int k = ci - b;
+            if (k >= max(1, ci + 1 - n) && k <= min(ci, ns)) {
+                acc += f19_value(a, q, k);
+                any = true;
+            }
+        }
+    }
+    if (any) {
+        const double freq = kClightCm / (a.grid[b] * 1e-7);
+        const double stim = 1.0 - exp(-freq * (kHPlanck / (kKboltz * a.temperature[d])));
+        cube[i] = (R)((double)cube[i] + acc * stim);
+    }
+}
+
 }  // namespace
+
+template <typename R>
+static cudaError_t launch_f19_t(const F19Args& a, R* cube, cudaStream_t s) {
+    if (a.n_f19 <= 0) return cudaSuccess;
+    const int64_t nhd = (int64_t)a.n_f19 * a.n_layers;
+    f19_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t cells = (int64_t)a.n_layers * a.n_wl;
+    if (cells > 0) f19_gather_kernel<R><<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(a, cube);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_f19_f32(const F19Args& a, float* cube, cudaStream_t s) { return launch_f19_t<float>(a, cube, s); }
+cudaError_t launch_f19_f64(const F19Args& a, double* cube, cudaStream_t s) { return launch_f19_t<double>(a, cube, s); }
 
 template <typename R>
 static cudaError_t launch_helium_t(const HeArgs& a, R* cube, cudaStream_t s) {

@@ -250,6 +250,32 @@ struct HeArgs {
     int2* walk;                               // [n_he, L, 2] walk offsets [x, y), red then blue
 };
 
+// One (fort.19 NORMAL line, depth): gates, KAPCEN and the wing of
+// _accumulate_metal_profile_kernel (near profile to N10DOP or the first value
+// below KAPMIN, else far wings X / n^2 to MAXSTEP).
+struct F19Par {
+    double kappa0, adamp, tabstep, dvoigt, x_far, kapcen;
+    int ci, cc, n10, nstep, early, active, kc_ok, d;
+};
+
+struct F19Args {
+    int n_f19, n_layers, n_ion, n_elem;
+    int64_t n_wl, n_lines;
+    int* flags;                               // FLAG_F19_LINE
+    const int32_t* rows;                      // per line: catalog row, in catalog order
+    const double *cgf, *gamma_rad, *gamma_stark, *gamma_vdw;  // per line: fort.19 record values
+                                              // (single-precision values held in double)
+    const double *wavelength, *elo;           // catalog columns
+    const int32_t *element_idx, *ion_stage, *center;
+    const double* grid;
+    const double *temperature, *vturb, *population;
+    const DepthPar* depth;
+    double cutoff, microturb_kms;
+    const void *cabs, *cscat;
+    const double *extab, *extabf, *h0, *h1, *h2;
+    F19Par* par;                              // [n_f19, L]
+};
+
 // ---- batched launches -------------------------------------------------------
 //
 // A batch runs every stage once over all its jobs: the launch walks a job

@@ -63,6 +63,8 @@ cudaError_t launch_hydrogen_f32(const HydArgs& a, float* cube, cudaStream_t s);
 cudaError_t launch_hydrogen_f64(const HydArgs& a, double* cube, cudaStream_t s);
 cudaError_t launch_helium_f32(const HeArgs& a, float* cube, cudaStream_t s);
 cudaError_t launch_helium_f64(const HeArgs& a, double* cube, cudaStream_t s);
+cudaError_t launch_f19_f32(const F19Args& a, float* cube, cudaStream_t s);
+cudaError_t launch_f19_f64(const F19Args& a, double* cube, cudaStream_t s);
 // device copy of the hydrogen profile tables (uploaded on first use per device)
 ks_status hydrogen_device_tables(const HydTables** out);
 

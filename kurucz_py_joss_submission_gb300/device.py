@@ -110,6 +110,12 @@ class DeviceGrid:
         self.rec = rec
 
 
+# fort.19's CODEX species (io/lines/fort19.py:21-24): the ions with
+# continuum-merge limits
+FORT19_CODEX = np.array([1.0, 2.0, 2.01, 6.0, 6.01, 12.0, 12.01, 13.0, 13.01, 14.0, 14.01, 20.0, 20.01, 8.0,
+                         11.0, 5.0, 19.0])
+
+
 def inv_order(order: np.ndarray) -> np.ndarray:
     """Catalog row -> device row, for a device order given as catalog rows."""
     inv = np.empty_like(order)
@@ -186,17 +192,39 @@ class DeviceCatalog:
             rec.hydrogen_rows = self.t["hydrogen_rows"].data_ptr()
             rec.hydrogen_n_lower = self.t["hydrogen_n_lower"].data_ptr()
             rec.hydrogen_n_upper = self.t["hydrogen_n_upper"].data_ptr()
-        # lines the reference routes to fort.19 besides hydrogen and helium
-        # (io/lines/fort19.py:343-347: autoionizing TYPE 1, merged-continuum
-        # TYPE > 3, others with NBLO/NBUP) get their special profiles there
-        # (engine/opacity.py:1335 _add_fort19_asynth), which are not computed here
+        # fort.19 lines (io/lines/fort19.py:343-347) other than hydrogen and
+        # helium: the NORMAL ones (line type 0 with NBLO/NBUP set) get
+        # _add_fort19_asynth's profiles (engine/opacity.py:1335-1488) here;
+        # autoionizing lines (TYPE 1) and NORMAL lines whose fort.19 record
+        # carries continuum-merge limits (NCON = ISO2 with ISO1 = 0, on a
+        # species of its CONTX table) are not modelled
         nb = np.abs(np.asarray(cat.n_lower)) + np.abs(np.asarray(cat.n_upper))
-        f19 = ((lt == 1) | (lt > 3) | ((nb != 0) & ~np.isin(lt, (-1, -2, -3, -4, -6))))
-        self.n_fort19_skipped = int(np.count_nonzero(f19))
+        ncon = np.where((np.asarray(cat.iso1) == 0) & (np.asarray(cat.iso2) > 0), np.asarray(cat.iso2), 0)
+        codex = np.any(np.isclose(np.asarray(cat.code)[:, None], FORT19_CODEX[None, :], rtol=0.0, atol=1e-3),
+                       axis=1)
+        normal = (lt == 0) & (nb != 0) & (np.asarray(cat.element_idx) >= 0) & (np.asarray(cat.ion_stages) >= 1)
+        tapered = normal & (ncon > 0) & codex
+        f19 = np.flatnonzero(normal & ~tapered)
+        self.n_fort19_skipped = int(np.count_nonzero(lt == 1) + np.count_nonzero(tapered))
         if self.n_fort19_skipped:
-            warnings.warn(f"{self.n_fort19_skipped} lines of the fort.19 classes (autoionizing, merged "
-                          "continuum, NBLO/NBUP-tagged metal lines) contribute no opacity here",
-                          RuntimeWarning, stacklevel=2)
+            warnings.warn(f"{self.n_fort19_skipped} fort.19 lines (autoionizing, or with continuum-merge "
+                          "limits) contribute no opacity here", RuntimeWarning, stacklevel=2)
+        self.n_f19 = int(f19.size)
+        if self.n_f19 > 256:
+            raise ValueError(f"{self.n_f19} fort.19 lines: the synthesis takes at most 256")
+        if self.n_f19:
+            wl = np.asarray(cat.wavelength)[f19]
+            gf = 10.0 ** np.asarray(cat.log_gf, dtype=np.float64)[f19]
+            freq = 2.99792458e17 / np.maximum(wl, 1.0e-30)
+            # the fort.19 record's single-precision fields (fort19.py:379-402)
+            f32 = lambda x: np.asarray(x, dtype=np.float32).astype(np.float64)  # noqa: E731
+            self.t["f19_rows"] = _dev(f19 if self.order is None else inv_order(self.order)[f19], np.int32, dev)
+            self.t["f19_cgf"] = _dev(f32((0.026538 / 1.77245) * gf / freq), np.float64, dev)
+            for k in ("gamma_rad", "gamma_stark", "gamma_vdw"):
+                self.t["f19_" + k] = _dev(f32(np.asarray(getattr(cat, k))[f19]), np.float64, dev)
+            rec.n_f19 = self.n_f19
+            for k in ("rows", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw"):
+                setattr(rec, "f19_" + k, self.t["f19_" + k].data_ptr())
         # helium lines (line types -3/-4/-6; engine/opacity.py:2531-2544): the
         # helium wing pass, device rows in catalog order
         he = np.flatnonzero(np.isin(lt, (-3, -4, -6)) & helium)

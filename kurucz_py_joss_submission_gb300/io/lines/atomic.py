@@ -41,6 +41,8 @@ class LineCatalog:
     catalog_index: np.ndarray
     n_lower: np.ndarray   # NBLO: lower principal quantum number (hydrogen lines), 0 if blank
     n_upper: np.ndarray   # NBUP
+    iso1: np.ndarray      # ISO1 / ISO2 (isotope numbers; ISO2 doubles as fort.19's continuum index)
+    iso2: np.ndarray
 
     def __len__(self) -> int:
         return int(self.wavelength.size)
@@ -89,6 +91,7 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
             line_types=np.zeros(n, np.int32), process_mask=np.zeros(n, np.uint8),
             asynth_mask=np.zeros(n, np.uint8), code=np.zeros(n), catalog_index=np.zeros(n, np.int64),
             n_lower=np.zeros(n, np.int32), n_upper=np.zeros(n, np.int32),
+            iso1=np.zeros(n, np.int32), iso2=np.zeros(n, np.int32),
         )
         order = ["wavelength", "log_gf", "gf", "cgf", "excitation_energy", "gamma_rad", "gamma_stark",
                  "gamma_vdw", "element_idx", "ion_stages", "line_types", "process_mask",
@@ -96,6 +99,8 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
         _native.check(L.ks_gfall_fetch(h, *[cols[k].ctypes.data_as(C.c_void_p) for k in order]))
         _native.check(L.ks_gfall_fetch_levels(h, cols["n_lower"].ctypes.data_as(C.c_void_p),
                                               cols["n_upper"].ctypes.data_as(C.c_void_p)))
+        _native.check(L.ks_gfall_fetch_iso(h, cols["iso1"].ctypes.data_as(C.c_void_p),
+                                           cols["iso2"].ctypes.data_as(C.c_void_p)))
     finally:
         L.ks_gfall_free(h)
     return LineCatalog(**cols)

@@ -1,0 +1,201 @@
+"""CPU restatement of the reference's fort.19 NORMAL-line profiles -- test
+infrastructure.
+
+Only ``tests/`` use this module, to check the GPU kernels for these lines.
+
+Lines with NBLO/NBUP set (and none of the hydrogen, helium, autoionizing,
+coronal or PRD types) leave the TRANSP/ASYNTH route (line_opacity.py:
+746-757) for fort.19 (io/lines/fort19.py:343-347) and get their profile in
+``_add_fort19_asynth`` (synthe_py/engine/opacity.py:1335-1488), added to
+ASYNTH as TMP x STIM per layer:
+
+* the fort.19 record keeps CGF and the damping constants in single
+  precision (fort19.py:368-402);
+* per (line, layer): population of the line's ion, the line's Doppler width
+  from the depth state (physics/populations.py:158-195: thermal velocity of
+  mass 56 -- the state is built without element masses, opacity.py:2204 --
+  and the model's plus the synthesis microturbulence), XNFDOP, the two
+  KAPMIN gates, KAPCEN at the clamped centre bin (opacity.py:1404-1447);
+* the wing of ``_accumulate_metal_profile_kernel`` (opacity.py:74-262):
+  N10DOP = int(10 DOPPLE RESOLU), the near profile with the incremental
+  TABI (ADAMP < 0.2) or the Voigt function, stopping at the first value below
+  KAPMIN, else far wings X / n^2 to MAXSTEP; then every step from 1 to NSTEP
+  added, red and blue, without a cutoff test.
+
+Lines whose fort.19 continuum index is set (NCON > 0 with an element of the
+CONTX table) taper their wings at WCON/WTAIL; they are not restated here.
+"""
+
+from __future__ import annotations
+
+import math
+from typing import Dict
+
+import numpy as np
+
+from . import hydrogen, oracle
+
+C_LIGHT_NM = 2.99792458e17
+C_LIGHT_CM = 2.99792458e10
+C_LIGHT_KMS = 299792.458
+KBOLTZ = 1.380649e-16
+AMU = 1.66054e-24
+CGF_FACTOR = 0.026538 / 1.77245
+MAX_PROFILE_STEPS = 1000000
+DEFAULT_ATOMIC_MASS = 56.0
+
+
+def normal_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
+    """Catalog rows taken as fort.19 NORMAL lines, in catalog (fort.19) order."""
+    lt = np.asarray(cat["line_type"])
+    nb = np.abs(np.asarray(cat["n_lower"])) + np.abs(np.asarray(cat["n_upper"]))
+    known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
+    return np.flatnonzero((lt == 0) & (nb != 0) & known & (np.asarray(cat["ion_stage"]) >= 1))
+
+
+def record_values(cat: Dict[str, np.ndarray], rows: np.ndarray) -> Dict[str, np.ndarray]:
+    """The fort.19 record fields of those lines, rounded to single precision
+    as the record stores them (fort19.py:379-387, :394-402)."""
+    wl = np.asarray(cat["wavelength"])[rows]
+    gf = 10.0 ** np.asarray(cat["log_gf"])[rows]
+    freq = C_LIGHT_NM / np.maximum(wl, 1.0e-30)
+    return dict(
+        cgf=np.asarray(CGF_FACTOR * gf / freq, dtype=np.float32).astype(np.float64),
+        gamma_rad=np.asarray(cat["gamma_rad"], dtype=np.float32)[rows].astype(np.float64),
+        gamma_stark=np.asarray(cat["gamma_stark"], dtype=np.float32)[rows].astype(np.float64),
+        gamma_vdw=np.asarray(cat["gamma_vdw"], dtype=np.float32)[rows].astype(np.float64),
+    )
+
+
+def line_doppler(atm: Dict[str, np.ndarray], d: int, wl: float, microturb_kms: float) -> float:
+    """Doppler width (nm) of a line in layer d, physics/populations.py:158-195."""
+    temp = max(float(atm["temperature"][d]), 1.0)
+    thermal = math.sqrt(2.0 * KBOLTZ * temp / (DEFAULT_ATOMIC_MASS * AMU)) / C_LIGHT_CM
+    vt = (float(atm["turbulent_velocity"][d]) / 1e5) / C_LIGHT_KMS
+    micro = microturb_kms / C_LIGHT_KMS if microturb_kms > 0 else 0.0
+    total = math.sqrt(vt * vt + micro * micro)
+    return wl * math.sqrt(total * total + thermal * thermal)
+
+
+def _metal_wing(tmp, cont, grid, ci, wl, kappa0, adamp, dw, cutoff, tb):
+    """_accumulate_metal_profile_kernel without WCON/WTAIL (opacity.py:74-262)."""
+    if dw <= 0.0 or kappa0 <= 0.0:
+        return
+    n = grid.size
+    a = max(adamp, 1e-12)
+    cc = max(0, min(ci, n - 1))
+    kapmin = cutoff * cont[cc]
+    if cc < n - 1:
+        resolu = 1.0 / (grid[cc + 1] / grid[cc] - 1.0)
+    elif cc > 0:
+        resolu = 1.0 / (grid[cc] / grid[cc - 1] - 1.0)
+    else:
+        resolu = 300000.0
+    dopple = dw / wl if wl > 0 else 1e-6
+    n10 = min(int(10.0 * dopple * resolu), MAX_PROFILE_STEPS)
+    prof = {}
+    early = False
+    nstep = 0
+    if a < 0.2:
+        tabstep = 200.0 / (dopple * resolu) if (dopple * resolu) > 0 else 200.0
+        tabi = 0.5
+        for k in range(1, n10 + 1):
+            tabi = tabi + tabstep
+            it = min(max(int(tabi), 0), tb["h0tab"].size - 1)
+            prof[k] = kappa0 * (tb["h0tab"][it] + a * tb["h1tab"][it])
+            if prof[k] < kapmin:
+                nstep, early = k, True
+                break
+    else:
+        dv = 1.0 / dopple / resolu if (dopple * resolu) > 0 else 1e-6
+        for k in range(1, n10 + 1):
+            prof[k] = kappa0 * oracle.voigt(float(k) * dv, a, tb)
+            if prof[k] < kapmin:
+                nstep, early = k, True
+                break
+    x_far = 0.0
+    if not early:
+        x_far = prof[n10] * float(n10) ** 2 if (n10 > 0 and prof.get(n10, 0.0) > 0) else 0.0
+        if x_far > 0 and kapmin > 0:
+            maxstep = min(int(np.sqrt(x_far / kapmin) + 1.0), MAX_PROFILE_STEPS)
+        else:
+            maxstep = n10
+        nstep = maxstep
+
+    def value(k):
+        if k in prof:
+            return prof[k]
+        return x_far / float(k) ** 2 if (not early and k > n10) else 0.0
+
+    if ci + nstep < 0 or ci - nstep >= n:
+        return
+    if ci < n - 1:
+        maxred = min(n - 1 - ci, nstep) if ci >= 0 else min(n - 1, nstep)
+        for k in range(max(1, -ci), maxred + 1):
+            b = ci + k
+            if 0 <= b < n:
+                tmp[b] += value(k)
+    if ci <= 0:
+        return
+    for k in range(max(1, ci + 1 - n), min(ci, nstep) + 1):
+        b = ci - k
+        if 0 <= b < n:
+            tmp[b] += value(k)
+
+
+def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np.ndarray,
+                continuum: np.ndarray, cutoff: float = 1e-3, microturb_kms: float = 0.0) -> np.ndarray:
+    """TMP x STIM [L, N]: what the fort.19 NORMAL lines add to ASYNTH.  ``cat``
+    (gfall.parse_gfall keys) with the centre bins in ``center``."""
+    tb = oracle.tables()
+    L, N = continuum.shape
+    rows = normal_rows(cat)
+    rec = record_values(cat, rows)
+    pop = np.asarray(atm["population_per_ion"])
+    rho = np.asarray(atm["mass_density"])
+    xne = np.asarray(atm["electron_density"])
+    hckt = np.asarray(atm["hckt"])
+    txn = oracle.txnxn(atm)
+    stim = 1.0 - np.exp(-(C_LIGHT_CM / (grid * 1e-7))[None, :]
+                        * (6.62607015e-27 / (KBOLTZ * np.asarray(atm["temperature"])))[:, None])
+    out = np.zeros((L, N))
+    for d in range(L):
+        tmp = np.zeros(N)
+        for j, i in enumerate(rows):
+            z = int(cat["nelem"][i]) - 1
+            ion = int(cat["ion_stage"][i])
+            pv = float(pop[d, ion - 1, z]) if ion <= pop.shape[1] else 0.0
+            if pv <= 0.0:
+                continue
+            boltz = hydrogen.fast_ex(float(cat["excitation_energy"][i]) * float(hckt[d]))
+            wl = float(cat["wavelength"][i])
+            ci = int(cat["center"][i])
+            if ci >= N:
+                continue
+            r = float(rho[d])
+            if r <= 0.0:
+                continue
+            dw = line_doppler(atm, d, wl, microturb_kms)
+            if wl <= 0.0 or dw <= 0.0:
+                continue
+            dopple = dw / wl
+            if dopple <= 0.0:
+                continue
+            xnfdop = pv / (r * dopple)
+            k0pre = rec["cgf"][j] * xnfdop
+            cc = max(0, min(ci, N - 1))
+            kapmin = float(continuum[d, cc]) * cutoff
+            if k0pre < kapmin:
+                continue
+            k0 = k0pre * boltz
+            if k0 < kapmin:
+                continue
+            gt = rec["gamma_rad"][j] + rec["gamma_stark"][j] * float(xne[d]) + rec["gamma_vdw"][j] * float(txn[d])
+            adamp = gt / dopple if dopple > 0.0 else 0.0
+            kapcen = k0 * (1.0 - 1.128 * adamp) if adamp < 0.2 else k0 * oracle.voigt(0.0, adamp, tb)
+            if kapcen >= kapmin:
+                tmp[cc] += kapcen
+            _metal_wing(tmp, continuum[d], grid, ci, wl, k0, adamp, dw, cutoff, tb)
+        if np.any(tmp > 0.0):
+            out[d] = tmp * stim[d]
+    return out

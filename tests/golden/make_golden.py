@@ -115,6 +115,12 @@ CASES = {
     "heii_468": dict(atm="t20000g400", wl_start=468.3, wl_end=469.1,
                      n_lines=120, draw=(468.15, 469.25), log_uniform=False, seed=22,
                      helium=True),
+    # metal lines with NBLO/NBUP set (every 4th line): routed to fort.19 and
+    # given _add_fort19_asynth's profiles (engine/opacity.py:1335-1488)
+    # instead of TRANSP/ASYNTH's
+    "fort19_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
+                           n_lines=160, draw=(499.85, 501.15), log_uniform=False, seed=24,
+                           nb_every=4),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -141,6 +147,15 @@ def case_lines(case: dict) -> workloads.LineDraw:
         lines = workloads.merge_lines(lines, workloads.balmer_lines(case["hydrogen"]))
     if case.get("helium"):
         lines = workloads.merge_lines(lines, workloads.helium_lines(*case["draw"]))
+    if case.get("nb_every"):
+        k = case["nb_every"]
+        lo, up = lines.levels()
+        lo, up = lo.copy(), up.copy()
+        lo[::k], up[::k] = 3, 5
+        lines.n_lower, lines.n_upper = lo, up
+        idx = np.arange(0, len(lines), k)
+        lines.log_gf[idx] = np.maximum(lines.log_gf[idx], -0.5)   # strong enough to pass the gates
+        lines.e_lower_cm[idx] = np.minimum(lines.e_lower_cm[idx], 20000.0)
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth
         # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)

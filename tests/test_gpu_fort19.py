@@ -1,0 +1,106 @@
+"""fort.19 NORMAL lines on the GPU (needs a GPU).
+
+Metal lines with NBLO/NBUP set leave TRANSP/ASYNTH for fort.19 and get the
+profiles of _add_fort19_asynth (engine/opacity.py:1335-1488), added to
+ASYNTH before the hydrogen lines.  Checked against the reference's golden
+(through the parity tests' fused FP64/mixed runs, which take every golden
+case) and here against the oracle where no golden exists: microturbulence
+in the lines' Doppler widths, damping large enough for the Voigt branch
+(ADAMP >= 0.2), a line centred below the grid (the reference's clamped
+KAPCEN bin and wing from bin 0), and a raised cutoff.
+
+Tolerance: FP64 cube within 1e-11 relative of the oracle's.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from _cases import atm_path, available_cases
+from kurucz_py_joss_submission_gb300 import workloads
+from kurucz_py_joss_submission_gb300.device import (DeviceAtmosphere, DeviceCatalog, DeviceGrid,
+                                                     Synthesizer, make_options)
+from kurucz_py_joss_submission_gb300.engine.continuum import build_depth_continuum
+from kurucz_py_joss_submission_gb300.io import atmosphere as atm_io
+from kurucz_py_joss_submission_gb300.io.lines import atomic
+from oracle import fort19, gfall, oracle
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-11
+ATM = atm_path("tiny_500_501")
+
+
+def gpu_cubes(cat, atm, grid, **opt):
+    dcat = DeviceCatalog(cat)
+    syn = Synthesizer(dcat, DeviceAtmosphere(atm), DeviceGrid(grid), make_options(precision="fp64", **opt))
+    st = syn.run(stats=True)
+    assert st["device_flags"] == 0
+    with_f = syn.asynth.cpu().numpy()
+    n = dcat.rec.n_f19
+    dcat.rec.n_f19 = 0
+    syn.run()
+    torch.cuda.synchronize()
+    without = syn.asynth.cpu().numpy()
+    dcat.rec.n_f19 = n
+    return dcat, with_f, without
+
+
+def draw(w0, w1, seed, gw_shift=0.0, extra=None):
+    d = workloads.random_atomic_lines(80, w0 - 0.15, w1 + 0.15, seed=seed)
+    lo, up = d.levels()
+    lo, up = lo.copy(), up.copy()
+    lo[::3], up[::3] = 4, 6
+    d.n_lower, d.n_upper = lo, up
+    idx = np.arange(0, len(d), 3)
+    d.log_gf[idx] = np.maximum(d.log_gf[idx], -0.5)
+    d.e_lower_cm[idx] = np.minimum(d.e_lower_cm[idx], 20000.0)
+    d.log_gamma_vdw[idx] += gw_shift
+    if extra is not None:
+        d = workloads.merge_lines(d, extra)
+    return d
+
+
+def below_grid_line(w0):
+    """One strong NB-tagged Fe I line 0.02 nm below the grid start."""
+    d = workloads.random_atomic_lines(1, w0 - 0.03, w0 - 0.02, seed=5)
+    d.log_gf[:] = 0.5
+    d.e_lower_cm[:] = 1000.0
+    d.code[:] = 26.00
+    d.n_lower, d.n_upper = np.array([2], np.int32), np.array([7], np.int32)
+    return d
+
+
+CASES = {
+    "micro": (500.0, 500.8, dict(seed=31), {"microturb_kms": 2.0}),
+    "voigt_branch": (500.0, 500.8, dict(seed=32, gw_shift=3.0), {}),
+    "below_grid": (500.0, 500.8, dict(seed=33, extra="below"), {}),
+    "cutoff": (500.0, 500.8, dict(seed=34), {"cutoff": 1e-2}),
+}
+
+
+@pytest.mark.parametrize("key", sorted(CASES))
+def test_fp64_matches_oracle(key, tmp_path):
+    w0, w1, kw, opt = CASES[key]
+    kw = dict(kw)
+    if kw.pop("extra", None) == "below":
+        kw["extra"] = below_grid_line(w0)
+    p = tmp_path / "lines.gf"
+    p.write_text(workloads.format_gfall(draw(w0, w1, **kw)))
+    cat = atomic.load_catalog_window(p, w0, w1)
+    grid = oracle.wavelength_grid(w0, w1, 300000.0)
+    atm = atm_io.load_cached(ATM)
+    dcat, with_f, without = gpu_cubes(cat, atm, grid, **opt)
+    assert dcat.n_f19 > 10
+    ocat = gfall.filter_window(gfall.parse_gfall(p, oracle.tables()["potion"]), w0, w1)
+    assert np.array_equal(ocat["wavelength"], cat.wavelength)
+    ca, cs = build_depth_continuum(atm, grid, precision="fp64")
+    term = fort19.asynth_term(dict(ocat, center=oracle.center_indices(grid, ocat["wavelength"])),
+                              oracle.load_atmosphere(ATM), grid, ca + cs, cutoff=opt.get("cutoff", 1e-3),
+                              microturb_kms=opt.get("microturb_kms", 0.0))
+    assert np.count_nonzero(term) > 1000
+    ref = without + term
+    assert float(np.max(np.abs(with_f - ref) / np.maximum(np.abs(ref), 1e-300))) < FP64_TOL
+    if key == "below_grid":
+        c = oracle.center_indices(grid, ocat["wavelength"])
+        assert np.any(c[fort19.normal_rows(dict(ocat, center=c))] < 0)
