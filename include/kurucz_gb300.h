@@ -121,7 +121,7 @@ typedef struct {
      * (device; n_helium = 0 for none; at most 256) */
     int32_t n_helium;
     const int32_t *helium_rows;
-    /* fort.19 NORMAL lines (NBLO/NBUP set, line type 0, no continuum-merge
+    /* fort.19 lines: NORMAL ones (NBLO/NBUP set, line type 0, no continuum-merge
      * limits): the profiles of _add_fort19_asynth (synthe_py/engine/
      * opacity.py:1335-1488) added to ASYNTH; their rows in catalog order and
      * the fort.19 record's CGF and damping constants, rounded to single
@@ -130,6 +130,11 @@ typedef struct {
     int32_t n_f19;
     const int32_t *f19_rows;
     const double *f19_cgf, *f19_gamma_rad, *f19_gamma_stark, *f19_gamma_vdw;
+    /* per fort.19 line: 0 NORMAL, 1 autoionizing (gfall AUT tag: the profile
+     * of _accumulate_autoionizing_profile, opacity.py:901-963, with KAPPA0 =
+     * BSHORE GF XNFPEL BOLT; f19_cgf then holds gf and f19_gamma_* the
+     * record's unnormalised GAMMAR, ASHORE, BSHORE, fort19.py:352-373) */
+    const int32_t *f19_kind;
 } ks_lines;
 
 typedef struct {
@@ -583,6 +588,12 @@ ks_status ks_gfall_fetch_levels(const ks_gfall *g, int32_t *n_lower, int32_t *n_
  * takes ISO2 as the continuum index NCON when ISO1 is 0
  * (io/lines/fort19.py:338).  Same order as ks_gfall_fetch. */
 ks_status ks_gfall_fetch_iso(const ks_gfall *g, int32_t *iso1, int32_t *iso2);
+/* The GR / GS / GW fields of every record as read (log10 damping constants,
+ * 0 when blank; synthe_py/io/lines/atomic.py:341-343): fort.19 keeps them
+ * unnormalised for autoionizing lines (io/lines/fort19.py:352-373).  Same
+ * order as ks_gfall_fetch. */
+ks_status ks_gfall_fetch_gamma_logs(const ks_gfall *g, double *gamma_rad_log, double *gamma_stark_log,
+                                    double *gamma_vdw_log);
 void ks_gfall_free(ks_gfall *g);
 
 #ifdef __cplusplus

@@ -74,7 +74,7 @@ class KsLines(C.Structure):
         ("hydrogen_rows", P), ("hydrogen_n_lower", P), ("hydrogen_n_upper", P),
         ("n_helium", C.c_int32), ("helium_rows", P),
         ("n_f19", C.c_int32), ("f19_rows", P), ("f19_cgf", P), ("f19_gamma_rad", P),
-        ("f19_gamma_stark", P), ("f19_gamma_vdw", P),
+        ("f19_gamma_stark", P), ("f19_gamma_vdw", P), ("f19_kind", P),
     ]
 
 
@@ -227,6 +227,7 @@ SIGNATURES = {
     "ks_gfall_fetch": (C.c_int32, [P] + [P] * 15),
     "ks_gfall_fetch_levels": (C.c_int32, [P, P, P]),
     "ks_gfall_fetch_iso": (C.c_int32, [P, P, P]),
+    "ks_gfall_fetch_gamma_logs": (C.c_int32, [P, P, P, P]),
     "ks_gfall_free": (None, [P]),
 }
 

@@ -43,7 +43,7 @@ ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(co
 
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
-    if (minor) *minor = 3;
+    if (minor) *minor = 4;
     return KS_OK;
 }
 
@@ -624,7 +624,8 @@ struct Workspace {
     int hyd_cap;
     HePar* he_par;    // helium lines: per (line, depth) wing parameters and walk limits
     int2* he_walk;
-    F19Par* f19_par;  // fort.19 NORMAL lines: per (line, depth) gates and wing
+    F19Par* f19_par;  // fort.19 lines: per (line, depth) gates and wing
+    int2* f19_walk;
     int64_t stride;
     int nchunks;
 };
@@ -669,6 +670,7 @@ static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl,
     w.he_par = c.take<HePar>((size_t)w.hyd_cap * L);
     w.he_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
     w.f19_par = c.take<F19Par>((size_t)w.hyd_cap * L);
+    w.f19_walk = c.take<int2>((size_t)w.hyd_cap * L * 2);
 }
 
 extern "C" ks_status ks_workspace_size(int64_t n_lines, int32_t n_layers, int64_t n_wavelengths,
@@ -739,7 +741,7 @@ static ks_status check_lines(const ks_lines* l) {
     if (l->n_f19 < 0 || l->n_f19 > l->n_lines) return fail(KS_ERR_INVALID, "n_f19 must lie in [0, n_lines]");
     if (l->n_f19 > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 fort.19 lines");
     if (l->n_f19 > 0 && (!l->f19_rows || !l->f19_cgf || !l->f19_gamma_rad || !l->f19_gamma_stark ||
-                         !l->f19_gamma_vdw))
+                         !l->f19_gamma_vdw || !l->f19_kind))
         return fail(KS_ERR_INVALID, "lines: a fort.19 column is NULL");
     return KS_OK;
 }
@@ -1245,9 +1247,9 @@ static ks_status run_hydrogen(const ks_lines* lines, const ks_atmos* atm, const 
     return KS_OK;
 }
 
-// fort.19 NORMAL lines (NBLO/NBUP set): _add_fort19_asynth's profiles, TMP x
-// STIM onto ASYNTH before the hydrogen lines (synthe_py/engine/opacity.py:
-// 1335-1488, called at :2366).
+// fort.19 NORMAL (NBLO/NBUP set) and autoionizing lines: _add_fort19_asynth's
+// profiles, TMP x STIM onto ASYNTH before the hydrogen lines
+// (synthe_py/engine/opacity.py:1335-1541, called at :2366).
 template <typename R>
 static ks_status run_f19(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid, const ks_options* opt,
                          const Workspace& w, const DevTables& t, const R* cabs, const R* cscat, R* cube,
@@ -1264,6 +1266,7 @@ static ks_status run_f19(const ks_lines* lines, const ks_atmos* atm, const ks_gr
     f.n_lines = lines->n_lines;
     f.flags = w.flags;
     f.rows = lines->f19_rows;
+    f.kind = lines->f19_kind;
     f.cgf = lines->f19_cgf;
     f.gamma_rad = lines->f19_gamma_rad;
     f.gamma_stark = lines->f19_gamma_stark;
@@ -1288,6 +1291,7 @@ static ks_status run_f19(const ks_lines* lines, const ks_atmos* atm, const ks_gr
     f.h1 = t.h1d;
     f.h2 = t.h2d;
     f.par = w.f19_par;
+    f.walk = w.f19_walk;
     cudaError_t e;
     if constexpr (sizeof(R) == 8) e = launch_f19_f64(f, cube, s);
     else e = launch_f19_f32(f, cube, s);

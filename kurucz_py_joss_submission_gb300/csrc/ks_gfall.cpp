@@ -40,6 +40,7 @@ const double kDellim[7] = {100.0, 30.0, 10.0, 3.0, 1.0, 0.3, 0.1};
 struct Rec {
     double wl, loggf, code, elo, gr, gs, gw;
     int nelem, ion, lt, nblo, nbup, line_size, anum, iso1, iso2;
+    double grl, gsl, gwl;  // the GR / GS / GW fields as read (log10; 0 when blank)
     bool is_h_elem;  // element symbol is H / D (DELLIM special case)
 };
 
@@ -268,6 +269,9 @@ bool parse_fixed(const char* line, int len, const double* potion, int np, Rec* r
     r->line_size = line_size;
     r->iso1 = iso1;
     r->iso2 = iso2;
+    r->grl = grl;
+    r->gsl = gsl;
+    r->gwl = gwl;
     // element symbol: tfort symbols up to U, else "Z<n>" (unknown to TRANSP)
     r->anum = (nelem > 0 && nelem < kNSym) ? nelem : 0;
     r->is_h_elem = nelem == 1;
@@ -327,6 +331,7 @@ bool parse_ws(const char* line, int len, Rec* r) {
     r->line_size = 0;
     r->iso1 = 0;
     r->iso2 = 0;
+    r->grl = r->gsl = r->gwl = 0.0;
     r->anum = z;
     std::string u;
     for (char ch : el) u += (char)std::toupper((unsigned char)ch);
@@ -476,6 +481,16 @@ extern "C" ks_status ks_gfall_fetch_iso(const ks_gfall* g, int32_t* iso1, int32_
     for (size_t k = 0; k < g->recs.size(); k++) {
         if (iso1) iso1[k] = g->recs[k].iso1;
         if (iso2) iso2[k] = g->recs[k].iso2;
+    }
+    return KS_OK;
+}
+
+extern "C" ks_status ks_gfall_fetch_gamma_logs(const ks_gfall* g, double* gr, double* gs, double* gw) {
+    if (!g) return KS_ERR_INVALID;
+    for (size_t k = 0; k < g->recs.size(); k++) {
+        if (gr) gr[k] = g->recs[k].grl;
+        if (gs) gs[k] = g->recs[k].gsl;
+        if (gw) gw[k] = g->recs[k].gwl;
     }
     return KS_OK;
 }

@@ -773,7 +773,7 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
     const int h = (int)(i / a.n_layers), d = (int)(i - (int64_t)h * a.n_layers);
     F19Par q;
     q.kappa0 = q.adamp = q.tabstep = q.dvoigt = q.x_far = q.kapcen = 0.0;
-    q.ci = q.cc = q.n10 = q.nstep = q.early = q.active = q.kc_ok = 0;
+    q.ci = q.cc = q.n10 = q.nstep = q.early = q.active = q.kc_ok = q.kind = q.pad = 0;
     q.d = d;
     const int row = a.rows[h];
     const int e = (row >= 0 && (int64_t)row < a.n_lines) ? a.element_idx[row] : -1;
@@ -793,6 +793,30 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
         return;
     }
     const double boltz = fastex(a.elo[row] * dp.hckt, a.extab, a.extabf);
+    if (a.kind[h] == 1) {
+        // autoionizing: KAPPA0 = BSHORE GF XNFPEL BOLT (opacity.py:1522-1541), then
+        // _accumulate_autoionizing_profile (:901-963); a centre bin -1 (line
+        // below the grid) is Python's index -1 there: the last bin
+        q.kind = 1;
+        const double k0 = a.gamma_vdw[h] * a.cgf[h] * (pv / dp.rho) * boltz;
+        const int cc = ci >= 0 ? ci : (int)n + ci;
+        if (cc < 0 || k0 < abtot_f19<R>(a, d, cc) * a.cutoff || k0 <= 0.0) {
+            a.par[i] = q;
+            return;
+        }
+        q.kappa0 = k0;
+        q.kapcen = k0;
+        q.kc_ok = 1;
+        q.ci = ci;
+        q.cc = cc;
+        q.tabstep = kClightCm / (wl * 1e-7);           // line frequency
+        q.dvoigt = fmax(fabs(a.gamma_rad[h]), 1e-30);  // width
+        q.x_far = a.gamma_stark[h];                    // ASHORE
+        q.adamp = fabs(a.gamma_vdw[h]) < 1e-30 ? 1e-30 : a.gamma_vdw[h];  // BSHORE
+        q.active = 1;
+        a.par[i] = q;
+        return;
+    }
     // the line's Doppler width in the depth state (populations.py:158-195):
     // thermal velocity of mass 56, model and synthesis microturbulence
     const double temp = fmax(a.temperature[d], 1.0);
@@ -887,6 +911,47 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
     a.par[i] = q;
 }
 
+// Autoionizing profile at grid point b (opacity.py:934-960).
+__device__ __forceinline__ double f19_aut_value(const F19Args& a, const F19Par& q, int64_t b) {
+    const double freq = kClightCm / (a.grid[b] * 1e-7);
+    const double eps = 2.0 * (freq - q.tabstep) / q.dvoigt;
+    return q.kappa0 * (q.x_far * eps + q.adamp) / (eps * eps + 1.0) / q.adamp;
+}
+
+// One warp per (autoionizing line, depth, side): offsets 1, 2, ... until the
+// grid ends or the value is <= 0 or below the cutoff (not added); [1, end).
+template <typename R>
+__global__ void __launch_bounds__(128) f19_march_kernel(F19Args a) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= (int64_t)a.n_f19 * a.n_layers * 2) return;
+    const int64_t pd = gw >> 1;
+    const bool red = (gw & 1) == 0;
+    const F19Par q = a.par[pd];
+    const int64_t n = a.n_wl;
+    int2 out = make_int2(1, 1);
+    if (q.active && q.kind == 1) {
+        const int64_t last = red ? n - 1 - q.ci : q.ci;  // offsets that stay inside the grid
+        int64_t end = last + 1;
+        for (int64_t o0 = 1; o0 <= last; o0 += 32) {
+            const int64_t o = o0 + lane;
+            bool stop = false;
+            if (o <= last) {
+                const int64_t b = red ? q.ci + o : q.ci - o;
+                const double v = f19_aut_value(a, q, b);
+                stop = v <= 0.0 || v < abtot_f19<R>(a, q.d, b) * a.cutoff;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, stop);
+            if (m) {
+                end = o0 + (__ffs(m) - 1);
+                break;
+            }
+        }
+        out = make_int2(1, (int)(end < 1 ? 1 : end));
+    }
+    if (lane == 0) a.walk[gw] = out;
+}
+
 __device__ __forceinline__ double f19_value(const F19Args& a, const F19Par& q, int k) {
     const int near_end = q.early ? q.nstep : q.n10;
     if (k <= near_end) return f19_near(a, q, k);
@@ -911,6 +976,18 @@ __global__ void __launch_bounds__(256) f19_gather_kernel(F19Args a, R* __restric
         if (q.kc_ok && b == q.cc) {
             acc += q.kapcen;
             any = true;
+        }
+        if (q.kind == 1) {
+            if (b == q.ci) continue;
+            const int64_t pd = (int64_t)h * a.n_layers + d;
+            const bool red = b > q.ci;
+            const int64_t o = red ? (int64_t)b - q.ci : (int64_t)q.ci - b;
+            const int2 wk = a.walk[pd * 2 + (red ? 0 : 1)];
+            if (o >= wk.x && o < wk.y) {
+                acc += f19_aut_value(a, q, b);
+                any = true;
+            }
+            continue;
         }
         const int ci = q.ci, ns = q.nstep;
         if (ns <= 0 || ci + ns < 0 || ci - ns >= n) continue;
@@ -944,6 +1021,9 @@ static cudaError_t launch_f19_t(const F19Args& a, R* cube, cudaStream_t s) {
     const int64_t nhd = (int64_t)a.n_f19 * a.n_layers;
     f19_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    f19_march_kernel<R><<<(unsigned)((nhd * 2 * 32 + 127) / 128), 128, 0, s>>>(a);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int64_t cells = (int64_t)a.n_layers * a.n_wl;
     if (cells > 0) f19_gather_kernel<R><<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(a, cube);

@@ -253,9 +253,12 @@ struct HeArgs {
 // One (fort.19 NORMAL line, depth): gates, KAPCEN and the wing of
 // _accumulate_metal_profile_kernel (near profile to N10DOP or the first value
 // below KAPMIN, else far wings X / n^2 to MAXSTEP).
+// Autoionizing lines (kind 1) use kappa0, kapcen (= kappa0 at the centre
+// bin cc), and tabstep/dvoigt/x_far as the line frequency, the width and
+// ASHORE, adamp as BSHORE, with their walks in F19Args::walk.
 struct F19Par {
     double kappa0, adamp, tabstep, dvoigt, x_far, kapcen;
-    int ci, cc, n10, nstep, early, active, kc_ok, d;
+    int ci, cc, n10, nstep, early, active, kc_ok, d, kind, pad;
 };
 
 struct F19Args {
@@ -263,8 +266,10 @@ struct F19Args {
     int64_t n_wl, n_lines;
     int* flags;                               // FLAG_F19_LINE
     const int32_t* rows;                      // per line: catalog row, in catalog order
+    const int32_t* kind;                      // per line: 0 NORMAL, 1 autoionizing
     const double *cgf, *gamma_rad, *gamma_stark, *gamma_vdw;  // per line: fort.19 record values
-                                              // (single-precision values held in double)
+                                              // (single-precision values held in double; the
+                                              // autoionizing lines' gf in cgf)
     const double *wavelength, *elo;           // catalog columns
     const int32_t *element_idx, *ion_stage, *center;
     const double* grid;
@@ -274,6 +279,7 @@ struct F19Args {
     const void *cabs, *cscat;
     const double *extab, *extabf, *h0, *h1, *h2;
     F19Par* par;                              // [n_f19, L]
+    int2* walk;                               // [n_f19, L, 2] autoionizing walks [x, y), red, blue
 };
 
 // ---- batched launches -------------------------------------------------------

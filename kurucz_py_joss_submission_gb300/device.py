@@ -193,37 +193,57 @@ class DeviceCatalog:
             rec.hydrogen_n_lower = self.t["hydrogen_n_lower"].data_ptr()
             rec.hydrogen_n_upper = self.t["hydrogen_n_upper"].data_ptr()
         # fort.19 lines (io/lines/fort19.py:343-347) other than hydrogen and
-        # helium: the NORMAL ones (line type 0 with NBLO/NBUP set) get
-        # _add_fort19_asynth's profiles (engine/opacity.py:1335-1488) here;
-        # autoionizing lines (TYPE 1) and NORMAL lines whose fort.19 record
-        # carries continuum-merge limits (NCON = ISO2 with ISO1 = 0, on a
-        # species of its CONTX table) are not modelled
+        # helium: the NORMAL ones (line type 0 with NBLO/NBUP set) and the
+        # autoionizing ones (TYPE 1) get _add_fort19_asynth's profiles
+        # (engine/opacity.py:1335-1541) here; NORMAL lines whose fort.19
+        # record carries continuum-merge limits (NCON = ISO2 with ISO1 = 0, on
+        # a species of its CONTX table) are not modelled
         nb = np.abs(np.asarray(cat.n_lower)) + np.abs(np.asarray(cat.n_upper))
         ncon = np.where((np.asarray(cat.iso1) == 0) & (np.asarray(cat.iso2) > 0), np.asarray(cat.iso2), 0)
         codex = np.any(np.isclose(np.asarray(cat.code)[:, None], FORT19_CODEX[None, :], rtol=0.0, atol=1e-3),
                        axis=1)
-        normal = (lt == 0) & (nb != 0) & (np.asarray(cat.element_idx) >= 0) & (np.asarray(cat.ion_stages) >= 1)
+        known = (np.asarray(cat.element_idx) >= 0) & (np.asarray(cat.ion_stages) >= 1)
+        normal = (lt == 0) & (nb != 0) & known
         tapered = normal & (ncon > 0) & codex
-        f19 = np.flatnonzero(normal & ~tapered)
-        self.n_fort19_skipped = int(np.count_nonzero(lt == 1) + np.count_nonzero(tapered))
+        aut = (lt == 1) & known
+        f19 = np.flatnonzero((normal & ~tapered) | aut)
+        self.n_fort19_skipped = int(np.count_nonzero(tapered))
         if self.n_fort19_skipped:
-            warnings.warn(f"{self.n_fort19_skipped} fort.19 lines (autoionizing, or with continuum-merge "
-                          "limits) contribute no opacity here", RuntimeWarning, stacklevel=2)
+            warnings.warn(f"{self.n_fort19_skipped} fort.19 lines with continuum-merge limits contribute "
+                          "no opacity here", RuntimeWarning, stacklevel=2)
         self.n_f19 = int(f19.size)
         if self.n_f19 > 256:
             raise ValueError(f"{self.n_f19} fort.19 lines: the synthesis takes at most 256")
         if self.n_f19:
+            is_aut = lt[f19] == 1
             wl = np.asarray(cat.wavelength)[f19]
             gf = 10.0 ** np.asarray(cat.log_gf, dtype=np.float64)[f19]
             freq = 2.99792458e17 / np.maximum(wl, 1.0e-30)
-            # the fort.19 record's single-precision fields (fort19.py:379-402)
+            denom = 12.5664 * freq
+            # the fort.19 record's single-precision fields (fort19.py:352-402):
+            # NORMAL lines CGF and the normalised damping constants,
+            # autoionizing lines gf and the damping constants of the gfall
+            # logs (a positive GS encodes a negative ASHORE)
             f32 = lambda x: np.asarray(x, dtype=np.float32).astype(np.float64)  # noqa: E731
+            grl, gsl, gwl = (np.asarray(getattr(cat, k))[f19] for k in
+                             ("gamma_rad_log", "gamma_stark_log", "gamma_vdw_log"))
+            g_r, g_s, g_w = (np.asarray(getattr(cat, k))[f19] for k in ("gamma_rad", "gamma_stark", "gamma_vdw"))
+            with np.errstate(over="ignore"):
+                aut_r = np.where(grl != 0.0, 10.0 ** grl, g_r * denom)
+                aut_s = np.where(gsl > 0.0, -(10.0 ** (-gsl)), np.where(gsl < 0.0, 10.0 ** gsl, g_s * denom))
+                aut_w = np.where(gwl != 0.0, 10.0 ** gwl, g_w * denom)
+            vals = {
+                "cgf": f32(np.where(is_aut, gf, (0.026538 / 1.77245) * gf / freq)),
+                "gamma_rad": f32(np.where(is_aut, aut_r, g_r)),
+                "gamma_stark": f32(np.where(is_aut, aut_s, g_s)),
+                "gamma_vdw": f32(np.where(is_aut, aut_w, g_w)),
+            }
             self.t["f19_rows"] = _dev(f19 if self.order is None else inv_order(self.order)[f19], np.int32, dev)
-            self.t["f19_cgf"] = _dev(f32((0.026538 / 1.77245) * gf / freq), np.float64, dev)
-            for k in ("gamma_rad", "gamma_stark", "gamma_vdw"):
-                self.t["f19_" + k] = _dev(f32(np.asarray(getattr(cat, k))[f19]), np.float64, dev)
+            self.t["f19_kind"] = _dev(is_aut.astype(np.int32), np.int32, dev)
+            for k, v in vals.items():
+                self.t["f19_" + k] = _dev(v, np.float64, dev)
             rec.n_f19 = self.n_f19
-            for k in ("rows", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw"):
+            for k in ("rows", "kind", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw"):
                 setattr(rec, "f19_" + k, self.t["f19_" + k].data_ptr())
         # helium lines (line types -3/-4/-6; engine/opacity.py:2531-2544): the
         # helium wing pass, device rows in catalog order

@@ -43,6 +43,9 @@ class LineCatalog:
     n_upper: np.ndarray   # NBUP
     iso1: np.ndarray      # ISO1 / ISO2 (isotope numbers; ISO2 doubles as fort.19's continuum index)
     iso2: np.ndarray
+    gamma_rad_log: np.ndarray    # GR / GS / GW as read (log10, 0 when blank)
+    gamma_stark_log: np.ndarray
+    gamma_vdw_log: np.ndarray
 
     def __len__(self) -> int:
         return int(self.wavelength.size)
@@ -92,6 +95,7 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
             asynth_mask=np.zeros(n, np.uint8), code=np.zeros(n), catalog_index=np.zeros(n, np.int64),
             n_lower=np.zeros(n, np.int32), n_upper=np.zeros(n, np.int32),
             iso1=np.zeros(n, np.int32), iso2=np.zeros(n, np.int32),
+            gamma_rad_log=np.zeros(n), gamma_stark_log=np.zeros(n), gamma_vdw_log=np.zeros(n),
         )
         order = ["wavelength", "log_gf", "gf", "cgf", "excitation_energy", "gamma_rad", "gamma_stark",
                  "gamma_vdw", "element_idx", "ion_stages", "line_types", "process_mask",
@@ -101,6 +105,8 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
                                               cols["n_upper"].ctypes.data_as(C.c_void_p)))
         _native.check(L.ks_gfall_fetch_iso(h, cols["iso1"].ctypes.data_as(C.c_void_p),
                                            cols["iso2"].ctypes.data_as(C.c_void_p)))
+        _native.check(L.ks_gfall_fetch_gamma_logs(h, *[cols[k].ctypes.data_as(C.c_void_p) for k in
+                                                       ("gamma_rad_log", "gamma_stark_log", "gamma_vdw_log")]))
     finally:
         L.ks_gfall_free(h)
     return LineCatalog(**cols)

@@ -220,6 +220,7 @@ class LineDraw:
     log_gamma_vdw: np.ndarray
     n_lower: Optional[np.ndarray] = None   # NBLO / NBUP of hydrogen lines (None: blank)
     n_upper: Optional[np.ndarray] = None
+    tag: Optional[np.ndarray] = None       # columns 142-144 ("AUT": autoionizing; None: blank)
 
     def __len__(self) -> int:
         return int(self.wavelength_nm.size)
@@ -374,12 +375,18 @@ def random_band_lines(n_lines: int, wl_min: float, wl_max: float, seed: int,
 
 def merge_lines(*draws: LineDraw) -> LineDraw:
     """Concatenate line draws, sorted by wavelength (stable)."""
+    tags = None
+    if any(d.tag is not None for d in draws):
+        tags = np.concatenate([d.tag if d.tag is not None else np.array([""] * len(d), dtype=object)
+                               for d in draws]).astype(object)
     cat = {f: np.concatenate([getattr(d, f) for d in draws]) for f in
            ("wavelength_nm", "log_gf", "code", "e_lower_cm", "log_gamma_rad", "log_gamma_stark",
             "log_gamma_vdw")}
     if any(d.n_lower is not None for d in draws):
         cat["n_lower"] = np.concatenate([d.levels()[0] for d in draws])
         cat["n_upper"] = np.concatenate([d.levels()[1] for d in draws])
+    if tags is not None:
+        cat["tag"] = tags
     order = np.argsort(cat["wavelength_nm"], kind="stable")
     return LineDraw(**{k: v[order] for k, v in cat.items()})
 
@@ -406,6 +413,9 @@ def format_gfall(lines: LineDraw) -> str:
         if nlo[i] > 0 or nup[i] > 0:
             # REF (4 columns) blank, then NBLO and NBUP (I2 each, columns 103-106)
             tail = f"{'':4s}{nlo[i]:2d}{nup[i]:2d}" + " " * (160 - 106)
+        if lines.tag is not None and str(lines.tag[i]).strip():
+            # the 3-character tag of columns 142-144 (AUT, COR, PRD)
+            tail = tail[:141 - 98] + f"{str(lines.tag[i]):3.3s}" + tail[144 - 98:]
         rows.append(
             f"{wl[i]:11.4f}{lines.log_gf[i]:7.3f}{lines.code[i]:6.2f}{e[i]:12.3f}"
             f"{1.0:5.1f} {'SYNTH   '}{'  '}{ep[i]:12.3f}{2.0:5.1f} {'SYNTH   '}{'  '}"

@@ -1,5 +1,5 @@
-"""CPU restatement of the reference's fort.19 NORMAL-line profiles -- test
-infrastructure.
+"""CPU restatement of the reference's fort.19 NORMAL-line and autoionizing-line
+profiles -- test infrastructure.
 
 Only ``tests/`` use this module, to check the GPU kernels for these lines.
 
@@ -22,8 +22,12 @@ ASYNTH as TMP x STIM per layer:
   KAPMIN, else far wings X / n^2 to MAXSTEP; then every step from 1 to NSTEP
   added, red and blue, without a cutoff test.
 
-Lines whose fort.19 continuum index is set (NCON > 0 with an element of the
-CONTX table) taper their wings at WCON/WTAIL; they are not restated here.
+Autoionizing lines (TYPE 1, the gfall AUT tag) take the Fano-type profile of
+``_accumulate_autoionizing_profile`` (opacity.py:901-963) with KAPPA0 =
+BSHORE GF XNFPEL BOLT (:1522-1541) in the same per-layer buffer, in fort.19
+order.  Lines whose fort.19 continuum index is set (NCON > 0 with an element
+of the CONTX table) taper their wings at WCON/WTAIL; they are not restated
+here, nor are merged-continuum records.
 """
 
 from __future__ import annotations
@@ -51,6 +55,55 @@ def normal_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
     nb = np.abs(np.asarray(cat["n_lower"])) + np.abs(np.asarray(cat["n_upper"]))
     known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
     return np.flatnonzero((lt == 0) & (nb != 0) & known & (np.asarray(cat["ion_stage"]) >= 1))
+
+
+def aut_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
+    """Catalog rows of autoionizing lines (TYPE 1: the gfall AUT tag)."""
+    known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
+    return np.flatnonzero((np.asarray(cat["line_type"]) == 1) & known & (np.asarray(cat["ion_stage"]) >= 1))
+
+
+def aut_record_values(cat: Dict[str, np.ndarray], rows: np.ndarray) -> Dict[str, np.ndarray]:
+    """fort.19 fields of autoionizing lines (fort19.py:352-373, :387): gf and
+    the unnormalised damping constants from the gfall logs (GS > 0 encodes a
+    negative ASHORE), single precision."""
+    wl = np.asarray(cat["wavelength"])[rows]
+    denom = 12.5664 * (C_LIGHT_NM / np.maximum(wl, 1.0e-30))
+    grl = np.asarray(cat["gamma_rad_log"])[rows]
+    gsl = np.asarray(cat["gamma_stark_log"])[rows]
+    gwl = np.asarray(cat["gamma_vdw_log"])[rows]
+    gr = np.where(grl != 0.0, 10.0 ** grl, np.asarray(cat["gamma_rad"])[rows] * denom)
+    gs = np.where(gsl > 0.0, -(10.0 ** (-gsl)),
+                  np.where(gsl < 0.0, 10.0 ** gsl, np.asarray(cat["gamma_stark"])[rows] * denom))
+    gw = np.where(gwl != 0.0, 10.0 ** gwl, np.asarray(cat["gamma_vdw"])[rows] * denom)
+    f32 = lambda x: np.asarray(x, dtype=np.float32).astype(np.float64)  # noqa: E731
+    return dict(gf=f32(10.0 ** np.asarray(cat["log_gf"])[rows]), gamma_rad=f32(gr), gamma_stark=f32(gs),
+                gamma_vdw=f32(gw))
+
+
+def _autoionizing(tmp, cont, grid, ci, wl, kappa0, gr, gs, gw, cutoff):
+    """_accumulate_autoionizing_profile (opacity.py:901-963), including its
+    Python indexing of a centre bin -1 (a line below the grid): the centre
+    value and its cutoff go to the last bin."""
+    n = grid.size
+    cc = ci if ci >= 0 else n + ci
+    if kappa0 < cont[cc] * cutoff or kappa0 <= 0.0:
+        return
+    fc = C_LIGHT_CM / (wl * 1e-7)
+    gamma = max(abs(gr), 1e-30)
+    ashore = gs
+    bshore = gw if abs(gw) >= 1e-30 else 1e-30
+    tmp[cc] += kappa0
+    for sgn in (1, -1):
+        for o in range(1, max(ci, n - ci - 1) + 1):
+            b = ci + sgn * o
+            if b >= n or b < 0:
+                break
+            eps = 2.0 * (C_LIGHT_CM / (grid[b] * 1e-7) - fc) / gamma
+            v = kappa0 * (ashore * eps + bshore) / (eps * eps + 1.0) / bshore
+            if v <= 0.0 or v < cont[b] * cutoff:
+                break
+            tmp[b] += v
 
 
 def record_values(cat: Dict[str, np.ndarray], rows: np.ndarray) -> Dict[str, np.ndarray]:
@@ -151,6 +204,12 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
     L, N = continuum.shape
     rows = normal_rows(cat)
     rec = record_values(cat, rows)
+    arows = aut_rows(cat)
+    arec = aut_record_values(cat, arows)
+    # fort.19 order = catalog order, both kinds interleaved
+    kind = {int(i): ("n", j) for j, i in enumerate(rows)}
+    kind.update({int(i): ("a", j) for j, i in enumerate(arows)})
+    order = sorted(kind)
     pop = np.asarray(atm["population_per_ion"])
     rho = np.asarray(atm["mass_density"])
     xne = np.asarray(atm["electron_density"])
@@ -161,7 +220,8 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
     out = np.zeros((L, N))
     for d in range(L):
         tmp = np.zeros(N)
-        for j, i in enumerate(rows):
+        for i in order:
+            k, j = kind[i]
             z = int(cat["nelem"][i]) - 1
             ion = int(cat["ion_stage"][i])
             pv = float(pop[d, ion - 1, z]) if ion <= pop.shape[1] else 0.0
@@ -174,6 +234,12 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
                 continue
             r = float(rho[d])
             if r <= 0.0:
+                continue
+            if k == "a":
+                # XLINOP label 700: KAPPA0 = BSHORE * GF * XNFPEL * BOLT (opacity.py:1522-1541)
+                k0 = arec["gamma_vdw"][j] * arec["gf"][j] * (pv / r) * boltz
+                _autoionizing(tmp, continuum[d], grid, ci, wl, k0, arec["gamma_rad"][j],
+                              arec["gamma_stark"][j], arec["gamma_vdw"][j], cutoff)
                 continue
             dw = line_doppler(atm, d, wl, microturb_kms)
             if wl <= 0.0 or dw <= 0.0:

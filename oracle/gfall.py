@@ -189,9 +189,10 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
             lt = -3
         elif nelem == 2 and ion == 2:
             lt = -6
-        rows.append((wavelength, log_gf, code, elo, gr, gs, gw, nelem, ion, lt, nblo, nbup, line_size))
+        rows.append((wavelength, log_gf, code, elo, gr, gs, gw, nelem, ion, lt, nblo, nbup, line_size,
+                     grl, gsl, gwl))
     if not rows:
-        arr = np.zeros((0, 13))
+        arr = np.zeros((0, 16))
     else:
         arr = np.array(rows, dtype=np.float64)
     return {
@@ -208,6 +209,9 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
         "n_lower": arr[:, 10].astype(np.int32),
         "n_upper": arr[:, 11].astype(np.int32),
         "line_size": arr[:, 12].astype(np.int32),
+        "gamma_rad_log": arr[:, 13].copy(),
+        "gamma_stark_log": arr[:, 14].copy(),
+        "gamma_vdw_log": arr[:, 15].copy(),
     }
 
 

@@ -121,6 +121,11 @@ CASES = {
     "fort19_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
                            n_lines=160, draw=(499.85, 501.15), log_uniform=False, seed=24,
                            nb_every=4),
+    # autoionizing lines (gfall AUT tag, every 5th line; ASHORE of both
+    # signs): the fort.19 Fano-type profile (engine/opacity.py:901-963)
+    "aut_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
+                        n_lines=150, draw=(499.85, 501.15), log_uniform=False, seed=25,
+                        aut_every=5),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -156,6 +161,16 @@ def case_lines(case: dict) -> workloads.LineDraw:
         idx = np.arange(0, len(lines), k)
         lines.log_gf[idx] = np.maximum(lines.log_gf[idx], -0.5)   # strong enough to pass the gates
         lines.e_lower_cm[idx] = np.minimum(lines.e_lower_cm[idx], 20000.0)
+    if case.get("aut_every"):
+        k = case["aut_every"]
+        idx = np.arange(0, len(lines), k)
+        tag = np.array([""] * len(lines), dtype=object)
+        tag[idx] = "AUT"
+        lines.tag = tag
+        lines.log_gamma_rad[idx] = 11.0
+        lines.log_gamma_stark[idx] = np.where(np.arange(idx.size) % 2 == 0, -0.5, 0.3)
+        lines.log_gamma_vdw[idx] = 0.3
+        lines.log_gf[idx] = np.minimum(lines.log_gf[idx], -1.0) - 12.0
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth
         # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)

@@ -36,6 +36,21 @@ def test_oracle_asynth_with_fort19_lines():
     assert np.count_nonzero(term) > 10000
 
 
+@pytest.mark.skipif("aut_500_501" not in available_cases(), reason="golden missing")
+def test_oracle_asynth_with_autoionizing_lines():
+    name = "aut_500_501"
+    g = golden(name)
+    w0, w1 = window(name)
+    tb = oracle.tables()
+    cat = gfall.filter_window(gfall.parse_gfall(gfall_path(name), tb["potion"]), w0, w1)
+    assert fort19.aut_rows(cat).size >= 20
+    gs = cat["gamma_stark_log"][fort19.aut_rows(cat)]
+    assert np.any(gs > 0) and np.any(gs < 0)   # ASHORE of both signs
+    r = oracle.synthesize(oracle.load_atmosphere(atm_path(name)), cat, w0, w1, tb=tb)
+    rel = np.abs(r["asynth"] - g["asynth"]) / np.maximum(np.abs(g["asynth"]), 1e-300)
+    assert float(rel.max()) < 1e-13
+
+
 def test_oracle_detects_planted_error():
     g = golden(CASE)
     w0, w1 = window(CASE)
@@ -55,6 +70,7 @@ def test_reader_fields_and_routing():
     nb = (cat.n_lower != 0) | (cat.n_upper != 0)
     assert nb.sum() >= 30 and np.all(cat.process_mask[nb] == 0)   # they leave TRANSP
     assert np.all(cat.iso1 == 0) and np.all(cat.iso2 == 0)
+    assert np.all(cat.gamma_rad_log[nb] != 0.0)   # the logs as read
 
 
 def test_batch_rejects_fort19_lines():

@@ -7,7 +7,9 @@ ASYNTH before the hydrogen lines.  Checked against the reference's golden
 case) and here against the oracle where no golden exists: microturbulence
 in the lines' Doppler widths, damping large enough for the Voigt branch
 (ADAMP >= 0.2), a line centred below the grid (the reference's clamped
-KAPCEN bin and wing from bin 0), and a raised cutoff.
+KAPCEN bin and wing from bin 0), a raised cutoff, and autoionizing lines
+(TYPE 1) interleaved with them, one of them below the grid (its centre value
+on the last grid point, as the reference's Python index -1 puts it).
 
 Tolerance: FP64 cube within 1e-11 relative of the oracle's.
 """
@@ -46,7 +48,7 @@ def gpu_cubes(cat, atm, grid, **opt):
     return dcat, with_f, without
 
 
-def draw(w0, w1, seed, gw_shift=0.0, extra=None):
+def draw(w0, w1, seed, gw_shift=0.0, extra=None, aut=False):
     d = workloads.random_atomic_lines(80, w0 - 0.15, w1 + 0.15, seed=seed)
     lo, up = d.levels()
     lo, up = lo.copy(), up.copy()
@@ -56,8 +58,31 @@ def draw(w0, w1, seed, gw_shift=0.0, extra=None):
     d.log_gf[idx] = np.maximum(d.log_gf[idx], -0.5)
     d.e_lower_cm[idx] = np.minimum(d.e_lower_cm[idx], 20000.0)
     d.log_gamma_vdw[idx] += gw_shift
+    if aut:
+        # autoionizing lines between them (interleaved in fort.19 order)
+        ia = np.arange(1, len(d), 4)
+        tag = np.array([""] * len(d), dtype=object)
+        tag[ia] = "AUT"
+        d.tag = tag
+        d.log_gamma_rad[ia] = 11.0
+        d.log_gamma_stark[ia] = np.where(np.arange(ia.size) % 2 == 0, -0.5, 0.3)
+        d.log_gamma_vdw[ia] = 0.3
+        d.log_gf[ia] = np.minimum(d.log_gf[ia], -1.0) - 12.0
     if extra is not None:
         d = workloads.merge_lines(d, extra)
+    return d
+
+
+def below_grid_aut(w0):
+    """One autoionizing Fe I line below the grid: the reference puts its centre
+    value on the last grid point (Python index -1)."""
+    d = below_grid_line(w0)
+    d.n_lower = d.n_upper = None
+    d.tag = np.array(["AUT"], dtype=object)
+    d.log_gamma_rad[:] = 11.0
+    d.log_gamma_stark[:] = -0.5
+    d.log_gamma_vdw[:] = 0.3
+    d.log_gf[:] = -13.0
     return d
 
 
@@ -76,6 +101,9 @@ CASES = {
     "voigt_branch": (500.0, 500.8, dict(seed=32, gw_shift=3.0), {}),
     "below_grid": (500.0, 500.8, dict(seed=33, extra="below"), {}),
     "cutoff": (500.0, 500.8, dict(seed=34), {"cutoff": 1e-2}),
+    # NORMAL and autoionizing lines interleaved; an autoionizing line below the grid
+    "with_aut": (500.0, 500.8, dict(seed=35, aut=True), {}),
+    "aut_below": (500.0, 500.8, dict(seed=36, aut=True, extra="below_aut"), {}),
 }
 
 
@@ -83,8 +111,11 @@ CASES = {
 def test_fp64_matches_oracle(key, tmp_path):
     w0, w1, kw, opt = CASES[key]
     kw = dict(kw)
-    if kw.pop("extra", None) == "below":
+    extra = kw.pop("extra", None)
+    if extra == "below":
         kw["extra"] = below_grid_line(w0)
+    elif extra == "below_aut":
+        kw["extra"] = below_grid_aut(w0)
     p = tmp_path / "lines.gf"
     p.write_text(workloads.format_gfall(draw(w0, w1, **kw)))
     cat = atomic.load_catalog_window(p, w0, w1)
@@ -101,6 +132,10 @@ def test_fp64_matches_oracle(key, tmp_path):
     assert np.count_nonzero(term) > 1000
     ref = without + term
     assert float(np.max(np.abs(with_f - ref) / np.maximum(np.abs(ref), 1e-300))) < FP64_TOL
+    c = oracle.center_indices(grid, ocat["wavelength"])
     if key == "below_grid":
-        c = oracle.center_indices(grid, ocat["wavelength"])
         assert np.any(c[fort19.normal_rows(dict(ocat, center=c))] < 0)
+    if key.startswith("aut") or key == "with_aut":
+        assert fort19.aut_rows(ocat).size >= 10
+    if key == "aut_below":
+        assert np.any(c[fort19.aut_rows(ocat)] < 0)
