@@ -130,11 +130,16 @@ typedef struct {
     int32_t n_f19;
     const int32_t *f19_rows;
     const double *f19_cgf, *f19_gamma_rad, *f19_gamma_stark, *f19_gamma_vdw;
-    /* per fort.19 line: 0 NORMAL, 1 autoionizing (gfall AUT tag: the profile
+    /* per fort.19 line: 0 NORMAL, 1 autoionizing, 2 merged continuum (the AUT tag: the profile
      * of _accumulate_autoionizing_profile, opacity.py:901-963, with KAPPA0 =
      * BSHORE GF XNFPEL BOLT; f19_cgf then holds gf and f19_gamma_* the
      * record's unnormalised GAMMAR, ASHORE, BSHORE, fort19.py:352-373) */
     const int32_t *f19_kind;
+    /* per fort.19 line, merged-continuum records (kind 2: LABELP CONTINUU,
+     * NLAST > 3; _accumulate_merged_continuum, opacity.py:863-898, f19_cgf
+     * holding gf (2 XJ + 1)): NLAST and the record's ion index NELION
+     * (fort19.py:323-328); unread for the other kinds */
+    const int32_t *f19_nlast, *f19_nelion;
 } ks_lines;
 
 typedef struct {
@@ -594,6 +599,11 @@ ks_status ks_gfall_fetch_iso(const ks_gfall *g, int32_t *iso1, int32_t *iso2);
  * order as ks_gfall_fetch. */
 ks_status ks_gfall_fetch_gamma_logs(const ks_gfall *g, double *gamma_rad_log, double *gamma_stark_log,
                                     double *gamma_vdw_log);
+/* XJ / XJP of every record (columns 37-41, 65-69) and whether its LABELP
+ * begins with CONTINUU (io/lines/atomic.py:338-340): fort.19 turns such a
+ * record into a merged-continuum record with NLAST = XJP (or NBUP) and gf x
+ * (2 XJ + 1) (io/lines/fort19.py:304-307).  Same order as ks_gfall_fetch. */
+ks_status ks_gfall_fetch_j(const ks_gfall *g, double *xj, double *xjp, uint8_t *continuum_label);
 void ks_gfall_free(ks_gfall *g);
 
 #ifdef __cplusplus

@@ -75,6 +75,7 @@ class KsLines(C.Structure):
         ("n_helium", C.c_int32), ("helium_rows", P),
         ("n_f19", C.c_int32), ("f19_rows", P), ("f19_cgf", P), ("f19_gamma_rad", P),
         ("f19_gamma_stark", P), ("f19_gamma_vdw", P), ("f19_kind", P),
+        ("f19_nlast", P), ("f19_nelion", P),
     ]
 
 
@@ -228,6 +229,7 @@ SIGNATURES = {
     "ks_gfall_fetch_levels": (C.c_int32, [P, P, P]),
     "ks_gfall_fetch_iso": (C.c_int32, [P, P, P]),
     "ks_gfall_fetch_gamma_logs": (C.c_int32, [P, P, P, P]),
+    "ks_gfall_fetch_j": (C.c_int32, [P, P, P, P]),
     "ks_gfall_free": (None, [P]),
 }
 

@@ -43,7 +43,7 @@ ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(co
 
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
-    if (minor) *minor = 4;
+    if (minor) *minor = 5;
     return KS_OK;
 }
 
@@ -741,7 +741,7 @@ static ks_status check_lines(const ks_lines* l) {
     if (l->n_f19 < 0 || l->n_f19 > l->n_lines) return fail(KS_ERR_INVALID, "n_f19 must lie in [0, n_lines]");
     if (l->n_f19 > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 fort.19 lines");
     if (l->n_f19 > 0 && (!l->f19_rows || !l->f19_cgf || !l->f19_gamma_rad || !l->f19_gamma_stark ||
-                         !l->f19_gamma_vdw || !l->f19_kind))
+                         !l->f19_gamma_vdw || !l->f19_kind || !l->f19_nlast || !l->f19_nelion))
         return fail(KS_ERR_INVALID, "lines: a fort.19 column is NULL");
     return KS_OK;
 }
@@ -1267,6 +1267,8 @@ static ks_status run_f19(const ks_lines* lines, const ks_atmos* atm, const ks_gr
     f.flags = w.flags;
     f.rows = lines->f19_rows;
     f.kind = lines->f19_kind;
+    f.nlast = lines->f19_nlast;
+    f.nelion = lines->f19_nelion;
     f.cgf = lines->f19_cgf;
     f.gamma_rad = lines->f19_gamma_rad;
     f.gamma_stark = lines->f19_gamma_stark;

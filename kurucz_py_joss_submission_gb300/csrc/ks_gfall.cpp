@@ -41,6 +41,8 @@ struct Rec {
     double wl, loggf, code, elo, gr, gs, gw;
     int nelem, ion, lt, nblo, nbup, line_size, anum, iso1, iso2;
     double grl, gsl, gwl;  // the GR / GS / GW fields as read (log10; 0 when blank)
+    double xj, xjp;        // J of the lower / upper level (columns 37-41, 65-69; 0 when blank)
+    bool continuum_label;  // LABELP begins with CONTINUU (a merged-continuum record)
     bool is_h_elem;  // element symbol is H / D (DELLIM special case)
 };
 
@@ -162,6 +164,21 @@ bool parse_fixed(const char* line, int len, const double* potion, int np, Rec* r
     if (em) gsl = 0.0;
     if (!field_float(line, len, 92, 98, &gwl, &em)) return false;
     if (em) gwl = 0.0;
+    double xj = 0.0, xjp = 0.0;
+    if (!field_float(line, len, 36, 41, &xj, &em)) return false;
+    if (em) xj = 0.0;
+    if (!field_float(line, len, 64, 69, &xjp, &em)) return false;
+    if (em) xjp = 0.0;
+    bool cont_label = false;
+    if (len >= 78) {
+        // LABELP (columns 71-78), stripped and upper-cased, starts with CONTINUU
+        int a0 = 70, a1 = 78;
+        while (a0 < a1 && std::isspace((unsigned char)line[a0])) a0++;
+        const char* key = "CONTINUU";
+        cont_label = a1 - a0 >= 8;
+        for (int k = 0; cont_label && k < 8; k++)
+            if (std::toupper((unsigned char)line[a0 + k]) != key[k]) cont_label = false;
+    }
     double x1 = 0.0, x2 = 0.0, v;
     if (len >= 115 && field_float(line, len, 109, 115, &v, &em) && !em) x1 = v;
     if (len >= 124 && field_float(line, len, 118, 124, &v, &em) && !em) x2 = v;
@@ -272,6 +289,9 @@ bool parse_fixed(const char* line, int len, const double* potion, int np, Rec* r
     r->grl = grl;
     r->gsl = gsl;
     r->gwl = gwl;
+    r->xj = xj;
+    r->xjp = xjp;
+    r->continuum_label = cont_label;
     // element symbol: tfort symbols up to U, else "Z<n>" (unknown to TRANSP)
     r->anum = (nelem > 0 && nelem < kNSym) ? nelem : 0;
     r->is_h_elem = nelem == 1;
@@ -332,6 +352,8 @@ bool parse_ws(const char* line, int len, Rec* r) {
     r->iso1 = 0;
     r->iso2 = 0;
     r->grl = r->gsl = r->gwl = 0.0;
+    r->xj = r->xjp = 0.0;
+    r->continuum_label = false;
     r->anum = z;
     std::string u;
     for (char ch : el) u += (char)std::toupper((unsigned char)ch);
@@ -491,6 +513,16 @@ extern "C" ks_status ks_gfall_fetch_gamma_logs(const ks_gfall* g, double* gr, do
         if (gr) gr[k] = g->recs[k].grl;
         if (gs) gs[k] = g->recs[k].gsl;
         if (gw) gw[k] = g->recs[k].gwl;
+    }
+    return KS_OK;
+}
+
+extern "C" ks_status ks_gfall_fetch_j(const ks_gfall* g, double* xj, double* xjp, uint8_t* continuum_label) {
+    if (!g) return KS_ERR_INVALID;
+    for (size_t k = 0; k < g->recs.size(); k++) {
+        if (xj) xj[k] = g->recs[k].xj;
+        if (xjp) xjp[k] = g->recs[k].xjp;
+        if (continuum_label) continuum_label[k] = g->recs[k].continuum_label ? 1 : 0;
     }
     return KS_OK;
 }

@@ -793,6 +793,76 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
         return;
     }
     const double boltz = fastex(a.elo[row] * dp.hckt, a.extab, a.extabf);
+    if (a.kind[h] == 2) {
+        // merged continuum: KAPPA = GF XNFPEL BOLT (opacity.py:1489-1497), the
+        // merge and tail wavelengths of _compute_merged_continuum_limits
+        // (:723-758) and the ramp of _accumulate_merged_continuum (:863-898)
+        q.kind = 2;
+        const double kappa = a.cgf[h] * (pv / dp.rho) * boltz;
+        if (!(kappa > 0.0)) {
+            a.par[i] = q;
+            return;
+        }
+        const double xne = fmax(dp.xne, 1e-40);
+        const double nmerge = fmax(1600.0 / pow(xne, 2.0 / 15.0) - 1.5, 1.0);
+        const double nm2 = fmax(nmerge * nmerge, 1e-12);
+        const int ionx = a.nelion[h], nlast = a.nlast[h];
+        double wmerge = wl, wtail = wl;
+        if (wl > 0.0 && nlast > 0) {
+            const double ryd = ionx == 1 ? 109677.576 : 109737.312;
+            const double dshift = 1.0e7 / wl - ryd / (double)(nlast * nlast);
+            if (fabs(dshift) > 1e-12) {
+                const double wshift = 1.0e7 / dshift;
+                const double em = ionx == 1 ? 109677.576 / nm2 : 109737.312 / nm2;
+                const double dmerge = 1.0e7 / wl - em;
+                if (fabs(dmerge) > 1e-12) {
+                    double wm = 1.0e7 / dmerge;
+                    if (wm < 0.0) wm = wshift + wshift;
+                    wm = wshift > wm ? wshift : wm;
+                    wm = (wshift + wshift) < wm ? wshift + wshift : wm;
+                    wmerge = wm;
+                    const double dtail = 1.0e7 / wm - 500.0;
+                    if (fabs(dtail) > 1e-12) {
+                        double wt = 1.0e7 / dtail;
+                        if (wt < 0.0) wt = wm + wm;
+                        wtail = (wm + wm) < wt ? wm + wm : wt;
+                    }
+                }
+            }
+        }
+        // searchsorted left / right on the grid
+        int64_t lo = 0, hi = n;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (a.grid[mid] < wmerge) lo = mid + 1;
+            else hi = mid;
+        }
+        const int64_t i_merge = lo;
+        lo = 0;
+        hi = n;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (a.grid[mid] <= wtail) lo = mid + 1;
+            else hi = mid;
+        }
+        const int64_t i_tail = lo < n ? lo : n;
+        const int64_t i_start = ci > 0 ? ci : 0;
+        if (i_tail <= i_start) {
+            a.par[i] = q;
+            return;
+        }
+        const int64_t denom = i_tail - (i_merge > i_start ? i_merge : i_start);
+        q.kappa0 = kappa;
+        q.tabstep = wl;
+        q.ci = ci;
+        q.cc = (int)i_start;
+        q.n10 = (int)i_merge;
+        q.nstep = (int)i_tail;
+        q.early = (int)(denom > 1 ? denom : 1);
+        q.active = 1;
+        a.par[i] = q;
+        return;
+    }
     if (a.kind[h] == 1) {
         // autoionizing: KAPPA0 = BSHORE GF XNFPEL BOLT (opacity.py:1522-1541), then
         // _accumulate_autoionizing_profile (:901-963); a centre bin -1 (line
@@ -918,6 +988,16 @@ __device__ __forceinline__ double f19_aut_value(const F19Args& a, const F19Par& 
     return q.kappa0 * (q.x_far * eps + q.adamp) / (eps * eps + 1.0) / q.adamp;
 }
 
+// Merged-continuum ramp value at grid point b (opacity.py:889-894).
+__device__ __forceinline__ double f19_cont_value(const F19Par& q, int64_t b) {
+    double v = q.kappa0;
+    if (b >= q.n10) {
+        const int64_t r = (int64_t)q.nstep - b;
+        v *= (double)(r > 0 ? r : 0) / (double)q.early;
+    }
+    return v;
+}
+
 // One warp per (autoionizing line, depth, side): offsets 1, 2, ... until the
 // grid ends or the value is <= 0 or below the cutoff (not added); [1, end).
 template <typename R>
@@ -930,7 +1010,23 @@ __global__ void __launch_bounds__(128) f19_march_kernel(F19Args a) {
     const F19Par q = a.par[pd];
     const int64_t n = a.n_wl;
     int2 out = make_int2(1, 1);
-    if (q.active && q.kind == 1) {
+    if (q.active && q.kind == 2 && red) {
+        // the ramp from the first bin: points blueward of the line are passed
+        // over, the first value under the cutoff ends it; [first, end) in bins
+        int64_t end = q.nstep;
+        for (int64_t b0 = q.cc; b0 < q.nstep; b0 += 32) {
+            const int64_t b = b0 + lane;
+            bool stop = false;
+            if (b < q.nstep && !(a.grid[b] < q.tabstep))
+                stop = f19_cont_value(q, b) < abtot_f19<R>(a, q.d, b) * a.cutoff;
+            const unsigned m = __ballot_sync(0xffffffffu, stop);
+            if (m) {
+                end = b0 + (__ffs(m) - 1);
+                break;
+            }
+        }
+        out = make_int2(q.cc, (int)end);
+    } else if (q.active && q.kind == 1) {
         const int64_t last = red ? n - 1 - q.ci : q.ci;  // offsets that stay inside the grid
         int64_t end = last + 1;
         for (int64_t o0 = 1; o0 <= last; o0 += 32) {
@@ -976,6 +1072,14 @@ __global__ void __launch_bounds__(256) f19_gather_kernel(F19Args a, R* __restric
         if (q.kc_ok && b == q.cc) {
             acc += q.kapcen;
             any = true;
+        }
+        if (q.kind == 2) {
+            const int2 wk = a.walk[((int64_t)h * a.n_layers + d) * 2];
+            if (b >= wk.x && b < wk.y && !(a.grid[b] < q.tabstep)) {
+                acc += f19_cont_value(q, b);
+                any = true;
+            }
+            continue;
         }
         if (q.kind == 1) {
             if (b == q.ci) continue;

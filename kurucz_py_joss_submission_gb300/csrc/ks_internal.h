@@ -255,7 +255,10 @@ struct HeArgs {
 // below KAPMIN, else far wings X / n^2 to MAXSTEP).
 // Autoionizing lines (kind 1) use kappa0, kapcen (= kappa0 at the centre
 // bin cc), and tabstep/dvoigt/x_far as the line frequency, the width and
-// ASHORE, adamp as BSHORE, with their walks in F19Args::walk.
+// ASHORE, adamp as BSHORE, with their walks in F19Args::walk.  Merged-
+// continuum records (kind 2) use kappa0 (KAPPA), tabstep (the wavelength),
+// cc / n10 / nstep / early as the first bin, the merge bin, the tail bin and
+// the ramp's denominator, with their walk (absolute bins) in F19Args::walk.
 struct F19Par {
     double kappa0, adamp, tabstep, dvoigt, x_far, kapcen;
     int ci, cc, n10, nstep, early, active, kc_ok, d, kind, pad;
@@ -266,7 +269,8 @@ struct F19Args {
     int64_t n_wl, n_lines;
     int* flags;                               // FLAG_F19_LINE
     const int32_t* rows;                      // per line: catalog row, in catalog order
-    const int32_t* kind;                      // per line: 0 NORMAL, 1 autoionizing
+    const int32_t* kind;                      // per line: 0 NORMAL, 1 autoionizing, 2 merged continuum
+    const int32_t *nlast, *nelion;            // per line (merged continuum): NLAST, the ion index
     const double *cgf, *gamma_rad, *gamma_stark, *gamma_vdw;  // per line: fort.19 record values
                                               // (single-precision values held in double; the
                                               // autoionizing lines' gf in cgf)

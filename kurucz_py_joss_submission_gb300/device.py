@@ -193,9 +193,10 @@ class DeviceCatalog:
             rec.hydrogen_n_lower = self.t["hydrogen_n_lower"].data_ptr()
             rec.hydrogen_n_upper = self.t["hydrogen_n_upper"].data_ptr()
         # fort.19 lines (io/lines/fort19.py:343-347) other than hydrogen and
-        # helium: the NORMAL ones (line type 0 with NBLO/NBUP set) and the
-        # autoionizing ones (TYPE 1) get _add_fort19_asynth's profiles
-        # (engine/opacity.py:1335-1541) here; NORMAL lines whose fort.19
+        # helium: the NORMAL ones (line type 0 with NBLO/NBUP set), the
+        # autoionizing ones (TYPE 1) and the merged-continuum records get
+        # _add_fort19_asynth's profiles (engine/opacity.py:1335-1541) here;
+        # NORMAL lines whose fort.19
         # record carries continuum-merge limits (NCON = ISO2 with ISO1 = 0, on
         # a species of its CONTX table) are not modelled
         nb = np.abs(np.asarray(cat.n_lower)) + np.abs(np.asarray(cat.n_upper))
@@ -203,19 +204,27 @@ class DeviceCatalog:
         codex = np.any(np.isclose(np.asarray(cat.code)[:, None], FORT19_CODEX[None, :], rtol=0.0, atol=1e-3),
                        axis=1)
         known = (np.asarray(cat.element_idx) >= 0) & (np.asarray(cat.ion_stages) >= 1)
-        normal = (lt == 0) & (nb != 0) & known
+        # merged-continuum records: LABELP CONTINUU makes the fort.19 type
+        # NLAST = XJP (or NBUP) and gf x (2 XJ + 1) (fort19.py:304-307)
+        clab = np.asarray(cat.continuum_label) != 0
+        nlast = np.where(np.asarray(cat.xjp) > 0.0, np.asarray(cat.xjp).astype(np.int64),
+                         np.asarray(cat.n_upper).astype(np.int64))
+        cont = clab & (nlast > 3) & known
+        normal = (lt == 0) & (nb != 0) & known & ~clab
         tapered = normal & (ncon > 0) & codex
-        aut = (lt == 1) & known
-        f19 = np.flatnonzero((normal & ~tapered) | aut)
-        self.n_fort19_skipped = int(np.count_nonzero(tapered))
+        aut = (lt == 1) & known & ~clab
+        f19 = np.flatnonzero((normal & ~tapered) | aut | cont)
+        odd = clab & ~cont & ((nlast == 1) | ((nlast <= 0) & (nb != 0)))
+        self.n_fort19_skipped = int(np.count_nonzero(tapered) + np.count_nonzero(odd))
         if self.n_fort19_skipped:
-            warnings.warn(f"{self.n_fort19_skipped} fort.19 lines with continuum-merge limits contribute "
-                          "no opacity here", RuntimeWarning, stacklevel=2)
+            warnings.warn(f"{self.n_fort19_skipped} fort.19 lines (continuum-merge limits, or CONTINUU "
+                          "records of NLAST <= 1) contribute no opacity here", RuntimeWarning, stacklevel=2)
         self.n_f19 = int(f19.size)
         if self.n_f19 > 256:
             raise ValueError(f"{self.n_f19} fort.19 lines: the synthesis takes at most 256")
         if self.n_f19:
-            is_aut = lt[f19] == 1
+            is_cont = cont[f19]
+            is_aut = (lt[f19] == 1) & ~is_cont
             wl = np.asarray(cat.wavelength)[f19]
             gf = 10.0 ** np.asarray(cat.log_gf, dtype=np.float64)[f19]
             freq = 2.99792458e17 / np.maximum(wl, 1.0e-30)
@@ -232,18 +241,27 @@ class DeviceCatalog:
                 aut_r = np.where(grl != 0.0, 10.0 ** grl, g_r * denom)
                 aut_s = np.where(gsl > 0.0, -(10.0 ** (-gsl)), np.where(gsl < 0.0, 10.0 ** gsl, g_s * denom))
                 aut_w = np.where(gwl != 0.0, 10.0 ** gwl, g_w * denom)
+            code = np.asarray(cat.code)[f19]
+            nelem = (code + 1e-6).astype(np.int64)
+            icharge = ((code - nelem) * 100.0 + 0.1).astype(np.int64)
+            nelion = nelem * 6 - 6 + (icharge + 1)
+            nelion = np.where((nelem > 19) & (nelem < 29) & (icharge > 5),
+                              6 * (nelem + icharge * 10 - 30) - 1, nelion)
+            gf_cont = gf * (2.0 * np.asarray(cat.xj)[f19] + 1.0)
             vals = {
-                "cgf": f32(np.where(is_aut, gf, (0.026538 / 1.77245) * gf / freq)),
+                "cgf": f32(np.where(is_cont, gf_cont, np.where(is_aut, gf, (0.026538 / 1.77245) * gf / freq))),
                 "gamma_rad": f32(np.where(is_aut, aut_r, g_r)),
                 "gamma_stark": f32(np.where(is_aut, aut_s, g_s)),
                 "gamma_vdw": f32(np.where(is_aut, aut_w, g_w)),
             }
             self.t["f19_rows"] = _dev(f19 if self.order is None else inv_order(self.order)[f19], np.int32, dev)
-            self.t["f19_kind"] = _dev(is_aut.astype(np.int32), np.int32, dev)
+            self.t["f19_kind"] = _dev(np.where(is_cont, 2, np.where(is_aut, 1, 0)), np.int32, dev)
+            self.t["f19_nlast"] = _dev(nlast[f19], np.int32, dev)
+            self.t["f19_nelion"] = _dev(nelion, np.int32, dev)
             for k, v in vals.items():
                 self.t["f19_" + k] = _dev(v, np.float64, dev)
             rec.n_f19 = self.n_f19
-            for k in ("rows", "kind", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw"):
+            for k in ("rows", "kind", "nlast", "nelion", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw"):
                 setattr(rec, "f19_" + k, self.t["f19_" + k].data_ptr())
         # helium lines (line types -3/-4/-6; engine/opacity.py:2531-2544): the
         # helium wing pass, device rows in catalog order

@@ -46,6 +46,9 @@ class LineCatalog:
     gamma_rad_log: np.ndarray    # GR / GS / GW as read (log10, 0 when blank)
     gamma_stark_log: np.ndarray
     gamma_vdw_log: np.ndarray
+    xj: np.ndarray               # J of the lower / upper level
+    xjp: np.ndarray
+    continuum_label: np.ndarray  # 1 where LABELP begins with CONTINUU (merged-continuum record)
 
     def __len__(self) -> int:
         return int(self.wavelength.size)
@@ -96,6 +99,7 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
             n_lower=np.zeros(n, np.int32), n_upper=np.zeros(n, np.int32),
             iso1=np.zeros(n, np.int32), iso2=np.zeros(n, np.int32),
             gamma_rad_log=np.zeros(n), gamma_stark_log=np.zeros(n), gamma_vdw_log=np.zeros(n),
+            xj=np.zeros(n), xjp=np.zeros(n), continuum_label=np.zeros(n, np.uint8),
         )
         order = ["wavelength", "log_gf", "gf", "cgf", "excitation_energy", "gamma_rad", "gamma_stark",
                  "gamma_vdw", "element_idx", "ion_stages", "line_types", "process_mask",
@@ -107,6 +111,8 @@ def _read(path: Path, wl_min: float, wl_max: float, sort: bool) -> LineCatalog:
                                            cols["iso2"].ctypes.data_as(C.c_void_p)))
         _native.check(L.ks_gfall_fetch_gamma_logs(h, *[cols[k].ctypes.data_as(C.c_void_p) for k in
                                                        ("gamma_rad_log", "gamma_stark_log", "gamma_vdw_log")]))
+        _native.check(L.ks_gfall_fetch_j(h, *[cols[k].ctypes.data_as(C.c_void_p) for k in
+                                              ("xj", "xjp", "continuum_label")]))
     finally:
         L.ks_gfall_free(h)
     return LineCatalog(**cols)

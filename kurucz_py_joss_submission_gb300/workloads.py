@@ -221,6 +221,8 @@ class LineDraw:
     n_lower: Optional[np.ndarray] = None   # NBLO / NBUP of hydrogen lines (None: blank)
     n_upper: Optional[np.ndarray] = None
     tag: Optional[np.ndarray] = None       # columns 142-144 ("AUT": autoionizing; None: blank)
+    labelp: Optional[np.ndarray] = None    # upper-level label (None: "SYNTH"; "CONTINUU": merged continuum)
+    xjp: Optional[np.ndarray] = None       # upper-level J (None: 2.0)
 
     def __len__(self) -> int:
         return int(self.wavelength_nm.size)
@@ -387,6 +389,11 @@ def merge_lines(*draws: LineDraw) -> LineDraw:
         cat["n_upper"] = np.concatenate([d.levels()[1] for d in draws])
     if tags is not None:
         cat["tag"] = tags
+    if any(d.labelp is not None for d in draws):
+        cat["labelp"] = np.concatenate([d.labelp if d.labelp is not None else np.array(["SYNTH"] * len(d), dtype=object)
+                                        for d in draws]).astype(object)
+    if any(d.xjp is not None for d in draws):
+        cat["xjp"] = np.concatenate([d.xjp if d.xjp is not None else np.full(len(d), 2.0) for d in draws])
     order = np.argsort(cat["wavelength_nm"], kind="stable")
     return LineDraw(**{k: v[order] for k, v in cat.items()})
 
@@ -416,9 +423,11 @@ def format_gfall(lines: LineDraw) -> str:
         if lines.tag is not None and str(lines.tag[i]).strip():
             # the 3-character tag of columns 142-144 (AUT, COR, PRD)
             tail = tail[:141 - 98] + f"{str(lines.tag[i]):3.3s}" + tail[144 - 98:]
+        lp = str(lines.labelp[i]) if lines.labelp is not None and str(lines.labelp[i]) else "SYNTH"
+        xjp = float(lines.xjp[i]) if lines.xjp is not None else 2.0
         rows.append(
             f"{wl[i]:11.4f}{lines.log_gf[i]:7.3f}{lines.code[i]:6.2f}{e[i]:12.3f}"
-            f"{1.0:5.1f} {'SYNTH   '}{'  '}{ep[i]:12.3f}{2.0:5.1f} {'SYNTH   '}{'  '}"
+            f"{1.0:5.1f} {'SYNTH   '}{'  '}{ep[i]:12.3f}{xjp:5.1f} {lp:8.8s}{'  '}"
             f"{gr[i]:6.2f}{gs[i]:6.2f}{gw[i]:6.2f}{tail}\n"
         )
     return "".join(rows)

@@ -25,9 +25,12 @@ ASYNTH as TMP x STIM per layer:
 Autoionizing lines (TYPE 1, the gfall AUT tag) take the Fano-type profile of
 ``_accumulate_autoionizing_profile`` (opacity.py:901-963) with KAPPA0 =
 BSHORE GF XNFPEL BOLT (:1522-1541) in the same per-layer buffer, in fort.19
-order.  Lines whose fort.19 continuum index is set (NCON > 0 with an element
-of the CONTX table) taper their wings at WCON/WTAIL; they are not restated
-here, nor are merged-continuum records.
+order, and so do the merged-continuum records (LABELP CONTINUU: fort.19 type
+NLAST = XJP, gf x (2 XJ + 1); the ramp of ``_accumulate_merged_continuum``,
+opacity.py:863-898, between the merge and tail wavelengths of
+``_compute_merged_continuum_limits``, :723-758).  Lines whose fort.19
+continuum index is set (NCON > 0 with an element of the CONTX table) taper
+their wings at WCON/WTAIL; they are not restated here.
 """
 
 from __future__ import annotations
@@ -54,13 +57,88 @@ def normal_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
     lt = np.asarray(cat["line_type"])
     nb = np.abs(np.asarray(cat["n_lower"])) + np.abs(np.asarray(cat["n_upper"]))
     known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
-    return np.flatnonzero((lt == 0) & (nb != 0) & known & (np.asarray(cat["ion_stage"]) >= 1))
+    clab = np.asarray(cat.get("continuum_label", np.zeros(lt.size))) != 0
+    return np.flatnonzero((lt == 0) & (nb != 0) & known & (np.asarray(cat["ion_stage"]) >= 1) & ~clab)
+
+
+def _nlast(cat: Dict[str, np.ndarray]) -> np.ndarray:
+    """fort.19 type of a CONTINUU record: XJP, else NBUP (fort19.py:304-306)."""
+    xjp = np.asarray(cat["xjp"])
+    return np.where(xjp > 0.0, xjp.astype(np.int64), np.asarray(cat["n_upper"]).astype(np.int64))
+
+
+def cont_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
+    """Catalog rows of merged-continuum records (LABELP CONTINUU, NLAST > 3)."""
+    known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
+    clab = np.asarray(cat["continuum_label"]) != 0
+    return np.flatnonzero(clab & (_nlast(cat) > 3) & known & (np.asarray(cat["ion_stage"]) >= 1))
 
 
 def aut_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
     """Catalog rows of autoionizing lines (TYPE 1: the gfall AUT tag)."""
     known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
-    return np.flatnonzero((np.asarray(cat["line_type"]) == 1) & known & (np.asarray(cat["ion_stage"]) >= 1))
+    clab = np.asarray(cat.get("continuum_label", np.zeros(len(cat["line_type"])))) != 0
+    return np.flatnonzero((np.asarray(cat["line_type"]) == 1) & known & (np.asarray(cat["ion_stage"]) >= 1)
+                          & ~clab)
+
+
+def _nelion(code: float) -> int:
+    """The fort.19 ion index (fort19.py:323-328)."""
+    nelem = int(code + 1.0e-6) if code > 0.0 else 0
+    icharge = int((code - nelem) * 100.0 + 0.1) if code > 0.0 else 0
+    nelion = nelem * 6 - 6 + int(icharge + 1)
+    if 19 < nelem < 29 and icharge > 5:
+        nelion = 6 * (nelem + icharge * 10 - 30) - 1
+    return nelion
+
+
+def _merged_limits(wl, nlast, emerge, emerge_h, ion_index):
+    """_compute_merged_continuum_limits (opacity.py:723-758), vacuum grid."""
+    if wl <= 0.0 or nlast <= 0:
+        return None, None
+    ryd = 109677.576 if ion_index == 1 else 109737.312
+    dshift = 1.0e7 / wl - ryd / float(nlast * nlast)
+    if abs(dshift) <= 1e-12:
+        return None, None
+    wshift = 1.0e7 / dshift
+    em = emerge_h if ion_index == 1 else emerge
+    dmerge = 1.0e7 / wl - em
+    if abs(dmerge) <= 1e-12:
+        return None, None
+    wmerge = 1.0e7 / dmerge
+    if wmerge < 0.0:
+        wmerge = wshift + wshift
+    wmerge = max(wmerge, wshift)
+    wmerge = min(wshift + wshift, wmerge)
+    dtail = 1.0e7 / wmerge - 500.0
+    if abs(dtail) <= 1e-12:
+        return wmerge, None
+    wtail = 1.0e7 / dtail
+    if wtail < 0.0:
+        wtail = wmerge + wmerge
+    return wmerge, min(wmerge + wmerge, wtail)
+
+
+def _merged_continuum(tmp, cont, grid, ci, wl, kappa, cutoff, merge_wl, tail_wl):
+    """_accumulate_merged_continuum (opacity.py:863-898)."""
+    if kappa <= 0.0:
+        return
+    n = grid.size
+    i0 = max(ci, 0)
+    im = int(np.searchsorted(grid, merge_wl, side="left"))
+    it = min(int(np.searchsorted(grid, tail_wl, side="right")), n)
+    if it <= i0:
+        return
+    denom = max(it - max(im, i0), 1)
+    for b in range(i0, it):
+        if grid[b] < wl:
+            continue
+        v = kappa
+        if b >= im:
+            v *= max(it - b, 0) / denom
+        if v < cont[b] * cutoff:
+            break
+        tmp[b] += v
 
 
 def aut_record_values(cat: Dict[str, np.ndarray], rows: np.ndarray) -> Dict[str, np.ndarray]:
@@ -206,15 +284,20 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
     rec = record_values(cat, rows)
     arows = aut_rows(cat)
     arec = aut_record_values(cat, arows)
-    # fort.19 order = catalog order, both kinds interleaved
+    crows = cont_rows(cat) if "continuum_label" in cat else np.zeros(0, np.int64)
+    # fort.19 order = catalog order, the kinds interleaved
     kind = {int(i): ("n", j) for j, i in enumerate(rows)}
     kind.update({int(i): ("a", j) for j, i in enumerate(arows)})
+    kind.update({int(i): ("c", j) for j, i in enumerate(crows)})
     order = sorted(kind)
     pop = np.asarray(atm["population_per_ion"])
     rho = np.asarray(atm["mass_density"])
     xne = np.asarray(atm["electron_density"])
     hckt = np.asarray(atm["hckt"])
     txn = oracle.txnxn(atm)
+    nmerge = np.maximum(1600.0 / np.power(np.maximum(xne, 1e-40), 2.0 / 15.0) - 1.5, 1.0)
+    emerge = 109737.312 / np.maximum(nmerge ** 2, 1e-12)
+    emerge_h = 109677.576 / np.maximum(nmerge ** 2, 1e-12)
     stim = 1.0 - np.exp(-(C_LIGHT_CM / (grid * 1e-7))[None, :]
                         * (6.62607015e-27 / (KBOLTZ * np.asarray(atm["temperature"])))[:, None])
     out = np.zeros((L, N))
@@ -234,6 +317,16 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
                 continue
             r = float(rho[d])
             if r <= 0.0:
+                continue
+            if k == "c":
+                # merged continuum (opacity.py:1489-1520): KAPPA = GF XNFPEL BOLT
+                gfc = float(np.float32(10.0 ** float(cat["log_gf"][i]) * (2.0 * float(cat["xj"][i]) + 1.0)))
+                kappa = gfc * (pv / r) * boltz
+                nl = int(_nlast(cat)[i])
+                wm, wt = _merged_limits(wl, nl, float(emerge[d]), float(emerge_h[d]),
+                                        _nelion(float(cat["code"][i])))
+                _merged_continuum(tmp, continuum[d], grid, ci, wl, kappa, cutoff,
+                                  wm if wm is not None else wl, wt if wt is not None else wl)
                 continue
             if k == "a":
                 # XLINOP label 700: KAPPA0 = BSHORE * GF * XNFPEL * BOLT (opacity.py:1522-1541)

@@ -93,8 +93,13 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
             eps = line[52:64].strip()
             ep_val = float(eps) if eps else 0.0
             grs, gss, gws = line[80:86].strip(), line[86:92].strip(), line[92:98].strip()
+            xjs, xjps = line[36:41].strip(), line[64:69].strip()
+            xj = float(xjs) if xjs else 0.0
+            xjp = float(xjps) if xjps else 0.0
         except ValueError:
             continue
+        labelp = line[70:78].strip() if len(line) >= 78 else ""
+        cont_label = 1 if labelp.upper().startswith("CONTINUU") else 0
         x1 = x2 = 0.0
         if len(line) >= 115 and line[109:115].strip():
             try:
@@ -190,9 +195,9 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
         elif nelem == 2 and ion == 2:
             lt = -6
         rows.append((wavelength, log_gf, code, elo, gr, gs, gw, nelem, ion, lt, nblo, nbup, line_size,
-                     grl, gsl, gwl))
+                     grl, gsl, gwl, xj, xjp, cont_label))
     if not rows:
-        arr = np.zeros((0, 16))
+        arr = np.zeros((0, 19))
     else:
         arr = np.array(rows, dtype=np.float64)
     return {
@@ -212,6 +217,9 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
         "gamma_rad_log": arr[:, 13].copy(),
         "gamma_stark_log": arr[:, 14].copy(),
         "gamma_vdw_log": arr[:, 15].copy(),
+        "xj": arr[:, 16].copy(),
+        "xjp": arr[:, 17].copy(),
+        "continuum_label": arr[:, 18].astype(np.int32),
     }
 
 

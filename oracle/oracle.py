@@ -229,7 +229,7 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
     t2 = time.perf_counter()
     asy, evals, reach = asynth(cat, route, atm, grid, tr, valid, cidx, widx, kapmin, tb, cutoff)
     from . import fort19
-    if fort19.normal_rows(cat).size or fort19.aut_rows(cat).size:
+    if fort19.normal_rows(cat).size or fort19.aut_rows(cat).size or fort19.cont_rows(cat).size:
         # fort.19 NORMAL and autoionizing lines: their profiles added to ASYNTH
         # (synthe_py/engine/opacity.py:2366-2390)
         asy = asy + fort19.asynth_term(dict(cat, center=cidx), atm, grid, kapmin, cutoff=cutoff,

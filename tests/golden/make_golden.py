@@ -126,6 +126,12 @@ CASES = {
     "aut_500_501": dict(atm="t5800g444", wl_start=500.0, wl_end=501.0,
                         n_lines=150, draw=(499.85, 501.15), log_uniform=False, seed=25,
                         aut_every=5),
+    # merged-continuum records (LABELP CONTINUU, NLAST = XJP): the fort.19
+    # ramp between the merge and tail wavelengths (engine/opacity.py:723-758,
+    # :863-898), one record below the window
+    "cont_505_507": dict(atm="t5800g444", wl_start=505.5, wl_end=507.5,
+                         n_lines=120, draw=(505.35, 507.65), log_uniform=False, seed=26,
+                         continuum_records=[(505.42, 40.0, -13.0), (505.62, 50.0, -12.5), (506.55, 30.0, -13.5)]),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -171,6 +177,15 @@ def case_lines(case: dict) -> workloads.LineDraw:
         lines.log_gamma_stark[idx] = np.where(np.arange(idx.size) % 2 == 0, -0.5, 0.3)
         lines.log_gamma_vdw[idx] = 0.3
         lines.log_gf[idx] = np.minimum(lines.log_gf[idx], -1.0) - 12.0
+    if case.get("continuum_records"):
+        recs = case["continuum_records"]
+        z = np.zeros(len(recs))
+        extra = workloads.LineDraw(
+            wavelength_nm=np.array([r[0] for r in recs]), log_gf=np.array([r[2] for r in recs]),
+            code=np.full(len(recs), 26.00), e_lower_cm=np.full(len(recs), 1500.0),
+            log_gamma_rad=z + 8.0, log_gamma_stark=z - 5.0, log_gamma_vdw=z - 7.5,
+            labelp=np.array(["CONTINUU"] * len(recs), dtype=object), xjp=np.array([r[1] for r in recs]))
+        lines = workloads.merge_lines(lines, extra)
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth
         # of their cores exceeds the last JOSH tau point (MAXJ = 1 path)

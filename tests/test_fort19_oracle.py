@@ -51,6 +51,20 @@ def test_oracle_asynth_with_autoionizing_lines():
     assert float(rel.max()) < 1e-13
 
 
+@pytest.mark.skipif("cont_505_507" not in available_cases(), reason="golden missing")
+def test_oracle_asynth_with_merged_continuum_records():
+    name = "cont_505_507"
+    g = golden(name)
+    w0, w1 = window(name)
+    tb = oracle.tables()
+    cat = gfall.filter_window(gfall.parse_gfall(gfall_path(name), tb["potion"]), w0, w1)
+    rows = fort19.cont_rows(cat)
+    assert rows.size == 3 and np.all(cat["xjp"][rows] > 3)
+    r = oracle.synthesize(oracle.load_atmosphere(atm_path(name)), cat, w0, w1, tb=tb)
+    rel = np.abs(r["asynth"] - g["asynth"]) / np.maximum(np.abs(g["asynth"]), 1e-300)
+    assert float(rel.max()) < 1e-13
+
+
 def test_oracle_detects_planted_error():
     g = golden(CASE)
     w0, w1 = window(CASE)

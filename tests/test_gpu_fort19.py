@@ -9,7 +9,8 @@ in the lines' Doppler widths, damping large enough for the Voigt branch
 (ADAMP >= 0.2), a line centred below the grid (the reference's clamped
 KAPCEN bin and wing from bin 0), a raised cutoff, and autoionizing lines
 (TYPE 1) interleaved with them, one of them below the grid (its centre value
-on the last grid point, as the reference's Python index -1 puts it).
+on the last grid point, as the reference's Python index -1 puts it), and
+merged-continuum records (LABELP CONTINUU), one of them below the grid.
 
 Tolerance: FP64 cube within 1e-11 relative of the oracle's.
 """
@@ -73,6 +74,17 @@ def draw(w0, w1, seed, gw_shift=0.0, extra=None, aut=False):
     return d
 
 
+def continuum_records(w0):
+    """Merged-continuum records (LABELP CONTINUU, NLAST = XJP): one below
+    the grid, two inside it."""
+    wl = np.array([w0 - 0.08, w0 + 0.12, w0 + 0.45])
+    z = np.zeros(3)
+    return workloads.LineDraw(wavelength_nm=wl, log_gf=np.array([-16.0, -15.5, -16.5]),
+                              code=np.full(3, 26.00), e_lower_cm=np.full(3, 1500.0),
+                              log_gamma_rad=z + 8.0, log_gamma_stark=z - 5.0, log_gamma_vdw=z - 7.5,
+                              labelp=np.array(["CONTINUU"] * 3, dtype=object), xjp=np.array([40.0, 50.0, 30.0]))
+
+
 def below_grid_aut(w0):
     """One autoionizing Fe I line below the grid: the reference puts its centre
     value on the last grid point (Python index -1)."""
@@ -104,6 +116,8 @@ CASES = {
     # NORMAL and autoionizing lines interleaved; an autoionizing line below the grid
     "with_aut": (500.0, 500.8, dict(seed=35, aut=True), {}),
     "aut_below": (500.0, 500.8, dict(seed=36, aut=True, extra="below_aut"), {}),
+    # merged-continuum ramps with NORMAL and autoionizing lines
+    "continuum": (505.5, 506.6, dict(seed=37, aut=True, extra="continuum"), {}),
 }
 
 
@@ -116,6 +130,8 @@ def test_fp64_matches_oracle(key, tmp_path):
         kw["extra"] = below_grid_line(w0)
     elif extra == "below_aut":
         kw["extra"] = below_grid_aut(w0)
+    elif extra == "continuum":
+        kw["extra"] = continuum_records(w0)
     p = tmp_path / "lines.gf"
     p.write_text(workloads.format_gfall(draw(w0, w1, **kw)))
     cat = atomic.load_catalog_window(p, w0, w1)
@@ -139,3 +155,5 @@ def test_fp64_matches_oracle(key, tmp_path):
         assert fort19.aut_rows(ocat).size >= 10
     if key == "aut_below":
         assert np.any(c[fort19.aut_rows(ocat)] < 0)
+    if key == "continuum":
+        assert fort19.cont_rows(ocat).size == 3 and dcat.t["f19_kind"].eq(2).sum().item() == 3
