@@ -141,7 +141,9 @@ def oracle_sample_catalogs(cat_path: Path):
     from oracle import gfall
 
     windows = WORKLOAD["sample"]
-    tag = _sha256(cat_path)[:20] + "_" + "_".join(f"{a:.3f}-{b:.3f}" for a, b in windows).replace(".", "p")
+    # the parser's field set is part of the key (a cache from an older reader lacks fields)
+    tag = ("v3_" + _sha256(cat_path)[:20] + "_"
+           + "_".join(f"{a:.3f}-{b:.3f}" for a, b in windows).replace(".", "p"))
     import hashlib
 
     cache = Path(os.environ.get("TMPDIR", "/tmp")) / f"kgb300_orcwin_{hashlib.sha256(tag.encode()).hexdigest()[:24]}.npz"

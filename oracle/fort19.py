@@ -69,6 +69,8 @@ def _nlast(cat: Dict[str, np.ndarray]) -> np.ndarray:
 
 def cont_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
     """Catalog rows of merged-continuum records (LABELP CONTINUU, NLAST > 3)."""
+    if "continuum_label" not in cat:
+        return np.zeros(0, np.int64)
     known = (np.asarray(cat["nelem"]) >= 1) & (np.asarray(cat["nelem"]) <= 99)
     clab = np.asarray(cat["continuum_label"]) != 0
     return np.flatnonzero(clab & (_nlast(cat) > 3) & known & (np.asarray(cat["ion_stage"]) >= 1))
