@@ -140,6 +140,11 @@ typedef struct {
      * holding gf (2 XJ + 1)): NLAST and the record's ion index NELION
      * (fort19.py:323-328); unread for the other kinds */
     const int32_t *f19_nlast, *f19_nelion;
+    /* fort.19 continuum-merge limits (opacity.py:657-702): per helium line
+     * and per fort.19 line, NCON (ISO2 when ISO1 is 0) and the CONTX column
+     * NELIONX of the record's species (fort19.py:330-338); 0 for none */
+    const int32_t *helium_ncon, *helium_nelionx;
+    const int32_t *f19_ncon, *f19_nelionx;
 } ks_lines;
 
 typedef struct {
@@ -213,6 +218,7 @@ typedef struct {
     const double *propbm, *c, *d, *pp, *beta, *stalph, *stwtal, *stcomp, *stcpwt;
     const int32_t *istal, *lnghal, *lncomp;
     const double *cutoff_h2_plus, *cutoff_h2, *asum_lyman, *asum, *y1wtm, *xknmtb, *ehyd, *conth;
+    const double *contx; /* [26*17] continuum edges of the fort.19 merge limits (tables.py:173) */
 } ks_hydrogen_tables;
 ks_status ks_init_hydrogen_tables(const ks_hydrogen_tables *tables);
 

@@ -76,6 +76,7 @@ class KsLines(C.Structure):
         ("n_f19", C.c_int32), ("f19_rows", P), ("f19_cgf", P), ("f19_gamma_rad", P),
         ("f19_gamma_stark", P), ("f19_gamma_vdw", P), ("f19_kind", P),
         ("f19_nlast", P), ("f19_nelion", P),
+        ("helium_ncon", P), ("helium_nelionx", P), ("f19_ncon", P), ("f19_nelionx", P),
     ]
 
 
@@ -122,7 +123,7 @@ class KsHydrogenTables(C.Structure):
     _fields_ = [(k, P) for k in (
         "propbm", "c", "d", "pp", "beta", "stalph", "stwtal", "stcomp", "stcpwt",
         "istal", "lnghal", "lncomp",
-        "cutoff_h2_plus", "cutoff_h2", "asum_lyman", "asum", "y1wtm", "xknmtb", "ehyd", "conth")]
+        "cutoff_h2_plus", "cutoff_h2", "asum_lyman", "asum", "y1wtm", "xknmtb", "ehyd", "conth", "contx")]
 
 
 HYDROGEN_INT_TABLES = ("istal", "lnghal", "lncomp")

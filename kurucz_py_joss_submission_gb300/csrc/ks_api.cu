@@ -43,7 +43,7 @@ ks_status ks::set_error(ks_status code, const std::string& msg) { return fail(co
 
 extern "C" ks_status ks_version(int32_t* major, int32_t* minor) {
     if (major) *major = 1;
-    if (minor) *minor = 5;
+    if (minor) *minor = 6;
     return KS_OK;
 }
 
@@ -737,11 +737,13 @@ static ks_status check_lines(const ks_lines* l) {
     if (l->n_helium < 0 || l->n_helium > l->n_lines)
         return fail(KS_ERR_INVALID, "n_helium must lie in [0, n_lines]");
     if (l->n_helium > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 helium lines");
-    if (l->n_helium > 0 && !l->helium_rows) return fail(KS_ERR_INVALID, "lines: helium_rows is NULL");
+    if (l->n_helium > 0 && (!l->helium_rows || !l->helium_ncon || !l->helium_nelionx))
+        return fail(KS_ERR_INVALID, "lines: a helium column is NULL");
     if (l->n_f19 < 0 || l->n_f19 > l->n_lines) return fail(KS_ERR_INVALID, "n_f19 must lie in [0, n_lines]");
     if (l->n_f19 > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 fort.19 lines");
     if (l->n_f19 > 0 && (!l->f19_rows || !l->f19_cgf || !l->f19_gamma_rad || !l->f19_gamma_stark ||
-                         !l->f19_gamma_vdw || !l->f19_kind || !l->f19_nlast || !l->f19_nelion))
+                         !l->f19_gamma_vdw || !l->f19_kind || !l->f19_nlast || !l->f19_nelion ||
+                         !l->f19_ncon || !l->f19_nelionx))
         return fail(KS_ERR_INVALID, "lines: a fort.19 column is NULL");
     return KS_OK;
 }
@@ -1269,6 +1271,12 @@ static ks_status run_f19(const ks_lines* lines, const ks_atmos* atm, const ks_gr
     f.kind = lines->f19_kind;
     f.nlast = lines->f19_nlast;
     f.nelion = lines->f19_nelion;
+    f.ncon = lines->f19_ncon;
+    f.nelionx = lines->f19_nelionx;
+    const HydTables* tab = nullptr;
+    ks_status st = hydrogen_device_tables(&tab);
+    if (st) return st;
+    f.tab = tab;
     f.cgf = lines->f19_cgf;
     f.gamma_rad = lines->f19_gamma_rad;
     f.gamma_stark = lines->f19_gamma_stark;
@@ -1319,6 +1327,12 @@ static ks_status run_helium(const ks_lines* lines, const ks_atmos* atm, const ks
     h.n_lines = lines->n_lines;
     h.flags = w.flags;
     h.rows = lines->helium_rows;
+    h.ncon = lines->helium_ncon;
+    h.nelionx = lines->helium_nelionx;
+    const HydTables* tab = nullptr;
+    ks_status st = hydrogen_device_tables(&tab);
+    if (st) return st;
+    h.tab = tab;
     h.wavelength = lines->wavelength;
     h.gf = lines->gf;
     h.elo = lines->elo_cm;

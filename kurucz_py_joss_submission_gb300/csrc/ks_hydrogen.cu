@@ -315,6 +315,44 @@ __device__ __forceinline__ double abtot(const HydArgs& a, int d, int64_t b) {
     return (double)((const R*)a.cabs)[i] + (double)((const R*)a.cscat)[i];
 }
 
+// WCON / WTAIL of a fort.19 line (opacity.py:657-702, vacuum grid):
+// the CONTX edge of (NCON, NELIONX) less the merge energy of the layer (the
+// hydrogen one for NELION 1); <= 0 where a limit is absent.
+__device__ __forceinline__ void continuum_limits(int ncon, int nelion, int nelionx, double xne,
+                                                 const HydTables& T, double* wcon, double* wtail) {
+    *wcon = -1.0;
+    *wtail = -1.0;
+    if (ncon <= 0 || nelionx <= 0 || nelionx > 17 || ncon > 26) return;
+    const double cv = T.contx[(ncon - 1) * 17 + (nelionx - 1)];
+    if (cv <= 0.0) return;
+    const double nmerge = fmax(1600.0 / pow(fmax(xne, 1e-40), 2.0 / 15.0) - 1.5, 1.0);
+    const double nm2 = fmax(nmerge * nmerge, 1e-12);
+    const double em = nelion == 1 ? 109677.576 / nm2 : 109737.312 / nm2;
+    const double denom = cv - em;
+    if (fabs(denom) <= 1e-8) return;
+    const double wc = 1.0e7 / denom;
+    double wt = -1.0;
+    const double dt = cv - em - 500.0;
+    if (fabs(dt) > 1e-8) {
+        wt = 1.0e7 / dt;
+        if (wt < 0.0) wt = 2.0 * wc;
+        wt = (2.0 * wc) < wt ? 2.0 * wc : wt;
+    }
+    if (wt > 0.0 && wt <= wc) wt = -1.0;
+    *wcon = wc;
+    *wtail = wt;
+}
+
+// The WTAIL taper of a wing value at wavelength w (opacity.py:1031-1032,
+// :236-240): (w - base) / (WTAIL - base) below WTAIL, base = WCON or the line.
+__device__ __forceinline__ double wing_taper(double v, double w, double wcon, double wtail, double wl0) {
+    if (wtail > 0.0 && w < wtail) {
+        const double base = wcon > 0.0 ? wcon : wl0;
+        v = v * (w - base) / fmax(wtail - base, 1e-12);
+    }
+    return v;
+}
+
 template <typename R>
 __device__ __forceinline__ double abtot_he(const HeArgs& a, int d, int64_t b) {
     const int64_t i = (int64_t)d * a.n_wl + b;
@@ -611,6 +649,7 @@ __global__ void __launch_bounds__(128) he_setup_kernel(HeArgs a) {
     q.ci = 0;
     q.pad = 0;
     q.wl0 = q.keff = q.dop = q.adamp = 0.0;
+    q.wcon = q.wtail = -1.0;
     const int row = a.rows[h];
     if (row < 0 || (int64_t)row >= a.n_lines) {
         if (d == 0) atomicOr(a.flags, FLAG_HELIUM_LINE);
@@ -659,13 +698,23 @@ __global__ void __launch_bounds__(128) he_setup_kernel(HeArgs a) {
     q.keff = keff;
     q.dop = dop;
     q.adamp = fmax(dn, 1e-12);
+    // fort.19 continuum-merge limits (process_depth, opacity.py:2760-2770, :2909)
+    continuum_limits(a.ncon[h], nelion, a.nelionx[h], dp.xne, *a.tab, &q.wcon, &q.wtail);
     q.active = 1;
     a.par[i] = q;
 }
 
 template <typename R>
 __device__ __forceinline__ double he_value(const HeArgs& a, const HePar& q, int64_t b) {
-    return q.keff * voigt_hv<double>(fabs(a.grid[b] - q.wl0) / q.dop, q.adamp, a.h0, a.h1, a.h2);
+    const double w = a.grid[b];
+    const double v = q.keff * voigt_hv<double>(fabs(w - q.wl0) / q.dop, q.adamp, a.h0, a.h1, a.h2);
+    return wing_taper(v, w, q.wcon, q.wtail, q.wl0);
+}
+
+// A red step at or below WCON is passed over; a blue one ends the walk
+// (opacity.py:1026-1028, :1043-1045).
+__device__ __forceinline__ bool he_below_wcon(const HeArgs& a, const HePar& q, int64_t b) {
+    return q.wcon > 0.0 && a.grid[b] <= q.wcon;
 }
 
 // One warp per (helium line, depth, side): the red walk takes offsets
@@ -694,14 +743,20 @@ __global__ void __launch_bounds__(128) he_march_kernel(HeArgs a) {
         for (int64_t o0 = first; o0 <= last; o0 += 32) {
             const int64_t o = o0 + lane;
             bool stop = false;
+            bool below = false;
             if (o <= last) {
                 const int64_t b = red ? q.ci + o : q.ci - o;
-                stop = he_value<R>(a, q, b) < abtot_he<R>(a, q.d, b) * a.cutoff;
+                below = he_below_wcon(a, q, b);
+                if (!below) stop = he_value<R>(a, q, b) < abtot_he<R>(a, q.d, b) * a.cutoff;
+                else if (!red) stop = true;
             }
             const unsigned m = __ballot_sync(0xffffffffu, stop);
             if (m) {
-                const int64_t hit = o0 + (__ffs(m) - 1);
-                end = red ? hit : hit + 1;
+                const int l = __ffs(m) - 1;
+                const int64_t hit = o0 + l;
+                // blue: the step that fails the cutoff is added, one at WCON is not
+                const bool hit_below = __shfl_sync(0xffffffffu, below, l);
+                end = red ? hit : (hit_below ? hit : hit + 1);
                 break;
             }
         }
@@ -730,6 +785,7 @@ __global__ void __launch_bounds__(256) he_gather_kernel(HeArgs a, R* __restrict_
         const int2 wk = a.walk[pd * 2 + (red ? 0 : 1)];
         if (o < wk.x || o >= wk.y) continue;
         const HePar q = a.par[pd];
+        if (he_below_wcon(a, q, b)) continue;   // red steps at or below WCON add nothing
         acc += he_value<R>(a, q, b);
         any = true;
     }
@@ -773,6 +829,7 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
     const int h = (int)(i / a.n_layers), d = (int)(i - (int64_t)h * a.n_layers);
     F19Par q;
     q.kappa0 = q.adamp = q.tabstep = q.dvoigt = q.x_far = q.kapcen = 0.0;
+    q.wcon = q.wtail = -1.0;
     q.ci = q.cc = q.n10 = q.nstep = q.early = q.active = q.kc_ok = q.kind = q.pad = 0;
     q.d = d;
     const int row = a.rows[h];
@@ -924,6 +981,9 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
     q.ci = ci;
     q.cc = cc;
     q.active = 1;
+    // continuum-merge limits of the record (opacity.py:1449-1461), with the
+    // fort.19 ion index as NELION
+    continuum_limits(a.ncon[h], a.nelion[h], a.nelionx[h], dp.xne, *a.tab, &q.wcon, &q.wtail);
     // wing (_accumulate_metal_profile_kernel, no WCON/WTAIL)
     if (k0 <= 0.0) {
         q.nstep = 0;
@@ -1095,17 +1155,21 @@ __global__ void __launch_bounds__(256) f19_gather_kernel(F19Args a, R* __restric
         }
         const int ci = q.ci, ns = q.nstep;
         if (ns <= 0 || ci + ns < 0 || ci - ns >= n) continue;
+        // at or below WCON nothing is added: the red loop passes over such
+        // steps, the blue one ends there (opacity.py:224-228, :264-267)
+        const double w = a.grid[b];
+        if (q.wcon > 0.0 && w <= q.wcon) continue;
         if (b > ci && ci < n - 1) {
             const int k = b - ci;
             const int maxred = ci >= 0 ? min(n - 1 - ci, ns) : min(n - 1, ns);
             if (k >= max(1, -ci) && k <= maxred) {
-                acc += f19_value(a, q, k);
+                acc += wing_taper(f19_value(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
                 any = true;
             }
         } else if (b < ci && ci > 0) {
             const int k = ci - b;
             if (k >= max(1, ci + 1 - n) && k <= min(ci, ns)) {
-                acc += f19_value(a, q, k);
+                acc += wing_taper(f19_value(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
                 any = true;
             }
         }
@@ -1207,7 +1271,7 @@ void copy_n(T* dst, const T* src, size_t n) {
 extern "C" ks_status ks_init_hydrogen_tables(const ks_hydrogen_tables* t) {
     if (!t || !t->propbm || !t->c || !t->d || !t->pp || !t->beta || !t->stalph || !t->stwtal || !t->stcomp ||
         !t->stcpwt || !t->istal || !t->lnghal || !t->lncomp || !t->cutoff_h2_plus || !t->cutoff_h2 ||
-        !t->asum_lyman || !t->asum || !t->y1wtm || !t->xknmtb || !t->ehyd || !t->conth)
+        !t->asum_lyman || !t->asum || !t->y1wtm || !t->xknmtb || !t->ehyd || !t->conth || !t->contx)
         return ks::set_error(KS_ERR_INVALID, "ks_init_hydrogen_tables: null table pointer");
     ks::HydTables h;
     copy_n(h.propbm, t->propbm, 7 * 5 * 15);
@@ -1238,6 +1302,7 @@ extern "C" ks_status ks_init_hydrogen_tables(const ks_hydrogen_tables* t) {
     copy_n(h.xknmtb, t->xknmtb, 12);
     copy_n(h.ehyd, t->ehyd, 8);
     copy_n(h.conth, t->conth, 15);
+    copy_n(h.contx, t->contx, 26 * 17);
     std::lock_guard<std::mutex> lk(g_hyd_mu);
     g_hyd_host = h;
     g_hyd_ready = true;

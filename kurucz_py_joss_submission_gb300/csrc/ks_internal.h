@@ -199,6 +199,7 @@ struct HydTables {
     int istal[4], lnghal[4], lncomp[4];
     double cutoff_h2_plus[111], cutoff_h2[91], asum_lyman[100], asum[96], y1wtm[2 * 2], xknmtb[4 * 3];
     double ehyd[8], conth[15];
+    double contx[26 * 17];  // continuum edges of the fort.19 merge limits, [NCON][NELIONX]
 };
 
 // One (hydrogen line, depth): gates, walk limits and the hydrogen depth state.
@@ -229,6 +230,7 @@ struct HydArgs {
 // / 1.155), the Doppler width in nm (3He: x 1.155) and the damping.
 struct HePar {
     double wl0, keff, dop, adamp;
+    double wcon, wtail;  // fort.19 continuum-merge limits (nm; <= 0: none)
     int ci, d, active, pad;
 };
 
@@ -237,6 +239,8 @@ struct HeArgs {
     int64_t n_wl, n_lines;
     int* flags;                               // FLAG_HELIUM_LINE
     const int32_t* rows;                      // per helium line: catalog row, in catalog order
+    const int32_t *ncon, *nelionx;            // per helium line: fort.19 NCON and CONTX column (0: none)
+    const HydTables* tab;                     // CONTX
     const double *wavelength, *gf, *elo, *gamma_rad, *gamma_stark, *gamma_vdw;  // catalog columns
     const int32_t *ion_stage, *line_type, *center;
     const double* grid;
@@ -261,6 +265,7 @@ struct HeArgs {
 // the ramp's denominator, with their walk (absolute bins) in F19Args::walk.
 struct F19Par {
     double kappa0, adamp, tabstep, dvoigt, x_far, kapcen;
+    double wcon, wtail;  // NORMAL lines: continuum-merge limits (nm; <= 0: none)
     int ci, cc, n10, nstep, early, active, kc_ok, d, kind, pad;
 };
 
@@ -271,6 +276,8 @@ struct F19Args {
     const int32_t* rows;                      // per line: catalog row, in catalog order
     const int32_t* kind;                      // per line: 0 NORMAL, 1 autoionizing, 2 merged continuum
     const int32_t *nlast, *nelion;            // per line (merged continuum): NLAST, the ion index
+    const int32_t *ncon, *nelionx;            // per line (NORMAL): NCON and the CONTX column (0: none)
+    const HydTables* tab;                     // CONTX
     const double *cgf, *gamma_rad, *gamma_stark, *gamma_vdw;  // per line: fort.19 record values
                                               // (single-precision values held in double; the
                                               // autoionizing lines' gf in cgf)

@@ -195,14 +195,14 @@ class DeviceCatalog:
         # fort.19 lines (io/lines/fort19.py:343-347) other than hydrogen and
         # helium: the NORMAL ones (line type 0 with NBLO/NBUP set), the
         # autoionizing ones (TYPE 1) and the merged-continuum records get
-        # _add_fort19_asynth's profiles (engine/opacity.py:1335-1541) here;
-        # NORMAL lines whose fort.19
-        # record carries continuum-merge limits (NCON = ISO2 with ISO1 = 0, on
-        # a species of its CONTX table) are not modelled
+        # _add_fort19_asynth's profiles (engine/opacity.py:1335-1541) here,
+        # with the records' continuum-merge limits
         nb = np.abs(np.asarray(cat.n_lower)) + np.abs(np.asarray(cat.n_upper))
+        # continuum-merge limits of fort.19 records (fort19.py:330-338): NCON
+        # = ISO2 when ISO1 is 0, NELIONX = the species' CONTX column
         ncon = np.where((np.asarray(cat.iso1) == 0) & (np.asarray(cat.iso2) > 0), np.asarray(cat.iso2), 0)
-        codex = np.any(np.isclose(np.asarray(cat.code)[:, None], FORT19_CODEX[None, :], rtol=0.0, atol=1e-3),
-                       axis=1)
+        match = np.isclose(np.asarray(cat.code)[:, None], FORT19_CODEX[None, :], rtol=0.0, atol=1e-3)
+        nelionx = np.where(match.any(axis=1), match.argmax(axis=1) + 1, 0)
         known = (np.asarray(cat.element_idx) >= 0) & (np.asarray(cat.ion_stages) >= 1)
         # merged-continuum records: LABELP CONTINUU makes the fort.19 type
         # NLAST = XJP (or NBUP) and gf x (2 XJ + 1) (fort19.py:304-307)
@@ -211,14 +211,13 @@ class DeviceCatalog:
                          np.asarray(cat.n_upper).astype(np.int64))
         cont = clab & (nlast > 3) & known
         normal = (lt == 0) & (nb != 0) & known & ~clab
-        tapered = normal & (ncon > 0) & codex
         aut = (lt == 1) & known & ~clab
-        f19 = np.flatnonzero((normal & ~tapered) | aut | cont)
+        f19 = np.flatnonzero(normal | aut | cont)
         odd = clab & ~cont & ((nlast == 1) | ((nlast <= 0) & (nb != 0)))
-        self.n_fort19_skipped = int(np.count_nonzero(tapered) + np.count_nonzero(odd))
+        self.n_fort19_skipped = int(np.count_nonzero(odd))
         if self.n_fort19_skipped:
-            warnings.warn(f"{self.n_fort19_skipped} fort.19 lines (continuum-merge limits, or CONTINUU "
-                          "records of NLAST <= 1) contribute no opacity here", RuntimeWarning, stacklevel=2)
+            warnings.warn(f"{self.n_fort19_skipped} CONTINUU records of NLAST <= 1 contribute no opacity here",
+                          RuntimeWarning, stacklevel=2)
         self.n_f19 = int(f19.size)
         if self.n_f19 > 256:
             raise ValueError(f"{self.n_f19} fort.19 lines: the synthesis takes at most 256")
@@ -258,10 +257,13 @@ class DeviceCatalog:
             self.t["f19_kind"] = _dev(np.where(is_cont, 2, np.where(is_aut, 1, 0)), np.int32, dev)
             self.t["f19_nlast"] = _dev(nlast[f19], np.int32, dev)
             self.t["f19_nelion"] = _dev(nelion, np.int32, dev)
+            self.t["f19_ncon"] = _dev(np.where(normal[f19], ncon[f19], 0), np.int32, dev)
+            self.t["f19_nelionx"] = _dev(nelionx[f19], np.int32, dev)
             for k, v in vals.items():
                 self.t["f19_" + k] = _dev(v, np.float64, dev)
             rec.n_f19 = self.n_f19
-            for k in ("rows", "kind", "nlast", "nelion", "cgf", "gamma_rad", "gamma_stark", "gamma_vdw"):
+            for k in ("rows", "kind", "nlast", "nelion", "ncon", "nelionx", "cgf", "gamma_rad", "gamma_stark",
+                      "gamma_vdw"):
                 setattr(rec, "f19_" + k, self.t["f19_" + k].data_ptr())
         # helium lines (line types -3/-4/-6; engine/opacity.py:2531-2544): the
         # helium wing pass, device rows in catalog order
@@ -271,8 +273,13 @@ class DeviceCatalog:
             raise ValueError(f"{self.n_helium} helium lines: the synthesis takes at most 256")
         if self.n_helium:
             self.t["helium_rows"] = _dev(he if self.order is None else inv_order(self.order)[he], np.int32, dev)
+            # only fort.19 records (NBLO/NBUP set) carry the merge limits
+            self.t["helium_ncon"] = _dev(np.where(nb[he] != 0, ncon[he], 0), np.int32, dev)
+            self.t["helium_nelionx"] = _dev(nelionx[he], np.int32, dev)
             rec.n_helium = self.n_helium
             rec.helium_rows = self.t["helium_rows"].data_ptr()
+            rec.helium_ncon = self.t["helium_ncon"].data_ptr()
+            rec.helium_nelionx = self.t["helium_nelionx"].data_ptr()
         self.rec = rec
 
     def to_catalog_order(self, per_line: np.ndarray) -> np.ndarray:

@@ -223,6 +223,7 @@ class LineDraw:
     tag: Optional[np.ndarray] = None       # columns 142-144 ("AUT": autoionizing; None: blank)
     labelp: Optional[np.ndarray] = None    # upper-level label (None: "SYNTH"; "CONTINUU": merged continuum)
     xjp: Optional[np.ndarray] = None       # upper-level J (None: 2.0)
+    iso2: Optional[np.ndarray] = None      # ISO2 (columns 117-119; with ISO1 blank, fort.19's NCON)
 
     def __len__(self) -> int:
         return int(self.wavelength_nm.size)
@@ -392,6 +393,8 @@ def merge_lines(*draws: LineDraw) -> LineDraw:
     if any(d.labelp is not None for d in draws):
         cat["labelp"] = np.concatenate([d.labelp if d.labelp is not None else np.array(["SYNTH"] * len(d), dtype=object)
                                         for d in draws]).astype(object)
+    if any(d.iso2 is not None for d in draws):
+        cat["iso2"] = np.concatenate([d.iso2 if d.iso2 is not None else np.zeros(len(d), np.int32) for d in draws])
     if any(d.xjp is not None for d in draws):
         cat["xjp"] = np.concatenate([d.xjp if d.xjp is not None else np.full(len(d), 2.0) for d in draws])
     order = np.argsort(cat["wavelength_nm"], kind="stable")
@@ -420,6 +423,9 @@ def format_gfall(lines: LineDraw) -> str:
         if nlo[i] > 0 or nup[i] > 0:
             # REF (4 columns) blank, then NBLO and NBUP (I2 each, columns 103-106)
             tail = f"{'':4s}{nlo[i]:2d}{nup[i]:2d}" + " " * (160 - 106)
+        if lines.iso2 is not None and int(lines.iso2[i]) > 0:
+            # ISO1 (columns 107-109) blank, ISO2 (I3, columns 117-119)
+            tail = tail[:116 - 98] + f"{int(lines.iso2[i]):3d}" + tail[119 - 98:]
         if lines.tag is not None and str(lines.tag[i]).strip():
             # the 3-character tag of columns 142-144 (AUT, COR, PRD)
             tail = tail[:141 - 98] + f"{str(lines.tag[i]):3.3s}" + tail[144 - 98:]

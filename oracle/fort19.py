@@ -84,6 +84,53 @@ def aut_rows(cat: Dict[str, np.ndarray]) -> np.ndarray:
                           & ~clab)
 
 
+CODEX = np.array([1.0, 2.0, 2.01, 6.0, 6.01, 12.0, 12.01, 13.0, 13.01, 14.0, 14.01, 20.0, 20.01, 8.0, 11.0,
+                  5.0, 19.0])
+
+
+def merge_index(cat: Dict[str, np.ndarray], i: int):
+    """NCON and NELIONX of record i (fort19.py:330-338); (0, 0) without
+    ISO fields."""
+    if "iso1" not in cat:
+        return 0, 0
+    iso1, iso2 = int(cat["iso1"][i]), int(cat["iso2"][i])
+    ncon = iso2 if iso1 == 0 and iso2 > 0 else 0
+    m = np.nonzero(np.isclose(CODEX, float(cat["code"][i]), rtol=0.0, atol=1e-3))[0]
+    return ncon, (int(m[0]) + 1 if m.size else 0)
+
+
+def continuum_limits(ncon, nelion, nelionx, emerge, emerge_h, contx):
+    """_compute_continuum_limits_jit (opacity.py:657-702), vacuum grid:
+    (WCON, WTAIL), None where absent."""
+    if ncon <= 0 or nelionx <= 0 or nelionx > contx.shape[1] or ncon > contx.shape[0]:
+        return None, None
+    cv = float(contx[ncon - 1, nelionx - 1])
+    if cv <= 0.0:
+        return None, None
+    em = emerge_h if nelion == 1 else emerge
+    denom = cv - em
+    if abs(denom) <= 1e-8:
+        return None, None
+    wcon = 1.0e7 / denom
+    wtail = -1.0
+    dt = cv - em - 500.0
+    if abs(dt) > 1e-8:
+        wtail = 1.0e7 / dt
+        if wtail < 0.0:
+            wtail = 2.0 * wcon
+        wtail = min(2.0 * wcon, wtail)
+    if wtail > 0.0 and wtail <= wcon:
+        wtail = -1.0
+    return (wcon if wcon > 0.0 else None), (wtail if wtail > 0.0 else None)
+
+
+def contx_table() -> np.ndarray:
+    from pathlib import Path
+    p = Path(__file__).resolve().parent.parent / "kurucz_py_joss_submission_gb300" / "data" / "hydrogen_tables.npz"
+    with np.load(p) as t:
+        return np.asarray(t["contx"])
+
+
 def _nelion(code: float) -> int:
     """The fort.19 ion index (fort19.py:323-328)."""
     nelem = int(code + 1.0e-6) if code > 0.0 else 0
@@ -210,8 +257,8 @@ def line_doppler(atm: Dict[str, np.ndarray], d: int, wl: float, microturb_kms: f
     return wl * math.sqrt(total * total + thermal * thermal)
 
 
-def _metal_wing(tmp, cont, grid, ci, wl, kappa0, adamp, dw, cutoff, tb):
-    """_accumulate_metal_profile_kernel without WCON/WTAIL (opacity.py:74-262)."""
+def _metal_wing(tmp, cont, grid, ci, wl, kappa0, adamp, dw, cutoff, tb, wcon=None, wtail=None):
+    """_accumulate_metal_profile_kernel (opacity.py:74-262)."""
     if dw <= 0.0 or kappa0 <= 0.0:
         return
     n = grid.size
@@ -262,18 +309,28 @@ def _metal_wing(tmp, cont, grid, ci, wl, kappa0, adamp, dw, cutoff, tb):
 
     if ci + nstep < 0 or ci - nstep >= n:
         return
+    def taper(v, w):
+        if wtail is not None and w < wtail:
+            base = wcon if wcon is not None else wl
+            v = v * (w - base) / max(wtail - base, 1e-12)
+        return v
+
     if ci < n - 1:
         maxred = min(n - 1 - ci, nstep) if ci >= 0 else min(n - 1, nstep)
         for k in range(max(1, -ci), maxred + 1):
             b = ci + k
             if 0 <= b < n:
-                tmp[b] += value(k)
+                if wcon is not None and grid[b] <= wcon:
+                    continue
+                tmp[b] += taper(value(k), grid[b])
     if ci <= 0:
         return
     for k in range(max(1, ci + 1 - n), min(ci, nstep) + 1):
         b = ci - k
         if 0 <= b < n:
-            tmp[b] += value(k)
+            if wcon is not None and grid[b] <= wcon:
+                break
+            tmp[b] += taper(value(k), grid[b])
 
 
 def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np.ndarray,
@@ -297,6 +354,7 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
     xne = np.asarray(atm["electron_density"])
     hckt = np.asarray(atm["hckt"])
     txn = oracle.txnxn(atm)
+    contx = contx_table()
     nmerge = np.maximum(1600.0 / np.power(np.maximum(xne, 1e-40), 2.0 / 15.0) - 1.5, 1.0)
     emerge = 109737.312 / np.maximum(nmerge ** 2, 1e-12)
     emerge_h = 109677.576 / np.maximum(nmerge ** 2, 1e-12)
@@ -356,7 +414,12 @@ def asynth_term(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np
             kapcen = k0 * (1.0 - 1.128 * adamp) if adamp < 0.2 else k0 * oracle.voigt(0.0, adamp, tb)
             if kapcen >= kapmin:
                 tmp[cc] += kapcen
-            _metal_wing(tmp, continuum[d], grid, ci, wl, k0, adamp, dw, cutoff, tb)
+            nc, nx = merge_index(cat, i)
+            wcon, wtail = (None, None)
+            if nc > 0 and nx > 0:
+                wcon, wtail = continuum_limits(nc, _nelion(float(cat["code"][i])), nx, float(emerge[d]),
+                                               float(emerge_h[d]), contx)
+            _metal_wing(tmp, continuum[d], grid, ci, wl, k0, adamp, dw, cutoff, tb, wcon, wtail)
         if np.any(tmp > 0.0):
             out[d] = tmp * stim[d]
     return out

@@ -169,6 +169,13 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
                 iso1 = int(i1)
             except ValueError:
                 iso1 = 0
+        iso2 = 0
+        i2 = line[116:119].strip() if len(line) >= 119 else ""
+        if i2:
+            try:
+                iso2 = int(i2)
+            except ValueError:
+                iso2 = 0
         line_size = 0
         tag = ""
         c2 = line[134:144] if len(line) >= 144 else ""
@@ -195,9 +202,9 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
         elif nelem == 2 and ion == 2:
             lt = -6
         rows.append((wavelength, log_gf, code, elo, gr, gs, gw, nelem, ion, lt, nblo, nbup, line_size,
-                     grl, gsl, gwl, xj, xjp, cont_label))
+                     grl, gsl, gwl, xj, xjp, cont_label, iso1, iso2))
     if not rows:
-        arr = np.zeros((0, 19))
+        arr = np.zeros((0, 21))
     else:
         arr = np.array(rows, dtype=np.float64)
     return {
@@ -220,6 +227,8 @@ def parse_gfall(path: Path, potion: np.ndarray) -> Dict[str, np.ndarray]:
         "xj": arr[:, 16].copy(),
         "xjp": arr[:, 17].copy(),
         "continuum_label": arr[:, 18].astype(np.int32),
+        "iso1": arr[:, 19].astype(np.int32),
+        "iso2": arr[:, 20].astype(np.int32),
     }
 
 

@@ -58,6 +58,11 @@ def wings(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np.ndarr
     hckt = np.asarray(atm["hckt"])
     txn = oracle.txnxn(atm)
     rows = helium_rows(cat)
+    from . import fort19
+    contx = fort19.contx_table()
+    nmerge = np.maximum(1600.0 / np.power(np.maximum(xne, 1e-40), 2.0 / 15.0) - 1.5, 1.0)
+    emerge = 109737.312 / np.maximum(nmerge ** 2, 1e-12)
+    emerge_h = 109677.576 / np.maximum(nmerge ** 2, 1e-12)
     for d in range(L):
         local = np.zeros(N)
         for i in rows:
@@ -94,16 +99,35 @@ def wings(cat: Dict[str, np.ndarray], atm: Dict[str, np.ndarray], grid: np.ndarr
             dn = (float(cat["gamma_rad"][i]) + float(cat["gamma_stark"][i]) * float(xne[d])
                   + float(cat["gamma_vdw"][i]) * float(txn[d])) / max(doppler / wl, 1e-40)
             a = max(dn, 1e-12)
+            # continuum-merge limits: only fort.19 records (NBLO/NBUP set) carry them
+            wcon = wtail = None
+            if "n_lower" in cat and (abs(int(cat["n_lower"][i])) + abs(int(cat["n_upper"][i]))) != 0:
+                nc, nx = fort19.merge_index(cat, i)
+                if nc > 0 and nx > 0:
+                    wcon, wtail = fort19.continuum_limits(nc, nelion, nx, float(emerge[d]), float(emerge_h[d]),
+                                                          contx)
+            base = wcon if wcon is not None else wl
+
+            def val(b):
+                v = keff * oracle.voigt(abs(grid[b] - wl) / doppler, a, tb)
+                if wtail is not None and grid[b] < wtail:
+                    v = v * (grid[b] - base) / max(wtail - base, 1e-12)
+                return v
+
             tmp = np.zeros(N)
             if wl <= grid[N - 1]:
                 for b in range(ci, N):
-                    v = keff * oracle.voigt(abs(grid[b] - wl) / doppler, a, tb)
+                    if wcon is not None and grid[b] <= wcon:
+                        continue
+                    v = val(b)
                     if v < continuum[d, b] * cutoff:
                         break
                     tmp[b] += v
             if ci > 0 and wl >= grid[0]:
                 for b in range(ci - 1, -1, -1):
-                    v = keff * oracle.voigt(abs(grid[b] - wl) / doppler, a, tb)
+                    if wcon is not None and grid[b] <= wcon:
+                        break
+                    v = val(b)
                     tmp[b] += v
                     if v < continuum[d, b] * cutoff:
                         break

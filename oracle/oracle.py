@@ -258,7 +258,11 @@ def synthesize(atm: Dict[str, np.ndarray], cat: Dict[str, np.ndarray], wl_start:
         from . import helium
         ec = dict(wavelength=cat["wavelength"], gf=10.0 ** cat["log_gf"], elo=cat["excitation_energy"],
                   gamma_rad=cat["gamma_rad"], gamma_stark=cat["gamma_stark"], gamma_vdw=cat["gamma_vdw"],
-                  ion_stage=cat["ion_stage"], line_type=lt, center=cidx)
+                  ion_stage=cat["ion_stage"], line_type=lt, center=cidx, code=cat["code"],
+                  n_lower=cat["n_lower"], n_upper=cat["n_upper"])
+        for k in ("iso1", "iso2"):
+            if k in cat:
+                ec[k] = cat[k]
         he = helium.line_opacity(ec, atm, grid, kapmin, cutoff=cutoff)
         line_op = line_op + he * (1.0 - fscat[:, None])
         line_sc = line_sc + he * fscat[:, None]

@@ -132,6 +132,15 @@ CASES = {
     "cont_505_507": dict(atm="t5800g444", wl_start=505.5, wl_end=507.5,
                          n_lines=120, draw=(505.35, 507.65), log_uniform=False, seed=26,
                          continuum_records=[(505.42, 40.0, -13.0), (505.62, 50.0, -12.5), (506.55, 30.0, -13.5)]),
+    # fort.19 continuum-merge limits: Mg I lines with NBLO/NBUP and ISO2 = 2
+    # (NCON 2: WCON near 252 nm, WTAIL near 256 nm, per layer) and a He II
+    # line with NBLO/NBUP and ISO2 = 5 (WCON near 587 nm, WTAIL near 605 nm)
+    "ncon_252": dict(atm="t5800g444", wl_start=251.6, wl_end=253.2,
+                     n_lines=80, draw=(251.45, 253.35), log_uniform=False, seed=27,
+                     ncon_lines=dict(code=12.00, iso2=2, every=4, nb=(3, 6))),
+    "heii_595": dict(atm="t20000g400", wl_start=594.6, wl_end=595.4,
+                     n_lines=80, draw=(594.45, 595.55), log_uniform=False, seed=28,
+                     ncon_extra=[(595.0, 1.5, 421352.5, 2.01, 5, 24, 5)], helium=True),
 }
 
 # Cases too large to commit every stage array for: keep a subset.
@@ -185,6 +194,29 @@ def case_lines(case: dict) -> workloads.LineDraw:
             code=np.full(len(recs), 26.00), e_lower_cm=np.full(len(recs), 1500.0),
             log_gamma_rad=z + 8.0, log_gamma_stark=z - 5.0, log_gamma_vdw=z - 7.5,
             labelp=np.array(["CONTINUU"] * len(recs), dtype=object), xjp=np.array([r[1] for r in recs]))
+        lines = workloads.merge_lines(lines, extra)
+    if case.get("ncon_lines"):
+        spec = case["ncon_lines"]
+        idx = np.arange(0, len(lines), spec["every"])
+        lo, up = lines.levels()
+        lo, up = lo.copy(), up.copy()
+        lo[idx], up[idx] = spec["nb"]
+        lines.n_lower, lines.n_upper = lo, up
+        iso2 = np.zeros(len(lines), np.int32)
+        iso2[idx] = spec["iso2"]
+        lines.iso2 = iso2
+        lines.code[idx] = spec["code"]
+        lines.log_gf[idx] = np.maximum(lines.log_gf[idx], -1.0)
+        lines.e_lower_cm[idx] = np.minimum(lines.e_lower_cm[idx], 20000.0)
+    if case.get("ncon_extra"):
+        recs = case["ncon_extra"]
+        z = np.zeros(len(recs))
+        extra = workloads.LineDraw(
+            wavelength_nm=np.array([r[0] for r in recs]), log_gf=np.array([r[1] for r in recs]),
+            code=np.array([r[3] for r in recs]), e_lower_cm=np.array([r[2] for r in recs]),
+            log_gamma_rad=z + 8.5, log_gamma_stark=z - 4.0, log_gamma_vdw=z - 7.6,
+            n_lower=np.array([r[4] for r in recs], np.int32), n_upper=np.array([r[5] for r in recs], np.int32),
+            iso2=np.array([r[6] for r in recs], np.int32))
         lines = workloads.merge_lines(lines, extra)
     if case.get("strong"):
         # push a handful of lines to saturation so the surface optical depth

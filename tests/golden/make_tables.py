@@ -96,6 +96,8 @@ def write_hydrogen_tables() -> None:
         out[k] = out[k].astype(np.int32)
     out["ehyd"] = np.asarray(eo._EHYD_CM, dtype=np.float64)
     out["conth"] = np.asarray(metal_wing_tables().conth, dtype=np.float64)
+    # continuum edges of the fort.19 merge limits (tables.py:173, CONTX [25, 17])
+    out["contx"] = np.asarray(metal_wing_tables().contx, dtype=np.float64)
     path = OUT.parent / "hydrogen_tables.npz"
     np.savez_compressed(path, **out)
     print(f"wrote {path}")

@@ -65,6 +65,23 @@ def test_oracle_asynth_with_merged_continuum_records():
     assert float(rel.max()) < 1e-13
 
 
+@pytest.mark.parametrize("name,key", [("ncon_252", "asynth"), ("heii_595", "line_opacity")])
+def test_oracle_continuum_merge_limits(name, key):
+    """fort.19 records with NCON set: the WCON cut and the WTAIL taper of a
+    NORMAL line's wings (Mg I, NCON 2) and of a helium line's (He II, NCON 5)."""
+    if name not in available_cases():
+        pytest.skip("golden missing")
+    g = golden(name)
+    w0, w1 = window(name)
+    tb = oracle.tables()
+    cat = gfall.filter_window(gfall.parse_gfall(gfall_path(name), tb["potion"]), w0, w1)
+    assert np.any(cat["iso2"] > 0)
+    r = oracle.synthesize(oracle.load_atmosphere(atm_path(name)), cat, w0, w1, tb=tb)
+    mine = r["line_opacity"] if key == "line_opacity" else r["asynth"]
+    rel = np.abs(mine - g[key]) / np.maximum(np.abs(g[key]), 1e-300)
+    assert float(rel.max()) < 1e-13
+
+
 def test_oracle_detects_planted_error():
     g = golden(CASE)
     w0, w1 = window(CASE)
