@@ -158,8 +158,24 @@ def _stage_dumps(path: Path, cfg, catalog, atm, wavelength, syn, ft_hz, fc_hz) -
     order = np.argsort(catalog.catalog_index)
     np.savez(path / "stage_3_transp.npz", transp=transp[order], valid_mask=valid[order],
              line_indices=cidx[order])
-    np.savez(path / "stage_4_asynth.npz", asynth=syn.asynth.double().cpu().numpy(),
-             wavelength=wavelength)
+    full = syn.asynth.double().cpu().numpy()
+    stage4 = full
+    rec = syn.catalog.rec
+    if rec.n_hydrogen or rec.n_helium:
+        # the reference's stage-4 ASYNTH precedes the hydrogen profiles and
+        # the helium wings (opacity.py:2395-2404, :2465, :3650): rerun without them
+        nh, nhe = rec.n_hydrogen, rec.n_helium
+        rec.n_hydrogen = rec.n_helium = 0
+        try:
+            syn.run()
+            stage4 = syn.asynth.double().cpu().numpy()
+        finally:
+            rec.n_hydrogen, rec.n_helium = nh, nhe
+    np.savez(path / "stage_4_asynth.npz", asynth=stage4, wavelength=wavelength)
+    # the transfer's line opacity: absorption ASYNTH (1 - FSCAT), scattering
+    # ASYNTH FSCAT (opacity.py:2416-2440, :3650-3661)
+    rhox = np.asarray(atm.depth, dtype=np.float64)
+    fscat = np.exp(-rhox / cfg.rhoxj_scale) if cfg.rhoxj_scale > 0.0 else np.zeros_like(rhox)
     np.savez(path / "stage_5_rt.npz", wavelength=wavelength, flux_total_hz=ft_hz, flux_cont_hz=fc_hz,
              flux_total=ft_hz, flux_cont=fc_hz, cont_abs=ca, cont_scat=cs,
-             line_opacity=syn.asynth.double().cpu().numpy())
+             line_opacity=full * (1.0 - fscat[:, None]), line_scattering=full * fscat[:, None])
