@@ -109,24 +109,28 @@ typedef struct {
     /* hydrogen lines (line types -1/-2 of neutral H), added with the HPROF4
      * profile (synthe_py/engine/opacity.py:1706): their rows, in catalog
      * order, and their principal quantum numbers (device; n_hydrogen = 0 for
-     * none; at most 256) */
+     * none; at most 65536: beyond 256 lines of a
+     * class ks_synthesize allocates their scratch on its stream, the
+     * no-allocation entry point rejects them) */
     int32_t n_hydrogen;
     const int32_t *hydrogen_rows;
     const int32_t *hydrogen_n_lower;
     const int32_t *hydrogen_n_upper;
-    /* helium lines (line types -3/-4/-6: He I, 3He I, He II) without fort.19
-     * continuum limits: the helium wing pass (synthe_py/engine/opacity.py:
+    /* helium lines (line types -3/-4/-6: He I, 3He I, He II; their fort.19
+     * continuum-merge limits in helium_ncon / helium_nelionx): the helium wing pass (synthe_py/engine/opacity.py:
      * 2515-3590, Voigt wings of _apply_fort19_profile :996-1061), added to the
      * line opacity as AHE x STIM (:3650-3660); their rows in catalog order
-     * (device; n_helium = 0 for none; at most 256) */
+     * (device; n_helium = 0 for none; at most 65536: beyond 256 lines of a
+     * class ks_synthesize allocates their scratch on its stream, the
+     * no-allocation entry point rejects them) */
     int32_t n_helium;
     const int32_t *helium_rows;
-    /* fort.19 lines: NORMAL ones (NBLO/NBUP set, line type 0, no continuum-merge
-     * limits): the profiles of _add_fort19_asynth (synthe_py/engine/
+    /* fort.19 lines: NORMAL ones (NBLO/NBUP set, line type 0; their continuum-
+     * merge limits in f19_ncon / f19_nelionx): the profiles of _add_fort19_asynth (synthe_py/engine/
      * opacity.py:1335-1488) added to ASYNTH; their rows in catalog order and
      * the fort.19 record's CGF and damping constants, rounded to single
      * precision as the record stores them (io/lines/fort19.py:368-402);
-     * device; n_f19 = 0 for none; at most 256 */
+     * device; n_f19 = 0 for none; at most 65536, see above */
     int32_t n_f19;
     const int32_t *f19_rows;
     const double *f19_cgf, *f19_gamma_rad, *f19_gamma_stark, *f19_gamma_vdw;

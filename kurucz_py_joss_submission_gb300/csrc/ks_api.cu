@@ -630,9 +630,13 @@ struct Workspace {
     int nchunks;
 };
 
-// Hydrogen lines, and helium lines, a synthesis takes (their scratch is part
-// of every workspace).
+// Special lines (hydrogen, helium, fort.19) whose per-(line, depth) scratch
+// every workspace holds; a synthesis with more allocates the rest on its
+// stream (stream-ordered, freed after use); the no-allocation entry point
+// takes at most this many of each.
 static const int kMaxHydrogenLines = 256;
+// Upper bound of special lines of one class in a synthesis.
+static const int kMaxSpecialLines = 1 << 16;
 
 static void layout(Carve& c, Workspace& w, int64_t n_lines, int L, int64_t n_wl, int n_ion,
                    int n_elem, bool fp64, bool need_cont, bool need_asynth, int tile_bins = 0) {
@@ -730,17 +734,16 @@ static ks_status check_lines(const ks_lines* l) {
     if (l->n_lines > 0x7fffffffLL) return fail(KS_ERR_UNSUPPORTED, "more than 2^31 lines");
     if (l->n_hydrogen < 0 || l->n_hydrogen > l->n_lines)
         return fail(KS_ERR_INVALID, "n_hydrogen must lie in [0, n_lines]");
-    if (l->n_hydrogen > kMaxHydrogenLines)
-        return fail(KS_ERR_UNSUPPORTED, "more than 256 hydrogen lines");
+    if (l->n_hydrogen > kMaxSpecialLines) return fail(KS_ERR_UNSUPPORTED, "more than 65536 hydrogen lines");
     if (l->n_hydrogen > 0 && (!l->hydrogen_rows || !l->hydrogen_n_lower || !l->hydrogen_n_upper))
         return fail(KS_ERR_INVALID, "lines: a hydrogen column is NULL");
     if (l->n_helium < 0 || l->n_helium > l->n_lines)
         return fail(KS_ERR_INVALID, "n_helium must lie in [0, n_lines]");
-    if (l->n_helium > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 helium lines");
+    if (l->n_helium > kMaxSpecialLines) return fail(KS_ERR_UNSUPPORTED, "more than 65536 helium lines");
     if (l->n_helium > 0 && (!l->helium_rows || !l->helium_ncon || !l->helium_nelionx))
         return fail(KS_ERR_INVALID, "lines: a helium column is NULL");
     if (l->n_f19 < 0 || l->n_f19 > l->n_lines) return fail(KS_ERR_INVALID, "n_f19 must lie in [0, n_lines]");
-    if (l->n_f19 > kMaxHydrogenLines) return fail(KS_ERR_UNSUPPORTED, "more than 256 fort.19 lines");
+    if (l->n_f19 > kMaxSpecialLines) return fail(KS_ERR_UNSUPPORTED, "more than 65536 fort.19 lines");
     if (l->n_f19 > 0 && (!l->f19_rows || !l->f19_cgf || !l->f19_gamma_rad || !l->f19_gamma_stark ||
                          !l->f19_gamma_vdw || !l->f19_kind || !l->f19_nlast || !l->f19_nelion ||
                          !l->f19_ncon || !l->f19_nelionx))
@@ -1368,7 +1371,8 @@ template <typename R>
 static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, const ks_grid* grid,
                                  const ks_options* opt, Workspace& w, const DevTables& t,
                                  double* flux_total, double* flux_cont, R* asynth,
-                                 cudaStream_t s, StageTimer& tm, bool do_transfer = true) {
+                                 cudaStream_t s, StageTimer& tm, bool do_transfer = true,
+                                 bool allow_alloc = true) {
     constexpr bool fp64 = sizeof(R) == 8;
     ks_status st;
     const int L = atm->n_layers;
@@ -1426,13 +1430,38 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f64(a, warps, (const PairDesc<double>*)w.desc, asynth, s));
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
-    if (lines->n_f19 > 0 && (st = run_f19<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
-        return st;
-    if (lines->n_hydrogen > 0 &&
-        (st = run_hydrogen<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
-        return st;
-    if (lines->n_helium > 0 && (st = run_helium<R>(lines, atm, grid, opt, w, t, cabs, cscat, asynth, s)))
-        return st;
+    const int n_special = std::max(lines->n_f19, std::max(lines->n_hydrogen, lines->n_helium));
+    if (n_special > 0) {
+        // more special lines than the workspace's scratch holds: the rest on
+        // the stream (freed once the special-line kernels are queued)
+        Workspace ws = w;
+        char* extra = nullptr;
+        if (n_special > w.hyd_cap) {
+            if (!allow_alloc)
+                return fail(KS_ERR_UNSUPPORTED, "more than 256 special lines of one class need stream-ordered "
+                                                "scratch, which this entry point does not allocate");
+            const size_t per = sizeof(HydPar) + sizeof(HePar) + sizeof(F19Par) + 6 * sizeof(int2);
+            const size_t bytes = (size_t)n_special * L * per + 1024;
+            KS_CUDA(cudaMallocAsync((void**)&extra, bytes, s));
+            Carve c{extra, bytes, 0, false};
+            ws.hyd_cap = n_special;
+            ws.hyd_par = c.take<HydPar>((size_t)n_special * L);
+            ws.hyd_walk = c.take<int2>((size_t)n_special * L * 2);
+            ws.he_par = c.take<HePar>((size_t)n_special * L);
+            ws.he_walk = c.take<int2>((size_t)n_special * L * 2);
+            ws.f19_par = c.take<F19Par>((size_t)n_special * L);
+            ws.f19_walk = c.take<int2>((size_t)n_special * L * 2);
+        }
+        st = KS_OK;
+        if (lines->n_f19 > 0) st = run_f19<R>(lines, atm, grid, opt, ws, t, cabs, cscat, asynth, s);
+        if (!st && lines->n_hydrogen > 0) st = run_hydrogen<R>(lines, atm, grid, opt, ws, t, cabs, cscat, asynth, s);
+        if (!st && lines->n_helium > 0) st = run_helium<R>(lines, atm, grid, opt, ws, t, cabs, cscat, asynth, s);
+        if (extra) {
+            cudaError_t fe = cudaFreeAsync(extra, s);
+            if (!st && fe != cudaSuccess) st = fail(KS_ERR_CUDA, std::string("cudaFreeAsync: ") + cudaGetErrorString(fe));
+        }
+        if (st) return st;
+    }
     tm.mark();
     if (do_transfer) {
         if ((st = run_transfer<R>(atm, grid, opt, w, t, cabs, cscat, asynth, flux_total, flux_cont, s)))
@@ -1784,6 +1813,10 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     if (!st) st = check_cont(atm);
     if (st) return st;
     if (!flux_total || !flux_cont) return fail(KS_ERR_INVALID, "ks_synthesize_noalloc: NULL flux output");
+    if (lines->n_hydrogen > kMaxHydrogenLines || lines->n_helium > kMaxHydrogenLines ||
+        lines->n_f19 > kMaxHydrogenLines)
+        return fail(KS_ERR_UNSUPPORTED, "ks_synthesize_noalloc: more than 256 special lines of one class "
+                                        "(their scratch would be allocated); use ks_synthesize");
     if ((st = check_tiling(opt))) return st;
     if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))
         return fail(KS_ERR_INVALID, "transfer_path must be 0 (streaming) or 1 (per-column)");
@@ -1824,8 +1857,12 @@ extern "C" ks_status ks_synthesize_noalloc(const ks_lines* lines, const ks_atmos
     StageTimer tm;  // off: no profiling in this entry point
     // synthesize_impl clears the counters, flags and reach classes in the
     // scratch before use; everything else is written before it is read.
-    if (fp64) st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s, tm);
-    else st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s, tm);
+    if (fp64)
+        st = synthesize_impl<double>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (double*)asy, s, tm, true,
+                                     false);
+    else
+        st = synthesize_impl<float>(lines, atm, grid, opt, w, t, flux_total, flux_cont, (float*)asy, s, tm, true,
+                                    false);
     return st;
 }
 

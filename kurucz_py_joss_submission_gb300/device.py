@@ -176,8 +176,8 @@ class DeviceCatalog:
         lt = np.asarray(cat.line_types)
         hyd = np.flatnonzero(((lt == -1) | (lt == -2)) & (np.asarray(cat.ion_stages) == 1) & hydrogen)
         self.n_hydrogen = int(hyd.size)
-        if self.n_hydrogen > 256:
-            raise ValueError(f"{self.n_hydrogen} hydrogen lines: the synthesis takes at most 256")
+        if self.n_hydrogen > 65536:
+            raise ValueError(f"{self.n_hydrogen} hydrogen lines: the synthesis takes at most 65536")
         if self.n_hydrogen:
             lo = np.asarray(cat.n_lower)[hyd]
             up = np.maximum(np.asarray(cat.n_upper)[hyd], lo + 1)
@@ -219,8 +219,8 @@ class DeviceCatalog:
             warnings.warn(f"{self.n_fort19_skipped} CONTINUU records of NLAST <= 1 contribute no opacity here",
                           RuntimeWarning, stacklevel=2)
         self.n_f19 = int(f19.size)
-        if self.n_f19 > 256:
-            raise ValueError(f"{self.n_f19} fort.19 lines: the synthesis takes at most 256")
+        if self.n_f19 > 65536:
+            raise ValueError(f"{self.n_f19} fort.19 lines: the synthesis takes at most 65536")
         if self.n_f19:
             is_cont = cont[f19]
             is_aut = (lt[f19] == 1) & ~is_cont
@@ -269,8 +269,8 @@ class DeviceCatalog:
         # helium wing pass, device rows in catalog order
         he = np.flatnonzero(np.isin(lt, (-3, -4, -6)) & helium)
         self.n_helium = int(he.size)
-        if self.n_helium > 256:
-            raise ValueError(f"{self.n_helium} helium lines: the synthesis takes at most 256")
+        if self.n_helium > 65536:
+            raise ValueError(f"{self.n_helium} helium lines: the synthesis takes at most 65536")
         if self.n_helium:
             self.t["helium_rows"] = _dev(he if self.order is None else inv_order(self.order)[he], np.int32, dev)
             # only fort.19 records (NBLO/NBUP set) carry the merge limits

@@ -157,3 +157,24 @@ def test_fp64_matches_oracle(key, tmp_path):
         assert np.any(c[fort19.aut_rows(ocat)] < 0)
     if key == "continuum":
         assert fort19.cont_rows(ocat).size == 3 and dcat.t["f19_kind"].eq(2).sum().item() == 3
+
+
+def test_more_lines_than_workspace_scratch(tmp_path):
+    """300 fort.19 lines (beyond the 256 a workspace holds scratch for): the
+    synthesis allocates the rest on its stream and matches the oracle."""
+    w0, w1 = 500.0, 500.6
+    d = workloads.random_atomic_lines(360, w0 - 0.15, w1 + 0.15, seed=38)
+    d.n_lower, d.n_upper = np.full(len(d), 3, np.int32), np.full(len(d), 5, np.int32)
+    p = tmp_path / "lines.gf"
+    p.write_text(workloads.format_gfall(d))
+    cat = atomic.load_catalog_window(p, w0, w1)
+    grid = oracle.wavelength_grid(w0, w1, 300000.0)
+    atm = atm_io.load_cached(ATM)
+    dcat, with_f, without = gpu_cubes(cat, atm, grid)
+    assert dcat.n_f19 > 256
+    ocat = gfall.filter_window(gfall.parse_gfall(p, oracle.tables()["potion"]), w0, w1)
+    ca, cs = build_depth_continuum(atm, grid, precision="fp64")
+    term = fort19.asynth_term(dict(ocat, center=oracle.center_indices(grid, ocat["wavelength"])),
+                              oracle.load_atmosphere(ATM), grid, ca + cs)
+    ref = without + term
+    assert float(np.max(np.abs(with_f - ref) / np.maximum(np.abs(ref), 1e-300))) < FP64_TOL
