@@ -643,6 +643,7 @@ FORMS = {
     "dense_10m": ["--workload", "dense_10m", "--steps", "3", "--warmup", "3", "--skip-cpu"],
     "diff_400_700": ["--workload", "diff_400_700", "--steps", "3", "--warmup", "3", "--fd-params", "40"],
     "pops_256": ["--workload", "pops_256", "--steps", "5", "--warmup", "3"],
+    "special_480_520": ["--workload", "special_480_520", "--steps", "5", "--warmup", "3"],
 }
 
 
@@ -942,6 +943,126 @@ def run_pops(args):
     return 0
 
 
+SPECIAL = dict(w0=480.0, w1=520.0, n_lines=20000, seed=406, nb_every=100, aut_every=400,
+               atm="atm_t5800g444.npz")
+
+
+def special_catalog_path() -> Path:
+    """The 480-520 nm list of the special-lines form: 20,000 seeded metal
+    lines, every 100th with NBLO/NBUP (fort.19 NORMAL), every 400th tagged AUT
+    (autoionizing), H beta and H gamma, the table's He I lines and three
+    merged-continuum (CONTINUU) records."""
+    from kurucz_py_joss_submission_gb300 import workloads
+
+    p = Path(os.environ.get("TMPDIR", "/tmp")) / f"kgb300_special_{SPECIAL['seed']}.gf"
+    if p.exists():
+        return p
+    d = workloads.random_atomic_lines(SPECIAL["n_lines"], SPECIAL["w0"] - 0.15, SPECIAL["w1"] + 0.15,
+                                      SPECIAL["seed"])
+    n = len(d)
+    lo, up = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    lo[::SPECIAL["nb_every"]], up[::SPECIAL["nb_every"]] = 3, 5
+    d.n_lower, d.n_upper = lo, up
+    ia = np.arange(SPECIAL["aut_every"] // 2, n, SPECIAL["aut_every"])
+    tag = np.array([""] * n, dtype=object)
+    tag[ia] = "AUT"
+    d.tag = tag
+    d.log_gamma_rad[ia], d.log_gamma_vdw[ia] = 11.0, 0.3
+    d.log_gamma_stark[ia] = np.where(np.arange(ia.size) % 2 == 0, -0.5, 0.3)
+    d.log_gf[ia] = np.minimum(d.log_gf[ia], -1.0) - 12.0
+    z = np.zeros(3)
+    cont = workloads.LineDraw(wavelength_nm=np.array([485.0, 495.0, 505.0]), log_gf=np.array([-16.0, -15.5, -16.5]),
+                              code=np.full(3, 26.00), e_lower_cm=np.full(3, 1500.0), log_gamma_rad=z + 8.0,
+                              log_gamma_stark=z - 5.0, log_gamma_vdw=z - 7.5,
+                              labelp=np.array(["CONTINUU"] * 3, dtype=object), xjp=np.array([40.0, 50.0, 30.0]))
+    d = workloads.merge_lines(d, workloads.balmer_lines([4, 5]), workloads.helium_lines(SPECIAL["w0"], SPECIAL["w1"]),
+                              cont)
+    tmpname = p.with_suffix(f".{os.getpid()}.tmp")
+    workloads.write_gfall(tmpname, d)
+    os.replace(tmpname, p)
+    return p
+
+
+def run_special(args):
+    """One 480-520 nm synthesis of a list holding every special line class
+    (hydrogen, helium, fort.19 NORMAL / autoionizing / merged continuum):
+    spectra/s, the special-line stage, the same synthesis without the special
+    lines, and the mixed path's error against FP64."""
+    import torch
+
+    from kurucz_py_joss_submission_gb300.device import (DeviceAtmosphere, DeviceCatalog, DeviceGrid,
+                                                         Synthesizer, make_options)
+    from kurucz_py_joss_submission_gb300.io import atmosphere as atm_io
+    from kurucz_py_joss_submission_gb300.io.lines import atomic
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if rank != 0:
+        return 0  # one window: replicas only
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w0, w1 = SPECIAL["w0"], SPECIAL["w1"]
+    cat = atomic.load_catalog_window(special_catalog_path(), w0, w1, sort=True)
+    atm = atm_io.load_cached(ROOT / "tests" / "golden" / SPECIAL["atm"])
+    grid = wavelength_grid(w0, w1)
+    dcat, datm, dgrid = DeviceCatalog(cat, dev), DeviceAtmosphere(atm, dev), DeviceGrid(grid, device=dev)
+    counts = {"hydrogen": dcat.n_hydrogen, "helium": dcat.n_helium, "fort19": dcat.n_f19}
+    syn = Synthesizer(dcat, datm, dgrid, make_options(precision="mixed"), keep_asynth=False)
+    st = syn.run(stats=True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # inputs fit in L2: flush per step
+
+    def timed(run):
+        for _ in range(args.warmup):
+            run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        total = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0.record()
+            run()
+            e1.record()
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+        return total / args.steps
+
+    with ClockSampler(local) as clk:
+        ms = timed(syn.run)
+    rec = dcat.rec
+    saved = (rec.n_hydrogen, rec.n_helium, rec.n_f19)
+    rec.n_hydrogen = rec.n_helium = rec.n_f19 = 0
+    ms_plain = timed(syn.run)
+    rec.n_hydrogen, rec.n_helium, rec.n_f19 = saved
+    prof = Synthesizer(dcat, datm, dgrid, make_options(precision="mixed", profile=True), keep_asynth=False)
+    stages = [prof.run(stats=True)["stage_ms"] for _ in range(5)]
+    stage_ms = {k: statistics.median(s[k] for s in stages) for k in stages[0]}
+    ft, fc = syn.flux_total.cpu().numpy(), syn.flux_cont.cpu().numpy()
+    ref = Synthesizer(dcat, datm, dgrid, make_options(precision="fp64"), keep_asynth=False)
+    ref.run()
+    torch.cuda.synchronize()
+    err = flux_errors(ft, fc, ref.flux_total.cpu().numpy(), ref.flux_cont.cpu().numpy())
+    line = {
+        "metric": "spectra/s (480-520 nm, 20,000 lines with hydrogen, helium and fort.19 lines, mixed)",
+        "value": 1e3 / ms, "unit": "spectra/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "special_480_520", "grid_points": int(grid.size), "lines": len(cat),
+                   "special_lines": counts, "atmosphere": SPECIAL["atm"], "seed": SPECIAL["seed"],
+                   "l2": "inputs smaller than L2: 256 MB written before every timed step",
+                   "parallelism": "1 GPU"},
+        "ms_without_special_lines": ms_plain,
+        "stage_ms": stage_ms,
+        "evaluations_per_step": int(st["evaluations"]),
+        "accuracy_vs_fp64": err,
+        "gpu_launches": int(st["kernel_launches"]) * args.steps,
+        "clocks": clk.summary(),
+        "roofline": None,
+        "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 DIFF_ELEMENTS = (1, 2, 6, 7, 8, 11, 12, 13, 14, 16, 19, 20, 22, 23, 24, 25, 26, 27, 28, 29)
 
 
@@ -1109,7 +1230,8 @@ def main():
                     help="diff_400_700: parameters checked by central finite differences")
     ap.add_argument("--window", type=float, nargs=2, default=None,
                     help="restrict the workload to a wavelength window (small profiling case)")
-    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS) + ["batch_256", "diff_400_700", "pops_256"],
+    ap.add_argument("--workload", choices=sorted(BENCH_WORKLOADS) + ["batch_256", "diff_400_700", "pops_256",
+                                                                     "special_480_520"],
                     default="full_300_1800",
                     help="full_300_1800 (headline: 1.5M lines, Teff 5800 K), window_500_510 (20k lines, "
                          "the CPU-runnable reference case), dense_10m (10M lines, Teff 2500 K, log g -1)")
@@ -1125,6 +1247,11 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "population workload: timed on the GPU path only"}))
             return 0
         return run_pops(args)
+    if args.workload == "special_480_520":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "special-lines workload: timed on the GPU path only"}))
+            return 0
+        return run_special(args)
     if args.workload == "batch_256":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "batched workload: timed on the GPU path only"}))

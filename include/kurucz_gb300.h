@@ -181,7 +181,8 @@ typedef struct {
     int32_t device_flags;       /* nonzero when a kernel hit an internal limit */
     int32_t kernel_launches;    /* kernels this call launched */
     float stage_ms[8];          /* with ks_options.profile: bins+prep, continuum, pair setup,
-                                   partition, accumulation, transfer, (unused), total */
+                                   partition, accumulation, transfer, special lines (hydrogen,
+                                   helium, fort.19; 0 without), total */
 } ks_stats;
 
 /* ---- library ---------------------------------------------------------- */

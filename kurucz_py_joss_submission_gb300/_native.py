@@ -109,11 +109,11 @@ class KsStats(C.Structure):
     ]
 
     STAGES = ("bins_prep", "continuum", "pair_setup", "partition", "accumulate", "transfer",
-              "unused", "total")
+              "special", "total")
 
     def as_dict(self) -> dict:
         d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "stage_ms"}
-        d["stage_ms"] = {n: float(v) for n, v in zip(self.STAGES, self.stage_ms) if n != "unused"}
+        d["stage_ms"] = {n: float(v) for n, v in zip(self.STAGES, self.stage_ms)}
         return d
 
 

@@ -1142,18 +1142,29 @@ extern "C" ks_status ks_formal_solution(const ks_atmos* atm, const ks_grid* grid
 struct StageTimer {
     bool on = false;
     cudaEvent_t ev[8];
+    cudaEvent_t ev_special;  // end of the special-line kernels (after the accumulation mark)
+    bool special = false;
     int n = 0;
     cudaStream_t s = nullptr;
     void start(cudaStream_t st, bool enable) {
         on = enable;
         s = st;
+        special = false;
         if (!on) return;
         for (int i = 0; i < 8; i++) cudaEventCreate(&ev[i]);
+        cudaEventCreate(&ev_special);
         cudaEventRecord(ev[0], s);
         n = 1;
     }
     void mark() {
         if (on && n < 8) cudaEventRecord(ev[n++], s);
+    }
+    // the hydrogen/helium/fort.19 kernels, queued right after the accumulation mark
+    void mark_special() {
+        if (on && n == 6) {
+            cudaEventRecord(ev_special, s);
+            special = true;
+        }
     }
     void finish(ks_stats* stats) {
         if (!on) return;
@@ -1161,9 +1172,15 @@ struct StageTimer {
         if (stats) {
             for (int i = 0; i < 8; i++) stats->stage_ms[i] = 0.f;
             for (int i = 1; i < n && i <= 6; i++) cudaEventElapsedTime(&stats->stage_ms[i - 1], ev[i - 1], ev[i]);
+            if (special) {
+                // stage 6: special lines; the transfer counts from their end
+                cudaEventElapsedTime(&stats->stage_ms[6], ev[5], ev_special);
+                if (n > 6) cudaEventElapsedTime(&stats->stage_ms[5], ev_special, ev[6]);
+            }
             cudaEventElapsedTime(&stats->stage_ms[7], ev[0], ev[n - 1]);
         }
         for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
+        cudaEventDestroy(ev_special);
         on = false;
     }
 };
@@ -1430,6 +1447,7 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
         KS_CUDA(launch_accumulate_f64(a, warps, (const PairDesc<double>*)w.desc, asynth, s));
     else
         KS_CUDA(launch_accumulate_f32(a, warps, (const PairDesc<float>*)w.desc, asynth, s));
+    tm.mark();
     const int n_special = std::max(lines->n_f19, std::max(lines->n_hydrogen, lines->n_helium));
     if (n_special > 0) {
         // more special lines than the workspace's scratch holds: the rest on
@@ -1461,8 +1479,8 @@ static ks_status synthesize_impl(const ks_lines* lines, const ks_atmos* atm, con
             if (!st && fe != cudaSuccess) st = fail(KS_ERR_CUDA, std::string("cudaFreeAsync: ") + cudaGetErrorString(fe));
         }
         if (st) return st;
+        tm.mark_special();
     }
-    tm.mark();
     if (do_transfer) {
         if ((st = run_transfer<R>(atm, grid, opt, w, t, cabs, cscat, asynth, flux_total, flux_cont, s)))
             return st;
