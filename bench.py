@@ -1033,6 +1033,7 @@ def run_special(args):
     rec.n_hydrogen = rec.n_helium = rec.n_f19 = 0
     ms_plain = timed(syn.run)
     rec.n_hydrogen, rec.n_helium, rec.n_f19 = saved
+    syn.run()   # the fluxes compared below: with the special lines again
     prof = Synthesizer(dcat, datm, dgrid, make_options(precision="mixed", profile=True), keep_asynth=False)
     stages = [prof.run(stats=True)["stage_ms"] for _ in range(5)]
     stage_ms = {k: statistics.median(s[k] for s in stages) for k in stages[0]}
