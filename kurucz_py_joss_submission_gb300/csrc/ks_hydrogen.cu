@@ -14,9 +14,9 @@
 //                      kappa0, the merge and tail wavelengths, the line's
 //                      series-neighbour wavelengths and the hydrogen depth
 //                      state (synthe_py/physics/populations.py:93-125);
-//   hyd_march_kernel   one warp per (line, depth, side): the walk, 32 offsets
-//                      at a time, each lane evaluating one offset; a ballot
-//                      finds where the walk ends;
+//   hyd_walk_*_kernel  where each (line, depth, side) walk ends: every offset
+//                      tested at once, one thread per (walk, offset), the
+//                      smallest stopping offset kept by atomicMin;
 //   hyd_gather_kernel  one thread per (depth, grid point): the contributions
 //                      of the lines whose walks cover the point, recomputed
 //                      and summed in catalog order (the order of the
@@ -26,7 +26,7 @@
 // (synthe_py/engine/opacity.py:2515-3590: per layer and line the TRANSP-style
 // gates, then ``_apply_fort19_profile``'s Voigt walk for TYPE < -2, :966-1061)
 // and enter the line opacity as AHE x STIM (:3650-3660), with the same three
-// kernel shapes (he_setup_kernel, he_march_kernel, he_gather_kernel).
+// kernel shapes (he_setup_kernel, he_walk_*_kernel, he_gather_kernel).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -539,19 +539,17 @@ __global__ void __launch_bounds__(128) hyd_setup_kernel(HydArgs a) {
     a.par[i] = q;
 }
 
-// One warp per (line, depth, side): the walk's first and end offsets.
+// The walks' first offsets and, as a start, their last possible end (one
+// thread per (line, depth, side)): offsets [x, y) with y = MAX_STEPS + 1.
 template <typename R>
-__global__ void __launch_bounds__(128) hyd_march_kernel(HydArgs a) {
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(128) hyd_walk_init_kernel(HydArgs a) {
+    const int64_t gw = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gw >= (int64_t)a.n_h * a.n_layers * 2) return;
-    const int64_t pd = gw >> 1;
+    const HydPar& q = a.par[gw >> 1];
     const int side = (gw & 1) ? -1 : 1;
-    const HydPar q = a.par[pd];
-    int2 out = make_int2(1, 1);  // walk offsets [x, y)
+    int2 out = make_int2(1, 1);
     if (q.active) {
-        const int64_t n = a.n_wl;
-        const int64_t ci = q.ci;
+        const int64_t n = a.n_wl, ci = q.ci;
         int64_t first = 1;
         bool alive = true;
         if (ci >= n) {
@@ -562,33 +560,36 @@ __global__ void __launch_bounds__(128) hyd_march_kernel(HydArgs a) {
             first = -ci > 1 ? -ci : 1;
         }
         const int64_t max_steps = ci > n - ci - 1 ? ci : n - ci - 1;
-        int64_t end = first;
-        if (alive) {
-            for (int64_t o0 = first; o0 <= max_steps; o0 += 32) {
-                const int64_t o = o0 + lane;
-                bool stop = false;
-                if (o <= max_steps) {
-                    const int64_t b = ci + side * o;
-                    if (b < 0 || b >= n) {
-                        stop = true;
-                    } else {
-                        bool add;
-                        walk_value<R>(a, q, b, side, &stop, &add);
-                    }
-                } else {
-                    stop = true;
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, stop);
-                if (m) {
-                    end = o0 + (__ffs(m) - 1);
-                    break;
-                }
-                end = o0 + 32;
-            }
-        }
-        out = make_int2((int)first, (int)end);
+        out = make_int2((int)first, (int)(alive ? max_steps + 1 : first));
     }
-    if (lane == 0) a.walk[gw] = out;
+    a.walk[gw] = out;
+}
+
+// Where each walk ends: the reference steps outward until the first offset
+// whose value stops it.  Here every offset is tested at once, one thread per
+// (walk, offset) in blocks of 256 consecutive offsets, and the smallest
+// stopping offset is kept with atomicMin (order-free, so the same on every
+// run); a block whose offsets all lie past the end found so far returns.
+template <typename R>
+__global__ void __launch_bounds__(256) hyd_walk_stop_kernel(HydArgs a, int64_t n_oblocks) {
+    const int64_t n_walks = (int64_t)a.n_h * a.n_layers * 2;
+    for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
+        const int64_t gw = blk / n_oblocks, ob = blk - gw * n_oblocks;
+        int* end = &a.walk[gw].y;
+        const int first = a.walk[gw].x;
+        const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
+        if ((int64_t)first + ob * 256 >= (int64_t)*(volatile int*)end) continue;  // block-uniform
+        if (o >= (int64_t)*(volatile int*)end) continue;
+        const HydPar q = a.par[gw >> 1];
+        const int side = (gw & 1) ? -1 : 1;
+        const int64_t b = (int64_t)q.ci + side * o;
+        bool stop = true;
+        if (b >= 0 && b < a.n_wl) {
+            bool add;
+            walk_value<R>(a, q, b, side, &stop, &add);
+        }
+        if (stop) atomicMin(end, (int)o);
+    }
 }
 
 // One thread per (depth, grid point): every line whose walk covers the point
@@ -717,52 +718,45 @@ __device__ __forceinline__ bool he_below_wcon(const HeArgs& a, const HePar& q, i
     return q.wcon > 0.0 && a.grid[b] <= q.wcon;
 }
 
-// One warp per (helium line, depth, side): the red walk takes offsets
-// 0, 1, ... from the centre bin and ends before the first value below the
-// cutoff; the blue walk takes 1, 2, ... and ends after it (the reference adds
-// that value, then stops).  Stored as offsets [x, y).
+// The helium walks: first offsets and their last possible ends (one thread
+// per (line, depth, side)).
 template <typename R>
-__global__ void __launch_bounds__(128) he_march_kernel(HeArgs a) {
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(128) he_walk_init_kernel(HeArgs a) {
+    const int64_t gw = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gw >= (int64_t)a.n_he * a.n_layers * 2) return;
-    const int64_t pd = gw >> 1;
+    const HePar& q = a.par[gw >> 1];
     const bool red = (gw & 1) == 0;
-    const HePar q = a.par[pd];
     const int64_t n = a.n_wl;
-    int2 out = make_int2(1, 1);
     bool alive = q.active != 0;
-    if (alive) {
-        if (red) alive = q.wl0 <= a.grid[n - 1];
-        else alive = q.ci > 0 && q.wl0 >= a.grid[0];
-    }
-    if (alive) {
-        const int64_t first = red ? 0 : 1;
-        const int64_t last = red ? n - 1 - q.ci : q.ci;  // largest offset inside the grid
-        int64_t end = last + 1;
-        for (int64_t o0 = first; o0 <= last; o0 += 32) {
-            const int64_t o = o0 + lane;
-            bool stop = false;
-            bool below = false;
-            if (o <= last) {
-                const int64_t b = red ? q.ci + o : q.ci - o;
-                below = he_below_wcon(a, q, b);
-                if (!below) stop = he_value<R>(a, q, b) < abtot_he<R>(a, q.d, b) * a.cutoff;
-                else if (!red) stop = true;
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, stop);
-            if (m) {
-                const int l = __ffs(m) - 1;
-                const int64_t hit = o0 + l;
-                // blue: the step that fails the cutoff is added, one at WCON is not
-                const bool hit_below = __shfl_sync(0xffffffffu, below, l);
-                end = red ? hit : (hit_below ? hit : hit + 1);
-                break;
-            }
+    if (alive) alive = red ? q.wl0 <= a.grid[n - 1] : (q.ci > 0 && q.wl0 >= a.grid[0]);
+    const int first = red ? 0 : 1;
+    const int64_t last = red ? n - 1 - q.ci : q.ci;  // largest offset inside the grid
+    a.walk[gw] = make_int2(first, alive ? (int)(last + 1) : first);
+}
+
+// Where each helium walk ends (one thread per (walk, offset), smallest end by
+// atomicMin): the red walk ends before the first step under the cutoff (steps
+// at or below WCON are passed over), the blue walk after it, or before the
+// first step at or below WCON (opacity.py:1019-1046).
+template <typename R>
+__global__ void __launch_bounds__(256) he_walk_stop_kernel(HeArgs a, int64_t n_oblocks) {
+    const int64_t n_walks = (int64_t)a.n_he * a.n_layers * 2;
+    for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
+        const int64_t gw = blk / n_oblocks, ob = blk - gw * n_oblocks;
+        int* end = &a.walk[gw].y;
+        const int first = a.walk[gw].x;
+        const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
+        if ((int64_t)first + ob * 256 >= (int64_t)*(volatile int*)end) continue;  // block-uniform
+        if (o >= (int64_t)*(volatile int*)end) continue;
+        const HePar q = a.par[gw >> 1];
+        const bool red = (gw & 1) == 0;
+        const int64_t b = red ? q.ci + o : q.ci - o;
+        if (he_below_wcon(a, q, b)) {
+            if (!red) atomicMin(end, (int)o);
+            continue;
         }
-        out = make_int2((int)first, (int)end);
+        if (he_value<R>(a, q, b) < abtot_he<R>(a, q.d, b) * a.cutoff) atomicMin(end, (int)(red ? o : o + 1));
     }
-    if (lane == 0) a.walk[gw] = out;
 }
 
 // One thread per (depth, grid point): the wing values of the helium lines
@@ -1058,54 +1052,53 @@ __device__ __forceinline__ double f19_cont_value(const F19Par& q, int64_t b) {
     return v;
 }
 
-// One warp per (autoionizing line, depth, side): offsets 1, 2, ... until the
-// grid ends or the value is <= 0 or below the cutoff (not added); [1, end).
+// The autoionizing walks (offsets 1, 2, ... on each side) and the merged-
+// continuum ramps (red slot only, absolute bins from the first bin of the
+// ramp): first positions and their last possible ends, one thread per
+// (line, depth, side).
 template <typename R>
-__global__ void __launch_bounds__(128) f19_march_kernel(F19Args a) {
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(128) f19_walk_init_kernel(F19Args a) {
+    const int64_t gw = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gw >= (int64_t)a.n_f19 * a.n_layers * 2) return;
-    const int64_t pd = gw >> 1;
+    const F19Par& q = a.par[gw >> 1];
     const bool red = (gw & 1) == 0;
-    const F19Par q = a.par[pd];
     const int64_t n = a.n_wl;
     int2 out = make_int2(1, 1);
     if (q.active && q.kind == 2 && red) {
-        // the ramp from the first bin: points blueward of the line are passed
-        // over, the first value under the cutoff ends it; [first, end) in bins
-        int64_t end = q.nstep;
-        for (int64_t b0 = q.cc; b0 < q.nstep; b0 += 32) {
-            const int64_t b = b0 + lane;
-            bool stop = false;
-            if (b < q.nstep && !(a.grid[b] < q.tabstep))
-                stop = f19_cont_value(q, b) < abtot_f19<R>(a, q.d, b) * a.cutoff;
-            const unsigned m = __ballot_sync(0xffffffffu, stop);
-            if (m) {
-                end = b0 + (__ffs(m) - 1);
-                break;
-            }
-        }
-        out = make_int2(q.cc, (int)end);
+        out = make_int2(q.cc, q.nstep);                   // bins [first, tail)
     } else if (q.active && q.kind == 1) {
         const int64_t last = red ? n - 1 - q.ci : q.ci;  // offsets that stay inside the grid
-        int64_t end = last + 1;
-        for (int64_t o0 = 1; o0 <= last; o0 += 32) {
-            const int64_t o = o0 + lane;
-            bool stop = false;
-            if (o <= last) {
-                const int64_t b = red ? q.ci + o : q.ci - o;
-                const double v = f19_aut_value(a, q, b);
-                stop = v <= 0.0 || v < abtot_f19<R>(a, q.d, b) * a.cutoff;
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, stop);
-            if (m) {
-                end = o0 + (__ffs(m) - 1);
-                break;
-            }
-        }
-        out = make_int2(1, (int)(end < 1 ? 1 : end));
+        out = make_int2(1, (int)(last >= 1 ? last + 1 : 1));
     }
-    if (lane == 0) a.walk[gw] = out;
+    a.walk[gw] = out;
+}
+
+// Where each autoionizing walk and merged-continuum ramp ends: one thread per
+// (walk, position), the smallest stopping position kept with atomicMin.  An
+// autoionizing step stops at a value <= 0 or under the cutoff
+// (opacity.py:944-958); a ramp point stops under the cutoff, points blueward
+// of the line being passed over (:885-897).
+template <typename R>
+__global__ void __launch_bounds__(256) f19_walk_stop_kernel(F19Args a, int64_t n_oblocks) {
+    const int64_t n_walks = (int64_t)a.n_f19 * a.n_layers * 2;
+    for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
+        const int64_t gw = blk / n_oblocks, ob = blk - gw * n_oblocks;
+        int* end = &a.walk[gw].y;
+        const int first = a.walk[gw].x;
+        const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
+        if ((int64_t)first + ob * 256 >= (int64_t)*(volatile int*)end) continue;  // block-uniform
+        if (o >= (int64_t)*(volatile int*)end) continue;
+        const F19Par q = a.par[gw >> 1];
+        const bool red = (gw & 1) == 0;
+        if (q.kind == 2) {
+            if (a.grid[o] < q.tabstep) continue;
+            if (f19_cont_value(q, o) < abtot_f19<R>(a, q.d, o) * a.cutoff) atomicMin(end, (int)o);
+            continue;
+        }
+        const int64_t b = red ? (int64_t)q.ci + o : (int64_t)q.ci - o;
+        const double v = f19_aut_value(a, q, b);
+        if (v <= 0.0 || v < abtot_f19<R>(a, q.d, b) * a.cutoff) atomicMin(end, (int)o);
+    }
 }
 
 __device__ __forceinline__ double f19_value(const F19Args& a, const F19Par& q, int k) {
@@ -1190,7 +1183,14 @@ static cudaError_t launch_f19_t(const F19Args& a, R* cube, cudaStream_t s) {
     f19_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    f19_march_kernel<R><<<(unsigned)((nhd * 2 * 32 + 127) / 128), 128, 0, s>>>(a);
+    f19_walk_init_kernel<R><<<(unsigned)((nhd * 2 + 127) / 128), 128, 0, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    {
+        const int64_t n_ob = (a.n_wl + 1 + 255) / 256;
+        const int64_t blocks = nhd * 2 * n_ob;
+        f19_walk_stop_kernel<R><<<(unsigned)(blocks < (1LL << 30) ? blocks : (1LL << 30)), 256, 0, s>>>(a, n_ob);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int64_t cells = (int64_t)a.n_layers * a.n_wl;
@@ -1208,7 +1208,14 @@ static cudaError_t launch_helium_t(const HeArgs& a, R* cube, cudaStream_t s) {
     he_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    he_march_kernel<R><<<(unsigned)((nhd * 2 * 32 + 127) / 128), 128, 0, s>>>(a);
+    he_walk_init_kernel<R><<<(unsigned)((nhd * 2 + 127) / 128), 128, 0, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    {
+        const int64_t n_ob = (a.n_wl + 1 + 255) / 256;
+        const int64_t blocks = nhd * 2 * n_ob;
+        he_walk_stop_kernel<R><<<(unsigned)(blocks < (1LL << 30) ? blocks : (1LL << 30)), 256, 0, s>>>(a, n_ob);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int64_t cells = (int64_t)a.n_layers * a.n_wl;
@@ -1230,7 +1237,14 @@ static cudaError_t launch_hydrogen_t(const HydArgs& a, R* cube, cudaStream_t s) 
     hyd_setup_kernel<R><<<(unsigned)((nhd + 127) / 128), 128, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    hyd_march_kernel<R><<<(unsigned)((nhd * 2 * 32 + 127) / 128), 128, 0, s>>>(a);
+    hyd_walk_init_kernel<R><<<(unsigned)((nhd * 2 + 127) / 128), 128, 0, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    {
+        const int64_t n_ob = (a.n_wl + 1 + 255) / 256;
+        const int64_t blocks = nhd * 2 * n_ob;
+        hyd_walk_stop_kernel<R><<<(unsigned)(blocks < (1LL << 30) ? blocks : (1LL << 30)), 256, 0, s>>>(a, n_ob);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int64_t cells = (int64_t)a.n_layers * a.n_wl;
