@@ -574,7 +574,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) hyd_walk_stop_kernel(HydArgs a, int64_t n_oblocks) {
     const int64_t n_walks = (int64_t)a.n_h * a.n_layers * 2;
     for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
-        const int64_t gw = blk / n_oblocks, ob = blk - gw * n_oblocks;
+        const int64_t ob = blk / n_walks, gw = blk - ob * n_walks;  // offset blocks in order: ends found early cut later blocks
         int* end = &a.walk[gw].y;
         const int first = a.walk[gw].x;
         const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
@@ -742,7 +742,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) he_walk_stop_kernel(HeArgs a, int64_t n_oblocks) {
     const int64_t n_walks = (int64_t)a.n_he * a.n_layers * 2;
     for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
-        const int64_t gw = blk / n_oblocks, ob = blk - gw * n_oblocks;
+        const int64_t ob = blk / n_walks, gw = blk - ob * n_walks;  // offset blocks in order: ends found early cut later blocks
         int* end = &a.walk[gw].y;
         const int first = a.walk[gw].x;
         const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
@@ -1082,7 +1082,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) f19_walk_stop_kernel(F19Args a, int64_t n_oblocks) {
     const int64_t n_walks = (int64_t)a.n_f19 * a.n_layers * 2;
     for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
-        const int64_t gw = blk / n_oblocks, ob = blk - gw * n_oblocks;
+        const int64_t ob = blk / n_walks, gw = blk - ob * n_walks;  // offset blocks in order: ends found early cut later blocks
         int* end = &a.walk[gw].y;
         const int first = a.walk[gw].x;
         const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
