@@ -146,21 +146,24 @@ __device__ double interp_cutoff(double dwn, const double* tab, int n, double sta
 
 // HPROF4 (profiles/hydrogen.py:1541-1710) for the transition n -> m at
 // wavelength offset dlam_nm from the line centre, in the depth state q.
-__device__ double hprof4(int n, int m, const HydPar& q, double dlam_nm, const HydTables& T, const double* extab,
-                         const double* extabf) {
+// The wavelength-independent part of HPROF4 (profiles/hydrogen.py:1430-1515,
+// :1842-1870) for the (n, m) profile of a line at one layer, computed once
+// per (line, layer) by the setup kernel.
+__device__ HprofConst hprof4_const(int n, int m, const HydPar& q, const HydTables& T) {
+    HprofConst K{};
     const int mmn = m - n;
+    K.mmn = mmn;
+    if (mmn <= 0) return K;
     const double xn = (double)n, xm = (double)m;
     const double xn2 = xn * xn, xm2 = xm * xm;
     const double xm2mn2 = xm2 - xn2;
     const double xmn2 = xm2 * xn2;
     const double gnm = xm2mn2 / xmn2;
-    if (mmn <= 0) return 0.0;
     double xknm;
     if (mmn <= 3 && n <= 4) xknm = T.xknmtb[(n - 1) * 3 + mmn - 1];
     else xknm = 5.5e-5 / gnm * xmn2 / (1.0 + 0.13 / (double)mmn);
     const double freqnm = kRydH * gnm;
     const double wavenm = kClightA / freqnm;
-    const double dbeta = kClightA / (freqnm * freqnm * xknm);
     const double c1con = xknm / wavenm * gnm * xm2mn2;
     const double c2con = pow(xknm / wavenm, 2.0);
     double radamp = T.asum[n - 1] + T.asum[m - 1];
@@ -177,18 +180,52 @@ __device__ double hprof4(int n, int m, const HydPar& q, double dlam_nm, const Hy
     const double hwres = resont * q.xnfph0 * 2.0;
     const double hwstk = stark * q.fo;
     const double hwlor = hwres + hwvdw + hwrad;
-    const double wl = wavenm + dlam_nm * 10.0;
+    const double dph = fmax(q.dopph, 1e-40);
+    K.freqnm = freqnm;
+    K.wavenm = wavenm;
+    K.dbeta = kClightA / (freqnm * freqnm * xknm);
+    K.dop = freqnm * dph;
+    K.hfwidth = freqnm * fmax(fmax(dph, hwlor), hwstk);
+    K.hhw = freqnm * hwlor;
+    K.hwres = hwres;
+    K.hwvdw = hwvdw;
+    K.hwrad = hwrad;
+    K.nwid = 1;
+    if (!(dph >= hwstk && dph >= hwlor)) {
+        K.nwid = 2;
+        if (hwlor < hwstk) K.nwid = 3;
+    }
+    const double y1num = m == 2 ? 550.0 : (m == 3 ? 380.0 : 320.0);
+    double y1wht = mmn <= 3 ? 1.0e14 : 1.0e13;
+    if (mmn <= 2 && n <= 2) y1wht = T.y1wtm[(n - 1) * 2 + mmn - 1];
+    const double wty1 = 1.0 / (1.0 + fmax(q.xne, 0.0) / fmax(y1wht, 1e-30));
+    const double y1_scal = y1num * q.y1s * wty1 + q.y1b * (1.0 - wty1);
+    K.c1 = q.c1d * c1con * y1_scal;
+    K.c2 = q.c2d * c2con;
+    K.g1 = 6.77 * sqrt(fmax(K.c1, 1e-30));
+    const double ratio = (K.c1 > 0.0 && K.c2 > 0.0) ? sqrt(K.c2) / fmax(K.c1, 1e-30) : 0.0;
+    const double log_term = ratio > 0.0 ? log(fmax(ratio, 1e-30)) : 0.0;
+    K.gamma0 = K.g1 * fmax(0.0, 0.2114 + log_term) * (1.0 - q.gcon1 - q.gcon2);
+    return K;
+}
+
+// HPROF4 at dlam_nm from the line centre (profiles/hydrogen.py:1430-1870):
+// Doppler core over the fine-structure components, Lorentz (resonance, van
+// der Waals, radiation) wings, the Stark profile with its quasi-static
+// cutoffs; K holds the (n, m) profile's wavelength-independent part.
+__device__ double hprof4(int n, int m, const HprofConst& K, const HydPar& q, double dlam_nm, const HydTables& T,
+                         const double* extab, const double* extabf) {
+    const int mmn = K.mmn;
+    if (mmn <= 0) return 0.0;
+    const double xn = (double)n;
+    const double xn2 = xn * xn;
+    const double freqnm = K.freqnm, dbeta = K.dbeta, dop = K.dop, hhw = K.hhw;
+    const double hwres = K.hwres, hwvdw = K.hwvdw, hwrad = K.hwrad;
+    const double wl = K.wavenm + dlam_nm * 10.0;
     const double freq = kClightA / wl;
     const double del_freq = fabs(freq - freqnm);
-    const double dph = fmax(q.dopph, 1e-40);
-    const double dop = freqnm * dph;
-    const double hfwidth = freqnm * fmax(fmax(dph, hwlor), hwstk);
-    const bool ifcore = del_freq <= hfwidth;
-    int nwid = 1;
-    if (!(dph >= hwstk && dph >= hwlor)) {
-        nwid = 2;
-        if (hwlor < hwstk) nwid = 3;
-    }
+    const bool ifcore = del_freq <= K.hfwidth;
+    const int nwid = K.nwid;
     // Doppler core over the fine-structure components (profiles/hydrogen.py:1516)
     double core = 0.0;
     {
@@ -215,7 +252,6 @@ __device__ double hprof4(int n, int m, const HydPar& q, double dlam_nm, const Hy
         }
     }
     double lorentz = 0.0;
-    const double hhw = freqnm * hwlor;
     if (n == 1 && m == 2) {
         // Lyman alpha (profiles/hydrogen.py:1731-1797)
         if (dop > 0.0) {
@@ -252,22 +288,12 @@ __device__ double hprof4(int n, int m, const HydPar& q, double dlam_nm, const Hy
         }
         if (hhw > 0.0) lorentz = top / kPi / (del_freq * del_freq + hhw * hhw) * 1.77245 * dop;
     }
-    const double y1num = m == 2 ? 550.0 : (m == 3 ? 380.0 : 320.0);
-    double y1wht = mmn <= 3 ? 1.0e14 : 1.0e13;
-    if (mmn <= 2 && n <= 2) y1wht = T.y1wtm[(n - 1) * 2 + mmn - 1];
-    const double wty1 = 1.0 / (1.0 + fmax(q.xne, 0.0) / fmax(y1wht, 1e-30));
-    const double y1_scal = y1num * q.y1s * wty1 + q.y1b * (1.0 - wty1);
-    const double c1 = q.c1d * c1con * y1_scal;
-    const double c2 = q.c2d * c2con;
     const double beta = del_freq / fmax(q.fo, 1e-30) * dbeta;
-    const double y1 = c1 * beta;
-    const double y2 = c2 * beta * beta;
-    const double g1 = 6.77 * sqrt(fmax(c1, 1e-30));
-    const double ratio = (c1 > 0.0 && c2 > 0.0) ? sqrt(c2) / fmax(c1, 1e-30) : 0.0;
-    const double log_term = ratio > 0.0 ? log(fmax(ratio, 1e-30)) : 0.0;
-    double gamma = g1 * fmax(0.0, 0.2114 + log_term) * (1.0 - q.gcon1 - q.gcon2);
+    const double y1 = K.c1 * beta;
+    const double y2 = K.c2 * beta * beta;
+    double gamma = K.gamma0;
     if (y2 > 1e-4 && y1 > 1e-5)
-        gamma = g1 *
+        gamma = K.g1 *
                 (0.5 * fastex(fmin(80.0, y1), extab, extabf) + vcse1f(y1, extab, extabf) -
                  0.5 * vcse1f(y2, extab, extabf)) *
                 (1.0 - q.gcon1 / (1.0 + pow(90.0 * y1, 3.0)) - q.gcon2 / (1.0 + 2000.0 * y1));
@@ -382,7 +408,7 @@ __device__ double walk_value(const HydArgs& a, const HydPar& q, int64_t b, int s
             *add = false;
             return 0.0;
         }
-        double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+        double v = q.kappa0 * hprof4(q.nl, q.nu, q.k_line, q, w - q.wl0, T, a.extab, a.extabf) * stim;
         if (taper && w < q.wtail) v *= (w - q.wcon) / (q.wtail - q.wcon);
         if (!(v >= cut)) *add = false;
         return v;
@@ -397,11 +423,11 @@ __device__ double walk_value(const HydArgs& a, const HydPar& q, int64_t b, int s
                 *add = false;
                 return 0.0;
             }
-            double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+            double v = q.kappa0 * hprof4(q.nl, q.nu, q.k_line, q, w - q.wl0, T, a.extab, a.extabf) * stim;
             if (taper && w < q.wtail) v *= (w - q.wcon) / (q.wtail - q.wcon);
             if (w > q.redcut) {
                 const int um2 = q.nu - 2 > q.nl + 1 ? q.nu - 2 : q.nl + 1;
-                double v2 = q.kappa0 * hprof4(q.nl, um2, q, w - q.wlm2, T, a.extab, a.extabf) * stim;
+                double v2 = q.kappa0 * hprof4(q.nl, um2, q.k_red, q, w - q.wlm2, T, a.extab, a.extabf) * stim;
                 if (taper && w < q.wtail) v2 *= (w - q.wcon) / (q.wtail - q.wcon);
                 if (v2 >= v) {
                     *stop = true;
@@ -411,7 +437,7 @@ __device__ double walk_value(const HydArgs& a, const HydPar& q, int64_t b, int s
             if (v <= 0.0 || v < cut) *stop = true;
             return v;
         }
-        const double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+        const double v = q.kappa0 * hprof4(q.nl, q.nu, q.k_line, q, w - q.wl0, T, a.extab, a.extabf) * stim;
         if (v <= 0.0 || v < cut) *stop = true;
         return v;
     }
@@ -419,11 +445,11 @@ __device__ double walk_value(const HydArgs& a, const HydPar& q, int64_t b, int s
         *stop = true;
         return 0.0;
     }
-    double v = q.kappa0 * hprof4(q.nl, q.nu, q, w - q.wl0, T, a.extab, a.extabf) * stim;
+    double v = q.kappa0 * hprof4(q.nl, q.nu, q.k_line, q, w - q.wl0, T, a.extab, a.extabf) * stim;
     if (!simple) {
         if (taper && w < q.wtail) v *= (w - q.wcon) / (q.wtail - q.wcon);
         if (w < q.bluecut) {
-            double v2 = q.kappa0 * hprof4(q.nl, q.nu + 2, q, w - q.wlp2, T, a.extab, a.extabf) * stim;
+            double v2 = q.kappa0 * hprof4(q.nl, q.nu + 2, q.k_blue, q, w - q.wlp2, T, a.extab, a.extabf) * stim;
             if (taper && w < q.wtail) v2 *= (w - q.wcon) / (q.wtail - q.wcon);
             if (v2 >= v) {
                 *stop = true;
@@ -536,6 +562,9 @@ __global__ void __launch_bounds__(128) hyd_setup_kernel(HydArgs a) {
     wtail = fmin(wcon + wcon, wtail);
     q.wcon = wcon;
     q.wtail = wtail;
+    q.k_line = hprof4_const(q.nl, q.nu, q, T);
+    q.k_red = hprof4_const(q.nl, q.nu - 2 > q.nl + 1 ? q.nu - 2 : q.nl + 1, q, T);
+    q.k_blue = hprof4_const(q.nl, q.nu + 2, q, T);
     a.par[i] = q;
 }
 
@@ -580,7 +609,7 @@ __global__ void __launch_bounds__(256) hyd_walk_stop_kernel(HydArgs a, int64_t n
         const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
         if ((int64_t)first + ob * 256 >= (int64_t)*(volatile int*)end) continue;  // block-uniform
         if (o >= (int64_t)*(volatile int*)end) continue;
-        const HydPar q = a.par[gw >> 1];
+        const HydPar& q = a.par[gw >> 1];
         const int side = (gw & 1) ? -1 : 1;
         const int64_t b = (int64_t)q.ci + side * o;
         bool stop = true;
@@ -622,7 +651,7 @@ __global__ void __launch_bounds__(256) hyd_gather_kernel(HydArgs a, R* __restric
             const int2 wk = a.walk[pd * 2 + (side > 0 ? 0 : 1)];
             if (o < wk.x || o >= wk.y) continue;
         }
-        const HydPar q = a.par[pd];
+        const HydPar& q = a.par[pd];
         bool stop, add;
         const double v = walk_value<R>(a, q, b, side, &stop, &add);
         if (!add) continue;
@@ -802,11 +831,26 @@ __device__ __forceinline__ double abtot_f19(const F19Args& a, int d, int64_t b) 
 
 // Near-wing profile value at step k (k <= N10DOP): the incremental TABI of
 // opacity.py:151-162 (k additions of TABSTEP to 0.5) or the Voigt function.
+// The truncated TABI after k additions: each addition of a positive TABSTEP
+// rounds by at most half an ulp of a partial sum no larger than the last, so
+// the sequential sum lies within (k + 1) |s| 2^-53 of s = fma(k, TABSTEP, 0.5);
+// where s is farther than twice that from an integer both truncate alike, and
+// only the other points replay the k additions.
+__device__ __forceinline__ int tabi_index(double tabstep, int k) {
+    if (tabstep > 0.0) {
+        const double s = fma((double)k, tabstep, 0.5);
+        const double f = floor(s);
+        const double bound = (double)(k + 1) * (s + 1.0) * 2.220446049250313e-16;
+        if (s - f > bound && (f + 1.0) - s > bound && s < 2.0e9) return (int)f;
+    }
+    double tabi = 0.5;
+    for (int j = 0; j < k; j++) tabi = tabi + tabstep;
+    return (int)tabi;
+}
+
 __device__ __forceinline__ double f19_near(const F19Args& a, const F19Par& q, int k) {
     if (q.adamp < 0.2) {
-        double tabi = 0.5;
-        for (int j = 0; j < k; j++) tabi = tabi + q.tabstep;
-        int it = (int)tabi;
+        int it = tabi_index(q.tabstep, k);
         it = it < 0 ? 0 : (it > VOIGT_N - 1 ? VOIGT_N - 1 : it);
         return q.kappa0 * (a.h0[it] + q.adamp * a.h1[it]);
     }
@@ -1077,33 +1121,57 @@ __global__ void __launch_bounds__(128) f19_walk_init_kernel(F19Args a) {
 // (walk, position), the smallest stopping position kept with atomicMin.  An
 // autoionizing step stops at a value <= 0 or under the cutoff
 // (opacity.py:944-958); a ramp point stops under the cutoff, points blueward
-// of the line being passed over (:885-897).
+// of the line being passed over (:885-897).  Most fort.19 walks are empty
+// (NORMAL lines have none) or end early, so a block takes 32 walks at one
+// block of 256 positions: one warp's ballot keeps those still running and the
+// block evaluates only them.  Blocks run position blocks in order across all
+// walks, so ends found by earlier blocks cut the later ones.
 template <typename R>
 __global__ void __launch_bounds__(256) f19_walk_stop_kernel(F19Args a, int64_t n_oblocks) {
+    __shared__ int live[32];
+    __shared__ int n_live;
     const int64_t n_walks = (int64_t)a.n_f19 * a.n_layers * 2;
-    for (int64_t blk = blockIdx.x; blk < n_walks * n_oblocks; blk += gridDim.x) {
-        const int64_t ob = blk / n_walks, gw = blk - ob * n_walks;  // offset blocks in order: ends found early cut later blocks
-        int* end = &a.walk[gw].y;
-        const int first = a.walk[gw].x;
-        const int64_t o = (int64_t)first + ob * 256 + threadIdx.x;
-        if ((int64_t)first + ob * 256 >= (int64_t)*(volatile int*)end) continue;  // block-uniform
-        if (o >= (int64_t)*(volatile int*)end) continue;
-        const F19Par q = a.par[gw >> 1];
-        const bool red = (gw & 1) == 0;
-        if (q.kind == 2) {
-            if (a.grid[o] < q.tabstep) continue;
-            if (f19_cont_value(q, o) < abtot_f19<R>(a, q.d, o) * a.cutoff) atomicMin(end, (int)o);
-            continue;
+    const int64_t n_chunks = (n_walks + 31) / 32;
+    for (int64_t blk = blockIdx.x; blk < n_chunks * n_oblocks; blk += gridDim.x) {
+        const int64_t ob = blk / n_chunks, c0 = (blk - ob * n_chunks) * 32;
+        if (threadIdx.x < 32) {
+            const int64_t gw = c0 + threadIdx.x;
+            bool alive = false;
+            if (gw < n_walks)
+                alive = (int64_t)a.walk[gw].x + ob * 256 < (int64_t)*(volatile int*)&a.walk[gw].y;
+            const unsigned m = __ballot_sync(0xffffffffu, alive);
+            if (alive) live[__popc(m & ((1u << threadIdx.x) - 1u))] = (int)threadIdx.x;
+            if (threadIdx.x == 0) n_live = __popc(m);
         }
-        const int64_t b = red ? (int64_t)q.ci + o : (int64_t)q.ci - o;
-        const double v = f19_aut_value(a, q, b);
-        if (v <= 0.0 || v < abtot_f19<R>(a, q.d, b) * a.cutoff) atomicMin(end, (int)o);
+        __syncthreads();
+        const int nl = n_live;
+        for (int k = 0; k < nl; ++k) {
+            const int64_t gw = c0 + live[k];
+            int* end = &a.walk[gw].y;
+            const int64_t o = (int64_t)a.walk[gw].x + ob * 256 + threadIdx.x;
+            if (o >= (int64_t)*(volatile int*)end) continue;
+            const F19Par q = a.par[gw >> 1];
+            if (q.kind == 2) {
+                if (a.grid[o] < q.tabstep) continue;
+                if (f19_cont_value(q, o) < abtot_f19<R>(a, q.d, o) * a.cutoff) atomicMin(end, (int)o);
+                continue;
+            }
+            const bool red = (gw & 1) == 0;
+            const int64_t b = red ? (int64_t)q.ci + o : (int64_t)q.ci - o;
+            const double v = f19_aut_value(a, q, b);
+            if (v <= 0.0 || v < abtot_f19<R>(a, q.d, b) * a.cutoff) atomicMin(end, (int)o);
+        }
+        __syncthreads();  // live[] and n_live are rewritten for the next chunk
     }
 }
 
+// Wing value at step k.  The far wing X / k^2 is an FP64 division in the FP64
+// path; the mixed path, whose cube holds FP32, divides in FP32.
+template <typename R>
 __device__ __forceinline__ double f19_value(const F19Args& a, const F19Par& q, int k) {
     const int near_end = q.early ? q.nstep : q.n10;
     if (k <= near_end) return f19_near(a, q, k);
+    if (sizeof(R) == sizeof(float)) return (double)((float)q.x_far / ((float)k * (float)k));
     return q.x_far / ((double)k * (double)k);
 }
 
@@ -1156,13 +1224,13 @@ __global__ void __launch_bounds__(256) f19_gather_kernel(F19Args a, R* __restric
             const int k = b - ci;
             const int maxred = ci >= 0 ? min(n - 1 - ci, ns) : min(n - 1, ns);
             if (k >= max(1, -ci) && k <= maxred) {
-                acc += wing_taper(f19_value(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
+                acc += wing_taper(f19_value<R>(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
                 any = true;
             }
         } else if (b < ci && ci > 0) {
             const int k = ci - b;
             if (k >= max(1, ci + 1 - n) && k <= min(ci, ns)) {
-                acc += wing_taper(f19_value(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
+                acc += wing_taper(f19_value<R>(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
                 any = true;
             }
         }
@@ -1188,7 +1256,7 @@ static cudaError_t launch_f19_t(const F19Args& a, R* cube, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     {
         const int64_t n_ob = (a.n_wl + 1 + 255) / 256;
-        const int64_t blocks = nhd * 2 * n_ob;
+        const int64_t blocks = (nhd * 2 + 31) / 32 * n_ob;
         f19_walk_stop_kernel<R><<<(unsigned)(blocks < (1LL << 30) ? blocks : (1LL << 30)), 256, 0, s>>>(a, n_ob);
     }
     e = cudaGetLastError();

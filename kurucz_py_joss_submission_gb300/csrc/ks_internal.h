@@ -203,10 +203,18 @@ struct HydTables {
 };
 
 // One (hydrogen line, depth): gates, walk limits and the hydrogen depth state.
+// The wavelength-independent part of one HPROF4 (n, m) profile at one layer:
+// line frequency and wavelength, the widths and the Stark constants.
+struct HprofConst {
+    double freqnm, wavenm, dbeta, dop, hfwidth, hhw, hwres, hwvdw, hwrad, c1, c2, g1, gamma0;
+    int mmn, nwid;
+};
+
 struct HydPar {
     double wl0, kappa0, wcon, wtail, wlm1, wlm2, wlp1, wlp2, redcut, bluecut;
     double pp, fo, y1b, y1s, t3nhe, t3nh2, c1d, c2d, gcon1, gcon2, xnfph0, xnfph1, dopph, xne, hkt;
     int ci, nl, nu, d, active;
+    HprofConst k_line, k_red, k_blue;  // (NBLO, NBUP), (NBLO, max(NBUP-2, NBLO+1)), (NBLO, NBUP+2)
 };
 
 struct HydArgs {
