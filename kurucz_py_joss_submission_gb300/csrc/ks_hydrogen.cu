@@ -831,6 +831,17 @@ __device__ __forceinline__ double abtot_f19(const F19Args& a, int d, int64_t b) 
 
 // Near-wing profile value at step k (k <= N10DOP): the incremental TABI of
 // opacity.py:151-162 (k additions of TABSTEP to 0.5) or the Voigt function.
+// Number of grid points at or below x (le) or below x; the grid ascends.
+__device__ __forceinline__ int grid_count(const double* g, int64_t n, double x, bool le) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (le ? g[mid] <= x : g[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return (int)lo;
+}
+
 // The truncated TABI after k additions: each addition of a positive TABSTEP
 // rounds by at most half an ulp of a partial sum no larger than the last, so
 // the sequential sum lies within (k + 1) |s| 2^-53 of s = fma(k, TABSTEP, 0.5);
@@ -868,7 +879,8 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
     F19Par q;
     q.kappa0 = q.adamp = q.tabstep = q.dvoigt = q.x_far = q.kapcen = 0.0;
     q.wcon = q.wtail = -1.0;
-    q.ci = q.cc = q.n10 = q.nstep = q.early = q.active = q.kc_ok = q.kind = q.pad = 0;
+    q.ci = q.cc = q.n10 = q.nstep = q.early = q.active = q.kc_ok = q.kind = q.bw_tail = 0;
+    q.bw_con = -1;
     q.d = d;
     const int row = a.rows[h];
     const int e = (row >= 0 && (int64_t)row < a.n_lines) ? a.element_idx[row] : -1;
@@ -1022,6 +1034,9 @@ __global__ void __launch_bounds__(128) f19_setup_kernel(F19Args a) {
     // continuum-merge limits of the record (opacity.py:1449-1461), with the
     // fort.19 ion index as NELION
     continuum_limits(a.ncon[h], a.nelion[h], a.nelionx[h], dp.xne, *a.tab, &q.wcon, &q.wtail);
+    // the limits as grid indices, so that the gather's per-line tests are integer ones
+    q.bw_con = q.wcon > 0.0 ? grid_count(a.grid, a.n_wl, q.wcon, true) - 1 : -1;
+    q.bw_tail = q.wtail > 0.0 ? grid_count(a.grid, a.n_wl, q.wtail, false) : 0;
     // wing (_accumulate_metal_profile_kernel, no WCON/WTAIL)
     if (k0 <= 0.0) {
         q.nstep = 0;
@@ -1218,21 +1233,21 @@ __global__ void __launch_bounds__(256) f19_gather_kernel(F19Args a, R* __restric
         if (ns <= 0 || ci + ns < 0 || ci - ns >= n) continue;
         // at or below WCON nothing is added: the red loop passes over such
         // steps, the blue one ends there (opacity.py:224-228, :264-267)
-        const double w = a.grid[b];
-        if (q.wcon > 0.0 && w <= q.wcon) continue;
+        // (grid[b] <= WCON exactly for b <= bw_con; the taper applies below bw_tail)
+        if (b <= q.bw_con) continue;
+        int k = 0;
         if (b > ci && ci < n - 1) {
-            const int k = b - ci;
+            const int kr = b - ci;
             const int maxred = ci >= 0 ? min(n - 1 - ci, ns) : min(n - 1, ns);
-            if (k >= max(1, -ci) && k <= maxred) {
-                acc += wing_taper(f19_value<R>(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
-                any = true;
-            }
+            if (kr >= max(1, -ci) && kr <= maxred) k = kr;
         } else if (b < ci && ci > 0) {
-            const int k = ci - b;
-            if (k >= max(1, ci + 1 - n) && k <= min(ci, ns)) {
-                acc += wing_taper(f19_value<R>(a, q, k), w, q.wcon, q.wtail, a.wavelength[a.rows[h]]);
-                any = true;
-            }
+            const int kb = ci - b;
+            if (kb >= max(1, ci + 1 - n) && kb <= min(ci, ns)) k = kb;
+        }
+        if (k > 0) {
+            const double v = f19_value<R>(a, q, k);
+            acc += b < q.bw_tail ? wing_taper(v, a.grid[b], q.wcon, q.wtail, a.wavelength[a.rows[h]]) : v;
+            any = true;
         }
     }
     if (any) {

@@ -274,7 +274,8 @@ struct HeArgs {
 struct F19Par {
     double kappa0, adamp, tabstep, dvoigt, x_far, kapcen;
     double wcon, wtail;  // NORMAL lines: continuum-merge limits (nm; <= 0: none)
-    int ci, cc, n10, nstep, early, active, kc_ok, d, kind, pad;
+    int ci, cc, n10, nstep, early, active, kc_ok, d, kind;
+    int bw_con, bw_tail;  // grid points at or below WCON (last index, -1: none) and below WTAIL (count)
 };
 
 struct F19Args {
