@@ -1,5 +1,6 @@
-// ks_hydrogen.cu -- hydrogen and helium line opacity (FP64), added to the line
-// opacity after the accumulation of the plain lines.
+// ks_hydrogen.cu -- the special line classes: hydrogen, helium and fort.19
+// line opacity (FP64), added to the line opacity after the accumulation of
+// the plain lines.
 //
 // The reference computes the opacity of the catalog's hydrogen lines (line
 // types -1/-2, neutral H) apart from ASYNTH, with Kurucz's HPROF4 profile
@@ -12,11 +13,15 @@
 // Three kernels, all FP64 with every product and sum rounded separately:
 //   hyd_setup_kernel   one thread per (line, depth): the TRANSP-style gates,
 //                      kappa0, the merge and tail wavelengths, the line's
-//                      series-neighbour wavelengths and the hydrogen depth
-//                      state (synthe_py/physics/populations.py:93-125);
+//                      series-neighbour wavelengths, the hydrogen depth
+//                      state (synthe_py/physics/populations.py:93-125) and
+//                      the wavelength-independent part of the line's three
+//                      HPROF4 profiles (the line and its two neighbours);
 //   hyd_walk_*_kernel  where each (line, depth, side) walk ends: every offset
 //                      tested at once, one thread per (walk, offset), the
-//                      smallest stopping offset kept by atomicMin;
+//                      smallest stopping offset kept by atomicMin, offset
+//                      blocks visited in order across all walks so that
+//                      ends already found cut the later blocks;
 //   hyd_gather_kernel  one thread per (depth, grid point): the contributions
 //                      of the lines whose walks cover the point, recomputed
 //                      and summed in catalog order (the order of the
@@ -27,6 +32,14 @@
 // gates, then ``_apply_fort19_profile``'s Voigt walk for TYPE < -2, :966-1061)
 // and enter the line opacity as AHE x STIM (:3650-3660), with the same three
 // kernel shapes (he_setup_kernel, he_walk_*_kernel, he_gather_kernel).
+//
+// The fort.19 records (NORMAL, autoionizing and merged-continuum lines) enter
+// ASYNTH (synthe_py/engine/opacity.py:1388-1486): f19_setup_kernel takes the
+// gates, KAPCEN and the continuum-merge limits per (line, depth);
+// f19_walk_*_kernel finds where the autoionizing walks and continuum ramps
+// end (32 walks per block, only those still running evaluated); and
+// f19_gather_kernel sums KAPCEN and the wing steps per (depth, grid point) in
+// fort.19 order, with the limits as integer grid bounds.
 #include <cuda_runtime.h>
 
 #include <cmath>
