@@ -1,6 +1,7 @@
 // ks_api.cu -- the C ABI (include/kurucz_gb300.h): constant tables, workspace
 // layout, the precision-independent kernels (grid scalars, line bins, reach-
 // class partition) and the pipeline drivers.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1995,6 +1996,17 @@ struct StageTable {
 
 }  // namespace
 
+// A job's special lines (hydrogen, helium, fort.19): its view of the shared
+// list with its own special rows (relative to the job's slice, in the job's
+// block of the workspace), and the records the special-line kernels read when
+// the batch runs.
+struct BatchSpecial {
+    bool any = false;
+    ks_lines lines{};
+    ks_atmos atm{};
+    ks_grid grid{};
+};
+
 struct ks_batch {
     int n_jobs = 0;
     int dev = 0;
@@ -2003,13 +2015,17 @@ struct ks_batch {
     StageTable st[BS_N];
     std::vector<Workspace> ws;
     std::vector<int64_t> n_wl;
+    std::vector<BatchSpecial> spec;
+    bool any_special = false;
+    ks_options opt{};
+    bool has_opt = false;
 };
 
 namespace {
 
 struct BatchLayout {
     size_t table_bytes = 0;
-    std::vector<size_t> job_off, job_bytes;
+    std::vector<size_t> job_off, job_bytes, rows_off;  // rows_off: the job's special rows
     size_t total = 0;
 };
 
@@ -2018,9 +2034,6 @@ size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 ks_status batch_check(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
     ks_status st = check_lines(lines);
     if (st) return st;
-    if (lines->n_hydrogen > 0 || lines->n_helium > 0 || lines->n_f19 > 0)
-        return fail(KS_ERR_UNSUPPORTED,
-                    "ks_batch: hydrogen, helium and fort.19 lines are taken by ks_synthesize only");
     if (n_jobs <= 0 || !jobs) return fail(KS_ERR_INVALID, "ks_batch: no jobs");
     if ((st = check_tiling(opt))) return st;
     if (opt && (opt->transfer_path < 0 || opt->transfer_path > 1))
@@ -2064,7 +2077,7 @@ size_t batch_job_record_bytes(bool fp64) {
     return r;
 }
 
-BatchLayout batch_layout(const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
+BatchLayout batch_layout(const ks_lines* lines, const ks_job* jobs, int32_t n_jobs, const ks_options* opt) {
     BatchLayout b;
     const bool fp64 = opt && opt->precision == KS_PREC_FP64;
     // job records (9 tables), then per stage the block prefix and the grids,
@@ -2077,12 +2090,127 @@ BatchLayout batch_layout(const ks_job* jobs, int32_t n_jobs, const ks_options* o
         Workspace w;
         layout(dry, w, jobs[i].line_count, jobs[i].atm->n_layers, jobs[i].grid->n, jobs[i].atm->n_ion,
                jobs[i].atm->n_elem, fp64, true, true, default_tile(opt, fp64));
+        // room for the job's special rows: at most its slice's lines of each class
+        const int64_t cnt = jobs[i].line_count;
+        const int64_t n_rows = std::min<int64_t>(cnt, lines->n_hydrogen) + std::min<int64_t>(cnt, lines->n_helium) +
+                               std::min<int64_t>(cnt, lines->n_f19);
+        const size_t rows_bytes = al256((size_t)n_rows * sizeof(int32_t));
         b.job_off.push_back(off);
-        b.job_bytes.push_back(al256(dry.used));
-        off += al256(dry.used);
+        b.rows_off.push_back(off + al256(dry.used));
+        b.job_bytes.push_back(al256(dry.used) + rows_bytes);
+        off += al256(dry.used) + rows_bytes;
     }
     b.total = off;
     return b;
+}
+
+// The jobs' special lines.  The shared list's special rows ascend (catalog
+// order), so a job's lines of each class are one contiguous run of them: its
+// per-line columns are the shared ones offset to the run, its rows are copied
+// relative to the job's slice into the job's block.  Synchronous (plan time).
+ks_status batch_special_build(ks_batch* b, const ks_lines* lines, const ks_job* jobs, int32_t n, char* base,
+                              const BatchLayout& lay) {
+    b->spec.assign(n, BatchSpecial{});
+    b->any_special = false;
+    if (lines->n_hydrogen <= 0 && lines->n_helium <= 0 && lines->n_f19 <= 0) return KS_OK;
+    auto fetch = [](const int32_t* d, int32_t cnt, std::vector<int32_t>& h) -> cudaError_t {
+        h.resize(cnt > 0 ? cnt : 0);
+        return cnt > 0 ? cudaMemcpy(h.data(), d, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost) : cudaSuccess;
+    };
+    std::vector<int32_t> hr, her, fr;
+    KS_CUDA(fetch(lines->hydrogen_rows, lines->n_hydrogen, hr));
+    KS_CUDA(fetch(lines->helium_rows, lines->n_helium, her));
+    KS_CUDA(fetch(lines->f19_rows, lines->n_f19, fr));
+    if (!std::is_sorted(hr.begin(), hr.end()) || !std::is_sorted(her.begin(), her.end()) ||
+        !std::is_sorted(fr.begin(), fr.end()))
+        return fail(KS_ERR_INVALID, "ks_batch: the special lines' rows must ascend (catalog order)");
+    if (lines->n_hydrogen > 0 || lines->n_helium > 0 || lines->n_f19 > 0) {
+        // the hydrogen tables' first copy to this device happens here, not in a captured run
+        const HydTables* tab = nullptr;
+        ks_status st = hydrogen_device_tables(&tab);
+        if (st) return st;
+    }
+    for (int i = 0; i < n; i++) {
+        const ks_job& J = jobs[i];
+        const int64_t r0 = J.line_first, r1 = J.line_first + J.line_count;
+        auto run = [&](const std::vector<int32_t>& v, int64_t* lo) -> int32_t {
+            const auto a = std::lower_bound(v.begin(), v.end(), r0);
+            const auto z = std::lower_bound(v.begin(), v.end(), r1);
+            *lo = a - v.begin();
+            return (int32_t)(z - a);
+        };
+        int64_t lh = 0, le = 0, lf = 0;
+        const int32_t nh = run(hr, &lh), ne = run(her, &le), nf = run(fr, &lf);
+        if (nh + ne + nf == 0) continue;
+        if (nh > kMaxHydrogenLines || ne > kMaxHydrogenLines || nf > kMaxHydrogenLines)
+            return fail(KS_ERR_UNSUPPORTED, "ks_batch: job " + std::to_string(i) +
+                                                " has more than 256 special lines of one class");
+        if (nh > 0 && (!J.atm->turbulent_velocity || J.atm->n_ion < 2))
+            return fail(KS_ERR_INVALID, "ks_batch: job " + std::to_string(i) +
+                                            ": hydrogen lines need ks_atmos.turbulent_velocity and n_ion >= 2");
+        std::vector<int32_t> local;
+        local.reserve((size_t)nh + ne + nf);
+        for (int32_t k = 0; k < nh; k++) local.push_back((int32_t)(hr[lh + k] - r0));
+        for (int32_t k = 0; k < ne; k++) local.push_back((int32_t)(her[le + k] - r0));
+        for (int32_t k = 0; k < nf; k++) local.push_back((int32_t)(fr[lf + k] - r0));
+        int32_t* d = (int32_t*)(base + lay.rows_off[i]);
+        KS_CUDA(cudaMemcpy(d, local.data(), sizeof(int32_t) * local.size(), cudaMemcpyHostToDevice));
+        BatchSpecial& sp = b->spec[i];
+        sp.any = true;
+        sp.atm = *J.atm;
+        sp.grid = *J.grid;
+        ks_lines& v = sp.lines;
+        v = job_lines(lines, J);
+        v.n_hydrogen = nh;
+        v.hydrogen_rows = nh ? d : nullptr;
+        v.hydrogen_n_lower = nh ? lines->hydrogen_n_lower + lh : nullptr;
+        v.hydrogen_n_upper = nh ? lines->hydrogen_n_upper + lh : nullptr;
+        v.n_helium = ne;
+        v.helium_rows = ne ? d + nh : nullptr;
+        v.helium_ncon = ne ? lines->helium_ncon + le : nullptr;
+        v.helium_nelionx = ne ? lines->helium_nelionx + le : nullptr;
+        v.n_f19 = nf;
+        v.f19_rows = nf ? d + nh + ne : nullptr;
+        v.f19_cgf = nf ? lines->f19_cgf + lf : nullptr;
+        v.f19_gamma_rad = nf ? lines->f19_gamma_rad + lf : nullptr;
+        v.f19_gamma_stark = nf ? lines->f19_gamma_stark + lf : nullptr;
+        v.f19_gamma_vdw = nf ? lines->f19_gamma_vdw + lf : nullptr;
+        v.f19_kind = nf ? lines->f19_kind + lf : nullptr;
+        v.f19_nlast = nf ? lines->f19_nlast + lf : nullptr;
+        v.f19_nelion = nf ? lines->f19_nelion + lf : nullptr;
+        v.f19_ncon = nf ? lines->f19_ncon + lf : nullptr;
+        v.f19_nelionx = nf ? lines->f19_nelionx + lf : nullptr;
+        b->any_special = true;
+    }
+    return KS_OK;
+}
+
+// Queues every job's special-line kernels (fort.19 into ASYNTH, then the
+// hydrogen and helium lines), in the order a single synthesis runs them,
+// between the batch's accumulation and transfer launches.
+template <typename R>
+ks_status batch_special_run(ks_batch* b, cudaStream_t s) {
+    DevTables t;
+    ks_status st = device_tables(&t);
+    if (st) return st;
+    const ks_options* opt = b->has_opt ? &b->opt : nullptr;
+    for (int i = 0; i < b->n_jobs; i++) {
+        const BatchSpecial& sp = b->spec[i];
+        if (!sp.any) continue;
+        const Workspace& w = b->ws[i];
+        const R* cabs = (const R*)w.cont_abs;
+        const R* cscat = (const R*)w.cont_scat;
+        R* cube = (R*)w.asynth;
+        if (sp.lines.n_f19 > 0 && (st = run_f19<R>(&sp.lines, &sp.atm, &sp.grid, opt, w, t, cabs, cscat, cube, s)))
+            return st;
+        if (sp.lines.n_hydrogen > 0 &&
+            (st = run_hydrogen<R>(&sp.lines, &sp.atm, &sp.grid, opt, w, t, cabs, cscat, cube, s)))
+            return st;
+        if (sp.lines.n_helium > 0 &&
+            (st = run_helium<R>(&sp.lines, &sp.atm, &sp.grid, opt, w, t, cabs, cscat, cube, s)))
+            return st;
+    }
+    return KS_OK;
 }
 
 template <typename R>
@@ -2227,6 +2355,8 @@ ks_status batch_build(ks_batch* b, const ks_lines* lines, const ks_job* jobs, in
     }
     if (overflow) return fail(KS_ERR_NOMEM, "ks_batch: internal table overflow");
     KS_CUDA(cudaMemcpy(base, host.data(), off, cudaMemcpyHostToDevice));
+    ks_status sst = batch_special_build(b, lines, jobs, n, base, lay);
+    if (sst) return sst;
     // persistent grids
     int64_t totals[6] = {b->st[BS_PREP].total, b->st[BS_CONT].total, b->st[BS_PAIR].total, b->st[BS_ACC].total,
                          b->st[BS_TRANS].total, b->st[BS_LIST].total};
@@ -2266,7 +2396,7 @@ extern "C" ks_status ks_batch_workspace_size(const ks_lines* lines, const ks_job
     ks_status st = batch_check(lines, jobs, n_jobs, opt);
     if (st) return st;
     if (!bytes) return fail(KS_ERR_INVALID, "ks_batch_workspace_size: NULL output");
-    *bytes = batch_layout(jobs, n_jobs, opt).total;
+    *bytes = batch_layout(lines, jobs, n_jobs, opt).total;
     return KS_OK;
 }
 
@@ -2279,7 +2409,7 @@ extern "C" ks_status ks_batch_create(const ks_lines* lines, const ks_job* jobs, 
     if (st) return st;
     DevTables t;
     if ((st = device_tables(&t))) return st;
-    BatchLayout lay = batch_layout(jobs, n_jobs, opt);
+    BatchLayout lay = batch_layout(lines, jobs, n_jobs, opt);
     if (!workspace || workspace_bytes < lay.total)
         return fail(KS_ERR_NOMEM, "ks_batch_create: workspace too small (see ks_batch_workspace_size)");
     if ((reinterpret_cast<uintptr_t>(workspace) & 255) != 0)
@@ -2291,6 +2421,10 @@ extern "C" ks_status ks_batch_create(const ks_lines* lines, const ks_job* jobs, 
     b->profile = opt && opt->profile;
     b->tile = default_tile(opt, b->fp64);
     b->warps = default_warps(opt);
+    if (opt) {
+        b->opt = *opt;
+        b->has_opt = true;
+    }
     cudaError_t e = cudaGetDevice(&b->dev);
     if (e != cudaSuccess) {
         delete b;
@@ -2345,6 +2479,11 @@ extern "C" ks_status ks_batch_run(ks_batch* b, ks_stats* stats, void* stream) {
                     : launch_accumulate_batch_f32(b->st[BS_ACC].jobs, G(BS_ACC), b->st[BS_ACC].grid, b->warps,
                                                   b->tile, s));
     tm.mark();
+    if (b->any_special) {
+        const ks_status sst = b->fp64 ? batch_special_run<double>(b, s) : batch_special_run<float>(b, s);
+        if (sst) return sst;
+        tm.mark_special();
+    }
     KS_CUDA(b->fp64 ? launch_transfer_batch_f64(b->st[BS_TRANS].jobs, G(BS_TRANS), G(BS_LIST), &g_tables.cj,
                                                 b->st[BS_TRANS].grid, b->st[BS_LIST].grid, false, s)
                     : launch_transfer_batch_f32(b->st[BS_TRANS].jobs, G(BS_TRANS), G(BS_LIST), &g_tables.cj,

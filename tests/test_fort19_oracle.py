@@ -104,7 +104,7 @@ def test_reader_fields_and_routing():
     assert np.all(cat.gamma_rad_log[nb] != 0.0)   # the logs as read
 
 
-def test_batch_rejects_fort19_lines():
+def test_batch_takes_fort19_lines():
     L = _native.load(build_if_missing=False)
     dummy = C.c_void_p(16)
     rec = _native.KsLines()
@@ -115,5 +115,6 @@ def test_batch_rejects_fort19_lines():
     rec.sorted_by_wavelength = 1
     rec.n_f19 = 1
     size = C.c_size_t(0)
-    assert L.ks_batch_workspace_size(C.byref(rec), None, 0, None, C.byref(size)) == _native.KS_ERR_UNSUPPORTED
-    assert b"fort.19" in L.ks_last_error()
+    # the lines pass the batch's checks (the call fails on the missing jobs)
+    assert L.ks_batch_workspace_size(C.byref(rec), None, 0, None, C.byref(size)) == _native.KS_ERR_INVALID
+    assert b"no jobs" in L.ks_last_error()

@@ -71,13 +71,15 @@ def _lines_record(n_lines, n_hydrogen):
     return rec
 
 
-def test_batch_rejects_hydrogen_lines():
+def test_batch_takes_hydrogen_lines():
+    # the lines pass the batch's checks (the call fails on the missing jobs);
+    # each job's hydrogen lines are found when the plan is made
     L = _native.load(build_if_missing=False)
     rec = _lines_record(10, 1)
     size = C.c_size_t(0)
     st = L.ks_batch_workspace_size(C.byref(rec), None, 0, None, C.byref(size))
-    assert st == _native.KS_ERR_UNSUPPORTED
-    assert b"hydrogen" in L.ks_last_error()
+    assert st == _native.KS_ERR_INVALID
+    assert b"no jobs" in L.ks_last_error()
     rec = _lines_record(10, 11)   # more hydrogen lines than lines
     assert L.ks_batch_workspace_size(C.byref(rec), None, 0, None, C.byref(size)) == _native.KS_ERR_INVALID
 
