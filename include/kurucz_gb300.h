@@ -427,6 +427,11 @@ typedef struct {
  * (job, block) work items with a precomputed per-job prefix, no atomics --
  * 15 launches per batch whatever the number of jobs.  Each job gets the
  * results a ks_synthesize call with the same options gives (bit for bit).
+ * Special lines (hydrogen, helium, fort.19) of the shared list are taken:
+ * their rows must ascend (catalog order), a job's are those in its slice
+ * (at most 256 of each class per job, else KS_ERR_UNSUPPORTED), and each
+ * job with some runs the special-line kernels of ks_synthesize between the
+ * accumulation and the transfer launch (a few launches per such job).
  * The options (precision, tiling, cutoff, microturbulence, RHOXJ) are shared
  * by all jobs.  No reference counterpart: the reference synthesises one
  * atmosphere per run (synthe_py/engine/opacity.py:2084); this replaces a
